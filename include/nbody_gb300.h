@@ -1,0 +1,160 @@
+/*
+ * nbody_gb300.h -- C ABI of the GB300 (sm_103a) N-body all-pairs step.
+ *
+ * This is the drop-in boundary for the compute behind UTC's nbody GPU task.
+ * In the reference the task class BodySystemSGPU<T> (benchapps/nbody/utc/
+ * sgpu/body_task_sgpu.h:16-41) owns the device buffers and launches
+ * _integrateNBodySystem_kernel<T> (benchapps/nbody/utc/sgpu/
+ * bodysystem_kernel.cu:87-138) once per step on its task stream.  Here the
+ * same work sits behind plain C entry points (pointers, sizes, status codes;
+ * no C++ or torch types), which the drop-in task BodySystemGB300<T>
+ * (utc_gb300/task/body_task_gb300.h) and the Python test harness call.
+ *
+ * Data layout (the reference's, body_task_sgpu.cu:55-58): per body 4 values
+ * of the state type, position (x, y, z, m) and velocity (vx, vy, vz, w);
+ * pos.w is the mass, vel.w is carried through unchanged.
+ *
+ * Update rule (bodysystem_kernel.cu:109-136, bodysystem.cc:135-182):
+ *   a_i = sum_j m_j r_ij / (|r_ij|^2 + eps2)^(3/2),  r_ij = x_j - x_i
+ *   v_i <- (v_i + (a_i * k_i) * dt) * damping
+ *   x_i <- x_i + v_i * dt
+ * with all a_i taken from the old positions.  k_i is pos.w of body i in
+ * NB_KICK_REFERENCE mode (what the reference computes) and the constant G in
+ * NB_KICK_PHYSICAL mode.
+ *
+ * Errors: every call returns an nb_status; nb_last_error() gives the message
+ * of the last failure on the calling thread.  No call resets the device or
+ * exits the process (the reference prints and calls cudaDeviceReset,
+ * UTC/include/gpu/helper_cuda.h:419-442; that is deliberately not kept).
+ *
+ * Streams are passed as void* holding a cudaStream_t (NULL = legacy default
+ * stream).  A context is used by one host thread at a time.
+ */
+#ifndef NBODY_GB300_H_
+#define NBODY_GB300_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NB_ABI_VERSION 1
+
+typedef enum {
+    NB_OK = 0,
+    NB_ERR_INVALID = 1,     /* bad argument */
+    NB_ERR_CUDA = 2,        /* a CUDA runtime call or launch failed */
+    NB_ERR_OOM = 3,         /* device or pinned allocation failed */
+    NB_ERR_STATE = 4,       /* call out of order (e.g. step before set_state) */
+    NB_ERR_UNSUPPORTED = 5, /* combination not provided */
+    NB_ERR_TIMEOUT = 6      /* a bounded device-side wait ran out */
+} nb_status;
+
+/* State type and arithmetic of a context. */
+typedef enum {
+    NB_F32 = 0,      /* float state (float4 pos/vel), float arithmetic */
+    NB_F64 = 1,      /* double state (double4 pos/vel), double arithmetic */
+    NB_F32_COMP = 2  /* double positions, float pair forces with compensated
+                        (two-sum) accumulation; host buffers are double4 */
+} nb_precision;
+
+/* Force algorithm. */
+typedef enum {
+    /* Stream-K tiled kernel: packed f32x2 FMA, rsqrt.approx, deterministic
+     * partial sums.  NB_F32 only. */
+    NB_ALGO_FAST = 0,
+    /* IEEE arithmetic in the reference's operation order, sources summed in
+     * index order: bit-identical to the reference's sequential BodySystem<T>
+     * for float and double. */
+    NB_ALGO_EXACT = 1
+} nb_algo;
+
+typedef enum { NB_KICK_REFERENCE = 0, NB_KICK_PHYSICAL = 1 } nb_kick;
+
+/* Where host-visible buffers passed to set/get live. */
+typedef enum { NB_HOST = 0, NB_DEVICE = 1 } nb_where;
+
+/* Device memory kind of the context's state buffers, mirroring the
+ * reference's MemType (UTC/include/gpu/GpuData.h:17-22) for the host side. */
+typedef enum { NB_MEM_PAGEABLE = 0, NB_MEM_PINNED = 1, NB_MEM_UNIFIED = 2 } nb_memtype;
+
+typedef struct nb_params {
+    int n;            /* bodies, >= 0 */
+    int precision;    /* nb_precision */
+    int algo;         /* nb_algo */
+    int kick;         /* nb_kick */
+    double eps2;      /* softening squared, as BodySystemSGPU::initImpl takes it */
+    double damping;
+    double dt;
+    double G;         /* used in NB_KICK_PHYSICAL mode */
+    int block;        /* fast kernel threads per CTA (0 = tuned/auto) */
+    int bpt;          /* fast kernel bodies per thread (0 = tuned/auto) */
+    int ctas_per_sm;  /* fast kernel persistent CTAs per SM (0 = occupancy) */
+    int memtype;      /* nb_memtype, for nb_run_host staging */
+    int reserved[4];
+} nb_params;
+
+typedef struct nb_ctx nb_ctx;
+
+/* Fill *p with defaults (F32, FAST, reference kick, eps2 0.00125,
+ * damping 0.995 as BodySystem's constructor, bodysystem.cc:13-25). */
+void nb_params_default(nb_params *p);
+
+/* Create a context on the current CUDA device; allocates its state and
+ * scratch buffers.  Replaces the GpuData allocations of
+ * body_task_sgpu.cu:55-58. */
+int nb_create(const nb_params *p, nb_ctx **out);
+int nb_destroy(nb_ctx *ctx);
+
+/* Load / read back the state.  pos and vel hold 4*n values of the state type
+ * (double4 for NB_F32_COMP).  where = NB_HOST or NB_DEVICE.  Replaces
+ * GpuData::sync / fetch (UTC/include/gpu/GpuData.h:31-354). */
+int nb_set_state(nb_ctx *ctx, const void *pos, const void *vel, int where, void *stream);
+int nb_get_state(nb_ctx *ctx, void *pos, void *vel, int where, void *stream);
+
+/* Advance `steps` steps on `stream` (asynchronous).  Replaces the launch
+ * loop of BodySystemSGPU::runImpl, body_task_sgpu.cu:85-127. */
+int nb_step(nb_ctx *ctx, int steps, void *stream);
+
+/* nb_step with a CUDA event pair around every kernel it launches, on the
+ * same stream.  Adds the summed device milliseconds of the force kernel and
+ * of the reduce/integrate kernel to *ms_force and *ms_integrate (the exact
+ * algorithm's single fused kernel counts as force).  Synchronises `stream`. */
+int nb_step_timed(nb_ctx *ctx, int steps, float *ms_force, float *ms_integrate, void *stream);
+
+/* Bare accelerations a_i (no kick factor) of the current state into a device
+ * buffer of n 4-vectors of the state type (w = 0). */
+int nb_accel(nb_ctx *ctx, void *acc_dev, void *stream);
+
+/* The whole task run with host buffers, as BodySystemSGPU::runImpl
+ * (body_task_sgpu.cu:40-137): copy pos/vel in, run `loops` steps, and after
+ * every out_interval-th step copy the positions to
+ * outbuffer + (step/out_interval - 1) * 4n.  pos/vel are not modified.
+ * timings (may be NULL) receives {total, kernel, copyin, copyout} seconds,
+ * the reference's runtime[4].  Synchronises `stream` before returning. */
+int nb_run_host(nb_ctx *ctx, const void *pos, const void *vel, int loops,
+                int out_interval, void *outbuffer, double *timings, void *stream);
+
+/* Device pointers of the current state (valid until the next nb_step). */
+int nb_state_ptrs(nb_ctx *ctx, void **pos_dev, void **vel_dev);
+
+/* Resolved launch shape of the fast kernel: {block, bpt, grid, target
+ * block size, slots}. */
+int nb_plan_info(nb_ctx *ctx, int *info5);
+
+/* Number of kernels nb_step launches per step for this context. */
+int nb_launches_per_step(nb_ctx *ctx);
+
+/* Peak FP32 FMA throughput probe: runs a kernel of independent packed-FMA
+ * chains on all SMs for `iters` iterations; *flops receives the FP32
+ * operations issued (2 per lane-FMA) and *ms the device time. */
+int nb_probe_fma_peak(int iters, int packed, double *flops, float *ms, void *stream);
+
+const char *nb_last_error(void);
+int nb_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

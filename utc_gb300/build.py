@@ -1,0 +1,113 @@
+"""In-tree build of the GB300 nbody library and its C++ drop-in task.
+
+Produces, next to this file:
+  libnbody_gb300.so  -- the CUDA kernels behind the C ABI (include/nbody_gb300.h)
+  libnbody_task.so   -- BodySystemGB300<T> (the UTC-task drop-in) + Task stand-in
+  nbody_main         -- the app driver with the reference's flags
+
+Every .cu file is compiled for sm_103a only, in parallel, then linked.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+TASK = os.path.join(PKG, "task")
+INCLUDE = os.path.join(REPO, "include")
+BUILD_DIR = os.path.join(REPO, "_build")
+
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v",
+              "--expt-relaxed-constexpr"]
+
+LIB = os.path.join(PKG, "libnbody_gb300.so")
+TASK_LIB = os.path.join(PKG, "libnbody_task.so")
+MAIN_BIN = os.path.join(PKG, "nbody_main")
+
+
+def cuda_home() -> str:
+    for cand in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if cand and os.path.exists(os.path.join(cand, "bin", "nvcc")):
+            return cand
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    raise RuntimeError("nvcc not found (set CUDA_HOME)")
+
+
+def _run(cmd, log):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    with open(log, "w") as f:
+        f.write(" ".join(cmd) + "\n" + r.stdout)
+    if r.returncode != 0:
+        raise RuntimeError(f"build step failed ({r.returncode}): {' '.join(cmd)}\n{r.stdout[-4000:]}")
+    return r.stdout
+
+
+def _newer(target, sources):
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(s) <= t for s in sources)
+
+
+def build(force: bool = False, verbose: bool = False) -> None:
+    home = cuda_home()
+    nvcc = os.path.join(home, "bin", "nvcc")
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    cus = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    objs = []
+    jobs = []
+    for cu in cus:
+        obj = os.path.join(BUILD_DIR, os.path.basename(cu) + ".o")
+        objs.append(obj)
+        if force or not _newer(obj, [cu] + headers):
+            cmd = [nvcc] + ARCH_FLAGS + NVCC_FLAGS + ["-I", INCLUDE, "-I", CSRC, "-c", cu, "-o", obj]
+            jobs.append((cmd, obj + ".log"))
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        outs = list(ex.map(lambda j: _run(*j), jobs))
+    if verbose:
+        for o in outs:
+            sys.stdout.write(o)
+    if force or jobs or not os.path.exists(LIB):
+        _run([nvcc] + ARCH_FLAGS + ["-shared", "-o", LIB] + objs + ["-lcuda"],
+             os.path.join(BUILD_DIR, "link.log"))
+
+    # C++ drop-in task + stand-in runtime + app driver (host code only)
+    task_srcs = [os.path.join(TASK, "body_task_gb300.cc")]
+    task_hdrs = glob.glob(os.path.join(TASK, "*.h")) + [os.path.join(INCLUDE, "nbody_gb300.h")]
+    cxx = os.environ.get("CXX", "g++")
+    common = ["-std=c++17", "-O2", "-fPIC", "-I", INCLUDE, "-I", TASK,
+              "-I", os.path.join(home, "include")]
+    libs = ["-L", PKG, "-lnbody_gb300", "-Wl,-rpath,$ORIGIN",
+            "-L", os.path.join(home, "lib64"), "-lcudart_static", "-ldl", "-lrt", "-lpthread"]
+    if force or not _newer(TASK_LIB, task_srcs + task_hdrs + [LIB]):
+        _run([cxx] + common + ["-shared", "-o", TASK_LIB] + task_srcs + libs,
+             os.path.join(BUILD_DIR, "task.log"))
+    main_src = os.path.join(TASK, "nbody_main.cc")
+    if force or not _newer(MAIN_BIN, [main_src] + task_hdrs + [TASK_LIB]):
+        _run([cxx] + common + ["-o", MAIN_BIN, main_src, "-L", PKG, "-lnbody_task"] + libs,
+             os.path.join(BUILD_DIR, "main.log"))
+
+
+def ptxas_report() -> str:
+    """Registers / spills / shared memory per kernel from the last build."""
+    out = []
+    for log in sorted(glob.glob(os.path.join(BUILD_DIR, "*.cu.o.log"))):
+        for line in open(log):
+            if "ptxas info" in line and ("Used" in line or "Compiling entry" in line) or "spill" in line:
+                out.append(line.rstrip())
+    return "\n".join(out)
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose="-v" in sys.argv)
+    print(ptxas_report())

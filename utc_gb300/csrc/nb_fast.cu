@@ -1,0 +1,306 @@
+// nb_fast.cu -- fast FP32 all-pairs force kernel for sm_103a.
+//
+// Replaces the reference's _computeNBodyForce_kernel / _integrateNBodySystem_
+// kernel pair (benchapps/nbody/cuda/bodysystem_kernel.cu:60-138), which gives
+// each thread one target, stages sources as four scalar loads per thread into
+// __shared__ T[4][512] and runs one fused launch of N/256 CTAs per step.
+//
+// Design here (one GB300, compute-bound on the FP32 pipe):
+//  * Each thread owns 2*NPAIR targets held as packed pairs, so that every
+//    pair-term operation is one sm_100+ f32x2 instruction (FADD2/FMUL2/FFMA2)
+//    doing two targets' work: per interaction 12 FP32 lane-operations and
+//    one MUFU.RSQ, issued in 6 packed instructions plus the MUFU.
+//  * Sources are staged through shared memory with each component stored
+//    twice, (x, x, y, y) and (z, z, m, m), so one LDS.128 broadcast yields the
+//    two packed operands a source contributes to a target pair.  The next
+//    tile is prefetched into registers while the current one is consumed.
+//  * Work is split stream-K style: the (target block, 32-source group)
+//    iteration space is cut into `grid` equal contiguous ranges, one per
+//    persistent CTA, so all SMs finish together at any N (no wave
+//    quantisation).  A CTA writes one partial acceleration per target block
+//    it touches; a second, bandwidth-bound kernel sums the partials of each
+//    target in CTA order (deterministic) and applies the kick/drift update.
+#include <algorithm>
+
+#include "nb_internal.cuh"
+
+namespace nb {
+
+template <int NT, int NPAIR>
+__global__ void __launch_bounds__(NT) sk_force_kernel(const float4 *__restrict__ pos, int n,
+                                                      float eps2, float4 *__restrict__ partial,
+                                                      long long total, int ngroups)
+{
+    constexpr int TB = NT * 2 * NPAIR;
+    __shared__ __align__(16) float4 sA[NT];  // (x, x, y, y)
+    __shared__ __align__(16) float4 sB[NT];  // (z, z, m, m)
+    const int t = threadIdx.x;
+    const int c = blockIdx.x;
+    long long it = sk_start(c, total, gridDim.x);
+    const long long end = sk_start(c + 1, total, gridDim.x);
+    const f2 EPS2 = f2_pack(eps2, eps2);
+    const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
+
+    while (it < end) {
+        const int tb = (int)(it / ngroups);
+        const long long tb_first = (long long)tb * ngroups;
+        const long long seg_end = end < tb_first + ngroups ? end : tb_first + ngroups;
+        const int j0 = (int)(it - tb_first) * kGroup;
+        const int j1 = min((int)(seg_end - tb_first) * kGroup, n);
+
+        f2 PX[NPAIR], PY[NPAIR], PZ[NPAIR], AX[NPAIR], AY[NPAIR], AZ[NPAIR];
+#pragma unroll
+        for (int p = 0; p < NPAIR; ++p) {
+            const int i0 = tb * TB + t + (2 * p) * NT;
+            const int i1 = i0 + NT;
+            const float4 q0 = i0 < n ? pos[i0] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 q1 = i1 < n ? pos[i1] : make_float4(0.f, 0.f, 0.f, 0.f);
+            PX[p] = f2_pack(q0.x, q1.x);
+            PY[p] = f2_pack(q0.y, q1.y);
+            PZ[p] = f2_pack(q0.z, q1.z);
+            AX[p] = f2_pack(0.f, 0.f);
+            AY[p] = AX[p];
+            AZ[p] = AX[p];
+        }
+
+        float4 nxt = (j0 + t < j1) ? pos[j0 + t] : pad;
+        for (int jt = j0; jt < j1; jt += NT) {
+            __syncthreads();  // the previous tile has been consumed by all warps
+            sA[t] = make_float4(nxt.x, nxt.x, nxt.y, nxt.y);
+            sB[t] = make_float4(nxt.z, nxt.z, nxt.w, nxt.w);
+            __syncthreads();
+            if (jt + NT < j1) {
+                const int jn = jt + NT + t;
+                nxt = jn < j1 ? pos[jn] : pad;
+            }
+            const int cnt = min(NT, j1 - jt);
+            const int cnt4 = (cnt + 3) & ~3;  // entries past cnt are zero-mass pads
+            for (int j = 0; j < cnt4; j += 4) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float4 a = sA[j + u];
+                    const float4 b = sB[j + u];
+                    const f2 X2 = f2_pack(a.x, a.y), Y2 = f2_pack(a.z, a.w);
+                    const f2 Z2 = f2_pack(b.x, b.y), M2 = f2_pack(b.z, b.w);
+#pragma unroll
+                    for (int p = 0; p < NPAIR; ++p) {
+                        const f2 rx = f2_sub(X2, PX[p]);
+                        const f2 ry = f2_sub(Y2, PY[p]);
+                        const f2 rz = f2_sub(Z2, PZ[p]);
+                        f2 d2 = f2_fma(rx, rx, EPS2);
+                        d2 = f2_fma(ry, ry, d2);
+                        d2 = f2_fma(rz, rz, d2);
+                        float dlo, dhi;
+                        f2_unpack(d2, dlo, dhi);
+                        const f2 inv = f2_pack(rsqrt_approx(dlo), rsqrt_approx(dhi));
+                        const f2 inv2 = f2_mul(inv, inv);
+                        const f2 s = f2_mul(f2_mul(M2, inv), inv2);
+                        AX[p] = f2_fma(rx, s, AX[p]);
+                        AY[p] = f2_fma(ry, s, AY[p]);
+                        AZ[p] = f2_fma(rz, s, AZ[p]);
+                    }
+                }
+            }
+        }
+
+        float4 *dst = partial + (size_t)(c + tb) * TB;
+#pragma unroll
+        for (int p = 0; p < NPAIR; ++p) {
+            float ax0, ax1, ay0, ay1, az0, az1;
+            f2_unpack(AX[p], ax0, ax1);
+            f2_unpack(AY[p], ay0, ay1);
+            f2_unpack(AZ[p], az0, az1);
+            dst[t + (2 * p) * NT] = make_float4(ax0, ay0, az0, 0.f);
+            dst[t + (2 * p + 1) * NT] = make_float4(ax1, ay1, az1, 0.f);
+        }
+        it = seg_end;
+    }
+}
+
+// Sum the partial slots of each target in CTA order, then the reference's
+// kick / damping / drift with unfused IEEE operations in its order
+// (bodysystem_kernel.cu:115-126).
+__global__ void sk_integrate_kernel(const float4 *__restrict__ pos_old, float4 *__restrict__ pos_new,
+                                    float4 *__restrict__ vel, const float4 *__restrict__ partial,
+                                    int n, int tbsize, long long total, int ngroups, int grid,
+                                    float damping, float dt, int kick, float G,
+                                    float4 *__restrict__ acc_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int tb = i / tbsize;
+    const int li = i - tb * tbsize;
+    const long long first = (long long)tb * ngroups;
+    const int c0 = sk_owner(first, total, grid);
+    const int c1 = sk_owner(first + ngroups - 1, total, grid);
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    for (int c = c0; c <= c1; ++c) {
+        const float4 q = partial[(size_t)(c + tb) * tbsize + li];
+        ax = __fadd_rn(ax, q.x);
+        ay = __fadd_rn(ay, q.y);
+        az = __fadd_rn(az, q.z);
+    }
+    if (acc_out) {
+        acc_out[i] = make_float4(ax, ay, az, 0.f);
+        return;
+    }
+    float4 p = pos_old[i];
+    float4 v = vel[i];
+    const float k = kick == NB_KICK_REFERENCE ? p.w : G;
+    v.x = __fadd_rn(v.x, __fmul_rn(__fmul_rn(ax, k), dt));
+    v.y = __fadd_rn(v.y, __fmul_rn(__fmul_rn(ay, k), dt));
+    v.z = __fadd_rn(v.z, __fmul_rn(__fmul_rn(az, k), dt));
+    v.x = __fmul_rn(v.x, damping);
+    v.y = __fmul_rn(v.y, damping);
+    v.z = __fmul_rn(v.z, damping);
+    p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
+    p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+    p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+    pos_new[i] = p;
+    vel[i] = v;
+}
+
+// ---------------------------------------------------------------------------
+// dispatch over the compiled (threads per CTA, target pairs per thread) shapes
+// ---------------------------------------------------------------------------
+typedef void (*sk_kernel_t)(const float4 *, int, float, float4 *, long long, int);
+
+static sk_kernel_t sk_kernel_for(int block, int npair)
+{
+    if (block == 128) {
+        if (npair == 1) return sk_force_kernel<128, 1>;
+        if (npair == 2) return sk_force_kernel<128, 2>;
+        if (npair == 4) return sk_force_kernel<128, 4>;
+    } else if (block == 256) {
+        if (npair == 1) return sk_force_kernel<256, 1>;
+        if (npair == 2) return sk_force_kernel<256, 2>;
+        if (npair == 4) return sk_force_kernel<256, 4>;
+    }
+    return nullptr;
+}
+
+int fast_plan(int n, int block, int bpt, int ctas_per_sm, int device, SkPlan *pl)
+{
+    if (n < 0) return set_error(NB_ERR_INVALID, "n must be >= 0");
+    if (block == 0 || bpt == 0) {
+        // default shape: wide blocks for large N, finer granularity below
+        if (block == 0) block = n >= 32768 ? 256 : 128;
+        if (bpt == 0) bpt = n >= 8192 ? 8 : (n >= 2048 ? 4 : 2);
+    }
+    if (bpt % 2 != 0) return set_error(NB_ERR_INVALID, "bodies per thread must be 2, 4 or 8");
+    sk_kernel_t k = sk_kernel_for(block, bpt / 2);
+    if (!k) return set_error(NB_ERR_UNSUPPORTED, "fast kernel shape (block, bodies per thread) not compiled");
+    SkPlan p;
+    p.n = n;
+    p.block = block;
+    p.npair = bpt / 2;
+    p.tbsize = block * bpt;
+    p.ntb = (n + p.tbsize - 1) / p.tbsize;
+    p.ngroups = (n + kGroup - 1) / kGroup;
+    p.total = (long long)p.ntb * p.ngroups;
+    int sms = 0, occ = 0;
+    NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, block, 0));
+    if (occ < 1) return set_error(NB_ERR_UNSUPPORTED, "fast kernel does not fit on an SM");
+    if (ctas_per_sm > 0 && ctas_per_sm < occ) occ = ctas_per_sm;
+    long long grid = (long long)sms * occ;
+    if (p.total > 0 && grid > p.total) grid = p.total;
+    p.grid = p.total > 0 ? (int)grid : 0;
+    p.slots = p.total > 0 ? p.grid + p.ntb - 1 : 0;
+    *pl = p;
+    return NB_OK;
+}
+
+int fast_force(const SkPlan &p, const float4 *pos, float eps2, float4 *partial, cudaStream_t s)
+{
+    if (p.total == 0) return NB_OK;
+    sk_kernel_t k = sk_kernel_for(p.block, p.npair);
+    if (!k) return set_error(NB_ERR_UNSUPPORTED, "fast kernel shape not compiled");
+    k<<<p.grid, p.block, 0, s>>>(pos, p.n, eps2, partial, p.total, p.ngroups);
+    NB_LAUNCH_CHECK("sk_force_kernel launch");
+    return NB_OK;
+}
+
+int fast_integrate(const SkPlan &p, const float4 *pos_old, float4 *pos_new, float4 *vel,
+                   const float4 *partial, float damping, float dt, int kick, float G,
+                   float4 *acc_out, cudaStream_t s)
+{
+    if (p.n == 0) return NB_OK;
+    const int bs = 256;
+    sk_integrate_kernel<<<(p.n + bs - 1) / bs, bs, 0, s>>>(pos_old, pos_new, vel, partial, p.n,
+                                                           p.tbsize, p.total, p.ngroups, p.grid,
+                                                           damping, dt, kick, G, acc_out);
+    NB_LAUNCH_CHECK("sk_integrate_kernel launch");
+    return NB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 FMA peak probe: independent FMA chains on every SM.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) probe_fma2_kernel(float *out, int iters)
+{
+    const float base = 1.0f + 1e-6f * (float)threadIdx.x;
+    f2 a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = f2_pack(base + k, base - k);
+    const f2 m = f2_pack(0.999999f, 0.999998f), c = f2_pack(1e-7f, 2e-7f);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = f2_fma(a[k], m, c);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        float lo, hi;
+        f2_unpack(a[k], lo, hi);
+        s += lo + hi;
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(256) probe_fma1_kernel(float *out, int iters)
+{
+    const float base = 1.0f + 1e-6f * (float)threadIdx.x;
+    float a[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) a[k] = base + k;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) a[k] = fmaf(a[k], 0.999999f, 1e-7f);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) s += a[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+int probe_fma(int iters, int packed, double *flops, float *ms, cudaStream_t s)
+{
+    if (iters <= 0 || !flops || !ms) return set_error(NB_ERR_INVALID, "probe_fma arguments");
+    int dev = 0, sms = 0, occ = 0;
+    NB_CUDA(cudaGetDevice(&dev));
+    NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    auto kern = packed ? probe_fma2_kernel : probe_fma1_kernel;
+    NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, 0));
+    const int grid = sms * std::max(occ, 1);
+    float *out = nullptr;
+    NB_CUDA(cudaMallocAsync((void **)&out, sizeof(float) * grid * 256, s));
+    cudaEvent_t e0, e1;
+    NB_CUDA(cudaEventCreate(&e0));
+    NB_CUDA(cudaEventCreate(&e1));
+    kern<<<grid, 256, 0, s>>>(out, 16);  // warm-up
+    NB_CUDA(cudaEventRecord(e0, s));
+    kern<<<grid, 256, 0, s>>>(out, iters);
+    NB_CUDA(cudaEventRecord(e1, s));
+    NB_CUDA(cudaEventSynchronize(e1));
+    NB_CUDA(cudaEventElapsedTime(ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    NB_CUDA(cudaFreeAsync(out, s));
+    NB_CUDA(cudaStreamSynchronize(s));
+    // 16 lane-FMAs per thread per iteration either way, 2 FLOP each
+    *flops = 2.0 * 16.0 * (double)iters * (double)grid * 256.0;
+    return NB_OK;
+}
+
+}  // namespace nb

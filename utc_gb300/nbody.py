@@ -1,0 +1,164 @@
+"""Python face of the C ABI: an NBodySystem owning one nb_ctx.
+
+State arrays are (n, 4): positions (x, y, z, m) and velocities
+(vx, vy, vz, w), float32 for precision "f32" and float64 for "f64", the
+layout of the reference's GpuData buffers (benchapps/nbody/utc/sgpu/
+body_task_sgpu.cu:55-58).  numpy arrays are host buffers; torch CUDA tensors
+are device buffers (used in place, no host round trip).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+_PREC = {"f32": N.NB_F32, "f64": N.NB_F64, "f32comp": N.NB_F32_COMP}
+_ALGO = {"fast": N.NB_ALGO_FAST, "exact": N.NB_ALGO_EXACT}
+_KICK = {"reference": N.NB_KICK_REFERENCE, "physical": N.NB_KICK_PHYSICAL}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def current_stream_handle():
+    """cudaStream_t of torch's current stream as an int (0 = legacy default)."""
+    torch = _torch()
+    if torch.cuda.is_available():
+        return int(torch.cuda.current_stream().cuda_stream)
+    return 0
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+class NBodySystem:
+    def __init__(self, n, precision="f32", algo="fast", kick="reference", eps2=0.00125,
+                 damping=0.995, dt=0.016, G=1.0, block=0, bpt=0, ctas_per_sm=0,
+                 memtype=N.NB_MEM_PAGEABLE):
+        self.lib = N.lib()
+        p = N.NbParams()
+        self.lib.nb_params_default(C.byref(p))
+        p.n = int(n)
+        p.precision = _PREC[precision]
+        p.algo = _ALGO[algo]
+        p.kick = _KICK[kick]
+        p.eps2, p.damping, p.dt, p.G = float(eps2), float(damping), float(dt), float(G)
+        p.block, p.bpt, p.ctas_per_sm, p.memtype = int(block), int(bpt), int(ctas_per_sm), int(memtype)
+        self.params = p
+        self.n = int(n)
+        self.dtype = np.float64 if precision == "f64" else np.float32
+        h = C.c_void_p()
+        N.check(self.lib.nb_create(C.byref(p), C.byref(h)), "nb_create")
+        self.handle = h
+
+    # ------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.nb_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------------------
+    def _buf(self, x):
+        if _is_torch(x):
+            assert x.is_cuda and x.is_contiguous() and x.shape == (self.n, 4)
+            return C.c_void_p(x.data_ptr()), N.NB_DEVICE, x
+        a = np.ascontiguousarray(x, dtype=self.dtype).reshape(self.n, 4)
+        return a.ctypes.data_as(C.c_void_p), N.NB_HOST, a
+
+    def set_state(self, pos, vel, stream=None):
+        pp, wp, keep_p = self._buf(pos)
+        vp, wv, keep_v = self._buf(vel)
+        assert wp == wv, "pos and vel must both be host or both be device buffers"
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_set_state(self.handle, pp, vp, wp, C.c_void_p(s)), "nb_set_state")
+        del keep_p, keep_v
+
+    def get_state(self, stream=None):
+        pos = np.empty((self.n, 4), self.dtype)
+        vel = np.empty((self.n, 4), self.dtype)
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_get_state(self.handle, pos.ctypes.data_as(C.c_void_p),
+                                      vel.ctypes.data_as(C.c_void_p), N.NB_HOST, C.c_void_p(s)),
+                "nb_get_state")
+        return pos, vel
+
+    def get_state_device(self, pos_t, vel_t, stream=None):
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_get_state(self.handle, C.c_void_p(pos_t.data_ptr()),
+                                      C.c_void_p(vel_t.data_ptr()), N.NB_DEVICE, C.c_void_p(s)),
+                "nb_get_state")
+
+    def step(self, steps=1, stream=None):
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_step(self.handle, int(steps), C.c_void_p(s)), "nb_step")
+
+    def step_timed(self, steps=1, stream=None):
+        """Step with per-kernel CUDA events; returns (force_ms, integrate_ms) summed."""
+        f, g = C.c_float(0.0), C.c_float(0.0)
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_step_timed(self.handle, int(steps), C.byref(f), C.byref(g), C.c_void_p(s)),
+                "nb_step_timed")
+        return f.value, g.value
+
+    def accel(self, stream=None):
+        """Bare accelerations of the current state, (n, 3) numpy."""
+        torch = _torch()
+        tdt = torch.float64 if self.dtype == np.float64 else torch.float32
+        out = torch.zeros((max(self.n, 1), 4), dtype=tdt, device="cuda")
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_accel(self.handle, C.c_void_p(out.data_ptr()), C.c_void_p(s)), "nb_accel")
+        torch.cuda.current_stream().synchronize()
+        return out[: self.n, :3].cpu().numpy()
+
+    def run_host(self, pos, vel, loops, out_interval, stream=None):
+        """Task-style run with host buffers; returns (frames (k, n, 4), timings[4])."""
+        pos = np.ascontiguousarray(pos, dtype=self.dtype)
+        vel = np.ascontiguousarray(vel, dtype=self.dtype)
+        k = loops // out_interval if out_interval > 0 else 0
+        out = np.zeros((max(k, 1), self.n, 4), self.dtype)
+        t = (C.c_double * 4)()
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_run_host(self.handle, pos.ctypes.data_as(C.c_void_p),
+                                     vel.ctypes.data_as(C.c_void_p), int(loops), int(out_interval),
+                                     out.ctypes.data_as(C.c_void_p), t, C.c_void_p(s)),
+                "nb_run_host")
+        return out[:k], list(t)
+
+    def state_ptrs(self):
+        p, v = C.c_void_p(), C.c_void_p()
+        N.check(self.lib.nb_state_ptrs(self.handle, C.byref(p), C.byref(v)), "nb_state_ptrs")
+        return p.value, v.value
+
+    def plan_info(self):
+        info = (C.c_int * 5)()
+        N.check(self.lib.nb_plan_info(self.handle, info), "nb_plan_info")
+        return dict(zip(["block", "bpt", "grid", "tbsize", "slots"], list(info)))
+
+    def launches_per_step(self):
+        return self.lib.nb_launches_per_step(self.handle)
+
+
+def probe_fma_peak(iters=20000, packed=True, stream=None):
+    """Measured FP32 FMA peak in FLOP/s on the current device."""
+    flops, ms = C.c_double(), C.c_float()
+    s = current_stream_handle() if stream is None else stream
+    N.check(N.lib().nb_probe_fma_peak(int(iters), int(bool(packed)), C.byref(flops), C.byref(ms),
+                                      C.c_void_p(s)), "nb_probe_fma_peak")
+    return flops.value / (ms.value * 1e-3), ms.value
