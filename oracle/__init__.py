@@ -22,6 +22,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_SEQ_DEFAULT = "/root/reference/utc-0.1/benchapps/nbody/seq"
+REF_CUDA_DEFAULT = "/root/reference/utc-0.1/benchapps/nbody/cuda"
+REF_CUBIN = os.path.join(HERE, "_ref", "ref_kernel_sm103a.cubin")
 
 KICK_REFERENCE = 0
 KICK_PHYSICAL = 1
@@ -41,8 +43,9 @@ def build(ref: bool | None = None) -> None:
     if ref is None:
         ref = os.path.isdir(os.environ.get("NB_REF_SEQ", REF_SEQ_DEFAULT))
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref",
-                        "REF_SEQ=" + os.environ.get("NB_REF_SEQ", REF_SEQ_DEFAULT)],
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "ref-gpu",
+                        "REF_SEQ=" + os.environ.get("NB_REF_SEQ", REF_SEQ_DEFAULT),
+                        "REF_CUDA=" + os.environ.get("NB_REF_CUDA", REF_CUDA_DEFAULT)],
                        check=True)
 
 
