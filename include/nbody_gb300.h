@@ -136,6 +136,22 @@ int nb_accel(nb_ctx *ctx, void *acc_dev, void *stream);
 int nb_run_host(nb_ctx *ctx, const void *pos, const void *vel, int loops,
                 int out_interval, void *outbuffer, double *timings, void *stream);
 
+/* One fast FP32 step (force + kick/drift, NB_ALGO_FAST arithmetic) that
+ * allocates nothing.  No counterpart in the reference: it exists for callers
+ * that cannot call cudaMalloc -- an application whose memory manager owns
+ * the GPU's memory and hands out sub-buffers itself, or a latency-critical
+ * loop that cannot take the device synchronisation cudaMalloc/cudaFree may
+ * cause.  The caller passes device buffers of n float4: pos_old (read),
+ * pos_new (written, distinct from pos_old) and vel (updated in place).
+ * The partial-force scratch is a 16 MiB array compiled into the library
+ * (present on every GPU that loads it until exit), which limits n to
+ * 262,144; larger n returns NB_ERR_INVALID.  The first call on a device
+ * looks up that array's device address, so make it before any stream
+ * capture on that device.  All calls share the array: calls whose kernels
+ * overlap on the GPU race and must be serialised. */
+int nb_step_f32_noalloc(const float *pos_old, float *pos_new, float *vel, int n, float eps2,
+                        float damping, float dt, int kick, float G, void *stream);
+
 /* Device pointers of the current state (valid until the next nb_step). */
 int nb_state_ptrs(nb_ctx *ctx, void **pos_dev, void **vel_dev);
 

@@ -54,6 +54,7 @@ def _declare(lib):
         "nb_step": (I, [vp, I, vp]),
         "nb_accel": (I, [vp, vp, vp]),
         "nb_step_timed": (I, [vp, I, P(C.c_float), P(C.c_float), vp]),
+        "nb_step_f32_noalloc": (I, [vp, vp, vp, I, C.c_float, C.c_float, C.c_float, I, C.c_float, vp]),
         "nb_run_host": (I, [vp, vp, vp, I, I, vp, P(D), vp]),
         "nb_state_ptrs": (I, [vp, P(vp), P(vp)]),
         "nb_plan_info": (I, [vp, P(I)]),

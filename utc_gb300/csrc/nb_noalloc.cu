@@ -1,0 +1,103 @@
+// nb_noalloc.cu -- one fast FP32 step that allocates no memory.
+//
+// Who needs it: some callers cannot call cudaMalloc.  A host application
+// whose memory manager reserves the GPU's memory up front and hands out
+// sub-buffers itself cannot have a library allocate behind its back (the
+// allocation fails, or it breaks the manager's accounting), and a
+// latency-critical loop cannot afford the device-wide synchronisation that
+// cudaMalloc and cudaFree may cause.  nb_step_f32_noalloc serves them: the
+// caller passes its own input and output buffers, and the partial-force
+// scratch the fast kernel needs lives in a fixed array compiled into this
+// library instead of memory obtained at run time.
+//
+// The array: kNoAllocScratchFloat4 float4 = 16 MiB, a file-scope __device__
+// array, so every GPU that loads this library holds it until the process
+// exits.  It bounds the system size: n <= kNoAllocMaxBodies = 262,144.
+//
+// Host code never hands the array's name to a kernel: on the host that name
+// is only a stand-in for the device symbol (using it as a pointer would fault,
+// or on a GPU that can reach host memory silently use the wrong memory).  The
+// first call on each device looks up the array's device address with
+// cudaGetSymbolAddress, with that device current, and caches it; that first
+// call should therefore come before any stream capture on that device.
+//
+// All calls share the one array and it keeps what the last call wrote.
+// Nothing in it has to start at zero: each call writes every scratch entry
+// it later reads.  Calls whose kernels overlap on the GPU (for example on two
+// streams at once) race on the array and corrupt each other's results;
+// serialise them.
+#include <mutex>
+
+#include "nb_internal.cuh"
+
+namespace {
+
+constexpr size_t kNoAllocScratchFloat4 = size_t(1) << 20;  // 16 MiB
+constexpr int kNoAllocMaxBodies = 262144;
+constexpr int kNoAllocBlock = 128;  // launch shape: 128 threads x 8 bodies
+constexpr int kNoAllocBpt = 8;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) float4 g_noalloc_scratch[kNoAllocScratchFloat4];
+
+std::mutex g_scratch_mu;
+float4 *g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once
+// per device, with that device current).
+int scratch_for_current_device(float4 **out)
+{
+    int dev = 0;
+    NB_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices)
+        return nb::set_error(NB_ERR_UNSUPPORTED, "nb_step_f32_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return nb::cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_scratch_ptr[dev] = static_cast<float4 *>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return NB_OK;
+}
+
+}  // namespace
+
+extern "C" int nb_step_f32_noalloc(const float *pos_old, float *pos_new, float *vel, int n,
+                                   float eps2, float damping, float dt, int kick, float G,
+                                   void *stream)
+{
+    if (n < 0 || n > kNoAllocMaxBodies)
+        return nb::set_error(NB_ERR_INVALID,
+                             "nb_step_f32_noalloc: n must be in [0, 262144] (the fixed 16 MiB "
+                             "scratch array holds the partial forces of at most 262,144 bodies)");
+    if (kick != NB_KICK_REFERENCE && kick != NB_KICK_PHYSICAL)
+        return nb::set_error(NB_ERR_INVALID, "nb_step_f32_noalloc: unknown kick mode");
+    if (n == 0) return NB_OK;
+    if (!pos_old || !pos_new || !vel)
+        return nb::set_error(NB_ERR_INVALID, "nb_step_f32_noalloc: NULL buffer");
+    if (pos_old == pos_new)
+        return nb::set_error(NB_ERR_INVALID, "nb_step_f32_noalloc: pos_old and pos_new must differ");
+    float4 *scratch = nullptr;
+    int st = scratch_for_current_device(&scratch);
+    if (st) return st;
+    int dev = 0;
+    NB_CUDA(cudaGetDevice(&dev));
+    nb::SkPlan plan;
+    st = nb::fast_plan(n, kNoAllocBlock, kNoAllocBpt, 0, dev, &plan);
+    if (st) return st;
+    // keep slots * tbsize within the array: fewer persistent CTAs if needed
+    const long long max_slots = (long long)(kNoAllocScratchFloat4 / (size_t)plan.tbsize);
+    if (plan.ntb > max_slots)
+        return nb::set_error(NB_ERR_INVALID, "nb_step_f32_noalloc: system too large for the scratch array");
+    const long long grid_cap = max_slots - plan.ntb + 1;
+    if (plan.grid > grid_cap) plan.grid = (int)grid_cap;
+    plan.slots = plan.grid + plan.ntb - 1;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    st = nb::fast_force(plan, reinterpret_cast<const float4 *>(pos_old), eps2, scratch, s);
+    if (st) return st;
+    return nb::fast_integrate(plan, reinterpret_cast<const float4 *>(pos_old),
+                              reinterpret_cast<float4 *>(pos_new), reinterpret_cast<float4 *>(vel),
+                              scratch, damping, dt, kick, G, nullptr, s);
+}
