@@ -11,6 +11,19 @@ interaction (benchapps/nbody/seq/bodysystem.h:75-95).
 
 Under torchrun each rank runs an independent replica of the workload
 (weak scaling, no data-path collective); rank 0 prints one JSON line.
+
+Extension workloads, one JSON line each (not the headline):
+  --workload precision  N=1,048,576 Plummer, 20 steps of dt=1e-4, plain FP32
+                        vs compensated FP32 + FP64 positions: per-step force
+                        and energy error against the FP64 oracle on a
+                        4096-body subsample; forward throughput at N=1M
+  --workload adjoint    N=16384 uniform cube, 200 steps, checkpoints every 20:
+                        adjoint/forward time ratio; gradient error against the
+                        FP64 reference adjoint (full size) and FP64 central
+                        differences (64 coordinates, N=2048 replica)
+  --workload batched    512 Plummer systems, N log-uniform in [128, 16384],
+                        eps2=1e-3, dt=1e-3, 50 steps: autotuned persistent
+                        launch in a CUDA graph vs per-system launches
 """
 from __future__ import annotations
 
@@ -350,6 +363,228 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# extension workloads
+# ---------------------------------------------------------------------------
+def _body_rel(got, want):
+    d = np.linalg.norm(np.asarray(got, np.float64) - want, axis=1)
+    w = np.linalg.norm(want, axis=1)
+    return d / np.maximum(w, 1e-300)
+
+
+def run_precision(args):
+    import torch
+
+    import oracle
+    from utc_gb300 import ics
+    from utc_gb300.nbody import NBodySystem, probe_fma_peak
+
+    n = args.n or 1048576
+    steps = args.steps if args.steps_given else 20
+    eps2, dt = 1e-4, 1e-4
+    p64, v64 = ics.plummer(n, seed=0)
+    tidx = np.sort(np.random.default_rng(7).choice(n, min(4096, n), replace=False)).astype(np.int32)
+    out = {"workload": "precision", "n": n, "steps": steps, "eps2": eps2, "dt": dt,
+           "subsample": int(tidx.size), "modes": {}}
+    for mode in ("f32", "f32comp"):
+        sysm = NBodySystem(n, mode, "fast", kick="physical", eps2=np.float32(eps2), damping=1.0,
+                           dt=np.float32(dt))
+        if mode == "f32":
+            sysm.set_state(ics.f32(p64), ics.f32(v64))
+        else:
+            sysm.set_state(p64, v64)
+        per_step = []
+        force_ms = 0.0
+        E0 = None
+        for t in range(steps + 1):
+            e, bodies = sysm.energy(with_bodies=True)
+            pos, vel = sysm.get_state()
+            # FP64 forces at the state the GPU holds (float positions in plain
+            # mode, FP64 absolute positions in the compensated mode)
+            ref_a, ref_phi = oracle.accel_phi_subset_f64(np.asarray(pos, np.float64), tidx, eps2)
+            fa = _body_rel(bodies[tidx, :3], ref_a)
+            fp = np.abs(bodies[tidx, 3].astype(np.float64) - ref_phi) / np.abs(ref_phi)
+            E = e[0] + e[1]
+            E0 = E if E0 is None else E0
+            per_step.append({"t": t, "force_rel_median": float(np.median(fa)),
+                             "force_rel_p99": float(np.quantile(fa, 0.99)),
+                             "force_rel_max": float(fa.max()),
+                             "phi_rel_max": float(fp.max()),
+                             "energy": float(E), "energy_drift": float((E - E0) / abs(E0))})
+            if t < steps:
+                f, g = sysm.step_timed(1)
+                force_ms += f
+        rate = float(n) ** 2 * steps / (force_ms * 1e-3) / 1e9
+        out["modes"][mode] = {
+            "force_kernel_G_interactions_per_s": rate,
+            "force_rel_max_over_steps": max(r["force_rel_max"] for r in per_step),
+            "force_rel_median_over_steps": float(np.median([r["force_rel_median"] for r in per_step])),
+            "phi_rel_max_over_steps": max(r["phi_rel_max"] for r in per_step),
+            "energy_drift_final": per_step[-1]["energy_drift"],
+            "per_step": per_step,
+        }
+        sysm.close()
+    peak, _ = probe_fma_peak(20000, True)
+    r = out["modes"]["f32"]["force_kernel_G_interactions_per_s"]
+    out["forward_N1M"] = {"G_interactions_per_s": r, "tflops_20flop": r * 20 / 1e3,
+                          "fp32_peak_tflops_probe": peak / 1e12,
+                          "frac_of_fp32_peak": r * 20e9 / peak}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_adjoint(args):
+    import torch
+
+    import oracle
+    from utc_gb300 import ics
+    from utc_gb300.nbody import NBodySystem
+
+    n = args.n or 16384
+    T, K = 200, 20
+    eps2, dt = np.float32(1e-2), np.float32(1e-3)
+    p64, v64 = ics.uniform_cube(n, seed=0)
+    y = ics.gaussian_targets(n, seed=1, sigma=0.5)
+    p32, v32 = ics.f32(p64), ics.f32(v64)
+    yt = torch.tensor(y, dtype=torch.float32, device="cuda")
+    sysm = NBodySystem(n, "f32", "fast", kick="physical", eps2=eps2, damping=1.0, dt=dt)
+    stream = torch.cuda.current_stream()
+    pT = torch.empty((n, 4), device="cuda")
+    vT = torch.empty((n, 4), device="cuda")
+    for _ in range(args.warmup):
+        sysm.set_state(p32, v32)
+        sysm.adj_forward(T, K)
+        sysm.get_state_device(pT, vT)
+        gw = torch.zeros((n, 4), device="cuda")
+        sysm.adj_backward(gw)
+    torch.cuda.synchronize()
+    # time the three phases separately (median of the repetitions)
+    def timed(fn):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+    ts = {"forward": [], "adj_forward": [], "adj_backward": []}
+    for _ in range(max(args.steps, 3)):
+        sysm.set_state(p32, v32)
+        ts["forward"].append(timed(lambda: sysm.step(T)))
+        sysm.set_state(p32, v32)
+        ts["adj_forward"].append(timed(lambda: sysm.adj_forward(T, K)))
+        sysm.get_state_device(pT, vT)
+        gx = torch.zeros((n, 4), device="cuda")
+        gx[:, :3] = 2.0 * (pT[:, :3] - yt)
+        res = {}
+        ts["adj_backward"].append(timed(lambda: res.update(g=sysm.adj_backward(gx))))
+    med = {k: float(np.median(v)) for k, v in ts.items()}
+    gx0, gv0, gm = [t.cpu().numpy() for t in res["g"]]
+    out = {"workload": "adjoint", "n": n, "steps": T, "ckpt_every": K, "eps2": float(eps2),
+           "dt": float(dt), "kick": "physical (G=1)", "ms_median": med,
+           "adjoint_over_forward": med["adj_backward"] / med["forward"],
+           "adjoint_incl_ckpt_forward_over_forward": (med["adj_backward"] + med["adj_forward"]) / med["forward"]}
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        L, rx, rv, rm = oracle.adjoint(p32.astype(np.float64), v32.astype(np.float64), y, float(eps2),
+                                       1.0, float(dt), T, kick_mode=oracle.KICK_PHYSICAL)
+        def rel(a, b):
+            return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+        out["vs_fp64_reference_adjoint"] = {"dx0": rel(gx0[:, :3], rx), "dv0": rel(gv0[:, :3], rv),
+                                            "dm": rel(gm, rm), "cpu_s": time.perf_counter() - t0}
+        # FP64 central differences on 64 coordinates, on an N=2048 replica
+        nf = 2048
+        pf, vf = ics.uniform_cube(nf, seed=3)
+        yf = ics.gaussian_targets(nf, seed=4, sigma=0.5)
+        pf32, vf32 = ics.f32(pf), ics.f32(vf)
+        with NBodySystem(nf, "f32", "fast", kick="physical", eps2=eps2, damping=1.0, dt=dt) as s2:
+            s2.set_state(pf32, vf32)
+            s2.adj_forward(T, K)
+            q, _ = s2.get_state()
+            g2 = torch.zeros((nf, 4), device="cuda")
+            g2[:, :3] = torch.tensor(2.0 * (q[:, :3].astype(np.float64) - yf), dtype=torch.float32, device="cuda")
+            ax, av, am = [t.cpu().numpy() for t in s2.adj_backward(g2)]
+        rng = np.random.default_rng(5)
+        base_p, base_v = pf32.astype(np.float64), vf32.astype(np.float64)
+        errs, h = [], 1e-6
+        for _ in range(64):
+            which, i, d = int(rng.integers(0, 3)), int(rng.integers(0, nf)), int(rng.integers(0, 3))
+            arr_p, arr_v = base_p.copy(), base_v.copy()
+            arr, col = {0: (arr_p, d), 1: (arr_v, d), 2: (arr_p, 3)}[which]
+            arr[i, col] += h
+            lp = oracle.loss(arr_p, arr_v, yf, float(eps2), 1.0, float(dt), T)
+            arr[i, col] -= 2 * h
+            lm = oracle.loss(arr_p, arr_v, yf, float(eps2), 1.0, float(dt), T)
+            fd = (lp - lm) / (2 * h)
+            an = {0: ax[i, d], 1: av[i, d], 2: am[i]}[which]
+            errs.append(abs(an - fd) / max(abs(fd), 1e-12))
+        out["vs_fp64_central_differences"] = {"n": nf, "coords": 64, "h": h,
+                                              "rel_err_median": float(np.median(errs)),
+                                              "rel_err_max": float(np.max(errs))}
+    sysm.close()
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_batched(args):
+    import torch
+
+    from utc_gb300 import ics
+    from utc_gb300.nbody import NBodyBatch
+
+    sizes = ics.batch_sizes(512, lo=128, hi=16384, seed=0)
+    steps = 50
+    ps, vs = [], []
+    for k, nn in enumerate(sizes):
+        p, v = ics.plummer(int(nn), seed=1000 + k)
+        ps.append(ics.f32(p))
+        vs.append(ics.f32(v))
+    pos, vel = np.concatenate(ps), np.concatenate(vs)
+    pairs = float(np.sum(sizes.astype(np.float64) ** 2))
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    cache = os.path.join(REPO, "_build", "batch_autotune.txt")
+    os.makedirs(os.path.dirname(cache), exist_ok=True)
+    out = {"workload": "batched", "systems": int(sizes.size), "bodies": int(sizes.sum()),
+           "n_min": int(sizes.min()), "n_max": int(sizes.max()), "interactions_per_step": pairs,
+           "steps": steps, "eps2": 1e-3, "dt": 1e-3}
+    with torch.cuda.stream(stream), NBodyBatch(sizes, kick="physical", eps2=np.float32(1e-3),
+                                               dt=np.float32(1e-3)) as b:
+        b.set_state(pos, vel, stream=sh)
+        out["autotune"] = b.autotune(reps=2, cache_path=cache, stream=sh)
+        out["plan"] = b.plan_info()
+
+        def timed(fn, reps):
+            ts = []
+            for _ in range(reps):
+                b.set_state(pos, vel, stream=sh)
+                stream.synchronize()
+                a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                c.record(stream)
+                c.synchronize()
+                ts.append(a.elapsed_time(c))
+            return float(np.median(ts))
+
+        t_graph = timed(lambda: b.run(steps, sh), 1 + max(args.steps, 3))
+        pb, _ = b.get_state(stream=sh)
+        t_launch = timed(lambda: b.step(steps, sh), 3)
+        t_base = timed(lambda: b.step_per_system(steps, sh), 2)
+        pr, _ = b.get_state(stream=sh)
+    d = np.linalg.norm(pb[:, :3].astype(np.float64) - pr[:, :3], axis=1)
+    w = np.linalg.norm(pr[:, :3].astype(np.float64), axis=1)
+    out.update({
+        "ms_batched_graph": t_graph, "ms_batched_launches": t_launch, "ms_per_system_launches": t_base,
+        "speedup_vs_per_system": t_base / t_graph,
+        "G_interactions_per_s_batched": pairs * steps / (t_graph * 1e-3) / 1e9,
+        "G_interactions_per_s_per_system": pairs * steps / (t_base * 1e-3) / 1e9,
+        "final_pos_rel_diff_max_vs_per_system": float((d / (w + 0.1)).max()),
+    })
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -357,11 +592,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="plain", choices=["plain", "precision", "adjoint", "batched"])
+    ap.add_argument("--n", type=int, default=0, help="body count override for extension workloads")
     args = ap.parse_args()
+    args.steps_given = "--steps" in sys.argv
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.workload == "precision":
+        return run_precision(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_ours(args)
 
 

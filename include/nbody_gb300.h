@@ -127,6 +127,27 @@ int nb_step_timed(nb_ctx *ctx, int steps, float *ms_force, float *ms_integrate, 
  * buffer of n 4-vectors of the state type (w = 0). */
 int nb_accel(nb_ctx *ctx, void *acc_dev, void *stream);
 
+/* Total energy and momentum of the current state, reduced in FP64 on the
+ * GPU: out5 = {kinetic sum 0.5 m |v|^2, potential -0.5 G sum_i sum_{j!=i}
+ * m_i m_j / sqrt(r^2 + eps2), momentum x, y, z}.  The pair terms are FP32
+ * (compensated in NB_F32_COMP).  accphi_dev (may be NULL) receives per body
+ * the bare acceleration and, in w, the potential sum over j != i, as n
+ * float4 (NB_F32) or double4 (NB_F32_COMP).  Needs eps2 > 0.  Synchronises
+ * `stream`.  No counterpart in the reference (used by the precision study). */
+int nb_energy(nb_ctx *ctx, double *out5, void *accphi_dev, void *stream);
+
+/* Adjoint (reverse mode) of `steps` steps; no counterpart in the reference.
+ * nb_adj_forward advances the state like nb_step and keeps a checkpoint
+ * (positions and velocities) every ckpt_every steps.  nb_adj_backward then
+ * takes the cotangents of the final positions gx_T and velocities gv_T
+ * (device, n float4, xyz used; gv_T may be NULL for zero) and writes
+ * dL/dx0, dL/dv0 (device n float4, w = 0) and dL/dm (device n float),
+ * recomputing each segment's trajectory from its checkpoint.  NB_F32 fast
+ * contexts only; both kick modes. */
+int nb_adj_forward(nb_ctx *ctx, int steps, int ckpt_every, void *stream);
+int nb_adj_backward(nb_ctx *ctx, const void *gx_T, const void *gv_T, void *gx0, void *gv0,
+                    void *gm, void *stream);
+
 /* The whole task run with host buffers, as BodySystemSGPU::runImpl
  * (body_task_sgpu.cu:40-137): copy pos/vel in, run `loops` steps, and after
  * every out_interval-th step copy the positions to
@@ -151,6 +172,39 @@ int nb_run_host(nb_ctx *ctx, const void *pos, const void *vel, int loops,
  * overlap on the GPU race and must be serialised. */
 int nb_step_f32_noalloc(const float *pos_old, float *pos_new, float *vel, int n, float eps2,
                         float damping, float dt, int kick, float G, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Batches: many independent systems of uneven size advanced together, one
+ * persistent launch per step for all of them.  Replaces running one
+ * Task<BodySystemSGPU<T>> per system (benchapps/nbody/utc/nbody_mtask.cc:
+ * 199-231).  Bodies of all systems are concatenated float4 (system s after
+ * systems 0..s-1); all systems share eps2, damping, dt, G and kick mode from
+ * *p (p->n is ignored; p->block / p->bpt, when set, give the initial warps per
+ * CTA * 32 and bodies per lane).
+ * ---------------------------------------------------------------------- */
+typedef struct nb_batch nb_batch;
+int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **out);
+int nb_batch_destroy(nb_batch *b);
+int nb_batch_set_state(nb_batch *b, const void *pos, const void *vel, int where, void *stream);
+int nb_batch_get_state(nb_batch *b, void *pos, void *vel, int where, void *stream);
+/* `steps` steps, launched one by one. */
+int nb_batch_step(nb_batch *b, int steps, void *stream);
+/* `steps` steps as one CUDA graph (captured on first use for this step count
+ * and parity, replayed afterwards); `stream` must not be the legacy default
+ * stream. */
+int nb_batch_run(nb_batch *b, int steps, void *stream);
+/* Time every compiled launch shape on this batch and keep the fastest
+ * (state preserved); cache_path (may be NULL) is a text file of earlier
+ * choices keyed by device and size histogram.  chosen2 = {warps per CTA,
+ * bodies per lane}. */
+int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *stream, int *chosen2);
+int nb_batch_set_shape(nb_batch *b, int warps_per_cta, int bodies_per_lane);
+/* {warps per CTA, bodies per lane, grid, workers, iterations, slots} */
+int nb_batch_plan_info(nb_batch *b, long long *info6);
+int nb_batch_launches_per_step(nb_batch *b);
+/* Baseline: each system stepped by its own plain launches (force +
+ * integrate per system per step), as separate per-system tasks would. */
+int nb_batch_step_per_system(nb_batch *b, int steps, void *stream);
 
 /* Device pointers of the current state (valid until the next nb_step). */
 int nb_state_ptrs(nb_ctx *ctx, void **pos_dev, void **vel_dev);

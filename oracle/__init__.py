@@ -55,6 +55,7 @@ def _declare(lib):
         "orc_accel_f32": (I, [I, _f32p, F, _f32p, I]),
         "orc_accel_f64": (I, [I, _f64p, D, _f64p, I]),
         "orc_accel_subset_f64": (I, [I, _f64p, I, _i32p, D, _f64p, I]),
+        "orc_accel_phi_subset_f64": (I, [I, _f64p, I, _i32p, D, _f64p, _f64p, I]),
         "orc_step_f32": (I, [I, _f32p, _f32p, F, F, F, I, I, F, I]),
         "orc_step_f64": (I, [I, _f64p, _f64p, D, D, D, I, I, D, I]),
         "orc_energy_f64": (I, [I, _f64p, _f64p, D, D, _f64p, I]),
@@ -146,6 +147,18 @@ def accel_subset_f64(pos, tidx, eps2, nthreads=None):
                                       float(eps2), out.reshape(-1), nthreads or default_threads()),
            "accel_subset_f64")
     return out
+
+
+def accel_phi_subset_f64(pos, tidx, eps2, nthreads=None):
+    """FP64 (acc (nt,3), phi over j != i (nt,)) for targets tidx against all bodies."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    tidx = np.ascontiguousarray(tidx, dtype=np.int32)
+    acc = np.zeros((tidx.shape[0], 3), np.float64)
+    phi = np.zeros(tidx.shape[0], np.float64)
+    _check(lib().orc_accel_phi_subset_f64(pos.shape[0], pos.reshape(-1), tidx.shape[0], tidx,
+                                          float(eps2), acc.reshape(-1), phi,
+                                          nthreads or default_threads()), "accel_phi_subset_f64")
+    return acc, phi
 
 
 def step(pos, vel, eps2, damping, dt, steps, kick_mode=KICK_REFERENCE, G=1.0, nthreads=None):

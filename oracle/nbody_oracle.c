@@ -172,6 +172,52 @@ int orc_accel_subset_f64(int n, const double *pos, int nt, const int *tidx,
     return 0;
 }
 
+typedef struct {
+    int n;
+    const double *pos;
+    double eps2;
+    double *acc;
+    double *phi;
+    const int *tidx;
+} accphi_ctx;
+
+static void accphi_range(void *vp, int lo, int hi)
+{
+    accphi_ctx *c = (accphi_ctx *)vp;
+    for (int t = lo; t < hi; ++t) {
+        int i = c->tidx[t];
+        const double *pi = c->pos + 4 * (size_t)i;
+        double a[3] = {0.0, 0.0, 0.0}, ph = 0.0;
+        for (int j = 0; j < c->n; ++j) {
+            const double *pj = c->pos + 4 * (size_t)j;
+            double r0 = pj[0] - pi[0], r1 = pj[1] - pi[1], r2 = pj[2] - pi[2];
+            double d2 = r0 * r0 + r1 * r1 + r2 * r2 + c->eps2;
+            double inv = 1.0 / sqrt(d2);
+            double mi = pj[3] * inv;
+            double s = mi * inv * inv;
+            a[0] += r0 * s;
+            a[1] += r1 * s;
+            a[2] += r2 * s;
+            if (j != i) ph += mi;
+        }
+        c->acc[3 * (size_t)t + 0] = a[0];
+        c->acc[3 * (size_t)t + 1] = a[1];
+        c->acc[3 * (size_t)t + 2] = a[2];
+        c->phi[t] = ph;
+    }
+}
+
+int orc_accel_phi_subset_f64(int n, const double *pos, int nt, const int *tidx,
+                             double eps2, double *acc, double *phi, int nthreads)
+{
+    if (n < 0 || nt < 0 || (nt > 0 && (!pos || !acc || !phi || !tidx))) return 1;
+    for (int t = 0; t < nt; ++t)
+        if (tidx[t] < 0 || tidx[t] >= n) return 1;
+    accphi_ctx c = {n, pos, eps2, acc, phi, tidx};
+    parallel_for(nt, nthreads, accphi_range, &c);
+    return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* integrator (bodysystem.cc:135-182)                                  */
 /* ------------------------------------------------------------------ */

@@ -45,6 +45,11 @@ int orc_accel_f64(int n, const double *pos, double eps2, double *acc, int nthrea
 int orc_accel_subset_f64(int n, const double *pos, int nt, const int *tidx,
                          double eps2, double *acc, int nthreads);
 
+/* For targets tidx[0..nt): acceleration sum (as above, acc 3*nt) and the
+ * potential sum phi = sum_{j != i} m_j / sqrt(r^2 + eps2) (phi nt), double. */
+int orc_accel_phi_subset_f64(int n, const double *pos, int nt, const int *tidx,
+                             double eps2, double *acc, double *phi, int nthreads);
+
 /* `steps` calls of BodySystem<T>::update(dt): all forces from the old
  * positions, then kick (x kick factor), damping, drift.  pos/vel (4*n) are
  * updated in place; pos.w and vel.w pass through unchanged. */

@@ -1,0 +1,134 @@
+"""Batched systems: one persistent launch per step over many uneven systems.
+
+Checks: every system's accelerations (one step from zero velocity) against
+the FP64 oracle at the fast-path tolerance; the CUDA-graph run equals
+step-by-step launches bitwise; the per-system baseline equals independent
+NBodySystem contexts bitwise; every compiled launch shape and the autotuner
+(with its cache file) keep the results within tolerance.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from utc_gb300 import ics
+from utc_gb300.nbody import NBodySystem, NBodyBatch
+
+pytestmark = pytest.mark.gpu
+
+EPS2, DT = np.float32(1e-3), np.float32(1e-3)
+
+
+def make_batch(sizes, seed=0):
+    ps, vs = [], []
+    for k, n in enumerate(sizes):
+        p, v = ics.plummer(int(n), seed=seed + k)
+        ps.append(ics.f32(p))
+        vs.append(ics.f32(v))
+    return np.concatenate(ps), np.concatenate(vs)
+
+
+def per_system(arr, sizes):
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    return [arr[off[i]:off[i + 1]] for i in range(len(sizes))]
+
+
+SIZES = [1, 2, 31, 33, 128, 300, 1024, 5000, 77]
+
+
+@pytest.mark.parametrize("shape", [(2, 4), (2, 8), (4, 2), (4, 4), (4, 8), (8, 2), (8, 4), (8, 8)])
+def test_batch_accelerations_vs_oracle(cuda, shape):
+    pos, _ = make_batch(SIZES, seed=10)
+    vel = np.zeros_like(pos)
+    with NBodyBatch(SIZES, eps2=EPS2, dt=DT, warps_per_cta=shape[0], bodies_per_lane=shape[1]) as b:
+        assert b.plan_info()["warps_per_cta"] == shape[0]
+        b.set_state(pos, vel)
+        b.step(1)
+        _, v1 = b.get_state()
+    for p, v in zip(per_system(pos, SIZES), per_system(v1, SIZES)):
+        a = v[:, :3].astype(np.float64) / float(DT)
+        ref = oracle.accel(p.astype(np.float64), float(EPS2))
+        d = np.linalg.norm(a - ref, axis=1)
+        w = np.linalg.norm(ref, axis=1)
+        assert (d <= 2e-5 * (w + w.mean())).all()
+
+
+def test_graph_run_equals_step_launches(cuda):
+    import torch
+
+    sizes = ics.batch_sizes(40, lo=128, hi=2048, seed=3)
+    pos, vel = make_batch(sizes, seed=1)
+    stream = torch.cuda.Stream()
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b:
+        b.set_state(pos, vel)
+        b.step(7)
+        want = b.get_state()
+        with torch.cuda.stream(stream):
+            b.set_state(pos, vel, stream=stream.cuda_stream)
+            b.run(7, stream.cuda_stream)
+            stream.synchronize()
+            got = b.get_state(stream=stream.cuda_stream)
+            # second replay continues from the advanced state (odd step count)
+            b.run(7, stream.cuda_stream)
+            b.run(7, stream.cuda_stream)
+            stream.synchronize()
+        b.set_state(pos, vel)
+        b.step(21)
+        want3 = b.get_state()
+        with torch.cuda.stream(stream):
+            got3 = b.get_state(stream=stream.cuda_stream)
+    assert got[0].tobytes() == want[0].tobytes() and got[1].tobytes() == want[1].tobytes()
+    assert got3[0].tobytes() == want3[0].tobytes()
+
+
+def test_per_system_baseline_equals_independent_contexts(cuda):
+    sizes = [64, 1000, 3, 4096]
+    pos, vel = make_batch(sizes, seed=7)
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b:
+        b.set_state(pos, vel)
+        b.step_per_system(3)
+        got, _ = b.get_state()
+    for p, v, g in zip(per_system(pos, sizes), per_system(vel, sizes), per_system(got, sizes)):
+        with NBodySystem(p.shape[0], "f32", "fast", kick="physical", eps2=EPS2, damping=1.0, dt=DT) as s:
+            s.set_state(p, v)
+            s.step(3)
+            want, _ = s.get_state()
+        assert g.tobytes() == want.tobytes()
+
+
+def test_batched_matches_per_system_within_tolerance(cuda):
+    sizes = ics.batch_sizes(24, lo=128, hi=4096, seed=5)
+    pos, vel = make_batch(sizes, seed=2)
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b:
+        b.set_state(pos, vel)
+        b.step(5)
+        bat, _ = b.get_state()
+        b.set_state(pos, vel)
+        b.step_per_system(5)
+        ref, _ = b.get_state()
+    d = np.linalg.norm(bat[:, :3].astype(np.float64) - ref[:, :3], axis=1)
+    w = np.linalg.norm(ref[:, :3].astype(np.float64), axis=1)
+    assert (d <= 1e-5 * (w + 0.1)).all()
+
+
+def test_autotune_and_cache(cuda, tmp_path):
+    sizes = ics.batch_sizes(64, lo=128, hi=4096, seed=11)
+    pos, vel = make_batch(sizes, seed=4)
+    cache = str(tmp_path / "tune.txt")
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b:
+        b.set_state(pos, vel)
+        w, k = b.autotune(reps=1, cache_path=cache)
+        info = b.plan_info()
+        assert (info["warps_per_cta"], info["bodies_per_lane"]) == (w, k)
+        p0, _ = b.get_state()
+        assert p0.tobytes() == pos.tobytes()  # tuning left the state as it was
+        b.step(2)
+        tuned, _ = b.get_state()
+    lines = open(cache).read().strip().splitlines()
+    assert len(lines) == 1 and lines[0].endswith(f"{w} {k}")
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b2:
+        b2.set_state(pos, vel)
+        assert b2.autotune(reps=1, cache_path=cache) == (w, k)  # served from the cache
+        assert len(open(cache).read().strip().splitlines()) == 1
+        b2.step(2)
+        again, _ = b2.get_state()
+    assert tuned.tobytes() == again.tobytes()

@@ -1,0 +1,117 @@
+"""Precision mode (NB_F32_COMP): FP32 pair forces with compensated (two-sum)
+accumulation, FP64 absolute positions, FP64 energy/momentum reduction.
+
+Tolerances: compensated accelerations per body within 2e-6 (|a| + mean|a|)
+of the FP64 oracle (the rsqrt.approx error of each pair term bounds it);
+energies within 1e-6 relative of the FP64 oracle; positions after the
+stated steps within 1e-9 relative (FP64 positions, 1e-9 covers the float
+velocity increments).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from utc_gb300 import ics
+from utc_gb300.nbody import NBodySystem
+
+pytestmark = pytest.mark.gpu
+
+
+def body_err(got, want):
+    """Per-body error relative to |a| + mean|a| (0 where both are exactly 0)."""
+    d = np.linalg.norm(np.asarray(got, np.float64) - want, axis=1)
+    w = np.linalg.norm(want, axis=1)
+    scale = w + w.mean()
+    return np.where(scale > 0, d / np.where(scale > 0, scale, 1.0), d)
+
+
+def test_state_roundtrip(cuda):
+    p, v = ics.plummer(1000, seed=2)
+    with NBodySystem(1000, "f32comp", "fast", eps2=1e-3) as s:
+        s.set_state(p, v)
+        p2, v2 = s.get_state()
+    assert p2.tobytes() == p.tobytes()
+    assert np.abs(v2[:, :3] - v[:, :3]).max() <= 1e-14 * np.abs(v[:, :3]).max()
+    assert np.array_equal(v2[:, 3], v[:, 3])
+
+
+@pytest.mark.parametrize("n", [1, 7, 1000, 4097])
+def test_compensated_accel_vs_fp64(cuda, n):
+    p, _ = ics.plummer(n, seed=n)
+    v = np.zeros_like(p)
+    with NBodySystem(n, "f32comp", "fast", eps2=1e-4) as s:
+        s.set_state(p, v)
+        a = s.accel()
+    p32 = p.astype(np.float32).astype(np.float64)  # the pair terms read float positions
+    ref = oracle.accel(p32, float(np.float32(1e-4)))
+    assert body_err(a, ref).max() <= 2e-6
+
+
+def test_compensated_beats_plain_at_scale(cuda):
+    n = 65536
+    p, _ = ics.plummer(n, seed=5)
+    v = np.zeros_like(p)
+    tidx = np.random.default_rng(1).choice(n, 256, replace=False).astype(np.int32)
+    p32 = p.astype(np.float32)
+    ref = oracle.accel_subset_f64(p32.astype(np.float64), tidx, float(np.float32(1e-4)))
+    with NBodySystem(n, "f32comp", "fast", eps2=1e-4) as s:
+        s.set_state(p, v)
+        ac = s.accel()[tidx]
+    with NBodySystem(n, "f32", "fast", eps2=np.float32(1e-4)) as s:
+        s.set_state(p32, v.astype(np.float32))
+        ap = s.accel()[tidx]
+    ec, ep = body_err(ac, ref).max(), body_err(ap, ref).max()
+    assert ec <= 2e-6
+    assert ec < ep
+
+
+def test_compensated_steps_vs_fp64_oracle(cuda):
+    n, steps = 2048, 10
+    p, v = ics.plummer(n, seed=9)
+    p32 = p.astype(np.float32).astype(np.float64)
+    p[:, :3] = p32[:, :3]  # same starting positions as the float working copy
+    with NBodySystem(n, "f32comp", "fast", kick="physical", eps2=1e-3, damping=1.0, dt=1e-3) as s:
+        s.set_state(p, v)
+        s.step(steps)
+        pg, vg = s.get_state()
+    pr, vr = oracle.step(p, v, 1e-3, 1.0, 1e-3, steps, kick_mode=oracle.KICK_PHYSICAL)
+    rel = np.linalg.norm(pg[:, :3] - pr[:, :3], axis=1) / (np.linalg.norm(pr[:, :3], axis=1) + 0.1)
+    assert rel.max() <= 1e-9, rel.max()
+    dv = np.linalg.norm(vg[:, :3] - vr[:, :3], axis=1) / (np.linalg.norm(vr[:, :3], axis=1) + 1e-3)
+    assert dv.max() <= 1e-6, dv.max()
+
+
+@pytest.mark.parametrize("precision", ["f32", "f32comp"])
+def test_energy_momentum_vs_fp64(cuda, precision):
+    n = 4096
+    p, v = ics.plummer(n, seed=4)
+    if precision == "f32":
+        p, v = p.astype(np.float32), v.astype(np.float32)
+    eps2 = np.float32(1e-3)
+    with NBodySystem(n, precision, "fast", kick="physical", eps2=eps2) as s:
+        s.set_state(p, v)
+        e, bodies = s.energy(with_bodies=True)
+    p64 = np.asarray(p, np.float64)
+    if precision == "f32comp":
+        p64 = p64.astype(np.float32).astype(np.float64)  # pair terms read float positions
+    ref = oracle.energy(p64, np.asarray(v, np.float64), float(eps2))
+    tol = 1e-6 if precision == "f32comp" else 2e-5
+    assert abs(e[0] - ref[0]) <= 1e-12 * abs(ref[0]) + 1e-300
+    assert abs(e[1] - ref[1]) <= tol * abs(ref[1])
+    pmag = np.abs(p64[:, 3] * np.linalg.norm(v[:, :3], axis=1)).sum()
+    assert np.abs(e[2:] - ref[2:]).max() <= 1e-12 * pmag
+    tidx = np.arange(0, n, 16, dtype=np.int32)
+    _, phi = oracle.accel_phi_subset_f64(p64, tidx, float(eps2))
+    assert np.abs(bodies[tidx, 3] - phi).max() <= tol * np.abs(phi).max()
+
+
+def test_energy_conserved_by_small_steps(cuda):
+    n = 4096
+    p, v = ics.plummer(n, seed=6)
+    with NBodySystem(n, "f32comp", "fast", kick="physical", eps2=1e-2, damping=1.0, dt=1e-4) as s:
+        s.set_state(p, v)
+        e0 = s.energy()
+        s.step(50)
+        e1 = s.energy()
+    E0, E1 = e0[0] + e0[1], e1[0] + e1[1]
+    assert abs(E1 - E0) <= 1e-5 * abs(E0)

@@ -54,12 +54,26 @@ def _declare(lib):
         "nb_step": (I, [vp, I, vp]),
         "nb_accel": (I, [vp, vp, vp]),
         "nb_step_timed": (I, [vp, I, P(C.c_float), P(C.c_float), vp]),
+        "nb_energy": (I, [vp, P(D), vp, vp]),
+        "nb_adj_forward": (I, [vp, I, I, vp]),
+        "nb_adj_backward": (I, [vp, vp, vp, vp, vp, vp, vp]),
         "nb_step_f32_noalloc": (I, [vp, vp, vp, I, C.c_float, C.c_float, C.c_float, I, C.c_float, vp]),
         "nb_run_host": (I, [vp, vp, vp, I, I, vp, P(D), vp]),
         "nb_state_ptrs": (I, [vp, P(vp), P(vp)]),
         "nb_plan_info": (I, [vp, P(I)]),
         "nb_launches_per_step": (I, [vp]),
         "nb_probe_fma_peak": (I, [I, I, P(D), P(C.c_float), vp]),
+        "nb_batch_create": (I, [P(NbParams), I, vp, P(vp)]),
+        "nb_batch_destroy": (I, [vp]),
+        "nb_batch_set_state": (I, [vp, vp, vp, I, vp]),
+        "nb_batch_get_state": (I, [vp, vp, vp, I, vp]),
+        "nb_batch_step": (I, [vp, I, vp]),
+        "nb_batch_run": (I, [vp, I, vp]),
+        "nb_batch_autotune": (I, [vp, I, C.c_char_p, vp, P(I)]),
+        "nb_batch_set_shape": (I, [vp, I, I]),
+        "nb_batch_plan_info": (I, [vp, P(C.c_longlong)]),
+        "nb_batch_launches_per_step": (I, [vp]),
+        "nb_batch_step_per_system": (I, [vp, I, vp]),
         "nb_last_error": (C.c_char_p, []),
         "nb_abi_version": (I, []),
     }

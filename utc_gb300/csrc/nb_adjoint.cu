@@ -1,0 +1,242 @@
+// nb_adjoint.cu -- reverse-mode (adjoint) kernels of the nbody step.
+//
+// No counterpart in the reference (it has no gradients).  The forward step is
+// the reference's update (benchapps/nbody/seq/bodysystem.cc:135-182):
+//   a_i = sum_j m_j r_ij inv_ij^3,  r_ij = x_j - x_i, inv = (|r|^2+eps2)^-1/2
+//   v'  = D (v + k a dt),            k_i = m_i (reference kick) or G
+//   x'  = x + v' dt
+// Given lx = dL/dx', lv = dL/dv' the step's vector-Jacobian product is
+//   mu = lv + dt lx,  dL/dv = D mu,  g_i = D dt k_i mu_i
+//   dL/dx_k = lx_k + sum_j K(r_kj) (m_k g_j - m_j g_k),
+//             K(r) = inv^3 I - 3 inv^5 r r^T
+//   dL/dm_k += -sum_j inv^3 (r_kj . g_j) [through a]
+//              + D dt mu_k . a_k          [through k, reference kick only]
+// The pair sum is evaluated as
+//   out_k = m_k P - q g_k - 3 Q,  P = sum inv^3 g_j,  q = sum inv^3 m_j,
+//   Q = sum inv^5 (m_k (r.g_j) - m_j (r.g_k)) r
+// (26 FP32 operations and one rsqrt per pair), split stream-K over
+// persistent CTAs like the forward force kernel; each CTA segment writes
+// (out, dm) to its partial slot and the update kernel sums them in CTA order.
+#include "nb_internal.cuh"
+
+namespace nb {
+
+template <int NT, int BPT>
+__global__ void __launch_bounds__(NT) vjp_pair_kernel(const float4 *__restrict__ pos,
+                                                      const float4 *__restrict__ gbuf, int n,
+                                                      float eps2, float4 *__restrict__ partial,
+                                                      long long total, int ngroups)
+{
+    constexpr int TB = NT * BPT;
+    __shared__ __align__(16) float4 sP[NT];
+    __shared__ __align__(16) float4 sG[NT];
+    const int t = threadIdx.x;
+    const int c = blockIdx.x;
+    long long it = sk_start(c, total, gridDim.x);
+    const long long end = sk_start(c + 1, total, gridDim.x);
+    const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+
+    while (it < end) {
+        const int tb = (int)(it / ngroups);
+        const long long tb_first = (long long)tb * ngroups;
+        const long long seg_end = end < tb_first + ngroups ? end : tb_first + ngroups;
+        const int j0 = (int)(it - tb_first) * kGroup;
+        const int j1 = min((int)(seg_end - tb_first) * kGroup, n);
+
+        float px[BPT], py[BPT], pz[BPT], pm[BPT], gx[BPT], gy[BPT], gz[BPT];
+        float Px[BPT], Py[BPT], Pz[BPT], Q0[BPT], Q1[BPT], Q2[BPT], q[BPT], dm[BPT];
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const int i = tb * TB + t + k * NT;
+            const float4 a = i < n ? pos[i] : zero;
+            const float4 g = i < n ? gbuf[i] : zero;
+            px[k] = a.x; py[k] = a.y; pz[k] = a.z; pm[k] = a.w;
+            gx[k] = g.x; gy[k] = g.y; gz[k] = g.z;
+            Px[k] = Py[k] = Pz[k] = Q0[k] = Q1[k] = Q2[k] = q[k] = dm[k] = 0.f;
+        }
+        float4 nxp = (j0 + t < j1) ? pos[j0 + t] : pad;
+        float4 nxg = (j0 + t < j1) ? gbuf[j0 + t] : zero;
+        for (int jt = j0; jt < j1; jt += NT) {
+            __syncthreads();
+            sP[t] = nxp;
+            sG[t] = nxg;
+            __syncthreads();
+            if (jt + NT < j1) {
+                const int jn = jt + NT + t;
+                nxp = jn < j1 ? pos[jn] : pad;
+                nxg = jn < j1 ? gbuf[jn] : zero;
+            }
+            const int cnt = min(NT, j1 - jt);
+            const int cnt2 = (cnt + 1) & ~1;  // entries past cnt are zero-mass, zero-g pads
+            for (int j = 0; j < cnt2; j += 2) {
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const float4 s = sP[j + u];
+                    const float4 g = sG[j + u];
+#pragma unroll
+                    for (int k = 0; k < BPT; ++k) {
+                        const float rx = s.x - px[k], ry = s.y - py[k], rz = s.z - pz[k];
+                        float d2 = fmaf(rx, rx, eps2);
+                        d2 = fmaf(ry, ry, d2);
+                        d2 = fmaf(rz, rz, d2);
+                        const float inv = rsqrt_approx(d2);
+                        const float inv2 = inv * inv;
+                        const float inv3 = inv2 * inv;
+                        const float inv5 = inv3 * inv2;
+                        Px[k] = fmaf(inv3, g.x, Px[k]);
+                        Py[k] = fmaf(inv3, g.y, Py[k]);
+                        Pz[k] = fmaf(inv3, g.z, Pz[k]);
+                        q[k] = fmaf(inv3, s.w, q[k]);
+                        const float rgj = fmaf(rz, g.z, fmaf(ry, g.y, rx * g.x));
+                        const float rgk = fmaf(rz, gz[k], fmaf(ry, gy[k], rx * gx[k]));
+                        const float cc = inv5 * fmaf(pm[k], rgj, -(s.w * rgk));
+                        Q0[k] = fmaf(cc, rx, Q0[k]);
+                        Q1[k] = fmaf(cc, ry, Q1[k]);
+                        Q2[k] = fmaf(cc, rz, Q2[k]);
+                        dm[k] = fmaf(inv3, rgj, dm[k]);
+                    }
+                }
+            }
+        }
+        float4 *dst = partial + (size_t)(c + tb) * TB;
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const float ox = fmaf(pm[k], Px[k], fmaf(-q[k], gx[k], -3.f * Q0[k]));
+            const float oy = fmaf(pm[k], Py[k], fmaf(-q[k], gy[k], -3.f * Q1[k]));
+            const float oz = fmaf(pm[k], Pz[k], fmaf(-q[k], gz[k], -3.f * Q2[k]));
+            dst[t + k * NT] = make_float4(ox, oy, oz, -dm[k]);
+        }
+        it = seg_end;
+    }
+}
+
+// g_i = D dt k_i (lv_i + dt lx_i) for the first reverse step.
+__global__ void adj_g_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ lx,
+                             const float4 *__restrict__ lv, float4 *__restrict__ gbuf, int n,
+                             float damping, float dt, int kick, float G)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float k = kick == NB_KICK_REFERENCE ? pos[i].w : G;
+    const float4 x = lx[i], v = lv[i];
+    const float f = damping * dt * k;
+    gbuf[i] = make_float4(f * fmaf(dt, x.x, v.x), f * fmaf(dt, x.y, v.y), f * fmaf(dt, x.z, v.z), 0.f);
+}
+
+// One reverse step's per-body update: sum the partial slots, then
+//   lx <- lx + out;  lv <- D mu;  gm += dm (+ D dt mu.a in reference mode)
+// and, when pos_prev != nullptr, g for the next reverse step (at the
+// previous state, whose masses are the same).
+__global__ void adj_update_kernel(const float4 *__restrict__ partial, int n, int tbsize,
+                                  long long total, int ngroups, int grid,
+                                  const float4 *__restrict__ pos, const float4 *__restrict__ acc,
+                                  float4 *__restrict__ lx, float4 *__restrict__ lv,
+                                  float *__restrict__ gm, float4 *__restrict__ gbuf, float damping,
+                                  float dt, int kick, float G, int want_next_g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int tb = i / tbsize;
+    const int li = i - tb * tbsize;
+    const long long first = (long long)tb * ngroups;
+    const int c0 = sk_owner(first, total, grid);
+    const int c1 = sk_owner(first + ngroups - 1, total, grid);
+    float ox = 0.f, oy = 0.f, oz = 0.f, odm = 0.f;
+    for (int c = c0; c <= c1; ++c) {
+        const float4 q = partial[(size_t)(c + tb) * tbsize + li];
+        ox += q.x;
+        oy += q.y;
+        oz += q.z;
+        odm += q.w;
+    }
+    const float4 x = lx[i], v = lv[i];
+    const float mux = fmaf(dt, x.x, v.x), muy = fmaf(dt, x.y, v.y), muz = fmaf(dt, x.z, v.z);
+    float dmi = odm;
+    if (kick == NB_KICK_REFERENCE) {
+        const float4 a = acc[i];
+        dmi = fmaf(damping * dt, mux * a.x + muy * a.y + muz * a.z, dmi);
+    }
+    gm[i] += dmi;
+    const float4 nx = make_float4(x.x + ox, x.y + oy, x.z + oz, 0.f);
+    const float4 nv = make_float4(damping * mux, damping * muy, damping * muz, 0.f);
+    lx[i] = nx;
+    lv[i] = nv;
+    if (want_next_g) {
+        const float k = kick == NB_KICK_REFERENCE ? pos[i].w : G;
+        const float f = damping * dt * k;
+        gbuf[i] = make_float4(f * fmaf(dt, nx.x, nv.x), f * fmaf(dt, nx.y, nv.y),
+                              f * fmaf(dt, nx.z, nv.z), 0.f);
+    }
+}
+
+typedef void (*vjp_kernel_t)(const float4 *, const float4 *, int, float, float4 *, long long, int);
+
+static vjp_kernel_t vjp_kernel_for(int block, int bpt)
+{
+    if (block == 128 && bpt == 2) return vjp_pair_kernel<128, 2>;
+    if (block == 128 && bpt == 4) return vjp_pair_kernel<128, 4>;
+    if (block == 256 && bpt == 2) return vjp_pair_kernel<256, 2>;
+    if (block == 256 && bpt == 4) return vjp_pair_kernel<256, 4>;
+    return nullptr;
+}
+
+int adj_plan(int n, int block, int bpt, int device, SkPlan *pl)
+{
+    if (block == 0) block = 256;
+    if (bpt == 0) bpt = 4;
+    vjp_kernel_t k = vjp_kernel_for(block, bpt);
+    if (!k) return set_error(NB_ERR_UNSUPPORTED, "adjoint kernel shape not compiled");
+    SkPlan p;
+    p.n = n;
+    p.block = block;
+    p.bpt = bpt;
+    p.tbsize = block * bpt;
+    p.ntb = (n + p.tbsize - 1) / p.tbsize;
+    p.ngroups = (n + kGroup - 1) / kGroup;
+    p.total = (long long)p.ntb * p.ngroups;
+    int sms = 0, occ = 0;
+    NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, block, 0));
+    if (occ < 1) return set_error(NB_ERR_UNSUPPORTED, "adjoint kernel does not fit on an SM");
+    long long grid = (long long)sms * occ;
+    if (p.total > 0 && grid > p.total) grid = p.total;
+    p.grid = p.total > 0 ? (int)grid : 0;
+    p.slots = p.total > 0 ? p.grid + p.ntb - 1 : 0;
+    *pl = p;
+    return NB_OK;
+}
+
+int adj_g(int n, const float4 *pos, const float4 *lx, const float4 *lv, float4 *gbuf, float damping,
+          float dt, int kick, float G, cudaStream_t s)
+{
+    if (n == 0) return NB_OK;
+    adj_g_kernel<<<(n + 255) / 256, 256, 0, s>>>(pos, lx, lv, gbuf, n, damping, dt, kick, G);
+    NB_LAUNCH_CHECK("adj_g_kernel launch");
+    return NB_OK;
+}
+
+int adj_vjp(const SkPlan &p, const float4 *pos, const float4 *gbuf, float eps2, float4 *partial,
+            cudaStream_t s)
+{
+    if (p.total == 0) return NB_OK;
+    vjp_kernel_t k = vjp_kernel_for(p.block, p.tbsize / p.block);
+    if (!k) return set_error(NB_ERR_UNSUPPORTED, "adjoint kernel shape not compiled");
+    k<<<p.grid, p.block, 0, s>>>(pos, gbuf, p.n, eps2, partial, p.total, p.ngroups);
+    NB_LAUNCH_CHECK("vjp_pair_kernel launch");
+    return NB_OK;
+}
+
+int adj_update(const SkPlan &p, const float4 *partial, const float4 *pos_prev, const float4 *acc,
+               float4 *lx, float4 *lv, float *gm, float4 *gbuf, float damping, float dt, int kick,
+               float G, int want_next_g, cudaStream_t s)
+{
+    if (p.n == 0) return NB_OK;
+    adj_update_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(partial, p.n, p.tbsize, p.total, p.ngroups,
+                                                       p.grid, pos_prev, acc, lx, lv, gm, gbuf,
+                                                       damping, dt, kick, G, want_next_g);
+    NB_LAUNCH_CHECK("adj_update_kernel launch");
+    return NB_OK;
+}
+
+}  // namespace nb

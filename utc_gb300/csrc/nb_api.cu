@@ -41,6 +41,30 @@ struct nb_ctx {
     void *stage_vel = nullptr;
     void *stage_out = nullptr;
     std::vector<cudaEvent_t> events;  // pool for nb_step_timed
+    // NB_F32_COMP state (pos[0] holds the double4 positions, vel the FP32
+    // velocity high parts)
+    float4 *pos32 = nullptr;
+    float4 *vel_lo = nullptr;
+    double4 *tmpA = nullptr;  // host-format staging for set/get
+    double4 *tmpB = nullptr;
+    // energy pass: its own launch plan, per-body output and FP64 partials
+    nb::SkPlan eplan;
+    void *acc_tmp = nullptr;
+    double *e_blocks = nullptr;
+    double *e_out = nullptr;
+    // adjoint: checkpoints of the last nb_adj_forward and reverse-pass buffers
+    struct Adj {
+        int steps = 0, every = 0, nckpt = 0;
+        int cap_ckpt = 0, cap_seg = 0;
+        float4 *ckpt_pos = nullptr, *ckpt_vel = nullptr;  // [nckpt][n]
+        float4 *seg_pos = nullptr;                        // [every + 1][n]
+        float4 *seg_acc = nullptr;                        // [every][n]
+        float4 *vel_tmp = nullptr, *lx = nullptr, *lv = nullptr, *gbuf = nullptr;
+        float *gm = nullptr;
+        float4 *partial = nullptr;
+        nb::SkPlan plan;
+        bool ready = false;
+    } adj;
 };
 
 using nb::set_error;
@@ -64,8 +88,10 @@ static int validate(const nb_params *p)
         return set_error(NB_ERR_INVALID, "eps2, damping, dt and G must be finite");
     if (p->precision == NB_F64 && p->algo == NB_ALGO_FAST)
         return set_error(NB_ERR_UNSUPPORTED, "NB_F64 runs the exact algorithm only");
-    if (p->precision == NB_F32_COMP)
-        return set_error(NB_ERR_UNSUPPORTED, "NB_F32_COMP is not available in this build");
+    if (p->precision == NB_F32_COMP && p->algo != NB_ALGO_FAST)
+        return set_error(NB_ERR_UNSUPPORTED, "NB_F32_COMP runs the fast (compensated) algorithm only");
+    if (p->precision == NB_F32_COMP && p->memtype == NB_MEM_UNIFIED)
+        return set_error(NB_ERR_UNSUPPORTED, "NB_F32_COMP keeps its state in device memory");
     return NB_OK;
 }
 
@@ -80,6 +106,23 @@ static void free_ctx(nb_ctx *c)
     cudaFreeHost(c->stage_vel);
     cudaFreeHost(c->stage_out);
     for (cudaEvent_t e : c->events) cudaEventDestroy(e);
+    cudaFree(c->pos32);
+    cudaFree(c->vel_lo);
+    cudaFree(c->tmpA);
+    cudaFree(c->tmpB);
+    cudaFree(c->acc_tmp);
+    cudaFree(c->e_blocks);
+    cudaFree(c->e_out);
+    cudaFree(c->adj.ckpt_pos);
+    cudaFree(c->adj.ckpt_vel);
+    cudaFree(c->adj.seg_pos);
+    cudaFree(c->adj.seg_acc);
+    cudaFree(c->adj.vel_tmp);
+    cudaFree(c->adj.lx);
+    cudaFree(c->adj.lv);
+    cudaFree(c->adj.gbuf);
+    cudaFree(c->adj.gm);
+    cudaFree(c->adj.partial);
     delete c;
 }
 
@@ -96,6 +139,16 @@ static int dalloc(nb_ctx *c, void **p, size_t bytes)
 }
 
 static bool uses_fast(const nb_ctx *c) { return c->p.precision == NB_F32 && c->p.algo == NB_ALGO_FAST; }
+static bool is_comp(const nb_ctx *c) { return c->p.precision == NB_F32_COMP; }
+
+static int dev_alloc(void **p, size_t bytes, const char *what)
+{
+    *p = nullptr;
+    if (!bytes) return NB_OK;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return nb::cuda_error(e, what);
+    return NB_OK;
+}
 
 extern "C" {
 
@@ -125,31 +178,53 @@ int nb_create(const nb_params *p, nb_ctx **out)
     if (st) return st;
     nb_ctx *c = new nb_ctx();
     c->p = *p;
-    c->elem = p->precision == NB_F64 ? 8 : 4;
+    c->elem = (p->precision == NB_F64 || p->precision == NB_F32_COMP) ? 8 : 4;
     cudaError_t e = cudaGetDevice(&c->device);
     if (e != cudaSuccess) {
         delete c;
         return nb::cuda_error(e, "cudaGetDevice");
     }
     const size_t sb = state_bytes(c);
-    if ((st = dalloc(c, &c->pos[0], sb)) || (st = dalloc(c, &c->pos[1], sb)) ||
-        (st = dalloc(c, &c->vel, sb))) {
+    const size_t n = (size_t)p->n;
+    if (is_comp(c)) {
+        if ((st = dev_alloc(&c->pos[0], n * sizeof(double4), "state allocation")) ||
+            (st = dev_alloc(&c->vel, n * sizeof(float4), "state allocation")) ||
+            (st = dev_alloc((void **)&c->pos32, n * sizeof(float4), "state allocation")) ||
+            (st = dev_alloc((void **)&c->vel_lo, n * sizeof(float4), "state allocation")) ||
+            (st = dev_alloc((void **)&c->tmpA, n * sizeof(double4), "staging allocation")) ||
+            (st = dev_alloc((void **)&c->tmpB, n * sizeof(double4), "staging allocation"))) {
+            free_ctx(c);
+            return st;
+        }
+    } else if ((st = dalloc(c, &c->pos[0], sb)) || (st = dalloc(c, &c->pos[1], sb)) ||
+               (st = dalloc(c, &c->vel, sb))) {
         free_ctx(c);
         return st;
     }
-    if (uses_fast(c)) {
-        st = nb::fast_plan(p->n, p->block, p->bpt, p->ctas_per_sm, c->device, &c->plan);
+    if (uses_fast(c) || is_comp(c)) {
+        const int flags = is_comp(c) ? nb::SK_COMP : 0;
+        const int block = p->block ? p->block : (is_comp(c) ? 256 : 0);
+        const int bpt = p->bpt ? p->bpt : (is_comp(c) ? 4 : 0);
+        st = nb::fast_plan(p->n, block, bpt, p->ctas_per_sm, c->device, &c->plan, flags);
+        if (!st)
+            st = nb::fast_plan(p->n, 256, is_comp(c) ? 4 : 8, 0, c->device, &c->eplan,
+                               flags | nb::SK_PHI);
         if (st) {
             free_ctx(c);
             return st;
         }
-        const size_t pb = (size_t)c->plan.slots * c->plan.tbsize * sizeof(float4);
-        if (pb) {
-            e = cudaMalloc((void **)&c->partial, pb);
-            if (e != cudaSuccess) {
-                free_ctx(c);
-                return nb::cuda_error(e, "partial-sum scratch allocation");
-            }
+        const size_t mult = is_comp(c) ? 2 : 1;
+        size_t pb = mult * (size_t)c->plan.slots * c->plan.tbsize * sizeof(float4);
+        const size_t pe = mult * (size_t)c->eplan.slots * c->eplan.tbsize * sizeof(float4);
+        if (pe > pb) pb = pe;
+        if ((st = dev_alloc((void **)&c->partial, pb, "partial-sum scratch allocation")) ||
+            (st = dev_alloc(&c->acc_tmp, n * sizeof(double4), "energy scratch allocation")) ||
+            (st = dev_alloc((void **)&c->e_blocks,
+                            (size_t)(nb::energy_blocks(p->n) + 1) * 5 * sizeof(double),
+                            "energy scratch allocation")) ||
+            (st = dev_alloc((void **)&c->e_out, 8 * sizeof(double), "energy scratch allocation"))) {
+            free_ctx(c);
+            return st;
         }
     }
     *out = c;
@@ -172,7 +247,14 @@ int nb_set_state(nb_ctx *c, const void *pos, const void *vel, int where, void *s
     if (where != NB_HOST && where != NB_DEVICE) return set_error(NB_ERR_INVALID, "where");
     cudaStream_t s = (cudaStream_t)stream;
     c->cur = 0;
-    if (sb) {
+    if (sb && is_comp(c)) {
+        NB_CUDA(cudaMemcpyAsync(c->tmpA, pos, sb, cudaMemcpyDefault, s));
+        NB_CUDA(cudaMemcpyAsync(c->tmpB, vel, sb, cudaMemcpyDefault, s));
+        int st = nb::comp_split(c->tmpA, c->tmpB, (double4 *)c->pos[0], c->pos32, (float4 *)c->vel,
+                                c->vel_lo, c->p.n, s);
+        if (st) return st;
+        if (where == NB_HOST) NB_CUDA(cudaStreamSynchronize(s));
+    } else if (sb) {
         NB_CUDA(cudaMemcpyAsync(c->pos[0], pos, sb, cudaMemcpyDefault, s));
         NB_CUDA(cudaMemcpyAsync(c->vel, vel, sb, cudaMemcpyDefault, s));
         if (where == NB_HOST) NB_CUDA(cudaStreamSynchronize(s));
@@ -188,7 +270,14 @@ int nb_get_state(nb_ctx *c, void *pos, void *vel, int where, void *stream)
     if (where != NB_HOST && where != NB_DEVICE) return set_error(NB_ERR_INVALID, "where");
     const size_t sb = state_bytes(c);
     cudaStream_t s = (cudaStream_t)stream;
-    if (sb) {
+    if (sb && is_comp(c)) {
+        int st = nb::comp_join((const double4 *)c->pos[0], (const float4 *)c->vel, c->vel_lo,
+                               c->tmpA, c->tmpB, c->p.n, s);
+        if (st) return st;
+        if (pos) NB_CUDA(cudaMemcpyAsync(pos, c->tmpA, sb, cudaMemcpyDefault, s));
+        if (vel) NB_CUDA(cudaMemcpyAsync(vel, c->tmpB, sb, cudaMemcpyDefault, s));
+        if (where == NB_HOST) NB_CUDA(cudaStreamSynchronize(s));
+    } else if (sb) {
         if (pos) NB_CUDA(cudaMemcpyAsync(pos, c->pos[c->cur], sb, cudaMemcpyDefault, s));
         if (vel) NB_CUDA(cudaMemcpyAsync(vel, c->vel, sb, cudaMemcpyDefault, s));
         if (where == NB_HOST) NB_CUDA(cudaStreamSynchronize(s));
@@ -199,7 +288,7 @@ int nb_get_state(nb_ctx *c, void *pos, void *vel, int where, void *stream)
 int nb_state_ptrs(nb_ctx *c, void **pos_dev, void **vel_dev)
 {
     if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
-    if (pos_dev) *pos_dev = c->pos[c->cur];
+    if (pos_dev) *pos_dev = is_comp(c) ? c->pos[0] : c->pos[c->cur];
     if (vel_dev) *vel_dev = c->vel;
     return NB_OK;
 }
@@ -212,6 +301,19 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
     void *po = c->pos[c->cur], *pn = c->pos[c->cur ^ 1];
     int st;
     if (ev) NB_CUDA(cudaEventRecord(ev[0], s));
+    if (is_comp(c)) {
+        st = nb::fast_force(c->plan, c->pos32, (float)p.eps2, c->partial, s, nb::SK_COMP);
+        if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
+        if (!st && acc_out)
+            st = nb::fast_reduce(c->plan, c->partial, 1, c->pos32, (float)p.eps2, nullptr,
+                                 (double4 *)acc_out, s);
+        else if (!st)
+            st = nb::comp_integrate(c->plan, c->partial, (double4 *)c->pos[0], c->pos32,
+                                    (float4 *)c->vel, c->vel_lo, (float)p.damping, (float)p.dt,
+                                    p.dt, p.kick, (float)p.G, s);
+        if (!st && ev) NB_CUDA(cudaEventRecord(ev[2], s));
+        return st;  // positions are updated in place: no ping-pong
+    }
     if (p.precision == NB_F64) {
         st = nb::exact_step_f64(p.n, (const double4 *)po, (double4 *)pn, (double4 *)c->vel, p.eps2,
                                 p.damping, p.dt, p.kick, p.G, (double4 *)acc_out, p.block, s);
@@ -287,18 +389,189 @@ int nb_accel(nb_ctx *c, void *acc_dev, void *stream)
     return step_once(c, (cudaStream_t)stream, acc_dev);
 }
 
+int nb_energy(nb_ctx *c, double *out5, void *accphi_dev, void *stream)
+{
+    if (!c || !out5) return set_error(NB_ERR_INVALID, "ctx/out is NULL");
+    if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
+    if (!(uses_fast(c) || is_comp(c)))
+        return set_error(NB_ERR_UNSUPPORTED, "nb_energy needs an NB_F32 fast or NB_F32_COMP context");
+    if (!(c->p.eps2 > 0.0)) return set_error(NB_ERR_INVALID, "nb_energy needs eps2 > 0");
+    cudaStream_t s = (cudaStream_t)stream;
+    const nb_params &p = c->p;
+    int st;
+    if (is_comp(c)) {
+        st = nb::fast_force(c->eplan, c->pos32, (float)p.eps2, c->partial, s, nb::SK_COMP | nb::SK_PHI);
+        if (!st)
+            st = nb::fast_reduce(c->eplan, c->partial, 1, c->pos32, (float)p.eps2, nullptr,
+                                 (double4 *)c->acc_tmp, s);
+        if (!st)
+            st = nb::energy_reduce(p.n, c->pos32, (const double4 *)c->pos[0], (const float4 *)c->vel,
+                                   c->vel_lo, nullptr, (const double4 *)c->acc_tmp, p.G,
+                                   c->e_blocks, c->e_out, s);
+    } else {
+        const float4 *pos = (const float4 *)c->pos[c->cur];
+        st = nb::fast_force(c->eplan, pos, (float)p.eps2, c->partial, s, nb::SK_PHI);
+        if (!st)
+            st = nb::fast_reduce(c->eplan, c->partial, 0, pos, (float)p.eps2, (float4 *)c->acc_tmp,
+                                 nullptr, s);
+        if (!st)
+            st = nb::energy_reduce(p.n, pos, nullptr, (const float4 *)c->vel, nullptr,
+                                   (const float4 *)c->acc_tmp, nullptr, p.G, c->e_blocks,
+                                   c->e_out, s);
+    }
+    if (st) return st;
+    if (accphi_dev && p.n)
+        NB_CUDA(cudaMemcpyAsync(accphi_dev, c->acc_tmp,
+                                (size_t)p.n * (is_comp(c) ? sizeof(double4) : sizeof(float4)),
+                                cudaMemcpyDeviceToDevice, s));
+    NB_CUDA(cudaMemcpyAsync(out5, c->e_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    NB_CUDA(cudaStreamSynchronize(s));
+    return NB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// adjoint: forward with checkpoints, reverse pass with per-segment recompute
+// ---------------------------------------------------------------------------
+static int adj_reserve(nb_ctx *c, int nckpt, int every)
+{
+    const size_t n = (size_t)c->p.n;
+    auto &A = c->adj;
+    int st;
+    if (!A.lx) {
+        if ((st = nb::adj_plan(c->p.n, 0, 0, c->device, &A.plan))) return st;
+        if ((st = dev_alloc((void **)&A.vel_tmp, n * sizeof(float4), "adjoint allocation")) ||
+            (st = dev_alloc((void **)&A.lx, n * sizeof(float4), "adjoint allocation")) ||
+            (st = dev_alloc((void **)&A.lv, n * sizeof(float4), "adjoint allocation")) ||
+            (st = dev_alloc((void **)&A.gbuf, n * sizeof(float4), "adjoint allocation")) ||
+            (st = dev_alloc((void **)&A.gm, n * sizeof(float), "adjoint allocation")) ||
+            (st = dev_alloc((void **)&A.partial,
+                            (size_t)A.plan.slots * A.plan.tbsize * sizeof(float4),
+                            "adjoint allocation")))
+            return st;
+    }
+    if (nckpt > A.cap_ckpt) {
+        cudaFree(A.ckpt_pos);
+        cudaFree(A.ckpt_vel);
+        A.ckpt_pos = A.ckpt_vel = nullptr;
+        A.cap_ckpt = 0;
+        if ((st = dev_alloc((void **)&A.ckpt_pos, n * nckpt * sizeof(float4), "checkpoint allocation")) ||
+            (st = dev_alloc((void **)&A.ckpt_vel, n * nckpt * sizeof(float4), "checkpoint allocation")))
+            return st;
+        A.cap_ckpt = nckpt;
+    }
+    if (every > A.cap_seg) {
+        cudaFree(A.seg_pos);
+        cudaFree(A.seg_acc);
+        A.seg_pos = A.seg_acc = nullptr;
+        A.cap_seg = 0;
+        if ((st = dev_alloc((void **)&A.seg_pos, n * (every + 1) * sizeof(float4), "segment allocation")) ||
+            (st = dev_alloc((void **)&A.seg_acc, n * every * sizeof(float4), "segment allocation")))
+            return st;
+        A.cap_seg = every;
+    }
+    return NB_OK;
+}
+
+int nb_adj_forward(nb_ctx *c, int steps, int ckpt_every, void *stream)
+{
+    if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
+    if (!uses_fast(c)) return set_error(NB_ERR_UNSUPPORTED, "the adjoint needs an NB_F32 fast context");
+    if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
+    if (steps < 1 || ckpt_every < 1) return set_error(NB_ERR_INVALID, "steps and ckpt_every must be >= 1");
+    if (ckpt_every > steps) ckpt_every = steps;
+    const int nckpt = (steps + ckpt_every - 1) / ckpt_every;
+    int st = adj_reserve(c, nckpt, ckpt_every);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t n = (size_t)c->p.n;
+    for (int t = 0; t < steps; ++t) {
+        if (t % ckpt_every == 0 && n) {
+            const size_t k = (size_t)(t / ckpt_every) * n;
+            NB_CUDA(cudaMemcpyAsync(c->adj.ckpt_pos + k, c->pos[c->cur], n * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, s));
+            NB_CUDA(cudaMemcpyAsync(c->adj.ckpt_vel + k, c->vel, n * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, s));
+        }
+        if ((st = step_once(c, s, nullptr))) return st;
+    }
+    c->adj.steps = steps;
+    c->adj.every = ckpt_every;
+    c->adj.nckpt = nckpt;
+    c->adj.ready = true;
+    return NB_OK;
+}
+
+int nb_adj_backward(nb_ctx *c, const void *gx_T, const void *gv_T, void *gx0, void *gv0, void *gm,
+                    void *stream)
+{
+    if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
+    if (!c->adj.ready) return set_error(NB_ERR_STATE, "nb_adj_backward needs a preceding nb_adj_forward");
+    if (c->p.n == 0) return NB_OK;
+    if (!gx_T || !gx0 || !gv0 || !gm) return set_error(NB_ERR_INVALID, "NULL gradient buffer");
+    auto &A = c->adj;
+    const nb_params &p = c->p;
+    const size_t n = (size_t)p.n;
+    const float eps2 = (float)p.eps2, D = (float)p.damping, dt = (float)p.dt, G = (float)p.G;
+    cudaStream_t s = (cudaStream_t)stream;
+    int st;
+    NB_CUDA(cudaMemcpyAsync(A.lx, gx_T, n * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    if (gv_T)
+        NB_CUDA(cudaMemcpyAsync(A.lv, gv_T, n * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    else
+        NB_CUDA(cudaMemsetAsync(A.lv, 0, n * sizeof(float4), s));
+    NB_CUDA(cudaMemsetAsync(A.gm, 0, n * sizeof(float), s));
+    bool have_g = false;
+    for (int seg = A.nckpt - 1; seg >= 0; --seg) {
+        const int t0 = seg * A.every;
+        const int len = (A.steps - t0) < A.every ? (A.steps - t0) : A.every;
+        // recompute the segment's positions (and accelerations) from its checkpoint
+        NB_CUDA(cudaMemcpyAsync(A.seg_pos, A.ckpt_pos + (size_t)seg * n, n * sizeof(float4),
+                                cudaMemcpyDeviceToDevice, s));
+        NB_CUDA(cudaMemcpyAsync(A.vel_tmp, A.ckpt_vel + (size_t)seg * n, n * sizeof(float4),
+                                cudaMemcpyDeviceToDevice, s));
+        for (int k = 0; k < len; ++k) {
+            const float4 *xk = A.seg_pos + (size_t)k * n;
+            if ((st = nb::fast_force(c->plan, xk, eps2, c->partial, s))) return st;
+            if (p.kick == NB_KICK_REFERENCE &&
+                (st = nb::fast_reduce(c->plan, c->partial, 0, xk, eps2, A.seg_acc + (size_t)k * n,
+                                      nullptr, s)))
+                return st;
+            if ((st = nb::fast_integrate(c->plan, xk, A.seg_pos + (size_t)(k + 1) * n, A.vel_tmp,
+                                         c->partial, D, dt, p.kick, G, nullptr, s)))
+                return st;
+        }
+        // reverse through the segment
+        for (int k = len - 1; k >= 0; --k) {
+            const float4 *xk = A.seg_pos + (size_t)k * n;
+            if (!have_g) {
+                if ((st = nb::adj_g(p.n, xk, A.lx, A.lv, A.gbuf, D, dt, p.kick, G, s))) return st;
+                have_g = true;
+            }
+            if ((st = nb::adj_vjp(A.plan, xk, A.gbuf, eps2, A.partial, s))) return st;
+            const bool more = !(seg == 0 && k == 0);
+            if ((st = nb::adj_update(A.plan, A.partial, xk, A.seg_acc + (size_t)k * n, A.lx, A.lv,
+                                     A.gm, A.gbuf, D, dt, p.kick, G, more ? 1 : 0, s)))
+                return st;
+        }
+    }
+    NB_CUDA(cudaMemcpyAsync(gx0, A.lx, n * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    NB_CUDA(cudaMemcpyAsync(gv0, A.lv, n * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    NB_CUDA(cudaMemcpyAsync(gm, A.gm, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    return NB_OK;
+}
+
 int nb_launches_per_step(nb_ctx *c)
 {
     if (!c) return -1;
     if (c->p.n == 0) return 0;
-    return uses_fast(c) ? 2 : 1;
+    return (uses_fast(c) || is_comp(c)) ? 2 : 1;
 }
 
 int nb_plan_info(nb_ctx *c, int *info5)
 {
     if (!c || !info5) return set_error(NB_ERR_INVALID, "ctx/info is NULL");
     info5[0] = c->plan.block;
-    info5[1] = c->plan.npair * 2;
+    info5[1] = c->plan.bpt;
     info5[2] = c->plan.grid;
     info5[3] = c->plan.tbsize;
     info5[4] = c->plan.slots;

@@ -9,7 +9,9 @@
 //  * Each thread owns 2*NPAIR targets held as packed pairs, so that every
 //    pair-term operation is one sm_100+ f32x2 instruction (FADD2/FMUL2/FFMA2)
 //    doing two targets' work: per interaction 12 FP32 lane-operations and
-//    one MUFU.RSQ, issued in 6 packed instructions plus the MUFU.
+//    one MUFU.RSQ, issued in 6 packed instructions plus the MUFU.  (Scalar
+//    FFMA versions of this loop were measured on the same GB300 and ran
+//    1-10 % slower.)
 //  * Sources are staged through shared memory with each component stored
 //    twice, (x, x, y, y) and (z, z, m, m), so one LDS.128 broadcast yields the
 //    two packed operands a source contributes to a target pair.  The next
@@ -26,12 +28,30 @@
 
 namespace nb {
 
-template <int NT, int NPAIR>
+// Packed two-sum (Knuth): s + e == a + b exactly, s = fl(a + b).  Inline
+// PTX keeps the compiler from reassociating it away.
+__device__ __forceinline__ void f2_two_sum(f2 a, f2 b, f2 &s, f2 &e)
+{
+    s = f2_add(a, b);
+    const f2 bb = f2_sub(s, a);
+    e = f2_add(f2_sub(a, f2_sub(s, bb)), f2_sub(b, bb));
+}
+
+// Each thread owns 2*NPAIR targets held as packed pairs (t + 2p*NT,
+// t + (2p+1)*NT).  FLAGS: SK_COMP -- fold each tile's partial sums into a
+// compensated (hi, lo) pair with a two-sum, and write both (lo at
+// partial + lo_offset); SK_PHI -- also accumulate the potential
+// sum_j m_j / sqrt(r^2 + eps2) in w.
+template <int NT, int NPAIR, int FLAGS>
 __global__ void __launch_bounds__(NT) sk_force_kernel(const float4 *__restrict__ pos, int n,
                                                       float eps2, float4 *__restrict__ partial,
-                                                      long long total, int ngroups)
+                                                      long long total, int ngroups,
+                                                      long long lo_offset)
 {
+    constexpr bool COMP = (FLAGS & SK_COMP) != 0;
+    constexpr bool PHI = (FLAGS & SK_PHI) != 0;
     constexpr int TB = NT * 2 * NPAIR;
+    constexpr int CP_ = COMP ? NPAIR : 1;
     __shared__ __align__(16) float4 sA[NT];  // (x, x, y, y)
     __shared__ __align__(16) float4 sB[NT];  // (z, z, m, m)
     const int t = threadIdx.x;
@@ -39,6 +59,7 @@ __global__ void __launch_bounds__(NT) sk_force_kernel(const float4 *__restrict__
     long long it = sk_start(c, total, gridDim.x);
     const long long end = sk_start(c + 1, total, gridDim.x);
     const f2 EPS2 = f2_pack(eps2, eps2);
+    const f2 ZERO = f2_pack(0.f, 0.f);
     const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
 
     while (it < end) {
@@ -48,7 +69,8 @@ __global__ void __launch_bounds__(NT) sk_force_kernel(const float4 *__restrict__
         const int j0 = (int)(it - tb_first) * kGroup;
         const int j1 = min((int)(seg_end - tb_first) * kGroup, n);
 
-        f2 PX[NPAIR], PY[NPAIR], PZ[NPAIR], AX[NPAIR], AY[NPAIR], AZ[NPAIR];
+        f2 PX[NPAIR], PY[NPAIR], PZ[NPAIR], AX[NPAIR], AY[NPAIR], AZ[NPAIR], AP[NPAIR];
+        f2 SX[CP_], SY[CP_], SZ[CP_], SP[CP_], CX[CP_], CY[CP_], CZ[CP_], CPh[CP_];
 #pragma unroll
         for (int p = 0; p < NPAIR; ++p) {
             const int i0 = tb * TB + t + (2 * p) * NT;
@@ -58,9 +80,8 @@ __global__ void __launch_bounds__(NT) sk_force_kernel(const float4 *__restrict__
             PX[p] = f2_pack(q0.x, q1.x);
             PY[p] = f2_pack(q0.y, q1.y);
             PZ[p] = f2_pack(q0.z, q1.z);
-            AX[p] = f2_pack(0.f, 0.f);
-            AY[p] = AX[p];
-            AZ[p] = AX[p];
+            AX[p] = AY[p] = AZ[p] = AP[p] = ZERO;
+            if constexpr (COMP) SX[p] = SY[p] = SZ[p] = SP[p] = CX[p] = CY[p] = CZ[p] = CPh[p] = ZERO;
         }
 
         float4 nxt = (j0 + t < j1) ? pos[j0 + t] : pad;
@@ -94,11 +115,30 @@ __global__ void __launch_bounds__(NT) sk_force_kernel(const float4 *__restrict__
                         f2_unpack(d2, dlo, dhi);
                         const f2 inv = f2_pack(rsqrt_approx(dlo), rsqrt_approx(dhi));
                         const f2 inv2 = f2_mul(inv, inv);
-                        const f2 s = f2_mul(f2_mul(M2, inv), inv2);
+                        const f2 mi = f2_mul(M2, inv);
+                        const f2 s = f2_mul(mi, inv2);
                         AX[p] = f2_fma(rx, s, AX[p]);
                         AY[p] = f2_fma(ry, s, AY[p]);
                         AZ[p] = f2_fma(rz, s, AZ[p]);
+                        if constexpr (PHI) AP[p] = f2_add(AP[p], mi);
                     }
+                }
+            }
+            if constexpr (COMP) {
+#pragma unroll
+                for (int p = 0; p < NPAIR; ++p) {
+                    f2 e;
+                    f2_two_sum(SX[p], AX[p], SX[p], e);
+                    CX[p] = f2_add(CX[p], e);
+                    f2_two_sum(SY[p], AY[p], SY[p], e);
+                    CY[p] = f2_add(CY[p], e);
+                    f2_two_sum(SZ[p], AZ[p], SZ[p], e);
+                    CZ[p] = f2_add(CZ[p], e);
+                    if constexpr (PHI) {
+                        f2_two_sum(SP[p], AP[p], SP[p], e);
+                        CPh[p] = f2_add(CPh[p], e);
+                    }
+                    AX[p] = AY[p] = AZ[p] = AP[p] = ZERO;
                 }
             }
         }
@@ -106,12 +146,28 @@ __global__ void __launch_bounds__(NT) sk_force_kernel(const float4 *__restrict__
         float4 *dst = partial + (size_t)(c + tb) * TB;
 #pragma unroll
         for (int p = 0; p < NPAIR; ++p) {
-            float ax0, ax1, ay0, ay1, az0, az1;
-            f2_unpack(AX[p], ax0, ax1);
-            f2_unpack(AY[p], ay0, ay1);
-            f2_unpack(AZ[p], az0, az1);
-            dst[t + (2 * p) * NT] = make_float4(ax0, ay0, az0, 0.f);
-            dst[t + (2 * p + 1) * NT] = make_float4(ax1, ay1, az1, 0.f);
+            float x0, x1, y0, y1, z0, z1, w0 = 0.f, w1 = 0.f;
+            if constexpr (COMP) {
+                f2_unpack(SX[p], x0, x1);
+                f2_unpack(SY[p], y0, y1);
+                f2_unpack(SZ[p], z0, z1);
+                if constexpr (PHI) f2_unpack(SP[p], w0, w1);
+            } else {
+                f2_unpack(AX[p], x0, x1);
+                f2_unpack(AY[p], y0, y1);
+                f2_unpack(AZ[p], z0, z1);
+                if constexpr (PHI) f2_unpack(AP[p], w0, w1);
+            }
+            dst[t + (2 * p) * NT] = make_float4(x0, y0, z0, w0);
+            dst[t + (2 * p + 1) * NT] = make_float4(x1, y1, z1, w1);
+            if constexpr (COMP) {
+                f2_unpack(CX[p], x0, x1);
+                f2_unpack(CY[p], y0, y1);
+                f2_unpack(CZ[p], z0, z1);
+                if constexpr (PHI) f2_unpack(CPh[p], w0, w1);
+                dst[lo_offset + t + (2 * p) * NT] = make_float4(x0, y0, z0, w0);
+                dst[lo_offset + t + (2 * p + 1) * NT] = make_float4(x1, y1, z1, w1);
+            }
         }
         it = seg_end;
     }
@@ -163,23 +219,34 @@ __global__ void sk_integrate_kernel(const float4 *__restrict__ pos_old, float4 *
 // ---------------------------------------------------------------------------
 // dispatch over the compiled (threads per CTA, target pairs per thread) shapes
 // ---------------------------------------------------------------------------
-typedef void (*sk_kernel_t)(const float4 *, int, float, float4 *, long long, int);
+typedef void (*sk_kernel_t)(const float4 *, int, float, float4 *, long long, int, long long);
 
-static sk_kernel_t sk_kernel_for(int block, int npair)
+// Compiled shapes (threads per CTA x bodies per thread): plain kernel
+// 128|256 x 2|4|8; compensated and potential variants 256 x 4|8.
+static sk_kernel_t sk_kernel_for(int block, int bpt, int flags)
 {
-    if (block == 128) {
-        if (npair == 1) return sk_force_kernel<128, 1>;
-        if (npair == 2) return sk_force_kernel<128, 2>;
-        if (npair == 4) return sk_force_kernel<128, 4>;
-    } else if (block == 256) {
-        if (npair == 1) return sk_force_kernel<256, 1>;
-        if (npair == 2) return sk_force_kernel<256, 2>;
-        if (npair == 4) return sk_force_kernel<256, 4>;
+#define NB_SK(NT, B, F) \
+    if (block == NT && bpt == B) return sk_force_kernel<NT, B / 2, F>;
+    if (flags == 0) {
+        NB_SK(128, 2, 0) NB_SK(128, 4, 0) NB_SK(128, 8, 0)
+        NB_SK(256, 2, 0) NB_SK(256, 4, 0) NB_SK(256, 8, 0)
+    } else if (flags == SK_PHI) {
+        NB_SK(256, 4, SK_PHI) NB_SK(256, 8, SK_PHI)
+    } else if (flags == SK_COMP) {
+        NB_SK(256, 4, SK_COMP) NB_SK(256, 8, SK_COMP)
+    } else if (flags == (SK_COMP | SK_PHI)) {
+        NB_SK(256, 4, SK_COMP | SK_PHI) NB_SK(256, 8, SK_COMP | SK_PHI)
     }
+#undef NB_SK
     return nullptr;
 }
 
-int fast_plan(int n, int block, int bpt, int ctas_per_sm, int device, SkPlan *pl)
+bool fast_shape_supported(int block, int bpt, int flags)
+{
+    return sk_kernel_for(block, bpt, flags) != nullptr;
+}
+
+int fast_plan(int n, int block, int bpt, int ctas_per_sm, int device, SkPlan *pl, int flags)
 {
     if (n < 0) return set_error(NB_ERR_INVALID, "n must be >= 0");
     if (block == 0 || bpt == 0) {
@@ -187,13 +254,12 @@ int fast_plan(int n, int block, int bpt, int ctas_per_sm, int device, SkPlan *pl
         if (block == 0) block = n >= 32768 ? 256 : 128;
         if (bpt == 0) bpt = n >= 8192 ? 8 : (n >= 2048 ? 4 : 2);
     }
-    if (bpt % 2 != 0) return set_error(NB_ERR_INVALID, "bodies per thread must be 2, 4 or 8");
-    sk_kernel_t k = sk_kernel_for(block, bpt / 2);
+    sk_kernel_t k = sk_kernel_for(block, bpt, flags);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "fast kernel shape (block, bodies per thread) not compiled");
     SkPlan p;
     p.n = n;
     p.block = block;
-    p.npair = bpt / 2;
+    p.bpt = bpt;
     p.tbsize = block * bpt;
     p.ntb = (n + p.tbsize - 1) / p.tbsize;
     p.ngroups = (n + kGroup - 1) / kGroup;
@@ -211,12 +277,14 @@ int fast_plan(int n, int block, int bpt, int ctas_per_sm, int device, SkPlan *pl
     return NB_OK;
 }
 
-int fast_force(const SkPlan &p, const float4 *pos, float eps2, float4 *partial, cudaStream_t s)
+int fast_force(const SkPlan &p, const float4 *pos, float eps2, float4 *partial, cudaStream_t s,
+               int flags)
 {
     if (p.total == 0) return NB_OK;
-    sk_kernel_t k = sk_kernel_for(p.block, p.npair);
-    if (!k) return set_error(NB_ERR_UNSUPPORTED, "fast kernel shape not compiled");
-    k<<<p.grid, p.block, 0, s>>>(pos, p.n, eps2, partial, p.total, p.ngroups);
+    sk_kernel_t k = sk_kernel_for(p.block, p.bpt, flags);
+    if (!k) return set_error(NB_ERR_UNSUPPORTED, "fast kernel shape not compiled for this variant");
+    const long long lo_offset = (long long)p.slots * p.tbsize;
+    k<<<p.grid, p.block, 0, s>>>(pos, p.n, eps2, partial, p.total, p.ngroups, lo_offset);
     NB_LAUNCH_CHECK("sk_force_kernel launch");
     return NB_OK;
 }

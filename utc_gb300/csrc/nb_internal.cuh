@@ -92,8 +92,8 @@ constexpr int kGroup = 32;
 struct SkPlan {
     int n = 0;
     int block = 0;     // threads per CTA
-    int npair = 0;     // packed target pairs per thread (bodies per thread / 2)
-    int tbsize = 0;    // targets per block = block * 2 * npair
+    int bpt = 0;       // bodies (targets) per thread
+    int tbsize = 0;    // targets per block = block * bpt
     int ntb = 0;       // target blocks
     int ngroups = 0;   // source groups per target block
     long long total = 0;
@@ -111,15 +111,49 @@ __host__ __device__ __forceinline__ int sk_owner(long long it, long long total, 
     return (int)(((it + 1) * (long long)grid - 1) / total);
 }
 
-// Fast-path entry points (nb_fast.cu)
-int fast_plan(int n, int block, int bpt, int ctas_per_sm, int device, SkPlan *plan);
+// Force-kernel variants: compensated (two-sum) tile accumulation writing
+// (hi, lo) partials, and the potential sum carried in w.
+enum : int { SK_COMP = 1, SK_PHI = 2 };
+
+// Fast-path entry points (nb_fast.cu).  With SK_COMP the partial scratch
+// holds 2 * slots * tbsize float4 (hi block, then lo block).
+int fast_plan(int n, int block, int bpt, int ctas_per_sm, int device, SkPlan *plan,
+              int flags = 0);
+bool fast_shape_supported(int block, int bpt, int flags);
 int fast_force(const SkPlan &plan, const float4 *pos, float eps2, float4 *partial,
-               cudaStream_t s);
+               cudaStream_t s, int flags = 0);
 // Reduce the partial slots and integrate (acc_out != nullptr: write the bare
 // acceleration instead of integrating).
 int fast_integrate(const SkPlan &plan, const float4 *pos_old, float4 *pos_new, float4 *vel,
                    const float4 *partial, float damping, float dt, int kick, float G,
                    float4 *acc_out, cudaStream_t s);
+
+// Precision mode, reductions and energy (nb_precision.cu)
+int comp_split(const double4 *pin, const double4 *vin, double4 *pos64, float4 *pos32,
+               float4 *vhi, float4 *vlo, int n, cudaStream_t s);
+int comp_join(const double4 *pos64, const float4 *vhi, const float4 *vlo, double4 *pout,
+              double4 *vout, int n, cudaStream_t s);
+// Sum the partial slots into bare accelerations with the potential over
+// j != i in w (out32 for plain slots, out64 = hi + lo for compensated ones).
+int fast_reduce(const SkPlan &p, const float4 *partial, int comp, const float4 *pos32, float eps2,
+                float4 *out32, double4 *out64, cudaStream_t s);
+int comp_integrate(const SkPlan &p, const float4 *partial, double4 *pos64, float4 *pos32,
+                   float4 *vhi, float4 *vlo, float damping, float dt, double dt64, int kick,
+                   float G, cudaStream_t s);
+int energy_blocks(int n);
+int energy_reduce(int n, const float4 *pos32, const double4 *pos64, const float4 *vel32,
+                  const float4 *vlo, const float4 *phi32, const double4 *phi64, double G,
+                  double *block_tmp, double *out_dev, cudaStream_t s);
+
+// Adjoint kernels (nb_adjoint.cu)
+int adj_plan(int n, int block, int bpt, int device, SkPlan *pl);
+int adj_g(int n, const float4 *pos, const float4 *lx, const float4 *lv, float4 *gbuf, float damping,
+          float dt, int kick, float G, cudaStream_t s);
+int adj_vjp(const SkPlan &p, const float4 *pos, const float4 *gbuf, float eps2, float4 *partial,
+            cudaStream_t s);
+int adj_update(const SkPlan &p, const float4 *partial, const float4 *pos_prev, const float4 *acc,
+               float4 *lx, float4 *lv, float *gm, float4 *gbuf, float damping, float dt, int kick,
+               float G, int want_next_g, cudaStream_t s);
 
 // Exact-path entry points (nb_exact.cu)
 int exact_step_f32(int n, const float4 *pos_old, float4 *pos_new, float4 *vel, float eps2,

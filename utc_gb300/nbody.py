@@ -51,7 +51,9 @@ class NBodySystem:
         p.block, p.bpt, p.ctas_per_sm, p.memtype = int(block), int(bpt), int(ctas_per_sm), int(memtype)
         self.params = p
         self.n = int(n)
-        self.dtype = np.float64 if precision == "f64" else np.float32
+        self.precision = precision
+        # host-side state type: double4 for f64 and for the compensated mode
+        self.dtype = np.float64 if precision in ("f64", "f32comp") else np.float32
         h = C.c_void_p()
         N.check(self.lib.nb_create(C.byref(p), C.byref(h)), "nb_create")
         self.handle = h
@@ -127,6 +129,49 @@ class NBodySystem:
         torch.cuda.current_stream().synchronize()
         return out[: self.n, :3].cpu().numpy()
 
+    def energy(self, with_bodies=False, stream=None):
+        """(kinetic, potential, px, py, pz) reduced in FP64 on the GPU; with
+        with_bodies, also the per-body (acc xyz, potential over j != i) (n, 4)."""
+        torch = _torch()
+        out = (C.c_double * 5)()
+        s = current_stream_handle() if stream is None else stream
+        buf = None
+        if with_bodies:
+            tdt = torch.float64 if self.precision == "f32comp" else torch.float32
+            buf = torch.zeros((max(self.n, 1), 4), dtype=tdt, device="cuda")
+        N.check(self.lib.nb_energy(self.handle, out, C.c_void_p(buf.data_ptr() if buf is not None else 0),
+                                   C.c_void_p(s)), "nb_energy")
+        e = np.array(list(out))
+        if with_bodies:
+            torch.cuda.current_stream().synchronize()
+            return e, buf[: self.n].cpu().numpy()
+        return e
+
+    def adj_forward(self, steps, ckpt_every, stream=None):
+        """Advance `steps` steps keeping a checkpoint every `ckpt_every` steps."""
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_adj_forward(self.handle, int(steps), int(ckpt_every), C.c_void_p(s)),
+                "nb_adj_forward")
+
+    def adj_backward(self, gx_T, gv_T=None, stream=None):
+        """Cotangents of the final (n,4) positions / velocities (torch CUDA
+        float32; gv_T may be None) -> (dL/dx0 (n,4), dL/dv0 (n,4), dL/dm (n,))."""
+        torch = _torch()
+        gx0 = torch.zeros((self.n, 4), dtype=torch.float32, device="cuda")
+        gv0 = torch.zeros((self.n, 4), dtype=torch.float32, device="cuda")
+        gm = torch.zeros((self.n,), dtype=torch.float32, device="cuda")
+        s = current_stream_handle() if stream is None else stream
+        gx_T = gx_T.contiguous()
+        gv_ptr = C.c_void_p(gv_T.contiguous().data_ptr()) if gv_T is not None else C.c_void_p(0)
+        keep = gv_T.contiguous() if gv_T is not None else None
+        if keep is not None:
+            gv_ptr = C.c_void_p(keep.data_ptr())
+        N.check(self.lib.nb_adj_backward(self.handle, C.c_void_p(gx_T.data_ptr()), gv_ptr,
+                                         C.c_void_p(gx0.data_ptr()), C.c_void_p(gv0.data_ptr()),
+                                         C.c_void_p(gm.data_ptr()), C.c_void_p(s)),
+                "nb_adj_backward")
+        return gx0, gv0, gm
+
     def run_host(self, pos, vel, loops, out_interval, stream=None):
         """Task-style run with host buffers; returns (frames (k, n, 4), timings[4])."""
         pos = np.ascontiguousarray(pos, dtype=self.dtype)
@@ -162,3 +207,96 @@ def probe_fma_peak(iters=20000, packed=True, stream=None):
     N.check(N.lib().nb_probe_fma_peak(int(iters), int(bool(packed)), C.byref(flops), C.byref(ms),
                                       C.c_void_p(s)), "nb_probe_fma_peak")
     return flops.value / (ms.value * 1e-3), ms.value
+
+
+class NBodyBatch:
+    """Many independent systems (sizes[s] bodies each) in one context; state
+    arrays are the systems' (n, 4) float32 arrays concatenated."""
+
+    def __init__(self, sizes, kick="physical", eps2=1e-3, damping=1.0, dt=1e-3, G=1.0,
+                 warps_per_cta=0, bodies_per_lane=0):
+        self.lib = N.lib()
+        p = N.NbParams()
+        self.lib.nb_params_default(C.byref(p))
+        p.kick = _KICK[kick]
+        p.eps2, p.damping, p.dt, p.G = float(eps2), float(damping), float(dt), float(G)
+        p.block = int(warps_per_cta) * 32
+        p.bpt = int(bodies_per_lane)
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+        self.nbody = int(self.sizes.sum())
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
+        h = C.c_void_p()
+        N.check(self.lib.nb_batch_create(C.byref(p), len(self.sizes),
+                                         self.sizes.ctypes.data_as(C.c_void_p), C.byref(h)),
+                "nb_batch_create")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.nb_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_state(self, pos, vel, stream=None):
+        s = current_stream_handle() if stream is None else stream
+        if _is_torch(pos):
+            N.check(self.lib.nb_batch_set_state(self.handle, C.c_void_p(pos.data_ptr()),
+                                                C.c_void_p(vel.data_ptr()), N.NB_DEVICE, C.c_void_p(s)),
+                    "nb_batch_set_state")
+            return
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(self.nbody, 4)
+        vel = np.ascontiguousarray(vel, dtype=np.float32).reshape(self.nbody, 4)
+        N.check(self.lib.nb_batch_set_state(self.handle, pos.ctypes.data_as(C.c_void_p),
+                                            vel.ctypes.data_as(C.c_void_p), N.NB_HOST, C.c_void_p(s)),
+                "nb_batch_set_state")
+
+    def get_state(self, stream=None):
+        pos = np.empty((self.nbody, 4), np.float32)
+        vel = np.empty((self.nbody, 4), np.float32)
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_batch_get_state(self.handle, pos.ctypes.data_as(C.c_void_p),
+                                            vel.ctypes.data_as(C.c_void_p), N.NB_HOST, C.c_void_p(s)),
+                "nb_batch_get_state")
+        return pos, vel
+
+    def step(self, steps=1, stream=None):
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_batch_step(self.handle, int(steps), C.c_void_p(s)), "nb_batch_step")
+
+    def run(self, steps, stream):
+        """`steps` steps as one CUDA graph on a non-default stream handle."""
+        N.check(self.lib.nb_batch_run(self.handle, int(steps), C.c_void_p(stream)), "nb_batch_run")
+
+    def step_per_system(self, steps=1, stream=None):
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_batch_step_per_system(self.handle, int(steps), C.c_void_p(s)),
+                "nb_batch_step_per_system")
+
+    def autotune(self, reps=2, cache_path=None, stream=None):
+        s = current_stream_handle() if stream is None else stream
+        out = (C.c_int * 2)()
+        N.check(self.lib.nb_batch_autotune(self.handle, int(reps),
+                                           cache_path.encode() if cache_path else None,
+                                           C.c_void_p(s), out), "nb_batch_autotune")
+        return int(out[0]), int(out[1])
+
+    def set_shape(self, warps_per_cta, bodies_per_lane):
+        N.check(self.lib.nb_batch_set_shape(self.handle, int(warps_per_cta), int(bodies_per_lane)),
+                "nb_batch_set_shape")
+
+    def plan_info(self):
+        info = (C.c_longlong * 6)()
+        N.check(self.lib.nb_batch_plan_info(self.handle, info), "nb_batch_plan_info")
+        return dict(zip(["warps_per_cta", "bodies_per_lane", "grid", "workers", "iterations", "slots"],
+                        list(info)))
