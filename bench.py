@@ -223,7 +223,7 @@ def run_ours(args):
     vel_d = torch.from_numpy(vel).to(dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    sysm = NBodySystem(N_BODIES, "f32", "fast", kick="physical", eps2=EPS2, damping=1.0, dt=DT, G=1.0)
+    sysm = NBodySystem(N_BODIES, "f32", args.algo, kick="physical", eps2=EPS2, damping=1.0, dt=DT, G=1.0)
     plan = sysm.plan_info()
     launches_per_leapfrog = sysm.launches_per_step()
 
@@ -323,6 +323,7 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Plummer sphere, float32)",
             "config": {"workload": WORKLOAD, "n": N_BODIES, "leapfrog_steps": LEAPFROG_STEPS,
+                       "algo": args.algo,
                        "kick": "physical (G=1)", "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "flushed between timed steps (256 MB write outside the event pair)",
                        "plan": plan},
@@ -330,13 +331,14 @@ def run_ours(args):
             "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak_tf,
                          "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak_tf,
                          "traffic": traffic.get("force_bytes_per_launch"),
-                         "kernel": "sk_force_kernel",
+                         "kernel": "sym_force_kernel" if args.algo == "sym" else "sk_force_kernel",
                          "flop_per_launch": force_flops,
                          "avg_launch_ms": force_avg_s * 1e3,
                          "peak_source": "packed-FMA probe measured in this run "
                                         "(MEASURED_PEAKS.json has no FP32 figure)",
                          "nominal_peak": nominal_tf},
-            "roofline_integrator": {"bound": "hbm", "kernel": "sk_integrate_kernel",
+            "roofline_integrator": {"bound": "hbm",
+                                    "kernel": "sym_integrate_kernel" if args.algo == "sym" else "sk_integrate_kernel",
                                     "achieved": integ_bytes / integ_avg_s / 1e9, "peak": hbm,
                                     "unit": "GB/s",
                                     "frac": (integ_bytes / integ_avg_s / 1e9) / hbm if hbm else None,
@@ -593,6 +595,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="plain", choices=["plain", "precision", "adjoint", "batched"])
+    ap.add_argument("--algo", default="fast", choices=["fast", "sym"],
+                    help="force algorithm of the plain workload")
     ap.add_argument("--n", type=int, default=0, help="body count override for extension workloads")
     args = ap.parse_args()
     args.steps_given = "--steps" in sys.argv

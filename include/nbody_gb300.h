@@ -67,7 +67,12 @@ typedef enum {
     /* IEEE arithmetic in the reference's operation order, sources summed in
      * index order: bit-identical to the reference's sequential BodySystem<T>
      * for float and double. */
-    NB_ALGO_EXACT = 1
+    NB_ALGO_EXACT = 1,
+    /* Each unordered pair evaluated once and applied to both bodies (the
+     * pair term is odd in r): 16 FP32 operations and one rsqrt per two
+     * interactions.  Same per-pair terms as NB_ALGO_FAST, different summation
+     * order; deterministic.  NB_F32 only. */
+    NB_ALGO_SYM = 2
 } nb_algo;
 
 typedef enum { NB_KICK_REFERENCE = 0, NB_KICK_PHYSICAL = 1 } nb_kick;

@@ -1,0 +1,88 @@
+"""NB_ALGO_SYM: each unordered pair evaluated once, applied to both bodies.
+
+Same tolerances as the directed fast path (tests/test_gpu_parity.py):
+accelerations per body within 2e-5 (|a| + mean|a|) of the FP64 oracle,
+positions within 1e-5 (|x| + 0.1); reruns bitwise identical.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from utc_gb300 import ics
+from utc_gb300.nbody import NBodySystem
+
+pytestmark = pytest.mark.gpu
+
+
+def close(got, want, tol=2e-5):
+    d = np.linalg.norm(np.asarray(got, np.float64) - want, axis=1)
+    w = np.linalg.norm(want, axis=1)
+    return bool((d <= tol * (w + w.mean())).all())
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 33, 255, 256, 257, 1000, 2047, 2048, 2049, 4097, 9000])
+@pytest.mark.parametrize("shape", [(256, 8), (256, 4), (128, 8)])
+def test_sym_accel_vs_fp64(cuda, n, shape):
+    p, _ = ics.plummer(n, seed=n)
+    pos = ics.f32(p)
+    with NBodySystem(n, "f32", "sym", eps2=np.float32(1e-3), block=shape[0], bpt=shape[1]) as s:
+        s.set_state(pos, np.zeros_like(pos))
+        a = s.accel()
+    assert close(a, oracle.accel(pos.astype(np.float64), float(np.float32(1e-3))))
+
+
+def test_sym_full_size_subsample_and_determinism(cuda):
+    n = 65536
+    p, v = ics.plummer(n, seed=0)
+    pos, vel = ics.f32(p), ics.f32(v)
+    outs = []
+    for _ in range(2):
+        with NBodySystem(n, "f32", "sym", kick="physical", eps2=np.float32(1e-4), damping=1.0,
+                         dt=np.float32(1e-4)) as s:
+            s.set_state(pos, vel)
+            a = s.accel()
+            s.step(20)
+            outs.append(s.get_state())
+    tidx = np.random.default_rng(3).choice(n, 512, replace=False).astype(np.int32)
+    ref = oracle.accel_subset_f64(pos.astype(np.float64), tidx, float(np.float32(1e-4)))
+    assert close(a[tidx], ref)
+    assert outs[0][0].tobytes() == outs[1][0].tobytes() and outs[0][1].tobytes() == outs[1][1].tobytes()
+
+
+@pytest.mark.parametrize("kick", ["reference", "physical"])
+def test_sym_steps_vs_oracle(cuda, kick):
+    n, steps = 4096, 10
+    p, v = ics.uniform_cube(n, seed=0)
+    pos, vel = ics.f32(p), ics.f32(v)
+    km = oracle.KICK_REFERENCE if kick == "reference" else oracle.KICK_PHYSICAL
+    with NBodySystem(n, "f32", "sym", kick=kick, eps2=np.float32(1e-2), damping=1.0,
+                     dt=np.float32(1e-3)) as s:
+        s.set_state(pos, vel)
+        s.step(steps)
+        got, _ = s.get_state()
+    want, _ = oracle.step(pos, vel, np.float32(1e-2), 1.0, np.float32(1e-3), steps, kick_mode=km)
+    d = np.linalg.norm(got[:, :3].astype(np.float64) - want[:, :3], axis=1)
+    w = np.linalg.norm(want[:, :3].astype(np.float64), axis=1)
+    assert (d <= 1e-5 * (w + 0.1)).all()
+
+
+def test_sym_adjoint_matches_directed_adjoint(cuda):
+    import torch
+
+    n, steps = 600, 12
+    p, v = ics.uniform_cube(n, seed=2)
+    y = ics.gaussian_targets(n, seed=3)
+    pos, vel = ics.f32(p), ics.f32(v)
+    grads = []
+    for algo in ("fast", "sym"):
+        with NBodySystem(n, "f32", algo, kick="physical", eps2=np.float32(1e-2), damping=1.0,
+                         dt=np.float32(1e-3)) as s:
+            s.set_state(pos, vel)
+            s.adj_forward(steps, 5)
+            pT, _ = s.get_state()
+            gx = torch.zeros((n, 4), device="cuda")
+            gx[:, :3] = torch.tensor(2 * (pT[:, :3].astype(np.float64) - y), dtype=torch.float32,
+                                     device="cuda")
+            grads.append([t.cpu().numpy() for t in s.adj_backward(gx)])
+    for a, b in zip(grads[0], grads[1]):
+        assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(b)

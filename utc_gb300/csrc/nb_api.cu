@@ -52,6 +52,9 @@ struct nb_ctx {
     void *acc_tmp = nullptr;
     double *e_blocks = nullptr;
     double *e_out = nullptr;
+    // symmetric algorithm: plan and its two partial arrays
+    nb::SymPlan splan;
+    float4 *sym_t = nullptr, *sym_s = nullptr;
     // adjoint: checkpoints of the last nb_adj_forward and reverse-pass buffers
     struct Adj {
         int steps = 0, every = 0, nckpt = 0;
@@ -77,8 +80,10 @@ static int validate(const nb_params *p)
     if (p->n < 0) return set_error(NB_ERR_INVALID, "n must be >= 0");
     if (p->precision != NB_F32 && p->precision != NB_F64 && p->precision != NB_F32_COMP)
         return set_error(NB_ERR_INVALID, "unknown precision");
-    if (p->algo != NB_ALGO_FAST && p->algo != NB_ALGO_EXACT)
+    if (p->algo != NB_ALGO_FAST && p->algo != NB_ALGO_EXACT && p->algo != NB_ALGO_SYM)
         return set_error(NB_ERR_INVALID, "unknown algo");
+    if (p->algo == NB_ALGO_SYM && p->precision != NB_F32)
+        return set_error(NB_ERR_UNSUPPORTED, "NB_ALGO_SYM runs on NB_F32 contexts");
     if (p->kick != NB_KICK_REFERENCE && p->kick != NB_KICK_PHYSICAL)
         return set_error(NB_ERR_INVALID, "unknown kick mode");
     if (p->memtype < NB_MEM_PAGEABLE || p->memtype > NB_MEM_UNIFIED)
@@ -123,6 +128,8 @@ static void free_ctx(nb_ctx *c)
     cudaFree(c->adj.gbuf);
     cudaFree(c->adj.gm);
     cudaFree(c->adj.partial);
+    cudaFree(c->sym_t);
+    cudaFree(c->sym_s);
     delete c;
 }
 
@@ -138,7 +145,13 @@ static int dalloc(nb_ctx *c, void **p, size_t bytes)
     return NB_OK;
 }
 
-static bool uses_fast(const nb_ctx *c) { return c->p.precision == NB_F32 && c->p.algo == NB_ALGO_FAST; }
+static bool uses_sym(const nb_ctx *c) { return c->p.precision == NB_F32 && c->p.algo == NB_ALGO_SYM; }
+// the directed stream-K plan (c->plan) also serves the symmetric context's
+// energy pass and adjoint
+static bool uses_fast(const nb_ctx *c)
+{
+    return c->p.precision == NB_F32 && (c->p.algo == NB_ALGO_FAST || c->p.algo == NB_ALGO_SYM);
+}
 static bool is_comp(const nb_ctx *c) { return c->p.precision == NB_F32_COMP; }
 
 static int dev_alloc(void **p, size_t bytes, const char *what)
@@ -203,8 +216,9 @@ int nb_create(const nb_params *p, nb_ctx **out)
     }
     if (uses_fast(c) || is_comp(c)) {
         const int flags = is_comp(c) ? nb::SK_COMP : 0;
-        const int block = p->block ? p->block : (is_comp(c) ? 256 : 0);
-        const int bpt = p->bpt ? p->bpt : (is_comp(c) ? 4 : 0);
+        const bool own_shape = !uses_sym(c);
+        const int block = (own_shape && p->block) ? p->block : (is_comp(c) ? 256 : 0);
+        const int bpt = (own_shape && p->bpt) ? p->bpt : (is_comp(c) ? 4 : 0);
         st = nb::fast_plan(p->n, block, bpt, p->ctas_per_sm, c->device, &c->plan, flags);
         if (!st)
             st = nb::fast_plan(p->n, 256, is_comp(c) ? 4 : 8, 0, c->device, &c->eplan,
@@ -217,6 +231,17 @@ int nb_create(const nb_params *p, nb_ctx **out)
         size_t pb = mult * (size_t)c->plan.slots * c->plan.tbsize * sizeof(float4);
         const size_t pe = mult * (size_t)c->eplan.slots * c->eplan.tbsize * sizeof(float4);
         if (pe > pb) pb = pe;
+        if (uses_sym(c)) {
+            if ((st = nb::sym_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan)) ||
+                (st = dev_alloc((void **)&c->sym_t,
+                                (size_t)c->splan.slots * c->splan.rb * sizeof(float4),
+                                "symmetric scratch allocation")) ||
+                (st = dev_alloc((void **)&c->sym_s, (size_t)c->splan.spart_size * sizeof(float4),
+                                "symmetric scratch allocation"))) {
+                free_ctx(c);
+                return st;
+            }
+        }
         if ((st = dev_alloc((void **)&c->partial, pb, "partial-sum scratch allocation")) ||
             (st = dev_alloc(&c->acc_tmp, n * sizeof(double4), "energy scratch allocation")) ||
             (st = dev_alloc((void **)&c->e_blocks,
@@ -321,6 +346,13 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
         st = nb::exact_step_f32(p.n, (const float4 *)po, (float4 *)pn, (float4 *)c->vel,
                                 (float)p.eps2, (float)p.damping, (float)p.dt, p.kick, (float)p.G,
                                 (float4 *)acc_out, p.block, s);
+    } else if (p.algo == NB_ALGO_SYM) {
+        st = nb::sym_force(c->splan, (const float4 *)po, (float)p.eps2, c->sym_t, c->sym_s, s);
+        if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
+        if (!st)
+            st = nb::sym_integrate(c->splan, (const float4 *)po, (float4 *)pn, (float4 *)c->vel,
+                                   c->sym_t, c->sym_s, (float)p.damping, (float)p.dt, p.kick,
+                                   (float)p.G, (float4 *)acc_out, s);
     } else {
         st = nb::fast_force(c->plan, (const float4 *)po, (float)p.eps2, c->partial, s);
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
@@ -330,7 +362,7 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
                                     (float4 *)acc_out, s);
     }
     if (!st && ev) {
-        if (!uses_fast(c)) NB_CUDA(cudaEventRecord(ev[1], s));
+        if (!uses_fast(c)) NB_CUDA(cudaEventRecord(ev[1], s));  // exact: one fused kernel
         NB_CUDA(cudaEventRecord(ev[2], s));
     }
     if (!st && !acc_out) c->cur ^= 1;
@@ -531,6 +563,18 @@ int nb_adj_backward(nb_ctx *c, const void *gx_T, const void *gv_T, void *gx0, vo
                                 cudaMemcpyDeviceToDevice, s));
         for (int k = 0; k < len; ++k) {
             const float4 *xk = A.seg_pos + (size_t)k * n;
+            if (uses_sym(c)) {
+                // recompute with the algorithm of the forward pass: same bits
+                if ((st = nb::sym_force(c->splan, xk, eps2, c->sym_t, c->sym_s, s))) return st;
+                if (p.kick == NB_KICK_REFERENCE &&
+                    (st = nb::sym_integrate(c->splan, xk, nullptr, nullptr, c->sym_t, c->sym_s, D,
+                                            dt, p.kick, G, A.seg_acc + (size_t)k * n, s)))
+                    return st;
+                if ((st = nb::sym_integrate(c->splan, xk, A.seg_pos + (size_t)(k + 1) * n, A.vel_tmp,
+                                            c->sym_t, c->sym_s, D, dt, p.kick, G, nullptr, s)))
+                    return st;
+                continue;
+            }
             if ((st = nb::fast_force(c->plan, xk, eps2, c->partial, s))) return st;
             if (p.kick == NB_KICK_REFERENCE &&
                 (st = nb::fast_reduce(c->plan, c->partial, 0, xk, eps2, A.seg_acc + (size_t)k * n,
@@ -570,6 +614,14 @@ int nb_launches_per_step(nb_ctx *c)
 int nb_plan_info(nb_ctx *c, int *info5)
 {
     if (!c || !info5) return set_error(NB_ERR_INVALID, "ctx/info is NULL");
+    if (uses_sym(c)) {
+        info5[0] = c->splan.warps * 32;
+        info5[1] = c->splan.bpt;
+        info5[2] = c->splan.grid;
+        info5[3] = c->splan.rb;
+        info5[4] = c->splan.slots;
+        return NB_OK;
+    }
     info5[0] = c->plan.block;
     info5[1] = c->plan.bpt;
     info5[2] = c->plan.grid;

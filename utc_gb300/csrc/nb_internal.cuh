@@ -145,6 +145,24 @@ int energy_reduce(int n, const float4 *pos32, const double4 *pos64, const float4
                   const float4 *vlo, const float4 *phi32, const double4 *phi64, double G,
                   double *block_tmp, double *out_dev, cudaStream_t s);
 
+// Symmetric force kernel (nb_sym.cu)
+struct SymPlan {
+    int n = 0, warps = 0, bpt = 0;
+    int rb = 0;          // bodies per row block (CTA targets)
+    int nc = 0;          // 32-body chunks
+    int nrb = 0;         // row blocks
+    long long total = 0; // (row, chunk) items
+    int grid = 0;
+    int slots = 0;       // grid + nrb - 1 target-side slots of rb float4
+    long long spart_size = 0;  // float4 entries of the source-side array
+};
+int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl);
+int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, float4 *spart,
+              cudaStream_t s);
+int sym_integrate(const SymPlan &p, const float4 *pos_old, float4 *pos_new, float4 *vel,
+                  const float4 *tpart, const float4 *spart, float damping, float dt, int kick,
+                  float G, float4 *acc_out, cudaStream_t s);
+
 // Adjoint kernels (nb_adjoint.cu)
 int adj_plan(int n, int block, int bpt, int device, SkPlan *pl);
 int adj_g(int n, const float4 *pos, const float4 *lx, const float4 *lv, float4 *gbuf, float damping,

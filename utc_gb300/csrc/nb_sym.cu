@@ -1,0 +1,280 @@
+// nb_sym.cu -- symmetric all-pairs force kernel (each unordered pair once).
+//
+// The reference evaluates every ordered pair (i, j) separately
+// (benchapps/nbody/cuda/bodysystem_kernel.cu:60-85).  The pair term is odd in
+// r, so the contribution of j to i and of i to j share r, d2, 1/sqrt(d2) and
+// inv^3: evaluating the pair once and applying it to both bodies costs 16
+// FP32 operations and one rsqrt for two interactions instead of 24 and two.
+// The individual terms are the same numbers as in the directed evaluation;
+// only the order in which each body's terms are summed changes.
+//
+// Layout of the work:
+//  * bodies are cut into row blocks of RB = W*32*BPT; a CTA of W warps owns a
+//    row block's targets (each lane BPT of them, in registers);
+//  * the columns are 32-body chunks; row I is paired with every chunk at or
+//    after its own start.  Chunks inside row I are evaluated directed (target
+//    side only: both orders of each pair occur there); chunks after row I are
+//    evaluated symmetrically;
+//  * in a symmetric chunk the 32 bodies sit in shared memory and rotate
+//    through the warp: at step r lane l pairs its targets with chunk body
+//    (l + r) mod 32 and carries that body's accumulated reaction, passing it
+//    to lane l - 1 with one shuffle per component, so after 32 steps lane l
+//    holds the reaction on chunk body l from the warp's targets; the W warps'
+//    reactions are summed in warp order through shared memory and stored in
+//    the source-side array spart (row I, body), a triangular layout;
+//  * (row, chunk) items are split stream-K over persistent CTAs; target-side
+//    partials go to slot cta + row as in the directed kernel.
+// The integrate kernel adds, per body, its target-side slots (CTA order) and
+// its source-side entries spart[0..I_b-1][b] (row order): deterministic.
+#include "nb_internal.cuh"
+
+namespace nb {
+
+__host__ __device__ __forceinline__ long long sym_prefix(long long I, int nc, int rc)
+{
+    // items of rows 0..I-1: row i pairs with chunks i*rc .. nc-1
+    return I * (long long)nc - (long long)rc * (I * (I - 1) / 2);
+}
+
+// Source-side array, triangular: row r keeps bodies i >= (r + 1) * rb at
+// soff(r) + i - (r + 1) * rb.
+__host__ __device__ __forceinline__ long long sym_soff(long long r, int n, int rb)
+{
+    return r * (long long)n - (long long)rb * (r * (r + 1) / 2);
+}
+
+__device__ __forceinline__ int sym_row_of(long long it, int nc, int rc, int nrb)
+{
+    int lo = 0, hi = nrb;  // prefix(lo) <= it < prefix(hi)
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (sym_prefix(mid, nc, rc) <= it) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int W, int BPT>
+__global__ void __launch_bounds__(32 * W) sym_force_kernel(const float4 *__restrict__ pos, int n,
+                                                           float eps2, float4 *__restrict__ tpart,
+                                                           float4 *__restrict__ spart,
+                                                           long long total, int nc, int nrb)
+{
+    constexpr int WB = 32 * BPT;
+    constexpr int RB = W * WB;
+    constexpr int RC = RB / 32;
+    __shared__ __align__(16) float4 sC[32];
+    __shared__ float sF[3][W][32];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const int c = blockIdx.x;
+    long long it = sk_start(c, total, gridDim.x);
+    const long long end = sk_start(c + 1, total, gridDim.x);
+    const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
+
+    while (it < end) {
+        const int I = sym_row_of(it, nc, RC, nrb);
+        const long long rfirst = sym_prefix(I, nc, RC);
+        const long long rend = sym_prefix(I + 1, nc, RC);
+        const long long seg_end = end < rend ? end : rend;
+        const int kc0 = I * RC + (int)(it - rfirst);
+        const int kc1 = I * RC + (int)(seg_end - rfirst);
+        const int tbase = I * RB + wid * WB;
+
+        float px[BPT], py[BPT], pz[BPT], pm[BPT], ax[BPT], ay[BPT], az[BPT];
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const int i = tbase + lane + 32 * k;
+            // missing targets get zero mass: their reactions on the chunk are 0
+            const float4 q = i < n ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            px[k] = q.x;
+            py[k] = q.y;
+            pz[k] = q.z;
+            pm[k] = q.w;
+            ax[k] = ay[k] = az[k] = 0.f;
+        }
+        for (int kc = kc0; kc < kc1; ++kc) {
+            const int jb = kc * 32;
+            __syncthreads();  // previous chunk: sC reads and sF reads are done
+            if (wid == 0) sC[lane] = (jb + lane < n) ? pos[jb + lane] : pad;
+            __syncthreads();
+            if (kc < (I + 1) * RC) {
+                // chunk inside the own row block: directed, target side only
+#pragma unroll 4
+                for (int j = 0; j < 32; ++j) {
+                    const float4 q = sC[j];
+#pragma unroll
+                    for (int k = 0; k < BPT; ++k) {
+                        const float rx = q.x - px[k], ry = q.y - py[k], rz = q.z - pz[k];
+                        float d2 = fmaf(rx, rx, eps2);
+                        d2 = fmaf(ry, ry, d2);
+                        d2 = fmaf(rz, rz, d2);
+                        const float inv = rsqrt_approx(d2);
+                        const float s = (q.w * inv) * (inv * inv);
+                        ax[k] = fmaf(rx, s, ax[k]);
+                        ay[k] = fmaf(ry, s, ay[k]);
+                        az[k] = fmaf(rz, s, az[k]);
+                    }
+                }
+            } else {
+                float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll 2
+                for (int r = 0; r < 32; ++r) {
+                    const float4 q = sC[(lane + r) & 31];
+#pragma unroll
+                    for (int k = 0; k < BPT; ++k) {
+                        const float rx = q.x - px[k], ry = q.y - py[k], rz = q.z - pz[k];
+                        float d2 = fmaf(rx, rx, eps2);
+                        d2 = fmaf(ry, ry, d2);
+                        d2 = fmaf(rz, rz, d2);
+                        const float inv = rsqrt_approx(d2);
+                        const float inv3 = inv * (inv * inv);
+                        const float st = q.w * inv3;    // on the target, from the chunk body
+                        const float ss = pm[k] * inv3;  // on the chunk body, from the target
+                        ax[k] = fmaf(rx, st, ax[k]);
+                        ay[k] = fmaf(ry, st, ay[k]);
+                        az[k] = fmaf(rz, st, az[k]);
+                        fx = fmaf(-rx, ss, fx);
+                        fy = fmaf(-ry, ss, fy);
+                        fz = fmaf(-rz, ss, fz);
+                    }
+                    const int from = (lane + 1) & 31;
+                    fx = __shfl_sync(0xffffffffu, fx, from);
+                    fy = __shfl_sync(0xffffffffu, fy, from);
+                    fz = __shfl_sync(0xffffffffu, fz, from);
+                }
+                // lane l now holds the reaction on chunk body l from this warp
+                sF[0][wid][lane] = fx;
+                sF[1][wid][lane] = fy;
+                sF[2][wid][lane] = fz;
+                __syncthreads();
+                if (wid == 0 && jb + lane < n) {
+                    float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+                    for (int w = 0; w < W; ++w) {
+                        sx += sF[0][w][lane];
+                        sy += sF[1][w][lane];
+                        sz += sF[2][w][lane];
+                    }
+                    spart[sym_soff(I, n, RB) + (jb + lane - (I + 1) * RB)] = make_float4(sx, sy, sz, 0.f);
+                }
+            }
+        }
+        float4 *dst = tpart + (size_t)(c + I) * RB + wid * WB;
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) dst[lane + 32 * k] = make_float4(ax[k], ay[k], az[k], 0.f);
+        it = seg_end;
+    }
+}
+
+// Per body: target-side slots (CTA order) + source-side rows 0..I_b-1 (row
+// order), then the reference's kick / damping / drift (unfused, its order).
+__global__ void sym_integrate_kernel(const float4 *__restrict__ pos_old, float4 *__restrict__ pos_new,
+                                     float4 *__restrict__ vel, const float4 *__restrict__ tpart,
+                                     const float4 *__restrict__ spart, int n, int rb, int nc,
+                                     int nrb, long long total, int grid, float damping, float dt,
+                                     int kick, float G, float4 *__restrict__ acc_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int rc = rb / 32;
+    const int I = i / rb;
+    const long long first = sym_prefix(I, nc, rc);
+    const long long last = sym_prefix(I + 1, nc, rc) - 1;
+    const int c0 = sk_owner(first, total, grid);
+    const int c1 = sk_owner(last, total, grid);
+    const int li = i - I * rb;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    for (int c = c0; c <= c1; ++c) {
+        const float4 q = tpart[(size_t)(c + I) * rb + li];
+        ax = __fadd_rn(ax, q.x);
+        ay = __fadd_rn(ay, q.y);
+        az = __fadd_rn(az, q.z);
+    }
+    for (int r = 0; r < I; ++r) {
+        const float4 q = spart[sym_soff(r, n, rb) + (i - (r + 1) * rb)];
+        ax = __fadd_rn(ax, q.x);
+        ay = __fadd_rn(ay, q.y);
+        az = __fadd_rn(az, q.z);
+    }
+    if (acc_out) {
+        acc_out[i] = make_float4(ax, ay, az, 0.f);
+        return;
+    }
+    float4 p = pos_old[i];
+    float4 v = vel[i];
+    const float k = kick == NB_KICK_REFERENCE ? p.w : G;
+    v.x = __fadd_rn(v.x, __fmul_rn(__fmul_rn(ax, k), dt));
+    v.y = __fadd_rn(v.y, __fmul_rn(__fmul_rn(ay, k), dt));
+    v.z = __fadd_rn(v.z, __fmul_rn(__fmul_rn(az, k), dt));
+    v.x = __fmul_rn(v.x, damping);
+    v.y = __fmul_rn(v.y, damping);
+    v.z = __fmul_rn(v.z, damping);
+    p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
+    p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+    p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+    pos_new[i] = p;
+    vel[i] = v;
+}
+
+typedef void (*sym_kernel_t)(const float4 *, int, float, float4 *, float4 *, long long, int, int);
+
+static sym_kernel_t sym_kernel_for(int w, int bpt)
+{
+    if (w == 4 && bpt == 8) return sym_force_kernel<4, 8>;
+    if (w == 8 && bpt == 4) return sym_force_kernel<8, 4>;
+    if (w == 8 && bpt == 8) return sym_force_kernel<8, 8>;
+    return nullptr;
+}
+
+int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl)
+{
+    if (warps == 0) warps = 8;
+    if (bpt == 0) bpt = 8;
+    sym_kernel_t k = sym_kernel_for(warps, bpt);
+    if (!k) return set_error(NB_ERR_UNSUPPORTED, "symmetric kernel shape not compiled");
+    SymPlan p;
+    p.n = n;
+    p.warps = warps;
+    p.bpt = bpt;
+    p.rb = warps * 32 * bpt;
+    p.nc = (n + 31) / 32;
+    p.nrb = (n + p.rb - 1) / p.rb;
+    p.total = n > 0 ? sym_prefix(p.nrb, p.nc, p.rb / 32) : 0;
+    int sms = 0, occ = 0;
+    NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * warps, 0));
+    if (occ < 1) return set_error(NB_ERR_UNSUPPORTED, "symmetric kernel does not fit on an SM");
+    long long grid = (long long)sms * occ;
+    if (p.total > 0 && grid > p.total) grid = p.total;
+    p.grid = p.total > 0 ? (int)grid : 0;
+    p.slots = p.total > 0 ? p.grid + p.nrb - 1 : 0;
+    p.spart_size = p.nrb > 1 ? sym_soff(p.nrb - 1, n, p.rb) : 0;
+    *pl = p;
+    return NB_OK;
+}
+
+int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, float4 *spart,
+              cudaStream_t s)
+{
+    if (p.total == 0) return NB_OK;
+    sym_kernel_t k = sym_kernel_for(p.warps, p.bpt);
+    if (!k) return set_error(NB_ERR_UNSUPPORTED, "symmetric kernel shape not compiled");
+    k<<<p.grid, 32 * p.warps, 0, s>>>(pos, p.n, eps2, tpart, spart, p.total, p.nc, p.nrb);
+    NB_LAUNCH_CHECK("sym_force_kernel launch");
+    return NB_OK;
+}
+
+int sym_integrate(const SymPlan &p, const float4 *pos_old, float4 *pos_new, float4 *vel,
+                  const float4 *tpart, const float4 *spart, float damping, float dt, int kick,
+                  float G, float4 *acc_out, cudaStream_t s)
+{
+    if (p.n == 0) return NB_OK;
+    sym_integrate_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(pos_old, pos_new, vel, tpart, spart, p.n,
+                                                           p.rb, p.nc, p.nrb, p.total, p.grid,
+                                                           damping, dt, kick, G, acc_out);
+    NB_LAUNCH_CHECK("sym_integrate_kernel launch");
+    return NB_OK;
+}
+
+}  // namespace nb
