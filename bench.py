@@ -574,14 +574,26 @@ def run_batched(args):
         t_launch = timed(lambda: b.step(steps, sh), 3)
         t_base = timed(lambda: b.step_per_system(steps, sh), 2)
         pr, _ = b.get_state(stream=sh)
+        ntasks = min(16, os.cpu_count() or 1)
+        b.set_state(pos, vel, stream=sh)
+        stream.synchronize()
+        t0 = time.perf_counter()
+        b.step_tasks(steps, ntasks)
+        t_tasks = (time.perf_counter() - t0) * 1e3
+        pt, _ = b.get_state(stream=sh)
     d = np.linalg.norm(pb[:, :3].astype(np.float64) - pr[:, :3], axis=1)
     w = np.linalg.norm(pr[:, :3].astype(np.float64), axis=1)
     out.update({
         "ms_batched_graph": t_graph, "ms_batched_launches": t_launch, "ms_per_system_launches": t_base,
         "speedup_vs_per_system": t_base / t_graph,
+        "ms_per_system_tasks": t_tasks, "tasks": ntasks,
+        "speedup_vs_per_system_tasks": t_tasks / t_graph,
+        "tasks_note": "reference multi-task pattern: one host thread + stream per task, "
+                      "stream synchronise after every system step (nbody_mtask.cc, body_task_sgpu.cu)",
         "G_interactions_per_s_batched": pairs * steps / (t_graph * 1e-3) / 1e9,
         "G_interactions_per_s_per_system": pairs * steps / (t_base * 1e-3) / 1e9,
         "final_pos_rel_diff_max_vs_per_system": float((d / (w + 0.1)).max()),
+        "tasks_equal_per_system_bitwise": bool(pt.tobytes() == pr.tobytes()),
     })
     print(json.dumps(out), flush=True)
     return 0
@@ -595,7 +607,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="plain", choices=["plain", "precision", "adjoint", "batched"])
-    ap.add_argument("--algo", default="fast", choices=["fast", "sym"],
+    ap.add_argument("--algo", default="sym", choices=["fast", "sym"],
                     help="force algorithm of the plain workload")
     ap.add_argument("--n", type=int, default=0, help="body count override for extension workloads")
     args = ap.parse_args()

@@ -157,8 +157,12 @@ int nb_adj_backward(nb_ctx *ctx, const void *gx_T, const void *gv_T, void *gx0, 
  * (body_task_sgpu.cu:40-137): copy pos/vel in, run `loops` steps, and after
  * every out_interval-th step copy the positions to
  * outbuffer + (step/out_interval - 1) * 4n.  pos/vel are not modified.
+ * Unlike the reference (which synchronises the stream after every step and
+ * copies each frame synchronously), frames are snapshotted on the GPU and
+ * copied to pinned staging on a second stream while the next steps run.
  * timings (may be NULL) receives {total, kernel, copyin, copyout} seconds,
- * the reference's runtime[4].  Synchronises `stream` before returning. */
+ * the reference's runtime[4] (copyout: device time of the frame copies,
+ * which overlap the kernels).  Synchronises `stream` before returning. */
 int nb_run_host(nb_ctx *ctx, const void *pos, const void *vel, int loops,
                 int out_interval, void *outbuffer, double *timings, void *stream);
 
@@ -210,6 +214,17 @@ int nb_batch_launches_per_step(nb_batch *b);
 /* Baseline: each system stepped by its own plain launches (force +
  * integrate per system per step), as separate per-system tasks would. */
 int nb_batch_step_per_system(nb_batch *b, int steps, void *stream);
+/* Baseline in the reference's multi-task pattern (benchapps/nbody/utc/
+ * nbody_mtask.cc:199-231): ntasks host threads with a stream each run their
+ * systems with a stream synchronise after every step (as
+ * BodySystemSGPU::runImpl does).  Synchronous. */
+int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks);
+/* Adjoint of `steps` batched steps, same contract as nb_adj_forward /
+ * nb_adj_backward over the concatenated bodies of all systems (no
+ * counterpart in the reference). */
+int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream);
+int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void *gx0, void *gv0,
+                          void *gm, void *stream);
 
 /* Device pointers of the current state (valid until the next nb_step). */
 int nb_state_ptrs(nb_ctx *ctx, void **pos_dev, void **vel_dev);

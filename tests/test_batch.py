@@ -132,3 +132,49 @@ def test_autotune_and_cache(cuda, tmp_path):
         b2.step(2)
         again, _ = b2.get_state()
     assert tuned.tobytes() == again.tobytes()
+
+
+@pytest.mark.parametrize("kick", ["physical", "reference"])
+def test_batched_adjoint_matches_per_system_adjoint(cuda, kick):
+    import torch
+
+    sizes = [1, 40, 300, 129, 1000]
+    steps, every = 12, 5
+    ps, vs, ys = [], [], []
+    for k, n in enumerate(sizes):
+        p, v = ics.uniform_cube(n, seed=20 + k)
+        if kick == "reference":
+            p[:, 3] *= n
+        ps.append(ics.f32(p))
+        vs.append(ics.f32(v))
+        ys.append(ics.gaussian_targets(n, seed=40 + k))
+    pos, vel, y = np.concatenate(ps), np.concatenate(vs), np.concatenate(ys)
+    eps2, dt = np.float32(1e-2), np.float32(1e-3)
+    with NBodyBatch(sizes, kick=kick, eps2=eps2, dt=dt) as b:
+        b.set_state(pos, vel)
+        b.adj_forward(steps, every)
+        pT, _ = b.get_state()
+        gx = torch.zeros((b.nbody, 4), device="cuda")
+        gx[:, :3] = torch.tensor(2 * (pT[:, :3].astype(np.float64) - y), dtype=torch.float32, device="cuda")
+        bx, bv, bm = [t.cpu().numpy() for t in b.adj_backward(gx)]
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    for k, n in enumerate(sizes):
+        sl = slice(off[k], off[k + 1])
+        L, rx, rv, rm = oracle.adjoint(ps[k].astype(np.float64), vs[k].astype(np.float64), ys[k],
+                                       float(eps2), 1.0, float(dt), steps,
+                                       kick_mode=oracle.KICK_PHYSICAL if kick == "physical" else oracle.KICK_REFERENCE)
+        for got, want in ((bx[sl, :3], rx), (bv[sl, :3], rv), (bm[sl], rm)):
+            assert np.linalg.norm(got - want) <= 1e-4 * np.linalg.norm(want) + 1e-12
+
+
+def test_task_pattern_baseline_equals_per_system(cuda):
+    sizes = [64, 1000, 3, 4096, 77, 500]
+    pos, vel = make_batch(sizes, seed=9)
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b:
+        b.set_state(pos, vel)
+        b.step_per_system(3)
+        want, _ = b.get_state()
+        b.set_state(pos, vel)
+        b.step_tasks(3, 4)
+        got, _ = b.get_state()
+    assert got.tobytes() == want.tobytes()

@@ -239,7 +239,7 @@ def test_drop_in_task_f32(cuda, memtype):
                                   np.float32(dt), out.ctypes.data_as(C.c_void_p), memtype, -1, 0)
     assert rc == 0
     assert p_in.tobytes() == pos.tobytes()  # the task does not write its inputs
-    with NBodySystem(n, "f32", "fast", eps2=eps2, damping=damp, dt=dt) as s:
+    with NBodySystem(n, "f32", "sym", eps2=eps2, damping=damp, dt=dt) as s:
         frames, _ = s.run_host(pos, vel, loops, oi)
     assert out.tobytes() == frames.tobytes()
     assert rt[0] > 0 and rt[1] > 0

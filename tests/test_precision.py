@@ -115,3 +115,18 @@ def test_energy_conserved_by_small_steps(cuda):
         e1 = s.energy()
     E0, E1 = e0[0] + e0[1], e1[0] + e1[1]
     assert abs(E1 - E0) <= 1e-5 * abs(E0)
+
+
+def test_compensated_run_host_frames(cuda):
+    n = 1500
+    p, v = ics.plummer(n, seed=12)
+    with NBodySystem(n, "f32comp", "fast", kick="physical", eps2=1e-3, damping=1.0, dt=1e-3) as s:
+        frames, t = s.run_host(p, v, 9, 2)
+        s.set_state(p, v)
+        want = []
+        for _ in range(4):
+            s.step(2)
+            want.append(s.get_state()[0])
+    assert frames.shape == (4, n, 4) and frames.dtype == np.float64
+    for k in range(4):
+        assert frames[k].tobytes() == want[k].tobytes()

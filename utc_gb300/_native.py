@@ -74,6 +74,9 @@ def _declare(lib):
         "nb_batch_plan_info": (I, [vp, P(C.c_longlong)]),
         "nb_batch_launches_per_step": (I, [vp]),
         "nb_batch_step_per_system": (I, [vp, I, vp]),
+        "nb_batch_adj_forward": (I, [vp, I, I, vp]),
+        "nb_batch_step_tasks": (I, [vp, I, I]),
+        "nb_batch_adj_backward": (I, [vp, vp, vp, vp, vp, vp, vp]),
         "nb_last_error": (C.c_char_p, []),
         "nb_abi_version": (I, []),
     }

@@ -40,7 +40,14 @@ struct nb_ctx {
     void *stage_pos = nullptr;  // pinned staging (NB_MEM_PINNED run_host)
     void *stage_vel = nullptr;
     void *stage_out = nullptr;
-    std::vector<cudaEvent_t> events;  // pool for nb_step_timed
+    std::vector<cudaEvent_t> events;  // pool for nb_step_timed and nb_run_host
+    // frame output of nb_run_host: device snapshots copied to pinned staging
+    // on their own stream while the next steps run
+    cudaStream_t copy_stream = nullptr;
+    void *snap[2] = {nullptr, nullptr};
+    void *stage[2] = {nullptr, nullptr};
+    cudaEvent_t ev_snap[2] = {nullptr, nullptr}, ev_c0[2] = {nullptr, nullptr},
+                ev_c1[2] = {nullptr, nullptr};
     // NB_F32_COMP state (pos[0] holds the double4 positions, vel the FP32
     // velocity high parts)
     float4 *pos32 = nullptr;
@@ -130,6 +137,14 @@ static void free_ctx(nb_ctx *c)
     cudaFree(c->adj.partial);
     cudaFree(c->sym_t);
     cudaFree(c->sym_s);
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(c->snap[k]);
+        cudaFreeHost(c->stage[k]);
+        if (c->ev_snap[k]) cudaEventDestroy(c->ev_snap[k]);
+        if (c->ev_c0[k]) cudaEventDestroy(c->ev_c0[k]);
+        if (c->ev_c1[k]) cudaEventDestroy(c->ev_c1[k]);
+    }
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     delete c;
 }
 
@@ -648,13 +663,13 @@ int nb_run_host(nb_ctx *c, const void *pos, const void *vel, int loops, int out_
         NB_CUDA(cudaMallocHost(&c->stage_vel, sb));
         NB_CUDA(cudaMallocHost(&c->stage_out, sb));
     }
-    cudaEvent_t ev[4];
-    for (int k = 0; k < 4; ++k) NB_CUDA(cudaEventCreate(&ev[k]));
+    cudaEvent_t ev[2];
+    for (int k = 0; k < 2; ++k) NB_CUDA(cudaEventCreate(&ev[k]));
     struct Guard {
         cudaEvent_t *e;
         ~Guard()
         {
-            for (int k = 0; k < 4; ++k) cudaEventDestroy(e[k]);
+            for (int k = 0; k < 2; ++k) cudaEventDestroy(e[k]);
         }
     } guard{ev};
 
@@ -674,31 +689,69 @@ int nb_run_host(nb_ctx *c, const void *pos, const void *vel, int loops, int out_
     NB_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
     copyin = ms * 1e-3;
 
-    // step loop with frame copy-out every out_interval steps
-    int done = 0;
+    // frames: snapshot on the compute stream, D2H on the copy stream
+    const int frames = loops / out_interval;
+    if (frames > 0 && sb && !c->copy_stream) {
+        NB_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            NB_CUDA(cudaMalloc(&c->snap[k], sb));
+            NB_CUDA(cudaMallocHost(&c->stage[k], sb));
+            NB_CUDA(cudaEventCreate(&c->ev_snap[k]));
+            NB_CUDA(cudaEventCreate(&c->ev_c0[k]));
+            NB_CUDA(cudaEventCreate(&c->ev_c1[k]));
+        }
+    }
+    const int nstretch = (loops + out_interval - 1) / out_interval;
+    while (c->events.size() < 2 * (size_t)nstretch) {
+        cudaEvent_t e;
+        NB_CUDA(cudaEventCreate(&e));
+        c->events.push_back(e);
+    }
+    int pending[2] = {-1, -1};
+    auto drain = [&](int slot) -> int {
+        if (pending[slot] < 0) return NB_OK;
+        NB_CUDA(cudaEventSynchronize(c->ev_c1[slot]));
+        float cms = 0;
+        NB_CUDA(cudaEventElapsedTime(&cms, c->ev_c0[slot], c->ev_c1[slot]));
+        copyout += cms * 1e-3;
+        std::memcpy((char *)outbuffer + (size_t)pending[slot] * sb, c->stage[slot], sb);
+        pending[slot] = -1;
+        return NB_OK;
+    };
+
+    // step loop; frame f (after step (f+1) * out_interval) goes to
+    // outbuffer + f * 4n (body_task_sgpu.cu:116-125)
+    int done = 0, k = 0;
     while (done < loops) {
         const int next_frame = (done / out_interval + 1) * out_interval;
         const int upto = next_frame < loops ? next_frame : loops;
-        NB_CUDA(cudaEventRecord(ev[0], s));
+        NB_CUDA(cudaEventRecord(c->events[2 * k], s));
         if ((st = nb_step(c, upto - done, stream))) return st;
-        NB_CUDA(cudaEventRecord(ev[1], s));
+        NB_CUDA(cudaEventRecord(c->events[2 * k + 1], s));
+        ++k;
         done = upto;
         if (done % out_interval == 0 && sb) {
-            char *dst = (char *)outbuffer + (size_t)(done / out_interval - 1) * sb;
-            NB_CUDA(cudaMemcpyAsync(pinned ? c->stage_out : dst, c->pos[c->cur], sb,
-                                    cudaMemcpyDefault, s));
-            NB_CUDA(cudaEventRecord(ev[2], s));
-            NB_CUDA(cudaEventSynchronize(ev[2]));
-            if (pinned) std::memcpy(dst, c->stage_out, sb);
-            NB_CUDA(cudaEventElapsedTime(&ms, ev[1], ev[2]));
-            copyout += ms * 1e-3;
-        } else {
-            NB_CUDA(cudaEventSynchronize(ev[1]));
+            const int f = done / out_interval - 1;
+            const int slot = f & 1;
+            if ((st = drain(slot))) return st;
+            const void *cur = is_comp(c) ? c->pos[0] : c->pos[c->cur];
+            NB_CUDA(cudaMemcpyAsync(c->snap[slot], cur, sb, cudaMemcpyDeviceToDevice, s));
+            NB_CUDA(cudaEventRecord(c->ev_snap[slot], s));
+            NB_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_snap[slot], 0));
+            NB_CUDA(cudaEventRecord(c->ev_c0[slot], c->copy_stream));
+            NB_CUDA(cudaMemcpyAsync(c->stage[slot], c->snap[slot], sb, cudaMemcpyDeviceToHost,
+                                    c->copy_stream));
+            NB_CUDA(cudaEventRecord(c->ev_c1[slot], c->copy_stream));
+            pending[slot] = f;
         }
-        NB_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+    }
+    for (int slot = 0; slot < 2; ++slot)
+        if ((st = drain(slot))) return st;
+    NB_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < k; ++i) {
+        NB_CUDA(cudaEventElapsedTime(&ms, c->events[2 * i], c->events[2 * i + 1]));
         kernel += ms * 1e-3;
     }
-    NB_CUDA(cudaStreamSynchronize(s));
     const double total =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     if (timings) {

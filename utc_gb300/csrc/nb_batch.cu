@@ -24,6 +24,7 @@
 #include <map>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "nb_internal.cuh"
@@ -168,6 +169,163 @@ __global__ void bk_integrate_kernel(const float4 *__restrict__ pos_old, float4 *
     vel[i] = v;
 }
 
+
+// Batched adjoint: the vector-Jacobian product of one step for every system
+// (same algebra as vjp_pair_kernel in nb_adjoint.cu: out_k = m_k P - q g_k -
+// 3 Q and dm_k = -sum inv^3 r.g_j), warp-level stream-K over the batch.
+template <int WPB, int BPT>
+__global__ void __launch_bounds__(32 * WPB) bk_vjp_kernel(const float4 *__restrict__ pos,
+                                                          const float4 *__restrict__ gbuf, BatchDev bd,
+                                                          float eps2, float4 *__restrict__ partial,
+                                                          long long total, int workers)
+{
+    constexpr int WTB = 32 * BPT;
+    __shared__ __align__(16) float4 sP[WPB][32];
+    __shared__ __align__(16) float4 sG[WPB][32];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const int w = blockIdx.x * WPB + wid;
+    if (w >= workers) return;
+    long long it = sk_start(w, total, workers);
+    const long long end = sk_start(w + 1, total, workers);
+    if (it >= end) return;
+    const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    int s = find_sys(bd.it_off, bd.nsys, it);
+    while (it < end) {
+        while (it >= bd.it_off[s + 1]) ++s;
+        const int o = bd.sys_off[s];
+        const int ns = bd.sys_off[s + 1] - o;
+        const int ngroups = (ns + kGroup - 1) / kGroup;
+        const long long base = bd.it_off[s];
+        const int tbl = (int)((it - base) / ngroups);
+        const long long blk_first = base + (long long)tbl * ngroups;
+        const long long seg_end = end < blk_first + ngroups ? end : blk_first + ngroups;
+        const int j0 = (int)(it - blk_first) * kGroup;
+        const int j1 = min((int)(seg_end - blk_first) * kGroup, ns);
+
+        float px[BPT], py[BPT], pz[BPT], pm[BPT], gx[BPT], gy[BPT], gz[BPT];
+        float Px[BPT], Py[BPT], Pz[BPT], Q0[BPT], Q1[BPT], Q2[BPT], q[BPT], dm[BPT];
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const int li = tbl * WTB + lane + 32 * k;
+            const float4 a = li < ns ? pos[o + li] : zero;
+            const float4 g = li < ns ? gbuf[o + li] : zero;
+            px[k] = a.x; py[k] = a.y; pz[k] = a.z; pm[k] = a.w;
+            gx[k] = g.x; gy[k] = g.y; gz[k] = g.z;
+            Px[k] = Py[k] = Pz[k] = Q0[k] = Q1[k] = Q2[k] = q[k] = dm[k] = 0.f;
+        }
+        float4 nxp = (j0 + lane < j1) ? pos[o + j0 + lane] : pad;
+        float4 nxg = (j0 + lane < j1) ? gbuf[o + j0 + lane] : zero;
+        for (int jt = j0; jt < j1; jt += kGroup) {
+            __syncwarp();
+            sP[wid][lane] = nxp;
+            sG[wid][lane] = nxg;
+            __syncwarp();
+            if (jt + kGroup < j1) {
+                const int jn = jt + kGroup + lane;
+                nxp = jn < j1 ? pos[o + jn] : pad;
+                nxg = jn < j1 ? gbuf[o + jn] : zero;
+            }
+            const int cnt = min(kGroup, j1 - jt);
+            for (int j = 0; j < cnt; ++j) {
+                const float4 sv = sP[wid][j];
+                const float4 g = sG[wid][j];
+#pragma unroll
+                for (int k = 0; k < BPT; ++k) {
+                    const float rx = sv.x - px[k], ry = sv.y - py[k], rz = sv.z - pz[k];
+                    float d2 = fmaf(rx, rx, eps2);
+                    d2 = fmaf(ry, ry, d2);
+                    d2 = fmaf(rz, rz, d2);
+                    const float inv = rsqrt_approx(d2);
+                    const float inv2 = inv * inv;
+                    const float inv3 = inv2 * inv;
+                    const float inv5 = inv3 * inv2;
+                    Px[k] = fmaf(inv3, g.x, Px[k]);
+                    Py[k] = fmaf(inv3, g.y, Py[k]);
+                    Pz[k] = fmaf(inv3, g.z, Pz[k]);
+                    q[k] = fmaf(inv3, sv.w, q[k]);
+                    const float rgj = fmaf(rz, g.z, fmaf(ry, g.y, rx * g.x));
+                    const float rgk = fmaf(rz, gz[k], fmaf(ry, gy[k], rx * gx[k]));
+                    const float cc = inv5 * fmaf(pm[k], rgj, -(sv.w * rgk));
+                    Q0[k] = fmaf(cc, rx, Q0[k]);
+                    Q1[k] = fmaf(cc, ry, Q1[k]);
+                    Q2[k] = fmaf(cc, rz, Q2[k]);
+                    dm[k] = fmaf(inv3, rgj, dm[k]);
+                }
+            }
+        }
+        const long long slot = (long long)w + bd.tb_off[s] + tbl;
+        float4 *dst = partial + slot * WTB;
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const float ox = fmaf(pm[k], Px[k], fmaf(-q[k], gx[k], -3.f * Q0[k]));
+            const float oy = fmaf(pm[k], Py[k], fmaf(-q[k], gy[k], -3.f * Q1[k]));
+            const float oz = fmaf(pm[k], Pz[k], fmaf(-q[k], gz[k], -3.f * Q2[k]));
+            dst[lane + 32 * k] = make_float4(ox, oy, oz, -dm[k]);
+        }
+        it = seg_end;
+    }
+}
+
+__global__ void bk_adj_update_kernel(const float4 *__restrict__ partial, BatchDev bd, int nbody,
+                                     int wtb, long long total, int workers,
+                                     const float4 *__restrict__ pos, const float4 *__restrict__ acc,
+                                     float4 *__restrict__ lx, float4 *__restrict__ lv,
+                                     float *__restrict__ gm, float4 *__restrict__ gbuf,
+                                     float damping, float dt, int kick, float G, int want_next_g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbody) return;
+    const int s = bd.body_sys[i];
+    const int o = bd.sys_off[s];
+    const int ns = bd.sys_off[s + 1] - o;
+    const int ngroups = (ns + kGroup - 1) / kGroup;
+    const int li = i - o;
+    const int tbl = li / wtb;
+    const long long first = bd.it_off[s] + (long long)tbl * ngroups;
+    const int c0 = sk_owner(first, total, workers);
+    const int c1 = sk_owner(first + ngroups - 1, total, workers);
+    const long long gtb = (long long)bd.tb_off[s] + tbl;
+    const int lj = li - tbl * wtb;
+    float ox = 0.f, oy = 0.f, oz = 0.f, odm = 0.f;
+    for (int c = c0; c <= c1; ++c) {
+        const float4 qv = partial[(c + gtb) * wtb + lj];
+        ox += qv.x;
+        oy += qv.y;
+        oz += qv.z;
+        odm += qv.w;
+    }
+    const float4 x = lx[i], v = lv[i];
+    const float mux = fmaf(dt, x.x, v.x), muy = fmaf(dt, x.y, v.y), muz = fmaf(dt, x.z, v.z);
+    float dmi = odm;
+    if (kick == NB_KICK_REFERENCE) {
+        const float4 a = acc[i];
+        dmi = fmaf(damping * dt, mux * a.x + muy * a.y + muz * a.z, dmi);
+    }
+    gm[i] += dmi;
+    const float4 nx = make_float4(x.x + ox, x.y + oy, x.z + oz, 0.f);
+    const float4 nv = make_float4(damping * mux, damping * muy, damping * muz, 0.f);
+    lx[i] = nx;
+    lv[i] = nv;
+    if (want_next_g) {
+        const float kf = kick == NB_KICK_REFERENCE ? pos[i].w : G;
+        const float f = damping * dt * kf;
+        gbuf[i] = make_float4(f * fmaf(dt, nx.x, nv.x), f * fmaf(dt, nx.y, nv.y),
+                              f * fmaf(dt, nx.z, nv.z), 0.f);
+    }
+}
+
+typedef void (*bk_vjp_t)(const float4 *, const float4 *, BatchDev, float, float4 *, long long, int);
+
+static bk_vjp_t bk_vjp_for(int wpb, int bpt)
+{
+    if (wpb == 4 && bpt == 2) return bk_vjp_kernel<4, 2>;
+    if (wpb == 4 && bpt == 4) return bk_vjp_kernel<4, 4>;
+    if (wpb == 8 && bpt == 4) return bk_vjp_kernel<8, 4>;
+    return nullptr;
+}
+
 typedef void (*bk_kernel_t)(const float4 *, BatchDev, float, float4 *, long long, int);
 
 static bk_kernel_t bk_kernel_for(int wpb, int bpt)
@@ -209,6 +367,16 @@ struct nb_batch {
     // per-system plain plans for the baseline
     std::vector<nb::SkPlan> sys_plans;
     float4 *sys_partial = nullptr;
+    // adjoint: VJP plan (own iteration tables), checkpoints, reverse buffers
+    BatchPlan vplan;
+    long long *d_it_off_v = nullptr;
+    int *d_tb_off_v = nullptr;
+    float4 *vpartial = nullptr;
+    int adj_steps = 0, adj_every = 0, adj_nckpt = 0, cap_ckpt = 0, cap_seg = 0;
+    bool adj_ready = false;
+    float4 *ckpt_pos = nullptr, *ckpt_vel = nullptr, *seg_pos = nullptr, *seg_acc = nullptr;
+    float4 *vel_tmp = nullptr, *lx = nullptr, *lv = nullptr, *gbuf = nullptr;
+    float *gm = nullptr;
 };
 
 using nb::set_error;
@@ -285,20 +453,73 @@ static nb::BatchDev batch_dev(const nb_batch *b)
     return d;
 }
 
-static int batch_step_once(nb_batch *b, cudaStream_t s)
+// One batched step from po into pn (vel in place); with acc_out the second
+// kernel writes the bare accelerations instead of integrating.
+static int batch_force_step(nb_batch *b, const float4 *po, float4 *pn, float4 *vel,
+                            float4 *acc_out, cudaStream_t s)
 {
     const BatchPlan &p = b->plan;
     if (b->nbody == 0) return NB_OK;
-    const float4 *po = b->pos[b->cur];
-    float4 *pn = b->pos[b->cur ^ 1];
     nb::bk_kernel_t k = nb::bk_kernel_for(p.wpb, p.bpt);
     k<<<p.grid, 32 * p.wpb, 0, s>>>(po, batch_dev(b), (float)b->p.eps2, b->partial, p.total, p.workers);
     NB_LAUNCH_CHECK("bk_force_kernel launch");
     nb::bk_integrate_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
-        po, pn, b->vel, b->partial, batch_dev(b), b->nbody, 32 * p.bpt, p.total, p.workers,
-        (float)b->p.damping, (float)b->p.dt, b->p.kick, (float)b->p.G, nullptr);
+        po, pn, vel, b->partial, batch_dev(b), b->nbody, 32 * p.bpt, p.total, p.workers,
+        (float)b->p.damping, (float)b->p.dt, b->p.kick, (float)b->p.G, acc_out);
     NB_LAUNCH_CHECK("bk_integrate_kernel launch");
+    return NB_OK;
+}
+
+static int batch_step_once(nb_batch *b, cudaStream_t s)
+{
+    if (b->nbody == 0) return NB_OK;
+    int st = batch_force_step(b, b->pos[b->cur], b->pos[b->cur ^ 1], b->vel, nullptr, s);
+    if (st) return st;
     b->cur ^= 1;
+    return NB_OK;
+}
+
+// VJP plan: its own (system, warp target block) tables for 32 * bpt targets
+static int batch_vplan_setup(nb_batch *b)
+{
+    if (b->d_it_off_v) return NB_OK;
+    const int wpb = 4, bpt = 4, wtb = 32 * bpt;
+    nb::bk_vjp_t k = nb::bk_vjp_for(wpb, bpt);
+    std::vector<long long> it_off(b->nsys + 1, 0);
+    std::vector<int> tb_off(b->nsys + 1, 0);
+    for (int q = 0; q < b->nsys; ++q) {
+        const long long n = b->sizes[q];
+        const long long ntb = (n + wtb - 1) / wtb, ng = (n + nb::kGroup - 1) / nb::kGroup;
+        it_off[q + 1] = it_off[q] + ntb * ng;
+        tb_off[q + 1] = tb_off[q] + (int)ntb;
+    }
+    int occ = 0;
+    NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * wpb, 0));
+    if (occ < 1) return set_error(NB_ERR_UNSUPPORTED, "batched adjoint kernel does not fit on an SM");
+    BatchPlan p;
+    p.wpb = wpb;
+    p.bpt = bpt;
+    p.total = it_off[b->nsys];
+    p.total_wtb = tb_off[b->nsys];
+    long long workers = (long long)b->sms * occ * wpb;
+    if (p.total > 0 && workers > p.total) workers = p.total;
+    p.workers = p.total > 0 ? (int)workers : 0;
+    p.grid = (p.workers + wpb - 1) / wpb;
+    p.slots = p.total > 0 ? p.workers + p.total_wtb - 1 : 0;
+    NB_CUDA(cudaMalloc((void **)&b->d_it_off_v, sizeof(long long) * (b->nsys + 1)));
+    NB_CUDA(cudaMalloc((void **)&b->d_tb_off_v, sizeof(int) * (b->nsys + 1)));
+    NB_CUDA(cudaMemcpy(b->d_it_off_v, it_off.data(), sizeof(long long) * (b->nsys + 1),
+                       cudaMemcpyHostToDevice));
+    NB_CUDA(cudaMemcpy(b->d_tb_off_v, tb_off.data(), sizeof(int) * (b->nsys + 1),
+                       cudaMemcpyHostToDevice));
+    NB_CUDA(cudaMalloc((void **)&b->vpartial, std::max<size_t>((size_t)p.slots * wtb, 1) * sizeof(float4)));
+    const size_t nb4 = std::max<size_t>((size_t)b->nbody, 1) * sizeof(float4);
+    NB_CUDA(cudaMalloc((void **)&b->vel_tmp, nb4));
+    NB_CUDA(cudaMalloc((void **)&b->lx, nb4));
+    NB_CUDA(cudaMalloc((void **)&b->lv, nb4));
+    NB_CUDA(cudaMalloc((void **)&b->gbuf, nb4));
+    NB_CUDA(cudaMalloc((void **)&b->gm, std::max<size_t>((size_t)b->nbody, 1) * sizeof(float)));
+    b->vplan = p;
     return NB_OK;
 }
 
@@ -315,6 +536,18 @@ static void free_batch(nb_batch *b)
     cudaFree(b->vel);
     cudaFree(b->partial);
     cudaFree(b->sys_partial);
+    cudaFree(b->d_it_off_v);
+    cudaFree(b->d_tb_off_v);
+    cudaFree(b->vpartial);
+    cudaFree(b->ckpt_pos);
+    cudaFree(b->ckpt_vel);
+    cudaFree(b->seg_pos);
+    cudaFree(b->seg_acc);
+    cudaFree(b->vel_tmp);
+    cudaFree(b->lx);
+    cudaFree(b->lv);
+    cudaFree(b->gbuf);
+    cudaFree(b->gm);
     delete b;
 }
 
@@ -623,6 +856,179 @@ int nb_batch_step_per_system(nb_batch *b, int steps, void *stream)
     return NB_OK;
 }
 
+// Baseline in the reference's multi-task pattern (benchapps/nbody/utc/
+// nbody_mtask.cc:199-231 with BodySystemSGPU::runImpl, body_task_sgpu.cu:
+// 85-127): `ntasks` host threads, each with its own stream, run their share
+// of the systems one after another; every system step is a force and an
+// integrate launch followed by a stream synchronise.  Blocks until done.
+int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
+{
+    if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
+    if (!b->has_state) return set_error(NB_ERR_STATE, "no state loaded");
+    if (ntasks < 1 || steps < 0) return set_error(NB_ERR_INVALID, "ntasks >= 1 and steps >= 0");
+    NB_CUDA(cudaDeviceSynchronize());
+    if (ntasks > b->nsys) ntasks = b->nsys > 0 ? b->nsys : 1;
+    std::vector<int> off(b->nsys + 1, 0);
+    for (int i = 0; i < b->nsys; ++i) off[i + 1] = off[i] + b->sizes[i];
+    std::vector<nb::SkPlan> plans(b->nsys);
+    size_t need = 1;
+    for (int i = 0; i < b->nsys; ++i) {
+        int st = nb::fast_plan(b->sizes[i], 0, 0, 0, b->device, &plans[i], 0);
+        if (st) return st;
+        need = std::max(need, (size_t)plans[i].slots * plans[i].tbsize);
+    }
+    std::vector<float4 *> scratch(ntasks, nullptr);
+    std::vector<cudaStream_t> streams(ntasks, nullptr);
+    for (int t = 0; t < ntasks; ++t) {
+        NB_CUDA(cudaMalloc((void **)&scratch[t], need * sizeof(float4)));
+        NB_CUDA(cudaStreamCreateWithFlags(&streams[t], cudaStreamNonBlocking));
+    }
+    const int cur = b->cur, dev = b->device;
+    std::vector<int> status(ntasks, NB_OK);
+    std::vector<std::thread> workers;
+    for (int t = 0; t < ntasks; ++t) {
+        workers.emplace_back([&, t] {
+            cudaSetDevice(dev);
+            for (int i = t; i < b->nsys && status[t] == NB_OK; i += ntasks) {
+                int c = cur;
+                for (int k = 0; k < steps && status[t] == NB_OK; ++k) {
+                    const float4 *po = b->pos[c] + off[i];
+                    float4 *pn = b->pos[c ^ 1] + off[i];
+                    int st = nb::fast_force(plans[i], po, (float)b->p.eps2, scratch[t], streams[t], 0);
+                    if (!st)
+                        st = nb::fast_integrate(plans[i], po, pn, b->vel + off[i], scratch[t],
+                                                (float)b->p.damping, (float)b->p.dt, b->p.kick,
+                                                (float)b->p.G, nullptr, streams[t]);
+                    if (!st && cudaStreamSynchronize(streams[t]) != cudaSuccess) st = NB_ERR_CUDA;
+                    status[t] = st;
+                    c ^= 1;
+                }
+            }
+        });
+    }
+    for (auto &w : workers) w.join();
+    for (int t = 0; t < ntasks; ++t) {
+        cudaFree(scratch[t]);
+        cudaStreamDestroy(streams[t]);
+    }
+    for (int t = 0; t < ntasks; ++t)
+        if (status[t]) return set_error(status[t], "per-system task baseline failed");
+    if (steps % 2) b->cur ^= 1;
+    return NB_OK;
+}
+
 int nb_batch_launches_per_step(nb_batch *b) { return b ? (b->nbody ? 2 : 0) : -1; }
+
+// Batched adjoint: every system's state advanced `steps` steps with a
+// checkpoint every ckpt_every steps, then the reverse pass for all systems
+// at once (same contract as nb_adj_forward / nb_adj_backward, over the
+// concatenated bodies).
+int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream)
+{
+    if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
+    if (!b->has_state) return set_error(NB_ERR_STATE, "no state loaded");
+    if (steps < 1 || ckpt_every < 1) return set_error(NB_ERR_INVALID, "steps and ckpt_every must be >= 1");
+    if (ckpt_every > steps) ckpt_every = steps;
+    int st = batch_vplan_setup(b);
+    if (st) return st;
+    const int nckpt = (steps + ckpt_every - 1) / ckpt_every;
+    const size_t n = (size_t)b->nbody;
+    if (nckpt > b->cap_ckpt) {
+        cudaFree(b->ckpt_pos);
+        cudaFree(b->ckpt_vel);
+        b->ckpt_pos = b->ckpt_vel = nullptr;
+        b->cap_ckpt = 0;
+        NB_CUDA(cudaMalloc((void **)&b->ckpt_pos, std::max<size_t>(n * nckpt, 1) * sizeof(float4)));
+        NB_CUDA(cudaMalloc((void **)&b->ckpt_vel, std::max<size_t>(n * nckpt, 1) * sizeof(float4)));
+        b->cap_ckpt = nckpt;
+    }
+    if (ckpt_every > b->cap_seg) {
+        cudaFree(b->seg_pos);
+        cudaFree(b->seg_acc);
+        b->seg_pos = b->seg_acc = nullptr;
+        b->cap_seg = 0;
+        NB_CUDA(cudaMalloc((void **)&b->seg_pos, std::max<size_t>(n * (ckpt_every + 1), 1) * sizeof(float4)));
+        NB_CUDA(cudaMalloc((void **)&b->seg_acc, std::max<size_t>(n * ckpt_every, 1) * sizeof(float4)));
+        b->cap_seg = ckpt_every;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int t = 0; t < steps; ++t) {
+        if (t % ckpt_every == 0 && n) {
+            const size_t k = (size_t)(t / ckpt_every) * n;
+            NB_CUDA(cudaMemcpyAsync(b->ckpt_pos + k, b->pos[b->cur], n * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, s));
+            NB_CUDA(cudaMemcpyAsync(b->ckpt_vel + k, b->vel, n * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, s));
+        }
+        if ((st = batch_step_once(b, s))) return st;
+    }
+    b->adj_steps = steps;
+    b->adj_every = ckpt_every;
+    b->adj_nckpt = nckpt;
+    b->adj_ready = true;
+    return NB_OK;
+}
+
+int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void *gx0, void *gv0,
+                          void *gm, void *stream)
+{
+    if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
+    if (!b->adj_ready) return set_error(NB_ERR_STATE, "nb_batch_adj_backward needs a preceding nb_batch_adj_forward");
+    if (b->nbody == 0) return NB_OK;
+    if (!gx_T || !gx0 || !gv0 || !gm) return set_error(NB_ERR_INVALID, "NULL gradient buffer");
+    const size_t n = (size_t)b->nbody;
+    const nb_params &p = b->p;
+    const float eps2 = (float)p.eps2, D = (float)p.damping, dt = (float)p.dt, G = (float)p.G;
+    cudaStream_t s = (cudaStream_t)stream;
+    nb::BatchDev vd = batch_dev(b);
+    vd.it_off = b->d_it_off_v;
+    vd.tb_off = b->d_tb_off_v;
+    const BatchPlan &vp = b->vplan;
+    nb::bk_vjp_t vk = nb::bk_vjp_for(vp.wpb, vp.bpt);
+    int st;
+    NB_CUDA(cudaMemcpyAsync(b->lx, gx_T, n * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    if (gv_T)
+        NB_CUDA(cudaMemcpyAsync(b->lv, gv_T, n * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    else
+        NB_CUDA(cudaMemsetAsync(b->lv, 0, n * sizeof(float4), s));
+    NB_CUDA(cudaMemsetAsync(b->gm, 0, n * sizeof(float), s));
+    bool have_g = false;
+    for (int seg = b->adj_nckpt - 1; seg >= 0; --seg) {
+        const int t0 = seg * b->adj_every;
+        const int len = (b->adj_steps - t0) < b->adj_every ? (b->adj_steps - t0) : b->adj_every;
+        NB_CUDA(cudaMemcpyAsync(b->seg_pos, b->ckpt_pos + (size_t)seg * n, n * sizeof(float4),
+                                cudaMemcpyDeviceToDevice, s));
+        NB_CUDA(cudaMemcpyAsync(b->vel_tmp, b->ckpt_vel + (size_t)seg * n, n * sizeof(float4),
+                                cudaMemcpyDeviceToDevice, s));
+        for (int k = 0; k < len; ++k) {
+            const float4 *xk = b->seg_pos + (size_t)k * n;
+            if (p.kick == NB_KICK_REFERENCE &&
+                (st = batch_force_step(b, xk, nullptr, nullptr, b->seg_acc + (size_t)k * n, s)))
+                return st;
+            if ((st = batch_force_step(b, xk, b->seg_pos + (size_t)(k + 1) * n, b->vel_tmp, nullptr, s)))
+                return st;
+        }
+        for (int k = len - 1; k >= 0; --k) {
+            const float4 *xk = b->seg_pos + (size_t)k * n;
+            if (!have_g) {
+                if ((st = nb::adj_g(b->nbody, xk, b->lx, b->lv, b->gbuf, D, dt, p.kick, G, s))) return st;
+                have_g = true;
+            }
+            if (vp.total > 0) {
+                vk<<<vp.grid, 32 * vp.wpb, 0, s>>>(xk, b->gbuf, vd, eps2, b->vpartial, vp.total, vp.workers);
+                NB_LAUNCH_CHECK("bk_vjp_kernel launch");
+            }
+            const bool more = !(seg == 0 && k == 0);
+            nb::bk_adj_update_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
+                b->vpartial, vd, b->nbody, 32 * vp.bpt, vp.total, vp.workers, xk,
+                b->seg_acc + (size_t)k * n, b->lx, b->lv, b->gm, b->gbuf, D, dt, p.kick, G, more ? 1 : 0);
+            NB_LAUNCH_CHECK("bk_adj_update_kernel launch");
+        }
+    }
+    NB_CUDA(cudaMemcpyAsync(gx0, b->lx, n * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    NB_CUDA(cudaMemcpyAsync(gv0, b->lv, n * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    NB_CUDA(cudaMemcpyAsync(gm, b->gm, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    return NB_OK;
+}
 
 }  // extern "C"

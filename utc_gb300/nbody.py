@@ -283,6 +283,10 @@ class NBodyBatch:
         N.check(self.lib.nb_batch_step_per_system(self.handle, int(steps), C.c_void_p(s)),
                 "nb_batch_step_per_system")
 
+    def step_tasks(self, steps, ntasks):
+        """Reference-pattern baseline: ntasks threads/streams, sync every step."""
+        N.check(self.lib.nb_batch_step_tasks(self.handle, int(steps), int(ntasks)), "nb_batch_step_tasks")
+
     def autotune(self, reps=2, cache_path=None, stream=None):
         s = current_stream_handle() if stream is None else stream
         out = (C.c_int * 2)()
@@ -290,6 +294,27 @@ class NBodyBatch:
                                            cache_path.encode() if cache_path else None,
                                            C.c_void_p(s), out), "nb_batch_autotune")
         return int(out[0]), int(out[1])
+
+    def adj_forward(self, steps, ckpt_every, stream=None):
+        s = current_stream_handle() if stream is None else stream
+        N.check(self.lib.nb_batch_adj_forward(self.handle, int(steps), int(ckpt_every), C.c_void_p(s)),
+                "nb_batch_adj_forward")
+
+    def adj_backward(self, gx_T, gv_T=None, stream=None):
+        """Cotangents (nbody, 4) torch CUDA float32 -> (dL/dx0, dL/dv0, dL/dm)."""
+        torch = _torch()
+        gx0 = torch.zeros((self.nbody, 4), dtype=torch.float32, device="cuda")
+        gv0 = torch.zeros((self.nbody, 4), dtype=torch.float32, device="cuda")
+        gm = torch.zeros((self.nbody,), dtype=torch.float32, device="cuda")
+        s = current_stream_handle() if stream is None else stream
+        gx_T = gx_T.contiguous()
+        gv_keep = gv_T.contiguous() if gv_T is not None else None
+        N.check(self.lib.nb_batch_adj_backward(
+            self.handle, C.c_void_p(gx_T.data_ptr()),
+            C.c_void_p(gv_keep.data_ptr() if gv_keep is not None else 0),
+            C.c_void_p(gx0.data_ptr()), C.c_void_p(gv0.data_ptr()), C.c_void_p(gm.data_ptr()),
+            C.c_void_p(s)), "nb_batch_adj_backward")
+        return gx0, gv0, gm
 
     def set_shape(self, warps_per_cta, bodies_per_lane):
         N.check(self.lib.nb_batch_set_shape(self.handle, int(warps_per_cta), int(bodies_per_lane)),
