@@ -226,6 +226,21 @@ int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream);
 int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void *gx0, void *gv0,
                           void *gm, void *stream);
 
+/* Seeded initial conditions generated on the GPU, one thread per body
+ * (counter-based: a body's draw depends only on (seed, index)).  kind 0:
+ * uniform cube, positions U[-1,1]^3, velocities U[-vmax,vmax]^3, masses
+ * U[0.5,1.5]/n; kind 1: Plummer sphere of scale a, total mass M and
+ * gravitational constant G (Aarseth, Henon & Wielen sampling), masses M/n,
+ * centre of mass and momentum moved to zero.  pos/vel: device, n 4-vectors of
+ * float (NB_F32) or double (NB_F64), vel.w = 1.  scratch_dev: device buffer of
+ * nb_ics_scratch_bytes(n) bytes (Plummer only).  Replaces the host-side
+ * randomizeBodies (benchapps/nbody/seq/nbody.h:89-250) for large synthetic
+ * inputs; the app's own initialiser stays on the host (it draws rand()). */
+int nb_ics_generate(int kind, int n, unsigned long long seed, double a, double G, double M,
+                    double vmax, int precision, void *pos_dev, void *vel_dev, void *scratch_dev,
+                    void *stream);
+size_t nb_ics_scratch_bytes(int n);
+
 /* Device pointers of the current state (valid until the next nb_step). */
 int nb_state_ptrs(nb_ctx *ctx, void **pos_dev, void **vel_dev);
 

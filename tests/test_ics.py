@@ -1,0 +1,50 @@
+"""Initial conditions drawn on the GPU (nb_ics_generate): deterministic per
+seed, and distributed as specified (checked against the analytic Plummer
+mass profile and the virial ratio, and the cube's ranges)."""
+import numpy as np
+import pytest
+
+import oracle
+from utc_gb300.nbody import NBodySystem, gpu_initial_conditions
+
+pytestmark = pytest.mark.gpu
+
+
+def test_deterministic_and_seeded(cuda):
+    a = gpu_initial_conditions("plummer", 5000, seed=3)
+    b = gpu_initial_conditions("plummer", 5000, seed=3)
+    c = gpu_initial_conditions("plummer", 5000, seed=4)
+    assert all((x.cpu().numpy().tobytes() == y.cpu().numpy().tobytes()) for x, y in zip(a, b))
+    assert a[0].cpu().numpy().tobytes() != c[0].cpu().numpy().tobytes()
+    # a body's draw does not depend on how many bodies are drawn
+    d = gpu_initial_conditions("cube", 1000, seed=5)[0].cpu().numpy()
+    e = gpu_initial_conditions("cube", 3000, seed=5)[0].cpu().numpy()
+    assert d.tobytes() == e[:1000].tobytes()
+
+
+def test_cube_ranges(cuda):
+    n = 20000
+    p, v = [t.cpu().numpy() for t in gpu_initial_conditions("cube", n, seed=1, vmax=0.01)]
+    assert np.abs(p[:, :3]).max() <= 1.0 and np.abs(v[:, :3]).max() <= 0.01
+    assert (p[:, 3] >= 0.5 / n).all() and (p[:, 3] <= 1.5 / n).all()
+    assert abs(p[:, :3].mean()) < 0.02 and abs(p[:, 3].sum() - 1.0) < 0.01
+    assert np.all(v[:, 3] == 1.0)
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_plummer_profile_and_virial(cuda, precision):
+    n = 100000
+    p, v = [t.cpu().numpy().astype(np.float64) for t in gpu_initial_conditions("plummer", n, seed=2,
+                                                                                 precision=precision)]
+    com = (p[:, :3] * p[:, 3:4]).sum(0)
+    mom = (v[:, :3] * p[:, 3:4]).sum(0)
+    assert np.abs(com).max() < 1e-6 and np.abs(mom).max() < 1e-6
+    r = np.linalg.norm(p[:, :3], axis=1)
+    for rr in (0.5, 1.0, 2.0, 5.0):
+        want = rr ** 3 / (rr * rr + 1) ** 1.5 / 0.999  # truncated at X <= 0.999
+        assert abs((r < rr).mean() - min(want, 1.0)) < 0.01
+    # virial ratio -K / W ~ 0.5 (potential from the GPU energy pass, small softening)
+    with NBodySystem(n, "f32", "fast", kick="physical", eps2=np.float32(1e-6)) as s:
+        s.set_state(p.astype(np.float32), v.astype(np.float32))
+        e = s.energy()
+    assert abs(-e[0] / e[1] - 0.5) < 0.03

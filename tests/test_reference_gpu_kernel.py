@@ -59,19 +59,69 @@ def test_fast_kernel_beats_reference_kernel(ref_kernel, capsys):
     pos, vel = ics.f32(p64), ics.f32(v64)
     run_ref(ref_kernel, pos, vel, 2, 1e-4, 1e-4)  # warm-up
     p_ref, _, ms_ref = run_ref(ref_kernel, pos, vel, steps, 1e-4, 1e-4)
-    with NBodySystem(n, "f32", "fast", kick="reference", eps2=1e-4, damping=1.0, dt=1e-4) as s:
-        s.set_state(pos, vel)
-        s.step(2)
-        s.set_state(pos, vel)
-        f, g = s.step_timed(steps)
-        p_ours, _ = s.get_state()
-    torch.cuda.synchronize()
-    # both run the reference's update rule (kick x pos.w) on the same input
-    assert np.abs(p_ours - p_ref).max() < 1e-5
     rate_ref = n * n * steps / (ms_ref * 1e-3) / 1e9
-    rate_ours = n * n * steps / ((f + g) * 1e-3) / 1e9
+    for algo in ("fast", "sym"):
+        with NBodySystem(n, "f32", algo, kick="reference", eps2=1e-4, damping=1.0, dt=1e-4) as s:
+            s.set_state(pos, vel)
+            s.step(2)
+            s.set_state(pos, vel)
+            f, g = s.step_timed(steps)
+            p_ours, _ = s.get_state()
+        torch.cuda.synchronize()
+        # both run the reference's update rule (kick x pos.w) on the same input
+        assert np.abs(p_ours - p_ref).max() < 1e-5
+        rate_ours = n * n * steps / ((f + g) * 1e-3) / 1e9
+        with capsys.disabled():
+            print(f"\n[gpu baseline] N={n}: reference kernel (sm_103a build) {rate_ref:.1f} G interactions/s, "
+                  f"{ms_ref / steps:.3f} ms/step; {algo} kernel {rate_ours:.1f} G interactions/s, "
+                  f"{(f + g) / steps:.3f} ms/step; speed-up {rate_ours / rate_ref:.2f}x")
+        assert rate_ours > rate_ref
+
+
+def test_batch_vs_reference_kernel_per_system(ref_kernel, capsys):
+    """The batched launch against the reference kernel launched once per
+    system per step (its own launch shape: block 128, one target per thread;
+    sizes rounded up to a multiple of 128 as the reference app rounds N)."""
+    import torch
+
+    from utc_gb300.nbody import NBodyBatch
+
+    sizes = (ics.batch_sizes(128, lo=128, hi=16384, seed=0) + 127) // 128 * 128
+    steps = 10
+    ps, vs = [], []
+    for k, nn in enumerate(sizes):
+        p, v = ics.plummer(int(nn), seed=500 + k)
+        ps.append(ics.f32(p))
+        vs.append(ics.f32(v))
+    pos, vel = np.concatenate(ps), np.concatenate(vs)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    s = torch.cuda.current_stream()
+    bufs = [torch.from_numpy(pos).cuda(), torch.from_numpy(pos).cuda()]
+    vt = torch.from_numpy(vel).cuda()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for t in range(steps):
+        for k, nn in enumerate(sizes):
+            o = int(off[k]) * 16
+            ref_kernel.step(bufs[t % 2].data_ptr() + o, bufs[(t + 1) % 2].data_ptr() + o,
+                            vt.data_ptr() + o, int(nn), 1e-3, 1e-3, 1.0, 128, s.cuda_stream)
+    e1.record(s)
+    e1.synchronize()
+    ms_ref = e0.elapsed_time(e1)
+    p_ref = bufs[steps % 2].cpu().numpy()
+    with NBodyBatch(sizes, kick="reference", eps2=np.float32(1e-3), dt=np.float32(1e-3)) as b:
+        b.set_state(pos, vel)
+        b.step(2)
+        b.set_state(pos, vel)
+        torch.cuda.synchronize()
+        e0.record(s)
+        b.step(steps)
+        e1.record(s)
+        e1.synchronize()
+        ms_b = e0.elapsed_time(e1)
+        p_b, _ = b.get_state()
+    assert np.abs(p_b - p_ref).max() < 1e-4
     with capsys.disabled():
-        print(f"\n[gpu baseline] N={n}: reference kernel (sm_103a build) {rate_ref:.1f} G interactions/s, "
-              f"{ms_ref / steps:.3f} ms/step; fast kernel {rate_ours:.1f} G interactions/s, "
-              f"{(f + g) / steps:.3f} ms/step; speed-up {rate_ours / rate_ref:.2f}x")
-    assert rate_ours > rate_ref
+        print(f"\n[batch baseline] {len(sizes)} systems, {steps} steps: reference kernel per system "
+              f"{ms_ref:.1f} ms, batched launch {ms_b:.1f} ms, speed-up {ms_ref / ms_b:.1f}x")
+    assert ms_b < ms_ref

@@ -77,6 +77,8 @@ def _declare(lib):
         "nb_batch_adj_forward": (I, [vp, I, I, vp]),
         "nb_batch_step_tasks": (I, [vp, I, I]),
         "nb_batch_adj_backward": (I, [vp, vp, vp, vp, vp, vp, vp]),
+        "nb_ics_generate": (I, [I, I, C.c_ulonglong, D, D, D, D, I, vp, vp, vp, vp]),
+        "nb_ics_scratch_bytes": (C.c_size_t, [I]),
         "nb_last_error": (C.c_char_p, []),
         "nb_abi_version": (I, []),
     }
