@@ -167,6 +167,136 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel(const float4 *__restr
     }
 }
 
+// Packed variant: each lane's targets as NP f32x2 pairs (targets k and
+// k + NP of the lane), every pair-term operation one FADD2/FMUL2/FFMA2 for
+// two targets; the chunk body is duplicated into register pairs; the
+// reaction on the chunk body is accumulated as a pair (one half per target of
+// the pair) and folded to a scalar before each shuffle.  Same work layout,
+// partials and results' order of summation as sym_force_kernel.
+template <int W, int NP>
+__global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__restrict__ pos, int n,
+                                                              float eps2, float4 *__restrict__ tpart,
+                                                              float4 *__restrict__ spart,
+                                                              long long total, int nc, int nrb)
+{
+    constexpr int BPT = 2 * NP;
+    constexpr int WB = 32 * BPT;
+    constexpr int RB = W * WB;
+    constexpr int RC = RB / 32;
+    __shared__ __align__(16) float4 sC[32];
+    __shared__ float sF[3][W][32];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const int c = blockIdx.x;
+    long long it = sk_start(c, total, gridDim.x);
+    const long long end = sk_start(c + 1, total, gridDim.x);
+    const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
+    const f2 EPS2 = f2_pack(eps2, eps2);
+    const f2 ZERO = f2_pack(0.f, 0.f);
+
+    while (it < end) {
+        const int I = sym_row_of(it, nc, RC, nrb);
+        const long long rfirst = sym_prefix(I, nc, RC);
+        const long long rend = sym_prefix(I + 1, nc, RC);
+        const long long seg_end = end < rend ? end : rend;
+        const int kc0 = I * RC + (int)(it - rfirst);
+        const int kc1 = I * RC + (int)(seg_end - rfirst);
+        const int tbase = I * RB + wid * WB;
+
+        f2 PX[NP], PY[NP], PZ[NP], NM[NP], AX[NP], AY[NP], AZ[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            const int i0 = tbase + lane + 32 * p;
+            const int i1 = i0 + 32 * NP;
+            const float4 q0 = i0 < n ? pos[i0] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 q1 = i1 < n ? pos[i1] : make_float4(0.f, 0.f, 0.f, 0.f);
+            PX[p] = f2_pack(q0.x, q1.x);
+            PY[p] = f2_pack(q0.y, q1.y);
+            PZ[p] = f2_pack(q0.z, q1.z);
+            NM[p] = f2_pack(-q0.w, -q1.w);  // negated: reactions point along -r
+            AX[p] = AY[p] = AZ[p] = ZERO;
+        }
+        for (int kc = kc0; kc < kc1; ++kc) {
+            const int jb = kc * 32;
+            __syncthreads();
+            if (wid == 0) sC[lane] = (jb + lane < n) ? pos[jb + lane] : pad;
+            __syncthreads();
+            const bool diag = kc < (I + 1) * RC;
+            float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll 2
+            for (int r = 0; r < 32; ++r) {
+                const float4 q = sC[diag ? r : ((lane + r) & 31)];
+                const f2 XB = f2_pack(q.x, q.x), YB = f2_pack(q.y, q.y);
+                const f2 ZB = f2_pack(q.z, q.z), MB = f2_pack(q.w, q.w);
+                f2 FX = f2_pack(fx, 0.f), FY = f2_pack(fy, 0.f), FZ = f2_pack(fz, 0.f);
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    const f2 rx = f2_sub(XB, PX[p]);
+                    const f2 ry = f2_sub(YB, PY[p]);
+                    const f2 rz = f2_sub(ZB, PZ[p]);
+                    f2 d2 = f2_fma(rx, rx, EPS2);
+                    d2 = f2_fma(ry, ry, d2);
+                    d2 = f2_fma(rz, rz, d2);
+                    float dlo, dhi;
+                    f2_unpack(d2, dlo, dhi);
+                    const f2 inv = f2_pack(rsqrt_approx(dlo), rsqrt_approx(dhi));
+                    const f2 inv3 = f2_mul(f2_mul(inv, inv), inv);
+                    const f2 st = f2_mul(MB, inv3);
+                    AX[p] = f2_fma(rx, st, AX[p]);
+                    AY[p] = f2_fma(ry, st, AY[p]);
+                    AZ[p] = f2_fma(rz, st, AZ[p]);
+                    if (!diag) {
+                        const f2 ss = f2_mul(NM[p], inv3);
+                        FX = f2_fma(rx, ss, FX);
+                        FY = f2_fma(ry, ss, FY);
+                        FZ = f2_fma(rz, ss, FZ);
+                    }
+                }
+                if (!diag) {
+                    float lo, hi;
+                    f2_unpack(FX, lo, hi);
+                    fx = lo + hi;
+                    f2_unpack(FY, lo, hi);
+                    fy = lo + hi;
+                    f2_unpack(FZ, lo, hi);
+                    fz = lo + hi;
+                    const int from = (lane + 1) & 31;
+                    fx = __shfl_sync(0xffffffffu, fx, from);
+                    fy = __shfl_sync(0xffffffffu, fy, from);
+                    fz = __shfl_sync(0xffffffffu, fz, from);
+                }
+            }
+            if (!diag) {
+                sF[0][wid][lane] = fx;
+                sF[1][wid][lane] = fy;
+                sF[2][wid][lane] = fz;
+                __syncthreads();
+                if (wid == 0 && jb + lane < n) {
+                    float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+                    for (int w = 0; w < W; ++w) {
+                        sx += sF[0][w][lane];
+                        sy += sF[1][w][lane];
+                        sz += sF[2][w][lane];
+                    }
+                    spart[sym_soff(I, n, RB) + (jb + lane - (I + 1) * RB)] = make_float4(sx, sy, sz, 0.f);
+                }
+            }
+        }
+        float4 *dst = tpart + (size_t)(c + I) * RB + wid * WB;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            float x0, x1, y0, y1, z0, z1;
+            f2_unpack(AX[p], x0, x1);
+            f2_unpack(AY[p], y0, y1);
+            f2_unpack(AZ[p], z0, z1);
+            dst[lane + 32 * p] = make_float4(x0, y0, z0, 0.f);
+            dst[lane + 32 * (p + NP)] = make_float4(x1, y1, z1, 0.f);
+        }
+        it = seg_end;
+    }
+}
+
 // Per body: target-side slots (CTA order) + source-side rows 0..I_b-1 (row
 // order), then the reference's kick / damping / drift (unfused, its order).
 __global__ void sym_integrate_kernel(const float4 *__restrict__ pos_old, float4 *__restrict__ pos_new,
@@ -219,11 +349,16 @@ __global__ void sym_integrate_kernel(const float4 *__restrict__ pos_old, float4 
 
 typedef void (*sym_kernel_t)(const float4 *, int, float, float4 *, float4 *, long long, int, int);
 
+// bpt > 0: scalar kernel with bpt bodies per lane; bpt < 0: packed f32x2
+// kernel with -bpt bodies per lane
 static sym_kernel_t sym_kernel_for(int w, int bpt)
 {
     if (w == 4 && bpt == 8) return sym_force_kernel<4, 8>;
     if (w == 8 && bpt == 4) return sym_force_kernel<8, 4>;
     if (w == 8 && bpt == 8) return sym_force_kernel<8, 8>;
+    if (w == 8 && bpt == -8) return sym_force_kernel_f2<8, 4>;
+    if (w == 4 && bpt == -8) return sym_force_kernel_f2<4, 4>;
+    if (w == 8 && bpt == -4) return sym_force_kernel_f2<8, 2>;
     return nullptr;
 }
 
@@ -237,7 +372,7 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl)
     p.n = n;
     p.warps = warps;
     p.bpt = bpt;
-    p.rb = warps * 32 * bpt;
+    p.rb = warps * 32 * (bpt < 0 ? -bpt : bpt);
     p.nc = (n + 31) / 32;
     p.nrb = (n + p.rb - 1) / p.rb;
     p.total = n > 0 ? sym_prefix(p.nrb, p.nc, p.rb / 32) : 0;
