@@ -60,6 +60,20 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value, world, device=None):
+    """Max of a per-rank float over all ranks (the timing rule: the slowest
+    rank's time).  Uses the initialised process group (NCCL on GPUs, gloo on
+    CPU); identity for one rank."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload_state():
     from utc_gb300 import ics
 
@@ -267,12 +281,7 @@ def run_ours(args):
     wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
 
-    t_max = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    dev_ms_max = float(t_max.item())
+    dev_ms_max = max_over_ranks(dev_ms, world, dev)
     interactions = float(N_BODIES) ** 2 * LEAPFROG_STEPS * args.steps * world
     value = interactions / (dev_ms_max * 1e-3) / 1e9
 
@@ -294,12 +303,7 @@ def run_ours(args):
                 "nb_run_host")
         if k >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
-    e2e_t = torch.tensor([sum(e2e_times)], dtype=torch.float64, device=dev)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_val = interactions / float(e2e_t.item()) / 1e9
+    e2e_val = interactions / max_over_ranks(sum(e2e_times), world, dev) / 1e9
     state_bytes = N_BODIES * 16
 
     line = None

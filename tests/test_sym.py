@@ -21,7 +21,7 @@ def close(got, want, tol=2e-5):
 
 
 @pytest.mark.parametrize("n", [1, 2, 31, 33, 255, 256, 257, 1000, 2047, 2048, 2049, 4097, 9000])
-@pytest.mark.parametrize("shape", [(256, 8), (256, 4), (128, 8)])
+@pytest.mark.parametrize("shape", [(256, 8), (256, 4), (128, 8), (256, -8), (128, -8), (256, -4)])
 def test_sym_accel_vs_fp64(cuda, n, shape):
     p, _ = ics.plummer(n, seed=n)
     pos = ics.f32(p)
