@@ -143,6 +143,38 @@ def measured_peaks():
         return {}
 
 
+def integrate_bytes(n, algo, plan):
+    """Bytes the integrate kernel has to move per launch: the state read and
+    written (pos and vel, 64 B per body) plus every partial-sum entry it adds,
+    16 B each: the target-side slots of the CTAs that worked on the body's
+    block and, on the symmetric path, one source-side entry per earlier row
+    block."""
+    grid, rb = plan["grid"], plan["tbsize"]
+    nblk = (n + rb - 1) // rb
+    if algo == "sym":
+        nc, rc = (n + 31) // 32, rb // 32
+
+        def first(b):
+            return b * nc - rc * (b * (b - 1) // 2)
+        total = first(nblk)
+    else:
+        ng = (n + 31) // 32
+
+        def first(b):
+            return b * ng
+        total = nblk * ng
+
+    def owner(it):
+        return ((it + 1) * grid - 1) // total
+    entries = 0
+    for b in range(nblk):
+        rows = min(rb, n - b * rb)
+        entries += (owner(first(b + 1) - 1) - owner(first(b)) + 1) * rows
+        if algo == "sym":
+            entries += b * rows  # source-side rows 0..b-1
+    return 64.0 * n + 16.0 * entries
+
+
 def committed_traffic():
     """Per-launch DRAM bytes of the top kernels from the committed ncu summary."""
     try:
@@ -319,7 +351,7 @@ def run_ours(args):
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         nominal_tf = sms * 128 * 2 * (clk.get("sm_max_mhz") or 2070.0) * 1e6 / 1e12
         traffic = committed_traffic()
-        integ_bytes = 80.0 * N_BODIES
+        integ_bytes = integrate_bytes(N_BODIES, args.algo, plan)
         hbm = peaks.get("hbm_gbs")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -334,7 +366,8 @@ def run_ours(args):
             "fp32_pipe_pct": 100.0 * achieved_tf / fp32_peak_tf,
             "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak_tf,
                          "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak_tf,
-                         "traffic": traffic.get("force_bytes_per_launch"),
+                         "traffic": traffic.get("force_bytes_per_launch" if args.algo == "sym"
+                                                else "directed_force_bytes_per_launch"),
                          "kernel": "sym_force_kernel" if args.algo == "sym" else "sk_force_kernel",
                          "flop_per_launch": force_flops,
                          "avg_launch_ms": force_avg_s * 1e3,
@@ -348,8 +381,9 @@ def run_ours(args):
                                     "frac": (integ_bytes / integ_avg_s / 1e9) / hbm if hbm else None,
                                     "bytes_per_launch": integ_bytes,
                                     "avg_launch_ms": integ_avg_s * 1e3,
-                                    "traffic": traffic.get("integrate_bytes_per_launch"),
-                                    "note": "80 B/body algorithmic; at N=65536 the state is L2-resident"},
+                                    "traffic": traffic.get("integrate_bytes_per_launch") if args.algo == "sym" else None,
+                                    "note": "state (64 B/body) + every partial entry the kernel adds "
+                                            "(16 B each); at N=65536 these are mostly L2-resident"},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * state_bytes,
                     "d2h_bytes_per_step": state_bytes,
                     "how": "nb_run_host (C ABI) from pinned host buffers, 100 leapfrog steps, "

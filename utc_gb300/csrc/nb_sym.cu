@@ -26,6 +26,15 @@
 //    partials go to slot cta + row as in the directed kernel.
 // The integrate kernel adds, per body, its target-side slots (CTA order) and
 // its source-side entries spart[0..I_b-1][b] (row order): deterministic.
+//
+// Shape.  The loop is issue-bound (16 FP32 instructions + 1 MUFU per pair,
+// plus one LDS and three SHFL per lane and rotation step), and its issue
+// rate improves with more independent targets per lane rather than with more
+// warps: one-warp CTAs with 16 targets per lane (225 registers, 8 warps per
+// SM) run 15 % faster than 8-warp CTAs with 8 targets per lane (80 registers,
+// 24 warps per SM) on GB300.  Small row blocks make the triangular
+// source-side array large (about N^2 / (2 rb) float4), so the default shape
+// grows the row block when that array would pass kSymSpartBudget.
 #include "nb_internal.cuh"
 
 namespace nb {
@@ -54,8 +63,8 @@ __device__ __forceinline__ int sym_row_of(long long it, int nc, int rc, int nrb)
     return lo;
 }
 
-template <int W, int BPT>
-__global__ void __launch_bounds__(32 * W) sym_force_kernel(const float4 *__restrict__ pos, int n,
+template <int W, int BPT, int MINB>
+__global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *__restrict__ pos, int n,
                                                            float eps2, float4 *__restrict__ tpart,
                                                            float4 *__restrict__ spart,
                                                            long long total, int nc, int nrb)
@@ -81,7 +90,8 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel(const float4 *__restr
         const int kc1 = I * RC + (int)(seg_end - rfirst);
         const int tbase = I * RB + wid * WB;
 
-        float px[BPT], py[BPT], pz[BPT], pm[BPT], ax[BPT], ay[BPT], az[BPT];
+        // nm = -m: the reaction on the chunk body points along -r
+        float px[BPT], py[BPT], pz[BPT], nm[BPT], ax[BPT], ay[BPT], az[BPT];
 #pragma unroll
         for (int k = 0; k < BPT; ++k) {
             const int i = tbase + lane + 32 * k;
@@ -90,7 +100,7 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel(const float4 *__restr
             px[k] = q.x;
             py[k] = q.y;
             pz[k] = q.z;
-            pm[k] = q.w;
+            nm[k] = -q.w;
             ax[k] = ay[k] = az[k] = 0.f;
         }
         for (int kc = kc0; kc < kc1; ++kc) {
@@ -130,13 +140,13 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel(const float4 *__restr
                         const float inv = rsqrt_approx(d2);
                         const float inv3 = inv * (inv * inv);
                         const float st = q.w * inv3;    // on the target, from the chunk body
-                        const float ss = pm[k] * inv3;  // on the chunk body, from the target
+                        const float ss = nm[k] * inv3;  // on the chunk body, from the target
                         ax[k] = fmaf(rx, st, ax[k]);
                         ay[k] = fmaf(ry, st, ay[k]);
                         az[k] = fmaf(rz, st, az[k]);
-                        fx = fmaf(-rx, ss, fx);
-                        fy = fmaf(-ry, ss, fy);
-                        fz = fmaf(-rz, ss, fz);
+                        fx = fmaf(rx, ss, fx);
+                        fy = fmaf(ry, ss, fy);
+                        fz = fmaf(rz, ss, fz);
                     }
                     const int from = (lane + 1) & 31;
                     fx = __shfl_sync(0xffffffffu, fx, from);
@@ -321,8 +331,28 @@ __global__ void sym_integrate_kernel(const float4 *__restrict__ pos_old, float4 
         ay = __fadd_rn(ay, q.y);
         az = __fadd_rn(az, q.z);
     }
-    for (int r = 0; r < I; ++r) {
-        const float4 q = spart[sym_soff(r, n, rb) + (i - (r + 1) * rb)];
+    // rows 0..I-1 in order; entry of row r at soff(r) + i - (r + 1) rb, and
+    // consecutive rows are n - (r + 2) rb apart.  Eight loads are issued
+    // before their adds so the row walk is not one load latency per row.
+    long long off = (long long)i - rb;
+    int r = 0;
+    for (; r + 8 <= I; r += 8) {
+        float4 q[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            q[u] = spart[off];
+            off += (long long)n - (long long)(r + u + 2) * rb;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            ax = __fadd_rn(ax, q[u].x);
+            ay = __fadd_rn(ay, q[u].y);
+            az = __fadd_rn(az, q[u].z);
+        }
+    }
+    for (; r < I; ++r) {
+        const float4 q = spart[off];
+        off += (long long)n - (long long)(r + 2) * rb;
         ax = __fadd_rn(ax, q.x);
         ay = __fadd_rn(ay, q.y);
         az = __fadd_rn(az, q.z);
@@ -349,21 +379,48 @@ __global__ void sym_integrate_kernel(const float4 *__restrict__ pos_old, float4 
 
 typedef void (*sym_kernel_t)(const float4 *, int, float, float4 *, float4 *, long long, int, int);
 
-// bpt > 0: scalar kernel with bpt bodies per lane; bpt < 0: packed f32x2
+// bpt > 0: scalar kernel with bpt bodies per lane (the third template
+// argument asks for that many resident CTAs per SM); bpt < 0: packed f32x2
 // kernel with -bpt bodies per lane
 static sym_kernel_t sym_kernel_for(int w, int bpt)
 {
-    if (w == 4 && bpt == 8) return sym_force_kernel<4, 8>;
-    if (w == 8 && bpt == 4) return sym_force_kernel<8, 4>;
-    if (w == 8 && bpt == 8) return sym_force_kernel<8, 8>;
+    if (w == 1 && bpt == 16) return sym_force_kernel<1, 16, 8>;
+    if (w == 1 && bpt == 20) return sym_force_kernel<1, 20, 8>;
+    if (w == 2 && bpt == 16) return sym_force_kernel<2, 16, 4>;
+    if (w == 4 && bpt == 20) return sym_force_kernel<4, 20, 2>;
+    if (w == 8 && bpt == 24) return sym_force_kernel<8, 24, 1>;
+    if (w == 4 && bpt == 8) return sym_force_kernel<4, 8, 1>;
+    if (w == 8 && bpt == 4) return sym_force_kernel<8, 4, 1>;
+    if (w == 8 && bpt == 8) return sym_force_kernel<8, 8, 1>;
     if (w == 8 && bpt == -8) return sym_force_kernel_f2<8, 4>;
     if (w == 4 && bpt == -8) return sym_force_kernel_f2<4, 4>;
     if (w == 8 && bpt == -4) return sym_force_kernel_f2<8, 2>;
     return nullptr;
 }
 
+// Largest source-side array the default shape accepts before it moves to a
+// bigger row block.
+constexpr long long kSymSpartBudget = 8ll << 30;
+
+static long long sym_spart_entries(int n, int rb)
+{
+    const int nrb = (n + rb - 1) / rb;
+    return nrb > 1 ? sym_soff(nrb - 1, n, rb) : 0;
+}
+
 int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl)
 {
+    if (warps == 0 && bpt == 0) {
+        // one-warp CTAs x 16 targets (row block 512); then 4 x 20 (2560),
+        // 8 x 24 (6144) while the source-side array is over budget
+        static const int shapes[3][2] = {{1, 16}, {4, 20}, {8, 24}};
+        int s = 0;
+        while (s < 2 && sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) * (long long)sizeof(float4) >
+                            kSymSpartBudget)
+            ++s;
+        warps = shapes[s][0];
+        bpt = shapes[s][1];
+    }
     if (warps == 0) warps = 8;
     if (bpt == 0) bpt = 8;
     sym_kernel_t k = sym_kernel_for(warps, bpt);
@@ -384,7 +441,7 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl)
     if (p.total > 0 && grid > p.total) grid = p.total;
     p.grid = p.total > 0 ? (int)grid : 0;
     p.slots = p.total > 0 ? p.grid + p.nrb - 1 : 0;
-    p.spart_size = p.nrb > 1 ? sym_soff(p.nrb - 1, n, p.rb) : 0;
+    p.spart_size = sym_spart_entries(n, p.rb);
     *pl = p;
     return NB_OK;
 }
