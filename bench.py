@@ -496,18 +496,8 @@ def run_adjoint(args):
     y = ics.gaussian_targets(n, seed=1, sigma=0.5)
     p32, v32 = ics.f32(p64), ics.f32(v64)
     yt = torch.tensor(y, dtype=torch.float32, device="cuda")
-    sysm = NBodySystem(n, "f32", "fast", kick="physical", eps2=eps2, damping=1.0, dt=dt)
     stream = torch.cuda.current_stream()
-    pT = torch.empty((n, 4), device="cuda")
-    vT = torch.empty((n, 4), device="cuda")
-    for _ in range(args.warmup):
-        sysm.set_state(p32, v32)
-        sysm.adj_forward(T, K)
-        sysm.get_state_device(pT, vT)
-        gw = torch.zeros((n, 4), device="cuda")
-        sysm.adj_backward(gw)
-    torch.cuda.synchronize()
-    # time the three phases separately (median of the repetitions)
+
     def timed(fn):
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -516,23 +506,45 @@ def run_adjoint(args):
         b.record(stream)
         b.synchronize()
         return a.elapsed_time(b)
-    ts = {"forward": [], "adj_forward": [], "adj_backward": []}
-    for _ in range(max(args.steps, 3)):
-        sysm.set_state(p32, v32)
-        ts["forward"].append(timed(lambda: sysm.step(T)))
-        sysm.set_state(p32, v32)
-        ts["adj_forward"].append(timed(lambda: sysm.adj_forward(T, K)))
-        sysm.get_state_device(pT, vT)
-        gx = torch.zeros((n, 4), device="cuda")
-        gx[:, :3] = 2.0 * (pT[:, :3] - yt)
+
+    def measure(algo):
+        """Median times of the plain forward, the checkpointed forward and the
+        backward (recompute + VJP) with one algorithm's kernels."""
+        sysm = NBodySystem(n, "f32", algo, kick="physical", eps2=eps2, damping=1.0, dt=dt)
+        pT = torch.empty((n, 4), device="cuda")
+        vT = torch.empty((n, 4), device="cuda")
+        for _ in range(args.warmup):
+            sysm.set_state(p32, v32)
+            sysm.adj_forward(T, K)
+            sysm.get_state_device(pT, vT)
+            sysm.adj_backward(torch.zeros((n, 4), device="cuda"))
+        torch.cuda.synchronize()
+        ts = {"forward": [], "adj_forward": [], "adj_backward": []}
         res = {}
-        ts["adj_backward"].append(timed(lambda: res.update(g=sysm.adj_backward(gx))))
-    med = {k: float(np.median(v)) for k, v in ts.items()}
-    gx0, gv0, gm = [t.cpu().numpy() for t in res["g"]]
+        for _ in range(max(args.steps, 3)):
+            sysm.set_state(p32, v32)
+            ts["forward"].append(timed(lambda: sysm.step(T)))
+            sysm.set_state(p32, v32)
+            ts["adj_forward"].append(timed(lambda: sysm.adj_forward(T, K)))
+            sysm.get_state_device(pT, vT)
+            gx = torch.zeros((n, 4), device="cuda")
+            gx[:, :3] = 2.0 * (pT[:, :3] - yt)
+            ts["adj_backward"].append(timed(lambda: res.update(g=sysm.adj_backward(gx))))
+        sysm.close()
+        med = {k: float(np.median(v)) for k, v in ts.items()}
+        return med, [t.cpu().numpy() for t in res["g"]]
+
+    algo = args.algo
+    other = "fast" if algo == "sym" else "sym"
+    med, (gx0, gv0, gm) = measure(algo)
+    med_o, g_o = measure(other)
     out = {"workload": "adjoint", "n": n, "steps": T, "ckpt_every": K, "eps2": float(eps2),
-           "dt": float(dt), "kick": "physical (G=1)", "ms_median": med,
+           "dt": float(dt), "kick": "physical (G=1)", "algo": algo, "ms_median": med,
            "adjoint_over_forward": med["adj_backward"] / med["forward"],
-           "adjoint_incl_ckpt_forward_over_forward": (med["adj_backward"] + med["adj_forward"]) / med["forward"]}
+           "adjoint_incl_ckpt_forward_over_forward": (med["adj_backward"] + med["adj_forward"]) / med["forward"],
+           "other_algo": {"algo": other, "ms_median": med_o,
+                          "adjoint_over_forward": med_o["adj_backward"] / med_o["forward"],
+                          "adjoint_over_default_forward": med_o["adj_backward"] / med["forward"]}}
     if not args.no_cpu_baseline:
         t0 = time.perf_counter()
         L, rx, rv, rm = oracle.adjoint(p32.astype(np.float64), v32.astype(np.float64), y, float(eps2),
@@ -541,12 +553,14 @@ def run_adjoint(args):
             return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
         out["vs_fp64_reference_adjoint"] = {"dx0": rel(gx0[:, :3], rx), "dv0": rel(gv0[:, :3], rv),
                                             "dm": rel(gm, rm), "cpu_s": time.perf_counter() - t0}
+        out["other_algo"]["vs_fp64_reference_adjoint"] = {"dx0": rel(g_o[0][:, :3], rx),
+                                                          "dv0": rel(g_o[1][:, :3], rv), "dm": rel(g_o[2], rm)}
         # FP64 central differences on 64 coordinates, on an N=2048 replica
         nf = 2048
         pf, vf = ics.uniform_cube(nf, seed=3)
         yf = ics.gaussian_targets(nf, seed=4, sigma=0.5)
         pf32, vf32 = ics.f32(pf), ics.f32(vf)
-        with NBodySystem(nf, "f32", "fast", kick="physical", eps2=eps2, damping=1.0, dt=dt) as s2:
+        with NBodySystem(nf, "f32", algo, kick="physical", eps2=eps2, damping=1.0, dt=dt) as s2:
             s2.set_state(pf32, vf32)
             s2.adj_forward(T, K)
             q, _ = s2.get_state()
@@ -570,7 +584,6 @@ def run_adjoint(args):
         out["vs_fp64_central_differences"] = {"n": nf, "coords": 64, "h": h,
                                               "rel_err_median": float(np.median(errs)),
                                               "rel_err_max": float(np.max(errs))}
-    sysm.close()
     print(json.dumps(out), flush=True)
     return 0
 

@@ -19,11 +19,12 @@ def rel(a, b):
     return float(np.linalg.norm(np.asarray(a, np.float64) - b) / (np.linalg.norm(b) + 1e-300))
 
 
-def gpu_grads(pos32, vel32, y, kick, eps2, dt, damping, steps, every, G=1.0):
+def gpu_grads(pos32, vel32, y, kick, eps2, dt, damping, steps, every, G=1.0, algo="fast"):
+    """algo "fast": directed forward and VJP kernels; "sym": symmetric ones."""
     import torch
 
     n = pos32.shape[0]
-    with NBodySystem(n, "f32", "fast", kick=kick, eps2=eps2, damping=damping, dt=dt, G=G) as s:
+    with NBodySystem(n, "f32", algo, kick=kick, eps2=eps2, damping=damping, dt=dt, G=G) as s:
         s.set_state(pos32, vel32)
         s.adj_forward(steps, every)
         pT, _ = s.get_state()
@@ -34,16 +35,17 @@ def gpu_grads(pos32, vel32, y, kick, eps2, dt, damping, steps, every, G=1.0):
         return pT, gx0[:, :3].cpu().numpy(), gv0[:, :3].cpu().numpy(), gm.cpu().numpy()
 
 
+@pytest.mark.parametrize("algo", ["fast", "sym"])
 @pytest.mark.parametrize("kick", ["physical", "reference"])
-@pytest.mark.parametrize("n,steps,every", [(96, 30, 7), (1000, 20, 20), (257, 12, 1)])
-def test_adjoint_matches_fp64_reference(cuda, kick, n, steps, every):
+@pytest.mark.parametrize("n,steps,every", [(96, 30, 7), (1000, 20, 20), (257, 12, 1), (3000, 6, 4)])
+def test_adjoint_matches_fp64_reference(cuda, algo, kick, n, steps, every):
     p64, v64 = ics.uniform_cube(n, seed=n)
     if kick == "reference":
         p64[:, 3] *= n  # O(1) masses so the kick x pos.w is not negligible
     y = ics.gaussian_targets(n, seed=n + 1)
     p32, v32 = ics.f32(p64), ics.f32(v64)
     eps2, dt = np.float32(1e-2), np.float32(1e-3)
-    _, gx, gv, gm = gpu_grads(p32, v32, y, kick, eps2, dt, 1.0, steps, every)
+    _, gx, gv, gm = gpu_grads(p32, v32, y, kick, eps2, dt, 1.0, steps, every, algo=algo)
     km = oracle.KICK_PHYSICAL if kick == "physical" else oracle.KICK_REFERENCE
     L, rx, rv, rm = oracle.adjoint(p32.astype(np.float64), v32.astype(np.float64), y, float(eps2), 1.0,
                                    float(dt), steps, kick_mode=km)
@@ -52,13 +54,14 @@ def test_adjoint_matches_fp64_reference(cuda, kick, n, steps, every):
     assert rel(gm, rm) <= 1e-4
 
 
-def test_checkpoint_interval_does_not_change_gradients(cuda):
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_checkpoint_interval_does_not_change_gradients(cuda, algo):
     n, steps = 300, 24
     p64, v64 = ics.uniform_cube(n, seed=3)
     y = ics.gaussian_targets(n, seed=4)
     p32, v32 = ics.f32(p64), ics.f32(v64)
-    outs = [gpu_grads(p32, v32, y, "physical", np.float32(1e-2), np.float32(1e-3), 1.0, steps, k)
-            for k in (1, 5, 24)]
+    outs = [gpu_grads(p32, v32, y, "physical", np.float32(1e-2), np.float32(1e-3), 1.0, steps, k,
+                      algo=algo) for k in (1, 5, 24)]
     for o in outs[1:]:
         for a, b in zip(o, outs[0]):
             assert np.asarray(a).tobytes() == np.asarray(b).tobytes()
@@ -109,3 +112,28 @@ def test_autograd_function_loss_gradients(cuda):
         dx, dv, dm = s.adj_backward(gx, gv)
     assert torch.equal(x0.grad, dx[:, :3]) and torch.equal(v0.grad, dv[:, :3])
     assert torch.equal(m.grad, dm)
+
+
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+@pytest.mark.parametrize("kick", ["physical", "reference"])
+def test_second_backward_recomputes_every_segment(cuda, algo, kick):
+    """The forward pass leaves the last segment's states in place and the first
+    backward uses them; a second backward after the same forward recomputes
+    that segment too and must give the same bits."""
+    import torch
+
+    n, steps, every = 700, 17, 5
+    p64, v64 = ics.uniform_cube(n, seed=21)
+    if kick == "reference":
+        p64[:, 3] *= n
+    p32, v32 = ics.f32(p64), ics.f32(v64)
+    with NBodySystem(n, "f32", algo, kick=kick, eps2=np.float32(1e-2), damping=0.999,
+                     dt=np.float32(1e-3)) as s:
+        s.set_state(p32, v32)
+        s.adj_forward(steps, every)
+        gx = torch.randn((n, 4), device="cuda")
+        gv = torch.randn((n, 4), device="cuda")
+        a = [t.cpu().numpy() for t in s.adj_backward(gx, gv)]
+        b = [t.cpu().numpy() for t in s.adj_backward(gx, gv)]
+    for x, y in zip(a, b):
+        assert x.tobytes() == y.tobytes()

@@ -73,7 +73,13 @@ struct nb_ctx {
         float *gm = nullptr;
         float4 *partial = nullptr;
         nb::SkPlan plan;
+        // symmetric contexts: symmetric VJP with its own layout
+        bool sym = false;
+        nb::SymPlan splan;
+        float4 *sym_t = nullptr, *sym_s = nullptr;
         bool ready = false;
+        // the forward pass left the last segment's states in seg_pos/seg_acc
+        bool live_last = false;
     } adj;
 };
 
@@ -135,6 +141,8 @@ static void free_ctx(nb_ctx *c)
     cudaFree(c->adj.gbuf);
     cudaFree(c->adj.gm);
     cudaFree(c->adj.partial);
+    cudaFree(c->adj.sym_t);
+    cudaFree(c->adj.sym_s);
     cudaFree(c->sym_t);
     cudaFree(c->sym_s);
     for (int k = 0; k < 2; ++k) {
@@ -485,15 +493,32 @@ static int adj_reserve(nb_ctx *c, int nckpt, int every)
     auto &A = c->adj;
     int st;
     if (!A.lx) {
-        if ((st = nb::adj_plan(c->p.n, 0, 0, c->device, &A.plan))) return st;
+        // a retry after a failed allocation starts from nothing
+        cudaFree(A.sym_t);
+        cudaFree(A.sym_s);
+        cudaFree(A.partial);
+        cudaFree(A.vel_tmp);
+        A.sym_t = A.sym_s = A.partial = A.vel_tmp = nullptr;
+        A.sym = uses_sym(c);
+        if (A.sym) {
+            if ((st = nb::sym_vjp_plan(c->p.n, 0, 0, c->device, &A.splan)) ||
+                (st = dev_alloc((void **)&A.sym_t, (size_t)A.splan.slots * A.splan.rb * sizeof(float4),
+                                "adjoint allocation")) ||
+                (st = dev_alloc((void **)&A.sym_s, (size_t)A.splan.spart_size * sizeof(float4),
+                                "adjoint allocation")))
+                return st;
+        } else {
+            if ((st = nb::adj_plan(c->p.n, 0, 0, c->device, &A.plan)) ||
+                (st = dev_alloc((void **)&A.partial,
+                                (size_t)A.plan.slots * A.plan.tbsize * sizeof(float4),
+                                "adjoint allocation")))
+                return st;
+        }
         if ((st = dev_alloc((void **)&A.vel_tmp, n * sizeof(float4), "adjoint allocation")) ||
             (st = dev_alloc((void **)&A.lx, n * sizeof(float4), "adjoint allocation")) ||
             (st = dev_alloc((void **)&A.lv, n * sizeof(float4), "adjoint allocation")) ||
             (st = dev_alloc((void **)&A.gbuf, n * sizeof(float4), "adjoint allocation")) ||
-            (st = dev_alloc((void **)&A.gm, n * sizeof(float), "adjoint allocation")) ||
-            (st = dev_alloc((void **)&A.partial,
-                            (size_t)A.plan.slots * A.plan.tbsize * sizeof(float4),
-                            "adjoint allocation")))
+            (st = dev_alloc((void **)&A.gm, n * sizeof(float), "adjoint allocation")))
             return st;
     }
     if (nckpt > A.cap_ckpt) {
@@ -531,20 +556,50 @@ int nb_adj_forward(nb_ctx *c, int steps, int ckpt_every, void *stream)
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
     const size_t n = (size_t)c->p.n;
+    auto &A = c->adj;
+    const nb_params &p = c->p;
+    // The last segment is the first one the reverse pass needs: its states
+    // (and, for the reference kick, its accelerations) are kept in the
+    // segment buffers as they are computed, so that segment is not
+    // recomputed.  Same kernels, same bits as a recompute.
+    const int t_last = (nckpt - 1) * ckpt_every;
+    A.ready = false;
+    A.live_last = false;
     for (int t = 0; t < steps; ++t) {
         if (t % ckpt_every == 0 && n) {
             const size_t k = (size_t)(t / ckpt_every) * n;
-            NB_CUDA(cudaMemcpyAsync(c->adj.ckpt_pos + k, c->pos[c->cur], n * sizeof(float4),
+            NB_CUDA(cudaMemcpyAsync(A.ckpt_pos + k, c->pos[c->cur], n * sizeof(float4),
                                     cudaMemcpyDeviceToDevice, s));
-            NB_CUDA(cudaMemcpyAsync(c->adj.ckpt_vel + k, c->vel, n * sizeof(float4),
+            NB_CUDA(cudaMemcpyAsync(A.ckpt_vel + k, c->vel, n * sizeof(float4),
                                     cudaMemcpyDeviceToDevice, s));
         }
+        const bool keep = n && t >= t_last;
+        const size_t k = (size_t)(t - t_last);
+        if (keep && t == t_last)
+            NB_CUDA(cudaMemcpyAsync(A.seg_pos, c->pos[c->cur], n * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, s));
+        const float4 *xk = (const float4 *)c->pos[c->cur];
         if ((st = step_once(c, s, nullptr))) return st;
+        if (!keep) continue;
+        if (p.kick == NB_KICK_REFERENCE) {
+            // the step's partial sums are still in the scratch: reduce them to
+            // the bare acceleration at x_k
+            float4 *ak = A.seg_acc + k * n;
+            if (uses_sym(c))
+                st = nb::sym_integrate(c->splan, xk, nullptr, nullptr, c->sym_t, c->sym_s,
+                                       (float)p.damping, (float)p.dt, p.kick, (float)p.G, ak, s);
+            else
+                st = nb::fast_reduce(c->plan, c->partial, 0, xk, (float)p.eps2, ak, nullptr, s);
+            if (st) return st;
+        }
+        NB_CUDA(cudaMemcpyAsync(A.seg_pos + (k + 1) * n, c->pos[c->cur], n * sizeof(float4),
+                                cudaMemcpyDeviceToDevice, s));
     }
-    c->adj.steps = steps;
-    c->adj.every = ckpt_every;
-    c->adj.nckpt = nckpt;
-    c->adj.ready = true;
+    A.steps = steps;
+    A.every = ckpt_every;
+    A.nckpt = nckpt;
+    A.ready = true;
+    A.live_last = n > 0;
     return NB_OK;
 }
 
@@ -571,12 +626,17 @@ int nb_adj_backward(nb_ctx *c, const void *gx_T, const void *gv_T, void *gx0, vo
     for (int seg = A.nckpt - 1; seg >= 0; --seg) {
         const int t0 = seg * A.every;
         const int len = (A.steps - t0) < A.every ? (A.steps - t0) : A.every;
-        // recompute the segment's positions (and accelerations) from its checkpoint
-        NB_CUDA(cudaMemcpyAsync(A.seg_pos, A.ckpt_pos + (size_t)seg * n, n * sizeof(float4),
-                                cudaMemcpyDeviceToDevice, s));
-        NB_CUDA(cudaMemcpyAsync(A.vel_tmp, A.ckpt_vel + (size_t)seg * n, n * sizeof(float4),
-                                cudaMemcpyDeviceToDevice, s));
-        for (int k = 0; k < len; ++k) {
+        // recompute the segment's positions (and accelerations) from its
+        // checkpoint, unless the forward pass left them in place
+        const bool recompute = !(seg == A.nckpt - 1 && A.live_last);
+        A.live_last = false;  // the buffers are reused from here on
+        if (recompute) {
+            NB_CUDA(cudaMemcpyAsync(A.seg_pos, A.ckpt_pos + (size_t)seg * n, n * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, s));
+            NB_CUDA(cudaMemcpyAsync(A.vel_tmp, A.ckpt_vel + (size_t)seg * n, n * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, s));
+        }
+        for (int k = 0; recompute && k < len; ++k) {
             const float4 *xk = A.seg_pos + (size_t)k * n;
             if (uses_sym(c)) {
                 // recompute with the algorithm of the forward pass: same bits
@@ -606,8 +666,15 @@ int nb_adj_backward(nb_ctx *c, const void *gx_T, const void *gv_T, void *gx0, vo
                 if ((st = nb::adj_g(p.n, xk, A.lx, A.lv, A.gbuf, D, dt, p.kick, G, s))) return st;
                 have_g = true;
             }
-            if ((st = nb::adj_vjp(A.plan, xk, A.gbuf, eps2, A.partial, s))) return st;
             const bool more = !(seg == 0 && k == 0);
+            if (A.sym) {
+                if ((st = nb::sym_vjp(A.splan, xk, A.gbuf, eps2, A.sym_t, A.sym_s, s)) ||
+                    (st = nb::adj_update_sym(A.splan, A.sym_t, A.sym_s, xk, A.seg_acc + (size_t)k * n,
+                                             A.lx, A.lv, A.gm, A.gbuf, D, dt, p.kick, G, more ? 1 : 0, s)))
+                    return st;
+                continue;
+            }
+            if ((st = nb::adj_vjp(A.plan, xk, A.gbuf, eps2, A.partial, s))) return st;
             if ((st = nb::adj_update(A.plan, A.partial, xk, A.seg_acc + (size_t)k * n, A.lx, A.lv,
                                      A.gm, A.gbuf, D, dt, p.kick, G, more ? 1 : 0, s)))
                 return st;

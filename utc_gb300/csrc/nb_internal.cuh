@@ -146,6 +146,32 @@ int energy_reduce(int n, const float4 *pos32, const double4 *pos64, const float4
                   double *block_tmp, double *out_dev, cudaStream_t s);
 
 // Symmetric force kernel (nb_sym.cu)
+// Work layout of the symmetric kernels (nb_sym.cu, nb_adjoint.cu): row
+// blocks of rb bodies paired with 32-body chunks at or after their start.
+__host__ __device__ __forceinline__ long long sym_prefix(long long I, int nc, int rc)
+{
+    // items of rows 0..I-1: row i pairs with chunks i*rc .. nc-1
+    return I * (long long)nc - (long long)rc * (I * (I - 1) / 2);
+}
+
+// Source-side array, triangular: row r keeps bodies i >= (r + 1) * rb at
+// soff(r) + i - (r + 1) * rb.
+__host__ __device__ __forceinline__ long long sym_soff(long long r, int n, int rb)
+{
+    return r * (long long)n - (long long)rb * (r * (r + 1) / 2);
+}
+
+__device__ __forceinline__ int sym_row_of(long long it, int nc, int rc, int nrb)
+{
+    int lo = 0, hi = nrb;  // prefix(lo) <= it < prefix(hi)
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (sym_prefix(mid, nc, rc) <= it) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 struct SymPlan {
     int n = 0, warps = 0, bpt = 0;
     int rb = 0;          // bodies per row block (CTA targets)
@@ -156,6 +182,16 @@ struct SymPlan {
     int slots = 0;       // grid + nrb - 1 target-side slots of rb float4
     long long spart_size = 0;  // float4 entries of the source-side array
 };
+// float4 entries of the source-side array for row blocks of rb bodies
+inline long long sym_spart_entries(int n, int rb)
+{
+    const int nrb = (n + rb - 1) / rb;
+    return nrb > 1 ? sym_soff(nrb - 1, n, rb) : 0;
+}
+// Largest source-side array a default shape accepts before it moves to a
+// bigger row block.
+constexpr long long kSymSpartBudget = 8ll << 30;
+
 int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl);
 int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, float4 *spart,
               cudaStream_t s);
@@ -172,6 +208,14 @@ int adj_vjp(const SkPlan &p, const float4 *pos, const float4 *gbuf, float eps2, 
 int adj_update(const SkPlan &p, const float4 *partial, const float4 *pos_prev, const float4 *acc,
                float4 *lx, float4 *lv, float *gm, float4 *gbuf, float damping, float dt, int kick,
                float G, int want_next_g, cudaStream_t s);
+// Symmetric vector-Jacobian product (each unordered pair once) on the
+// symmetric work layout; tpart/spart as in sym_force.
+int sym_vjp_plan(int n, int warps, int bpt, int device, SymPlan *pl);
+int sym_vjp(const SymPlan &p, const float4 *pos, const float4 *gbuf, float eps2, float4 *tpart,
+            float4 *spart, cudaStream_t s);
+int adj_update_sym(const SymPlan &p, const float4 *tpart, const float4 *spart, const float4 *pos_prev,
+                   const float4 *acc, float4 *lx, float4 *lv, float *gm, float4 *gbuf, float damping,
+                   float dt, int kick, float G, int want_next_g, cudaStream_t s);
 
 // Exact-path entry points (nb_exact.cu)
 int exact_step_f32(int n, const float4 *pos_old, float4 *pos_new, float4 *vel, float eps2,

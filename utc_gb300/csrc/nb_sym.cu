@@ -39,30 +39,6 @@
 
 namespace nb {
 
-__host__ __device__ __forceinline__ long long sym_prefix(long long I, int nc, int rc)
-{
-    // items of rows 0..I-1: row i pairs with chunks i*rc .. nc-1
-    return I * (long long)nc - (long long)rc * (I * (I - 1) / 2);
-}
-
-// Source-side array, triangular: row r keeps bodies i >= (r + 1) * rb at
-// soff(r) + i - (r + 1) * rb.
-__host__ __device__ __forceinline__ long long sym_soff(long long r, int n, int rb)
-{
-    return r * (long long)n - (long long)rb * (r * (r + 1) / 2);
-}
-
-__device__ __forceinline__ int sym_row_of(long long it, int nc, int rc, int nrb)
-{
-    int lo = 0, hi = nrb;  // prefix(lo) <= it < prefix(hi)
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (sym_prefix(mid, nc, rc) <= it) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
 template <int W, int BPT, int MINB>
 __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *__restrict__ pos, int n,
                                                            float eps2, float4 *__restrict__ tpart,
@@ -396,16 +372,6 @@ static sym_kernel_t sym_kernel_for(int w, int bpt)
     if (w == 4 && bpt == -8) return sym_force_kernel_f2<4, 4>;
     if (w == 8 && bpt == -4) return sym_force_kernel_f2<8, 2>;
     return nullptr;
-}
-
-// Largest source-side array the default shape accepts before it moves to a
-// bigger row block.
-constexpr long long kSymSpartBudget = 8ll << 30;
-
-static long long sym_spart_entries(int n, int rb)
-{
-    const int nrb = (n + rb - 1) / rb;
-    return nrb > 1 ? sym_soff(nrb - 1, n, rb) : 0;
 }
 
 int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl)
