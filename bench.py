@@ -426,9 +426,11 @@ def run_precision(args):
     tidx = np.sort(np.random.default_rng(7).choice(n, min(4096, n), replace=False)).astype(np.int32)
     out = {"workload": "precision", "n": n, "steps": steps, "eps2": eps2, "dt": dt,
            "subsample": int(tidx.size), "modes": {}}
-    for mode in ("f32", "f32sym", "f32comp"):
-        prec = "f32" if mode in ("f32", "f32sym") else "f32comp"
-        algo = "sym" if mode == "f32sym" else "fast"
+    # mode: (precision, algorithm); "fast" = directed kernels, "sym" = each
+    # unordered pair once
+    modes = {"f32": ("f32", "fast"), "f32sym": ("f32", "sym"), "f32comp": ("f32comp", "fast"),
+             "f32comp_sym": ("f32comp", "sym")}
+    for mode, (prec, algo) in modes.items():
         sysm = NBodySystem(n, prec, algo, kick="physical", eps2=np.float32(eps2), damping=1.0,
                            dt=np.float32(dt))
         if prec == "f32":
@@ -440,11 +442,11 @@ def run_precision(args):
         E0 = None
         for t in range(steps + 1):
             e, bodies = sysm.energy(with_bodies=True)
-            if mode == "f32sym":
+            if algo == "sym":
                 # the energy pass uses the directed kernel; take this mode's
                 # own accelerations for the force error
-                bodies = bodies.copy()
-                bodies[:, :3] = sysm.accel()
+                bodies = np.array(bodies, dtype=np.float64)
+                bodies[:, :3] = np.asarray(sysm.accel(), np.float64)[:, :3]
             pos, vel = sysm.get_state()
             # FP64 forces at the state the GPU holds (float positions in plain
             # mode, FP64 absolute positions in the compensated mode)
@@ -473,7 +475,7 @@ def run_precision(args):
         sysm.close()
     peak, _ = probe_fma_peak(20000, True)
     out["forward_N1M"] = {}
-    for mode in ("f32", "f32sym", "f32comp"):
+    for mode in modes:
         r = out["modes"][mode]["force_kernel_G_interactions_per_s"]
         out["forward_N1M"][mode] = {"G_interactions_per_s": r, "tflops_20flop": r * 20 / 1e3,
                                     "frac_of_fp32_peak": r * 20e9 / peak}

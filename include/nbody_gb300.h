@@ -62,7 +62,7 @@ typedef enum {
 /* Force algorithm. */
 typedef enum {
     /* Stream-K tiled kernel: packed f32x2 FMA, rsqrt.approx, deterministic
-     * partial sums.  NB_F32 only. */
+     * partial sums.  NB_F32 and NB_F32_COMP. */
     NB_ALGO_FAST = 0,
     /* IEEE arithmetic in the reference's operation order, sources summed in
      * index order: bit-identical to the reference's sequential BodySystem<T>
@@ -71,7 +71,8 @@ typedef enum {
     /* Each unordered pair evaluated once and applied to both bodies (the
      * pair term is odd in r): 16 FP32 operations and one rsqrt per two
      * interactions.  Same per-pair terms as NB_ALGO_FAST, different summation
-     * order; deterministic.  NB_F32 only. */
+     * order; deterministic.  NB_F32 and NB_F32_COMP (compensated partial
+     * sums). */
     NB_ALGO_SYM = 2
 } nb_algo;
 

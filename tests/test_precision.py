@@ -35,11 +35,12 @@ def test_state_roundtrip(cuda):
     assert np.array_equal(v2[:, 3], v[:, 3])
 
 
-@pytest.mark.parametrize("n", [1, 7, 1000, 4097])
-def test_compensated_accel_vs_fp64(cuda, n):
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+@pytest.mark.parametrize("n", [1, 7, 383, 385, 1000, 4097])
+def test_compensated_accel_vs_fp64(cuda, n, algo):
     p, _ = ics.plummer(n, seed=n)
     v = np.zeros_like(p)
-    with NBodySystem(n, "f32comp", "fast", eps2=1e-4) as s:
+    with NBodySystem(n, "f32comp", algo, eps2=1e-4) as s:
         s.set_state(p, v)
         a = s.accel()
     p32 = p.astype(np.float32).astype(np.float64)  # the pair terms read float positions
@@ -47,14 +48,15 @@ def test_compensated_accel_vs_fp64(cuda, n):
     assert body_err(a, ref).max() <= 2e-6
 
 
-def test_compensated_beats_plain_at_scale(cuda):
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_compensated_beats_plain_at_scale(cuda, algo):
     n = 65536
     p, _ = ics.plummer(n, seed=5)
     v = np.zeros_like(p)
     tidx = np.random.default_rng(1).choice(n, 256, replace=False).astype(np.int32)
     p32 = p.astype(np.float32)
     ref = oracle.accel_subset_f64(p32.astype(np.float64), tidx, float(np.float32(1e-4)))
-    with NBodySystem(n, "f32comp", "fast", eps2=1e-4) as s:
+    with NBodySystem(n, "f32comp", algo, eps2=1e-4) as s:
         s.set_state(p, v)
         ac = s.accel()[tidx]
     with NBodySystem(n, "f32", "fast", eps2=np.float32(1e-4)) as s:
@@ -65,12 +67,13 @@ def test_compensated_beats_plain_at_scale(cuda):
     assert ec < ep
 
 
-def test_compensated_steps_vs_fp64_oracle(cuda):
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_compensated_steps_vs_fp64_oracle(cuda, algo):
     n, steps = 2048, 10
     p, v = ics.plummer(n, seed=9)
     p32 = p.astype(np.float32).astype(np.float64)
     p[:, :3] = p32[:, :3]  # same starting positions as the float working copy
-    with NBodySystem(n, "f32comp", "fast", kick="physical", eps2=1e-3, damping=1.0, dt=1e-3) as s:
+    with NBodySystem(n, "f32comp", algo, kick="physical", eps2=1e-3, damping=1.0, dt=1e-3) as s:
         s.set_state(p, v)
         s.step(steps)
         pg, vg = s.get_state()
@@ -105,10 +108,11 @@ def test_energy_momentum_vs_fp64(cuda, precision):
     assert np.abs(bodies[tidx, 3] - phi).max() <= tol * np.abs(phi).max()
 
 
-def test_energy_conserved_by_small_steps(cuda):
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_energy_conserved_by_small_steps(cuda, algo):
     n = 4096
     p, v = ics.plummer(n, seed=6)
-    with NBodySystem(n, "f32comp", "fast", kick="physical", eps2=1e-2, damping=1.0, dt=1e-4) as s:
+    with NBodySystem(n, "f32comp", algo, kick="physical", eps2=1e-2, damping=1.0, dt=1e-4) as s:
         s.set_state(p, v)
         e0 = s.energy()
         s.step(50)
@@ -117,10 +121,11 @@ def test_energy_conserved_by_small_steps(cuda):
     assert abs(E1 - E0) <= 1e-5 * abs(E0)
 
 
-def test_compensated_run_host_frames(cuda):
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_compensated_run_host_frames(cuda, algo):
     n = 1500
     p, v = ics.plummer(n, seed=12)
-    with NBodySystem(n, "f32comp", "fast", kick="physical", eps2=1e-3, damping=1.0, dt=1e-3) as s:
+    with NBodySystem(n, "f32comp", algo, kick="physical", eps2=1e-3, damping=1.0, dt=1e-3) as s:
         frames, t = s.run_host(p, v, 9, 2)
         s.set_state(p, v)
         want = []
@@ -130,3 +135,12 @@ def test_compensated_run_host_frames(cuda):
     assert frames.shape == (4, n, 4) and frames.dtype == np.float64
     for k in range(4):
         assert frames[k].tobytes() == want[k].tobytes()
+
+
+@pytest.mark.parametrize("n,shape", [(65536, (32, 12)), (1048576, (256, 12))])
+def test_compensated_sym_default_shape(cuda, n, shape):
+    """Compensated symmetric plan: one-warp CTAs x 12 targets unless the
+    source-side array's hi and lo halves would pass 8 GiB (then 4 and 8 warps)."""
+    with NBodySystem(n, "f32comp", "sym") as s:
+        info = s.plan_info()
+    assert (info["block"], info["bpt"]) == shape

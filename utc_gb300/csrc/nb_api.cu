@@ -95,8 +95,8 @@ static int validate(const nb_params *p)
         return set_error(NB_ERR_INVALID, "unknown precision");
     if (p->algo != NB_ALGO_FAST && p->algo != NB_ALGO_EXACT && p->algo != NB_ALGO_SYM)
         return set_error(NB_ERR_INVALID, "unknown algo");
-    if (p->algo == NB_ALGO_SYM && p->precision != NB_F32)
-        return set_error(NB_ERR_UNSUPPORTED, "NB_ALGO_SYM runs on NB_F32 contexts");
+    if (p->algo == NB_ALGO_SYM && p->precision == NB_F64)
+        return set_error(NB_ERR_UNSUPPORTED, "NB_ALGO_SYM runs on NB_F32 and NB_F32_COMP contexts");
     if (p->kick != NB_KICK_REFERENCE && p->kick != NB_KICK_PHYSICAL)
         return set_error(NB_ERR_INVALID, "unknown kick mode");
     if (p->memtype < NB_MEM_PAGEABLE || p->memtype > NB_MEM_UNIFIED)
@@ -106,8 +106,9 @@ static int validate(const nb_params *p)
         return set_error(NB_ERR_INVALID, "eps2, damping, dt and G must be finite");
     if (p->precision == NB_F64 && p->algo == NB_ALGO_FAST)
         return set_error(NB_ERR_UNSUPPORTED, "NB_F64 runs the exact algorithm only");
-    if (p->precision == NB_F32_COMP && p->algo != NB_ALGO_FAST)
-        return set_error(NB_ERR_UNSUPPORTED, "NB_F32_COMP runs the fast (compensated) algorithm only");
+    if (p->precision == NB_F32_COMP && p->algo == NB_ALGO_EXACT)
+        return set_error(NB_ERR_UNSUPPORTED,
+                         "NB_F32_COMP runs the fast or symmetric (compensated) algorithms only");
     if (p->precision == NB_F32_COMP && p->memtype == NB_MEM_UNIFIED)
         return set_error(NB_ERR_UNSUPPORTED, "NB_F32_COMP keeps its state in device memory");
     return NB_OK;
@@ -169,6 +170,8 @@ static int dalloc(nb_ctx *c, void **p, size_t bytes)
 }
 
 static bool uses_sym(const nb_ctx *c) { return c->p.precision == NB_F32 && c->p.algo == NB_ALGO_SYM; }
+// compensated context stepping with the compensated symmetric kernel
+static bool comp_sym(const nb_ctx *c) { return c->p.precision == NB_F32_COMP && c->p.algo == NB_ALGO_SYM; }
 // the directed stream-K plan (c->plan) also serves the symmetric context's
 // energy pass and adjoint
 static bool uses_fast(const nb_ctx *c)
@@ -239,7 +242,7 @@ int nb_create(const nb_params *p, nb_ctx **out)
     }
     if (uses_fast(c) || is_comp(c)) {
         const int flags = is_comp(c) ? nb::SK_COMP : 0;
-        const bool own_shape = !uses_sym(c);
+        const bool own_shape = !(uses_sym(c) || comp_sym(c));
         const int block = (own_shape && p->block) ? p->block : (is_comp(c) ? 256 : 0);
         const int bpt = (own_shape && p->bpt) ? p->bpt : (is_comp(c) ? 4 : 0);
         st = nb::fast_plan(p->n, block, bpt, p->ctas_per_sm, c->device, &c->plan, flags);
@@ -254,12 +257,14 @@ int nb_create(const nb_params *p, nb_ctx **out)
         size_t pb = mult * (size_t)c->plan.slots * c->plan.tbsize * sizeof(float4);
         const size_t pe = mult * (size_t)c->eplan.slots * c->eplan.tbsize * sizeof(float4);
         if (pe > pb) pb = pe;
-        if (uses_sym(c)) {
-            if ((st = nb::sym_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan)) ||
+        if (uses_sym(c) || comp_sym(c)) {
+            const size_t halves = comp_sym(c) ? 2 : 1;  // compensated: hi and lo blocks
+            if ((st = nb::sym_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan,
+                                   comp_sym(c) ? 1 : 0)) ||
                 (st = dev_alloc((void **)&c->sym_t,
-                                (size_t)c->splan.slots * c->splan.rb * sizeof(float4),
+                                halves * c->splan.slots * c->splan.rb * sizeof(float4),
                                 "symmetric scratch allocation")) ||
-                (st = dev_alloc((void **)&c->sym_s, (size_t)c->splan.spart_size * sizeof(float4),
+                (st = dev_alloc((void **)&c->sym_s, halves * c->splan.spart_size * sizeof(float4),
                                 "symmetric scratch allocation"))) {
                 free_ctx(c);
                 return st;
@@ -349,6 +354,16 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
     void *po = c->pos[c->cur], *pn = c->pos[c->cur ^ 1];
     int st;
     if (ev) NB_CUDA(cudaEventRecord(ev[0], s));
+    if (comp_sym(c)) {
+        st = nb::sym_force(c->splan, c->pos32, (float)p.eps2, c->sym_t, c->sym_s, s);
+        if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
+        if (!st)
+            st = nb::sym_comp_integrate(c->splan, c->sym_t, c->sym_s, (double4 *)c->pos[0], c->pos32,
+                                        (float4 *)c->vel, c->vel_lo, (float)p.damping, (float)p.dt,
+                                        p.dt, p.kick, (float)p.G, (double4 *)acc_out, s);
+        if (!st && ev) NB_CUDA(cudaEventRecord(ev[2], s));
+        return st;  // positions are updated in place: no ping-pong
+    }
     if (is_comp(c)) {
         st = nb::fast_force(c->plan, c->pos32, (float)p.eps2, c->partial, s, nb::SK_COMP);
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
@@ -696,7 +711,7 @@ int nb_launches_per_step(nb_ctx *c)
 int nb_plan_info(nb_ctx *c, int *info5)
 {
     if (!c || !info5) return set_error(NB_ERR_INVALID, "ctx/info is NULL");
-    if (uses_sym(c)) {
+    if (uses_sym(c) || comp_sym(c)) {
         info5[0] = c->splan.warps * 32;
         info5[1] = c->splan.bpt;
         info5[2] = c->splan.grid;

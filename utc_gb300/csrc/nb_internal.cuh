@@ -67,6 +67,13 @@ __device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c)
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
     return r;
 }
+// Knuth's two-sum: s + e == a + b exactly (round-to-nearest, no FMA).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
 __device__ __forceinline__ float rsqrt_approx(float x)
 {
     float r;
@@ -174,6 +181,7 @@ __device__ __forceinline__ int sym_row_of(long long it, int nc, int rc, int nrb)
 
 struct SymPlan {
     int n = 0, warps = 0, bpt = 0;
+    int comp = 0;        // compensated (hi, lo) partials: tpart and spart hold a lo block after the hi block
     int rb = 0;          // bodies per row block (CTA targets)
     int nc = 0;          // 32-body chunks
     int nrb = 0;         // row blocks
@@ -192,12 +200,18 @@ inline long long sym_spart_entries(int n, int rb)
 // bigger row block.
 constexpr long long kSymSpartBudget = 8ll << 30;
 
-int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl);
+int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp = 0);
 int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, float4 *spart,
               cudaStream_t s);
 int sym_integrate(const SymPlan &p, const float4 *pos_old, float4 *pos_new, float4 *vel,
                   const float4 *tpart, const float4 *spart, float damping, float dt, int kick,
                   float G, float4 *acc_out, cudaStream_t s);
+
+// Compensated kick / drift from compensated symmetric partials, or
+// (acc_out != nullptr) the bare FP64 accelerations (nb_precision.cu)
+int sym_comp_integrate(const SymPlan &p, const float4 *tpart, const float4 *spart, double4 *pos64,
+                       float4 *pos32, float4 *vhi, float4 *vlo, float damping, float dt,
+                       double dt64, int kick, float G, double4 *acc_out, cudaStream_t s);
 
 // Adjoint kernels (nb_adjoint.cu)
 int adj_plan(int n, int block, int bpt, int device, SkPlan *pl);

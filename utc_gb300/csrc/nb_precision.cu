@@ -14,13 +14,6 @@
 
 namespace nb {
 
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
-{
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
 // host double4 state -> pos64, pos32, vel_hi, vel_lo
 __global__ void comp_split_kernel(const double4 *__restrict__ pin, const double4 *__restrict__ vin,
                                   double4 *__restrict__ pos64, float4 *__restrict__ pos32,
@@ -111,19 +104,13 @@ __global__ void sk_reduce_kernel(const float4 *__restrict__ partial, int n, int 
     out32[i] = a;
 }
 
-// Compensated kick / damping (FP32 with a carried low part) and FP64 drift.
-__global__ void comp_integrate_kernel(const float4 *__restrict__ partial, int n, int tbsize,
-                                      long long total, int ngroups, int grid, long long lo_off,
-                                      double4 *__restrict__ pos64, float4 *__restrict__ pos32,
-                                      float4 *__restrict__ vhi, float4 *__restrict__ vlo,
-                                      float damping, float dt, double dt64, int kick, float G)
+// Compensated kick / damping (FP32 with a carried low part) and FP64 drift,
+// given the acceleration as a compensated sum S + C.
+__device__ __forceinline__ void comp_kick_drift(int i, float4 S, float4 C, double4 *__restrict__ pos64,
+                                                float4 *__restrict__ pos32, float4 *__restrict__ vhi,
+                                                float4 *__restrict__ vlo, float damping, float dt,
+                                                double dt64, int kick, float G)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int tb = i / tbsize;
-    const int li = i - tb * tbsize;
-    float4 S, C;
-    comp_slot_sum(partial, lo_off, tb, li, tbsize, total, ngroups, grid, S, C);
     const float ax = __fadd_rn(S.x, C.x), ay = __fadd_rn(S.y, C.y), az = __fadd_rn(S.z, C.z);
     double4 p = pos64[i];
     float4 h = vhi[i], l = vlo[i];
@@ -150,6 +137,63 @@ __global__ void comp_integrate_kernel(const float4 *__restrict__ partial, int n,
     pos32[i] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
     vhi[i] = h;
     vlo[i] = l;
+}
+
+__global__ void comp_integrate_kernel(const float4 *__restrict__ partial, int n, int tbsize,
+                                      long long total, int ngroups, int grid, long long lo_off,
+                                      double4 *__restrict__ pos64, float4 *__restrict__ pos32,
+                                      float4 *__restrict__ vhi, float4 *__restrict__ vlo,
+                                      float damping, float dt, double dt64, int kick, float G)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int tb = i / tbsize;
+    const int li = i - tb * tbsize;
+    float4 S, C;
+    comp_slot_sum(partial, lo_off, tb, li, tbsize, total, ngroups, grid, S, C);
+    comp_kick_drift(i, S, C, pos64, pos32, vhi, vlo, damping, dt, dt64, kick, G);
+}
+
+// Compensated symmetric partials: the target-side slots (CTA order) and the
+// source-side rows 0..I-1 (row order), hi and lo halves, summed with
+// two-sums; then the compensated kick / drift, or (acc_out != nullptr) the
+// bare acceleration hi + lo in FP64.
+__global__ void sym_comp_integrate_kernel(const float4 *__restrict__ tpart, const float4 *__restrict__ spart,
+                                          long long tlo, long long slo, int n, int rb, int nc, int nrb,
+                                          long long total, int grid, double4 *__restrict__ pos64,
+                                          float4 *__restrict__ pos32, float4 *__restrict__ vhi,
+                                          float4 *__restrict__ vlo, float damping, float dt,
+                                          double dt64, int kick, float G, double4 *__restrict__ acc_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int rc = rb / 32;
+    const int I = i / rb;
+    const int c0 = sk_owner(sym_prefix(I, nc, rc), total, grid);
+    const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1, total, grid);
+    const int li = i - I * rb;
+    float4 S = make_float4(0.f, 0.f, 0.f, 0.f), C = S;
+    float e;
+    auto add = [&](const float4 h, const float4 l) {
+        two_sum(S.x, h.x, S.x, e); C.x = __fadd_rn(C.x, __fadd_rn(e, l.x));
+        two_sum(S.y, h.y, S.y, e); C.y = __fadd_rn(C.y, __fadd_rn(e, l.y));
+        two_sum(S.z, h.z, S.z, e); C.z = __fadd_rn(C.z, __fadd_rn(e, l.z));
+    };
+    for (int c = c0; c <= c1; ++c) {
+        const size_t k = (size_t)(c + I) * rb + li;
+        add(tpart[k], tpart[tlo + k]);
+    }
+    long long off = (long long)i - rb;  // row r at soff(r) + i - (r + 1) rb
+    for (int r = 0; r < I; ++r) {
+        add(spart[off], spart[slo + off]);
+        off += (long long)n - (long long)(r + 2) * rb;
+    }
+    if (acc_out) {
+        acc_out[i] = make_double4((double)S.x + (double)C.x, (double)S.y + (double)C.y,
+                                  (double)S.z + (double)C.z, 0.0);
+        return;
+    }
+    comp_kick_drift(i, S, C, pos64, pos32, vhi, vlo, damping, dt, dt64, kick, G);
 }
 
 // Energy and momentum, FP64 reduction.  Per body: kinetic 0.5 m |v|^2,
@@ -248,6 +292,19 @@ int comp_integrate(const SkPlan &p, const float4 *partial, double4 *pos64, float
                                                            p.ngroups, p.grid, lo_off, pos64, pos32,
                                                            vhi, vlo, damping, dt, dt64, kick, G);
     NB_LAUNCH_CHECK("comp_integrate_kernel launch");
+    return NB_OK;
+}
+
+int sym_comp_integrate(const SymPlan &p, const float4 *tpart, const float4 *spart, double4 *pos64,
+                       float4 *pos32, float4 *vhi, float4 *vlo, float damping, float dt,
+                       double dt64, int kick, float G, double4 *acc_out, cudaStream_t s)
+{
+    if (p.n == 0) return NB_OK;
+    if (!p.comp) return set_error(NB_ERR_INVALID, "sym_comp_integrate needs a compensated plan");
+    sym_comp_integrate_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(
+        tpart, spart, (long long)p.slots * p.rb, p.spart_size, p.n, p.rb, p.nc, p.nrb, p.total,
+        p.grid, pos64, pos32, vhi, vlo, damping, dt, dt64, kick, G, acc_out);
+    NB_LAUNCH_CHECK("sym_comp_integrate_kernel launch");
     return NB_OK;
 }
 

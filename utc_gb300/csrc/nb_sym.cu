@@ -27,6 +27,12 @@
 // The integrate kernel adds, per body, its target-side slots (CTA order) and
 // its source-side entries spart[0..I_b-1][b] (row order): deterministic.
 //
+// Compensated variant (COMP): each target's per-chunk partial sum (32
+// sources) is folded into a two-sum (hi, lo) pair, the W warps' reactions on
+// a chunk body are combined with two-sums, and both halves are written (lo
+// block after the hi block of tpart and of spart); the compensated
+// integrator sums them with two-sums.
+//
 // Shape.  The loop is issue-bound (16 FP32 instructions + 1 MUFU per pair,
 // plus one LDS and three SHFL per lane and rotation step), and its issue
 // rate improves with more independent targets per lane rather than with more
@@ -39,11 +45,12 @@
 
 namespace nb {
 
-template <int W, int BPT, int MINB>
+template <int W, int BPT, int MINB, bool COMP>
 __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *__restrict__ pos, int n,
                                                            float eps2, float4 *__restrict__ tpart,
                                                            float4 *__restrict__ spart,
-                                                           long long total, int nc, int nrb)
+                                                           long long total, int nc, int nrb,
+                                                           long long tlo, long long slo)
 {
     constexpr int WB = 32 * BPT;
     constexpr int RB = W * WB;
@@ -68,6 +75,9 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
 
         // nm = -m: the reaction on the chunk body points along -r
         float px[BPT], py[BPT], pz[BPT], nm[BPT], ax[BPT], ay[BPT], az[BPT];
+        // COMP: compensated target sums (hi in h*, lo in l*)
+        constexpr int CB = COMP ? BPT : 1;
+        float hx[CB], hy[CB], hz[CB], lx[CB], ly[CB], lz[CB];
 #pragma unroll
         for (int k = 0; k < BPT; ++k) {
             const int i = tbase + lane + 32 * k;
@@ -78,6 +88,7 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
             pz[k] = q.z;
             nm[k] = -q.w;
             ax[k] = ay[k] = az[k] = 0.f;
+            if constexpr (COMP) hx[k] = hy[k] = hz[k] = lx[k] = ly[k] = lz[k] = 0.f;
         }
         for (int kc = kc0; kc < kc1; ++kc) {
             const int jb = kc * 32;
@@ -135,20 +146,57 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
                 sF[2][wid][lane] = fz;
                 __syncthreads();
                 if (wid == 0 && jb + lane < n) {
-                    float sx = 0.f, sy = 0.f, sz = 0.f;
+                    const long long so = sym_soff(I, n, RB) + (jb + lane - (I + 1) * RB);
+                    if constexpr (COMP) {
+                        float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f, e;
 #pragma unroll
-                    for (int w = 0; w < W; ++w) {
-                        sx += sF[0][w][lane];
-                        sy += sF[1][w][lane];
-                        sz += sF[2][w][lane];
+                        for (int w = 0; w < W; ++w) {
+                            two_sum(sx, sF[0][w][lane], sx, e);
+                            cx = __fadd_rn(cx, e);
+                            two_sum(sy, sF[1][w][lane], sy, e);
+                            cy = __fadd_rn(cy, e);
+                            two_sum(sz, sF[2][w][lane], sz, e);
+                            cz = __fadd_rn(cz, e);
+                        }
+                        spart[so] = make_float4(sx, sy, sz, 0.f);
+                        spart[slo + so] = make_float4(cx, cy, cz, 0.f);
+                    } else {
+                        float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+                        for (int w = 0; w < W; ++w) {
+                            sx += sF[0][w][lane];
+                            sy += sF[1][w][lane];
+                            sz += sF[2][w][lane];
+                        }
+                        spart[so] = make_float4(sx, sy, sz, 0.f);
                     }
-                    spart[sym_soff(I, n, RB) + (jb + lane - (I + 1) * RB)] = make_float4(sx, sy, sz, 0.f);
+                }
+            }
+            if constexpr (COMP) {
+                // fold this chunk's 32-source partial sums into (hi, lo)
+#pragma unroll
+                for (int k = 0; k < BPT; ++k) {
+                    float e;
+                    two_sum(hx[k], ax[k], hx[k], e);
+                    lx[k] = __fadd_rn(lx[k], e);
+                    two_sum(hy[k], ay[k], hy[k], e);
+                    ly[k] = __fadd_rn(ly[k], e);
+                    two_sum(hz[k], az[k], hz[k], e);
+                    lz[k] = __fadd_rn(lz[k], e);
+                    ax[k] = ay[k] = az[k] = 0.f;
                 }
             }
         }
         float4 *dst = tpart + (size_t)(c + I) * RB + wid * WB;
 #pragma unroll
-        for (int k = 0; k < BPT; ++k) dst[lane + 32 * k] = make_float4(ax[k], ay[k], az[k], 0.f);
+        for (int k = 0; k < BPT; ++k) {
+            if constexpr (COMP) {
+                dst[lane + 32 * k] = make_float4(hx[k], hy[k], hz[k], 0.f);
+                dst[tlo + lane + 32 * k] = make_float4(lx[k], ly[k], lz[k], 0.f);
+            } else {
+                dst[lane + 32 * k] = make_float4(ax[k], ay[k], az[k], 0.f);
+            }
+        }
         it = seg_end;
     }
 }
@@ -163,7 +211,8 @@ template <int W, int NP>
 __global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__restrict__ pos, int n,
                                                               float eps2, float4 *__restrict__ tpart,
                                                               float4 *__restrict__ spart,
-                                                              long long total, int nc, int nrb)
+                                                              long long total, int nc, int nrb,
+                                                              long long, long long)
 {
     constexpr int BPT = 2 * NP;
     constexpr int WB = 32 * BPT;
@@ -353,35 +402,51 @@ __global__ void sym_integrate_kernel(const float4 *__restrict__ pos_old, float4 
     vel[i] = v;
 }
 
-typedef void (*sym_kernel_t)(const float4 *, int, float, float4 *, float4 *, long long, int, int);
+typedef void (*sym_kernel_t)(const float4 *, int, float, float4 *, float4 *, long long, int, int,
+                             long long, long long);
 
 // bpt > 0: scalar kernel with bpt bodies per lane (the third template
 // argument asks for that many resident CTAs per SM); bpt < 0: packed f32x2
-// kernel with -bpt bodies per lane
-static sym_kernel_t sym_kernel_for(int w, int bpt)
+// kernel with -bpt bodies per lane.  comp: the compensated kernel (scalar
+// shapes with up to 12 targets per lane: 13 registers per target).
+static sym_kernel_t sym_kernel_for(int w, int bpt, int comp)
 {
-    if (w == 1 && bpt == 16) return sym_force_kernel<1, 16, 8>;
-    if (w == 1 && bpt == 20) return sym_force_kernel<1, 20, 8>;
-    if (w == 2 && bpt == 16) return sym_force_kernel<2, 16, 4>;
-    if (w == 4 && bpt == 20) return sym_force_kernel<4, 20, 2>;
-    if (w == 8 && bpt == 24) return sym_force_kernel<8, 24, 1>;
-    if (w == 4 && bpt == 8) return sym_force_kernel<4, 8, 1>;
-    if (w == 8 && bpt == 4) return sym_force_kernel<8, 4, 1>;
-    if (w == 8 && bpt == 8) return sym_force_kernel<8, 8, 1>;
+    if (comp) {
+        if (w == 1 && bpt == 12) return sym_force_kernel<1, 12, 8, true>;
+        if (w == 4 && bpt == 12) return sym_force_kernel<4, 12, 2, true>;
+        if (w == 8 && bpt == 12) return sym_force_kernel<8, 12, 1, true>;
+        if (w == 1 && bpt == 8) return sym_force_kernel<1, 8, 8, true>;
+        if (w == 8 && bpt == 8) return sym_force_kernel<8, 8, 1, true>;
+        return nullptr;
+    }
+    if (w == 1 && bpt == 16) return sym_force_kernel<1, 16, 8, false>;
+    if (w == 1 && bpt == 20) return sym_force_kernel<1, 20, 8, false>;
+    if (w == 2 && bpt == 16) return sym_force_kernel<2, 16, 4, false>;
+    if (w == 4 && bpt == 20) return sym_force_kernel<4, 20, 2, false>;
+    if (w == 8 && bpt == 24) return sym_force_kernel<8, 24, 1, false>;
+    if (w == 4 && bpt == 8) return sym_force_kernel<4, 8, 1, false>;
+    if (w == 8 && bpt == 4) return sym_force_kernel<8, 4, 1, false>;
+    if (w == 8 && bpt == 8) return sym_force_kernel<8, 8, 1, false>;
     if (w == 8 && bpt == -8) return sym_force_kernel_f2<8, 4>;
     if (w == 4 && bpt == -8) return sym_force_kernel_f2<4, 4>;
     if (w == 8 && bpt == -4) return sym_force_kernel_f2<8, 2>;
     return nullptr;
 }
 
-int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl)
+int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp)
 {
     if (warps == 0 && bpt == 0) {
-        // one-warp CTAs x 16 targets (row block 512); then 4 x 20 (2560),
-        // 8 x 24 (6144) while the source-side array is over budget
-        static const int shapes[3][2] = {{1, 16}, {4, 20}, {8, 24}};
+        // plain: one-warp CTAs x 16 targets (row block 512); then 4 x 20
+        // (2560), 8 x 24 (6144) while the source-side array is over budget.
+        // Compensated (hi and lo halves): 1 x 12 (384), 4 x 12 (1536),
+        // 8 x 12 (3072).
+        static const int plain[3][2] = {{1, 16}, {4, 20}, {8, 24}};
+        static const int compd[3][2] = {{1, 12}, {4, 12}, {8, 12}};
+        const int(*shapes)[2] = comp ? compd : plain;
+        const long long halves = comp ? 2 : 1;
         int s = 0;
-        while (s < 2 && sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) * (long long)sizeof(float4) >
+        while (s < 2 && halves * sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) *
+                                (long long)sizeof(float4) >
                             kSymSpartBudget)
             ++s;
         warps = shapes[s][0];
@@ -389,12 +454,13 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl)
     }
     if (warps == 0) warps = 8;
     if (bpt == 0) bpt = 8;
-    sym_kernel_t k = sym_kernel_for(warps, bpt);
+    sym_kernel_t k = sym_kernel_for(warps, bpt, comp);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "symmetric kernel shape not compiled");
     SymPlan p;
     p.n = n;
     p.warps = warps;
     p.bpt = bpt;
+    p.comp = comp;
     p.rb = warps * 32 * (bpt < 0 ? -bpt : bpt);
     p.nc = (n + 31) / 32;
     p.nrb = (n + p.rb - 1) / p.rb;
@@ -416,9 +482,11 @@ int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, fl
               cudaStream_t s)
 {
     if (p.total == 0) return NB_OK;
-    sym_kernel_t k = sym_kernel_for(p.warps, p.bpt);
+    sym_kernel_t k = sym_kernel_for(p.warps, p.bpt, p.comp);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "symmetric kernel shape not compiled");
-    k<<<p.grid, 32 * p.warps, 0, s>>>(pos, p.n, eps2, tpart, spart, p.total, p.nc, p.nrb);
+    // lo blocks (compensated plans) follow the hi blocks
+    const long long tlo = (long long)p.slots * p.rb, slo = p.spart_size;
+    k<<<p.grid, 32 * p.warps, 0, s>>>(pos, p.n, eps2, tpart, spart, p.total, p.nc, p.nrb, tlo, slo);
     NB_LAUNCH_CHECK("sym_force_kernel launch");
     return NB_OK;
 }
