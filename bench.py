@@ -612,8 +612,35 @@ def run_batched(args):
     out = {"workload": "batched", "systems": int(sizes.size), "bodies": int(sizes.sum()),
            "n_min": int(sizes.min()), "n_max": int(sizes.max()), "interactions_per_step": pairs,
            "steps": steps, "eps2": 1e-3, "dt": 1e-3}
+    out["algo"] = args.algo
+    other = "fast" if args.algo == "sym" else "sym"
+
+    def graph_and_per_system(algo):
+        """Graph time and per-system time with the other algorithm's kernels."""
+        with torch.cuda.stream(stream), NBodyBatch(sizes, kick="physical", eps2=np.float32(1e-3),
+                                                   dt=np.float32(1e-3), algo=algo) as b:
+            b.set_state(pos, vel, stream=sh)
+            tune = b.autotune(reps=2, cache_path=cache, stream=sh)
+            res = {}
+            for name, fn in (("graph", lambda: b.run(steps, sh)),
+                             ("per_system", lambda: b.step_per_system(steps, sh))):
+                b.set_state(pos, vel, stream=sh)
+                fn()  # warm-up
+                b.set_state(pos, vel, stream=sh)
+                stream.synchronize()
+                a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                c.record(stream)
+                c.synchronize()
+                res[name] = a.elapsed_time(c)
+            return {"algo": algo, "autotune": tune, "ms_batched_graph": res["graph"],
+                    "ms_per_system_launches": res["per_system"],
+                    "speedup_vs_per_system": res["per_system"] / res["graph"],
+                    "G_interactions_per_s_batched": pairs * steps / (res["graph"] * 1e-3) / 1e9}
+
     with torch.cuda.stream(stream), NBodyBatch(sizes, kick="physical", eps2=np.float32(1e-3),
-                                               dt=np.float32(1e-3)) as b:
+                                               dt=np.float32(1e-3), algo=args.algo) as b:
         b.set_state(pos, vel, stream=sh)
         out["autotune"] = b.autotune(reps=2, cache_path=cache, stream=sh)
         out["plan"] = b.plan_info()
@@ -657,6 +684,8 @@ def run_batched(args):
         "final_pos_rel_diff_max_vs_per_system": float((d / (w + 0.1)).max()),
         "tasks_equal_per_system_bitwise": bool(pt.tobytes() == pr.tobytes()),
     })
+    out["other_algo"] = graph_and_per_system(other)
+    out["speedup_vs_other_algo_per_system"] = out["other_algo"]["ms_per_system_launches"] / t_graph
     print(json.dumps(out), flush=True)
     return 0
 
@@ -670,7 +699,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="plain", choices=["plain", "precision", "adjoint", "batched"])
     ap.add_argument("--algo", default="sym", choices=["fast", "sym"],
-                    help="force algorithm of the plain workload")
+                    help="force algorithm (plain, adjoint and batched workloads)")
     ap.add_argument("--n", type=int, default=0, help="body count override for extension workloads")
     args = ap.parse_args()
     args.steps_given = "--steps" in sys.argv

@@ -35,11 +35,14 @@ def per_system(arr, sizes):
 SIZES = [1, 2, 31, 33, 128, 300, 1024, 5000, 77]
 
 
-@pytest.mark.parametrize("shape", [(2, 4), (2, 8), (4, 2), (4, 4), (4, 8), (8, 2), (8, 4), (8, 8)])
-def test_batch_accelerations_vs_oracle(cuda, shape):
+@pytest.mark.parametrize("algo,shape", [("fast", s) for s in [(2, 4), (2, 8), (4, 2), (4, 4), (4, 8), (8, 2),
+                                                                (8, 4), (8, 8)]] +
+                         [("sym", s) for s in [(1, 8), (1, 12), (1, 16), (2, 8), (2, 16), (4, 8), (4, 16)]])
+def test_batch_accelerations_vs_oracle(cuda, algo, shape):
     pos, _ = make_batch(SIZES, seed=10)
     vel = np.zeros_like(pos)
-    with NBodyBatch(SIZES, eps2=EPS2, dt=DT, warps_per_cta=shape[0], bodies_per_lane=shape[1]) as b:
+    with NBodyBatch(SIZES, eps2=EPS2, dt=DT, warps_per_cta=shape[0], bodies_per_lane=shape[1],
+                    algo=algo) as b:
         assert b.plan_info()["warps_per_cta"] == shape[0]
         b.set_state(pos, vel)
         b.step(1)
@@ -52,13 +55,14 @@ def test_batch_accelerations_vs_oracle(cuda, shape):
         assert (d <= 2e-5 * (w + w.mean())).all()
 
 
-def test_graph_run_equals_step_launches(cuda):
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_graph_run_equals_step_launches(cuda, algo):
     import torch
 
     sizes = ics.batch_sizes(40, lo=128, hi=2048, seed=3)
     pos, vel = make_batch(sizes, seed=1)
     stream = torch.cuda.Stream()
-    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b:
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT, algo=algo) as b:
         b.set_state(pos, vel)
         b.step(7)
         want = b.get_state()
@@ -80,25 +84,27 @@ def test_graph_run_equals_step_launches(cuda):
     assert got3[0].tobytes() == want3[0].tobytes()
 
 
-def test_per_system_baseline_equals_independent_contexts(cuda):
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_per_system_baseline_equals_independent_contexts(cuda, algo):
     sizes = [64, 1000, 3, 4096]
     pos, vel = make_batch(sizes, seed=7)
-    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b:
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT, algo=algo) as b:
         b.set_state(pos, vel)
         b.step_per_system(3)
         got, _ = b.get_state()
     for p, v, g in zip(per_system(pos, sizes), per_system(vel, sizes), per_system(got, sizes)):
-        with NBodySystem(p.shape[0], "f32", "fast", kick="physical", eps2=EPS2, damping=1.0, dt=DT) as s:
+        with NBodySystem(p.shape[0], "f32", algo, kick="physical", eps2=EPS2, damping=1.0, dt=DT) as s:
             s.set_state(p, v)
             s.step(3)
             want, _ = s.get_state()
         assert g.tobytes() == want.tobytes()
 
 
-def test_batched_matches_per_system_within_tolerance(cuda):
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_batched_matches_per_system_within_tolerance(cuda, algo):
     sizes = ics.batch_sizes(24, lo=128, hi=4096, seed=5)
     pos, vel = make_batch(sizes, seed=2)
-    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b:
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT, algo=algo) as b:
         b.set_state(pos, vel)
         b.step(5)
         bat, _ = b.get_state()
@@ -110,11 +116,12 @@ def test_batched_matches_per_system_within_tolerance(cuda):
     assert (d <= 1e-5 * (w + 0.1)).all()
 
 
-def test_autotune_and_cache(cuda, tmp_path):
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_autotune_and_cache(cuda, tmp_path, algo):
     sizes = ics.batch_sizes(64, lo=128, hi=4096, seed=11)
     pos, vel = make_batch(sizes, seed=4)
     cache = str(tmp_path / "tune.txt")
-    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b:
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT, algo=algo) as b:
         b.set_state(pos, vel)
         w, k = b.autotune(reps=1, cache_path=cache)
         info = b.plan_info()
@@ -125,7 +132,7 @@ def test_autotune_and_cache(cuda, tmp_path):
         tuned, _ = b.get_state()
     lines = open(cache).read().strip().splitlines()
     assert len(lines) == 1 and lines[0].endswith(f"{w} {k}")
-    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b2:
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT, algo=algo) as b2:
         b2.set_state(pos, vel)
         assert b2.autotune(reps=1, cache_path=cache) == (w, k)  # served from the cache
         assert len(open(cache).read().strip().splitlines()) == 1
@@ -134,8 +141,9 @@ def test_autotune_and_cache(cuda, tmp_path):
     assert tuned.tobytes() == again.tobytes()
 
 
+@pytest.mark.parametrize("algo", ["fast", "sym"])
 @pytest.mark.parametrize("kick", ["physical", "reference"])
-def test_batched_adjoint_matches_per_system_adjoint(cuda, kick):
+def test_batched_adjoint_matches_per_system_adjoint(cuda, kick, algo):
     import torch
 
     sizes = [1, 40, 300, 129, 1000]
@@ -150,7 +158,7 @@ def test_batched_adjoint_matches_per_system_adjoint(cuda, kick):
         ys.append(ics.gaussian_targets(n, seed=40 + k))
     pos, vel, y = np.concatenate(ps), np.concatenate(vs), np.concatenate(ys)
     eps2, dt = np.float32(1e-2), np.float32(1e-3)
-    with NBodyBatch(sizes, kick=kick, eps2=eps2, dt=dt) as b:
+    with NBodyBatch(sizes, kick=kick, eps2=eps2, dt=dt, algo=algo) as b:
         b.set_state(pos, vel)
         b.adj_forward(steps, every)
         pT, _ = b.get_state()
@@ -167,10 +175,11 @@ def test_batched_adjoint_matches_per_system_adjoint(cuda, kick):
             assert np.linalg.norm(got - want) <= 1e-4 * np.linalg.norm(want) + 1e-12
 
 
-def test_task_pattern_baseline_equals_per_system(cuda):
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_task_pattern_baseline_equals_per_system(cuda, algo):
     sizes = [64, 1000, 3, 4096, 77, 500]
     pos, vel = make_batch(sizes, seed=9)
-    with NBodyBatch(sizes, eps2=EPS2, dt=DT) as b:
+    with NBodyBatch(sizes, eps2=EPS2, dt=DT, algo=algo) as b:
         b.set_state(pos, vel)
         b.step_per_system(3)
         want, _ = b.get_state()

@@ -16,7 +16,16 @@
 //    warp + global block index; the integrate kernel sums them in warp order.
 // The step loop is captured in a CUDA graph (nb_batch_run), and an autotuner
 // picks the warps per CTA and bodies per lane.
+//
+// NB_ALGO_SYM batches use the single-system symmetric layout per system (a
+// warp's row block of 32*BPT targets paired with every 32-body chunk at or
+// after its start, each unordered pair once; the chunk rotates through the
+// warp carrying its reaction), all systems' (row, chunk) items concatenated
+// and split over warps the same way.  Each item belongs to one warp, which
+// writes the reactions on its chunk bodies to the system's triangular
+// source-side array; target-side partials go to slot warp + global row.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -123,6 +132,34 @@ __global__ void __launch_bounds__(32 * WPB) bk_force_kernel(const float4 *__rest
     }
 }
 
+// The reference's kick / damping / drift (unfused, its order), or the bare
+// acceleration when acc_out != nullptr.
+__device__ __forceinline__ void batch_kick_drift(int i, float ax, float ay, float az,
+                                                 const float4 *__restrict__ pos_old,
+                                                 float4 *__restrict__ pos_new, float4 *__restrict__ vel,
+                                                 float damping, float dt, int kick, float G,
+                                                 float4 *__restrict__ acc_out)
+{
+    if (acc_out) {
+        acc_out[i] = make_float4(ax, ay, az, 0.f);
+        return;
+    }
+    float4 p = pos_old[i];
+    float4 v = vel[i];
+    const float k = kick == NB_KICK_REFERENCE ? p.w : G;
+    v.x = __fadd_rn(v.x, __fmul_rn(__fmul_rn(ax, k), dt));
+    v.y = __fadd_rn(v.y, __fmul_rn(__fmul_rn(ay, k), dt));
+    v.z = __fadd_rn(v.z, __fmul_rn(__fmul_rn(az, k), dt));
+    v.x = __fmul_rn(v.x, damping);
+    v.y = __fmul_rn(v.y, damping);
+    v.z = __fmul_rn(v.z, damping);
+    p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
+    p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+    p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+    pos_new[i] = p;
+    vel[i] = v;
+}
+
 __global__ void bk_integrate_kernel(const float4 *__restrict__ pos_old, float4 *__restrict__ pos_new,
                                     float4 *__restrict__ vel, const float4 *__restrict__ partial,
                                     BatchDev bd, int nbody, int wtb, long long total, int workers,
@@ -149,26 +186,176 @@ __global__ void bk_integrate_kernel(const float4 *__restrict__ pos_old, float4 *
         ay = __fadd_rn(ay, q.y);
         az = __fadd_rn(az, q.z);
     }
-    if (acc_out) {
-        acc_out[i] = make_float4(ax, ay, az, 0.f);
-        return;
-    }
-    float4 p = pos_old[i];
-    float4 v = vel[i];
-    const float k = kick == NB_KICK_REFERENCE ? p.w : G;
-    v.x = __fadd_rn(v.x, __fmul_rn(__fmul_rn(ax, k), dt));
-    v.y = __fadd_rn(v.y, __fmul_rn(__fmul_rn(ay, k), dt));
-    v.z = __fadd_rn(v.z, __fmul_rn(__fmul_rn(az, k), dt));
-    v.x = __fmul_rn(v.x, damping);
-    v.y = __fmul_rn(v.y, damping);
-    v.z = __fmul_rn(v.z, damping);
-    p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
-    p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
-    p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
-    pos_new[i] = p;
-    vel[i] = v;
+    batch_kick_drift(i, ax, ay, az, pos_old, pos_new, vel, damping, dt, kick, G, acc_out);
 }
 
+
+struct BatchSymDev {
+    const int *sys_off;       // [nsys + 1] body offsets
+    const long long *it_off;  // [nsys + 1] (row, chunk) item offsets
+    const int *row_off;       // [nsys + 1] global row offsets
+    const long long *sp_off;  // [nsys + 1] source-side array offsets (float4)
+    const int *body_sys;      // [nbody] system of each body
+    int nsys;
+};
+
+template <int WPB, int BPT>
+__global__ void __launch_bounds__(32 * WPB) bks_force_kernel(const float4 *__restrict__ pos, BatchSymDev bd,
+                                                             float eps2, float4 *__restrict__ tpart,
+                                                             float4 *__restrict__ spart, long long total,
+                                                             int workers)
+{
+    constexpr int RB = 32 * BPT;
+    constexpr int RC = BPT;
+    __shared__ __align__(16) float4 sC[WPB][32];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const int w = blockIdx.x * WPB + wid;
+    if (w >= workers) return;
+    long long it = sk_start(w, total, workers);
+    const long long end = sk_start(w + 1, total, workers);
+    if (it >= end) return;
+    const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
+    int s = find_sys(bd.it_off, bd.nsys, it);
+    while (it < end) {
+        while (it >= bd.it_off[s + 1]) ++s;
+        const int o = bd.sys_off[s];
+        const int ns = bd.sys_off[s + 1] - o;
+        const int nc = (ns + 31) / 32, nrb = (ns + RB - 1) / RB;
+        const long long base = bd.it_off[s];
+        const int I = sym_row_of(it - base, nc, RC, nrb);
+        const long long rfirst = base + sym_prefix(I, nc, RC);
+        const long long rend = base + sym_prefix(I + 1, nc, RC);
+        const long long seg_end = end < rend ? end : rend;
+        const int kc0 = I * RC + (int)(it - rfirst);
+        const int kc1 = I * RC + (int)(seg_end - rfirst);
+        const int tbase = I * RB;
+
+        float px[BPT], py[BPT], pz[BPT], nm[BPT], ax[BPT], ay[BPT], az[BPT];
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const int li = tbase + lane + 32 * k;
+            // missing targets get zero mass: their reactions on the chunk are 0
+            const float4 q = li < ns ? pos[o + li] : make_float4(0.f, 0.f, 0.f, 0.f);
+            px[k] = q.x;
+            py[k] = q.y;
+            pz[k] = q.z;
+            nm[k] = -q.w;
+            ax[k] = ay[k] = az[k] = 0.f;
+        }
+        for (int kc = kc0; kc < kc1; ++kc) {
+            const int jb = kc * 32;
+            __syncwarp();  // previous chunk's reads are done
+            sC[wid][lane] = (jb + lane < ns) ? pos[o + jb + lane] : pad;
+            __syncwarp();
+            if (kc < (I + 1) * RC) {
+                // chunk inside the own row block: directed, target side only
+#pragma unroll 4
+                for (int j = 0; j < 32; ++j) {
+                    const float4 q = sC[wid][j];
+#pragma unroll
+                    for (int k = 0; k < BPT; ++k) {
+                        const float rx = q.x - px[k], ry = q.y - py[k], rz = q.z - pz[k];
+                        float d2 = fmaf(rx, rx, eps2);
+                        d2 = fmaf(ry, ry, d2);
+                        d2 = fmaf(rz, rz, d2);
+                        const float inv = rsqrt_approx(d2);
+                        const float sc = (q.w * inv) * (inv * inv);
+                        ax[k] = fmaf(rx, sc, ax[k]);
+                        ay[k] = fmaf(ry, sc, ay[k]);
+                        az[k] = fmaf(rz, sc, az[k]);
+                    }
+                }
+            } else {
+                float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll 2
+                for (int r = 0; r < 32; ++r) {
+                    const float4 q = sC[wid][(lane + r) & 31];
+#pragma unroll
+                    for (int k = 0; k < BPT; ++k) {
+                        const float rx = q.x - px[k], ry = q.y - py[k], rz = q.z - pz[k];
+                        float d2 = fmaf(rx, rx, eps2);
+                        d2 = fmaf(ry, ry, d2);
+                        d2 = fmaf(rz, rz, d2);
+                        const float inv = rsqrt_approx(d2);
+                        const float inv3 = inv * (inv * inv);
+                        const float st = q.w * inv3;
+                        const float ss = nm[k] * inv3;
+                        ax[k] = fmaf(rx, st, ax[k]);
+                        ay[k] = fmaf(ry, st, ay[k]);
+                        az[k] = fmaf(rz, st, az[k]);
+                        fx = fmaf(rx, ss, fx);
+                        fy = fmaf(ry, ss, fy);
+                        fz = fmaf(rz, ss, fz);
+                    }
+                    const int from = (lane + 1) & 31;
+                    fx = __shfl_sync(0xffffffffu, fx, from);
+                    fy = __shfl_sync(0xffffffffu, fy, from);
+                    fz = __shfl_sync(0xffffffffu, fz, from);
+                }
+                // lane l holds the reaction on chunk body l
+                if (jb + lane < ns)
+                    spart[bd.sp_off[s] + sym_soff(I, ns, RB) + (jb + lane - (I + 1) * RB)] =
+                        make_float4(fx, fy, fz, 0.f);
+            }
+        }
+        float4 *dst = tpart + ((long long)w + bd.row_off[s] + I) * RB;
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) dst[lane + 32 * k] = make_float4(ax[k], ay[k], az[k], 0.f);
+        it = seg_end;
+    }
+}
+
+// Per body: target-side slots of its row (warp order), then the source-side
+// entries of rows 0..I-1 of its system (row order), then kick / drift.
+__global__ void bks_integrate_kernel(const float4 *__restrict__ pos_old, float4 *__restrict__ pos_new,
+                                     float4 *__restrict__ vel, const float4 *__restrict__ tpart,
+                                     const float4 *__restrict__ spart, BatchSymDev bd, int nbody, int rb,
+                                     long long total, int workers, float damping, float dt, int kick,
+                                     float G, float4 *__restrict__ acc_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbody) return;
+    const int s = bd.body_sys[i];
+    const int o = bd.sys_off[s];
+    const int ns = bd.sys_off[s + 1] - o;
+    const int li = i - o;
+    const int rc = rb / 32;
+    const int nc = (ns + 31) / 32;
+    const int I = li / rb;
+    const long long base = bd.it_off[s];
+    const int c0 = sk_owner(base + sym_prefix(I, nc, rc), total, workers);
+    const int c1 = sk_owner(base + sym_prefix(I + 1, nc, rc) - 1, total, workers);
+    const long long grow = (long long)bd.row_off[s] + I;
+    const int lj = li - I * rb;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    for (int c = c0; c <= c1; ++c) {
+        const float4 q = tpart[(c + grow) * rb + lj];
+        ax = __fadd_rn(ax, q.x);
+        ay = __fadd_rn(ay, q.y);
+        az = __fadd_rn(az, q.z);
+    }
+    long long off = bd.sp_off[s] + li - rb;  // row r at soff(r) + li - (r + 1) rb
+    for (int r = 0; r < I; ++r) {
+        const float4 q = spart[off];
+        off += (long long)ns - (long long)(r + 2) * rb;
+        ax = __fadd_rn(ax, q.x);
+        ay = __fadd_rn(ay, q.y);
+        az = __fadd_rn(az, q.z);
+    }
+    batch_kick_drift(i, ax, ay, az, pos_old, pos_new, vel, damping, dt, kick, G, acc_out);
+}
+
+typedef void (*bks_kernel_t)(const float4 *, BatchSymDev, float, float4 *, float4 *, long long, int);
+
+static bks_kernel_t bks_kernel_for(int wpb, int bpt)
+{
+#define NB_BKS(W, B) \
+    if (wpb == W && bpt == B) return bks_force_kernel<W, B>;
+    NB_BKS(1, 8) NB_BKS(1, 12) NB_BKS(1, 16) NB_BKS(2, 8) NB_BKS(2, 16) NB_BKS(4, 8) NB_BKS(4, 16)
+#undef NB_BKS
+    return nullptr;
+}
 
 // Batched adjoint: the vector-Jacobian product of one step for every system
 // (same algebra as vjp_pair_kernel in nb_adjoint.cu: out_k = m_k P - q g_k -
@@ -345,6 +532,7 @@ static bk_kernel_t bk_kernel_for(int wpb, int bpt)
 struct BatchPlan {
     int wpb = 0, bpt = 0, grid = 0, workers = 0;
     long long total = 0, total_wtb = 0, slots = 0;
+    long long spart = 0;  // symmetric: float4 entries of all source-side arrays
 };
 
 struct nb_batch {
@@ -360,13 +548,17 @@ struct nb_batch {
     bool has_state = false;
     float4 *partial = nullptr;
     size_t partial_cap = 0;  // float4 entries
+    // NB_ALGO_SYM: source-side arrays of all systems and their offsets
+    bool sym = false;
+    long long *d_sp_off = nullptr;
+    float4 *spart = nullptr;
+    size_t spart_cap = 0;
     BatchPlan plan;
     // graph of `graph_steps` steps starting from pos[graph_cur]
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0, graph_cur = -1;
-    // per-system plain plans for the baseline
-    std::vector<nb::SkPlan> sys_plans;
-    float4 *sys_partial = nullptr;
+    // scratch of the per-system baseline (target-side and source-side)
+    float4 *sys_partial = nullptr, *sys_spart = nullptr;
     // adjoint: VJP plan (own iteration tables), checkpoints, reverse buffers
     BatchPlan vplan;
     long long *d_it_off_v = nullptr;
@@ -382,18 +574,23 @@ struct nb_batch {
 using nb::set_error;
 
 static int batch_plan_for(nb_batch *b, int wpb, int bpt, BatchPlan *out, std::vector<long long> *it_off,
-                          std::vector<int> *tb_off)
+                          std::vector<int> *tb_off, std::vector<long long> *sp_off)
 {
-    nb::bk_kernel_t k = nb::bk_kernel_for(wpb, bpt);
+    const void *k = b->sym ? (const void *)nb::bks_kernel_for(wpb, bpt) : (const void *)nb::bk_kernel_for(wpb, bpt);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "batched kernel shape not compiled");
     const int wtb = 32 * bpt;
     it_off->assign(b->nsys + 1, 0);
     tb_off->assign(b->nsys + 1, 0);
+    sp_off->assign(b->nsys + 1, 0);
     for (int s = 0; s < b->nsys; ++s) {
         const long long n = b->sizes[s];
         const long long ntb = (n + wtb - 1) / wtb, ng = (n + nb::kGroup - 1) / nb::kGroup;
-        (*it_off)[s + 1] = (*it_off)[s] + ntb * ng;
+        // directed: (target block, source group) items; symmetric: (row,
+        // chunk) items of the triangular layout, rows of 32 * bpt bodies
+        const long long items = b->sym ? nb::sym_prefix(ntb, (int)ng, bpt) : ntb * ng;
+        (*it_off)[s + 1] = (*it_off)[s] + items;
         (*tb_off)[s + 1] = (*tb_off)[s] + (int)ntb;
+        (*sp_off)[s + 1] = (*sp_off)[s] + (b->sym ? nb::sym_spart_entries((int)n, wtb) : 0);
     }
     int occ = 0;
     NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * wpb, 0));
@@ -403,6 +600,7 @@ static int batch_plan_for(nb_batch *b, int wpb, int bpt, BatchPlan *out, std::ve
     p.bpt = bpt;
     p.total = (*it_off)[b->nsys];
     p.total_wtb = (*tb_off)[b->nsys];
+    p.spart = (*sp_off)[b->nsys];
     long long workers = (long long)b->sms * occ * wpb;
     if (p.total > 0 && workers > p.total) workers = p.total;
     p.workers = p.total > 0 ? (int)workers : 0;
@@ -415,9 +613,9 @@ static int batch_plan_for(nb_batch *b, int wpb, int bpt, BatchPlan *out, std::ve
 static int batch_apply_plan(nb_batch *b, int wpb, int bpt, cudaStream_t s)
 {
     BatchPlan p;
-    std::vector<long long> it_off;
+    std::vector<long long> it_off, sp_off;
     std::vector<int> tb_off;
-    int st = batch_plan_for(b, wpb, bpt, &p, &it_off, &tb_off);
+    int st = batch_plan_for(b, wpb, bpt, &p, &it_off, &tb_off, &sp_off);
     if (st) return st;
     const size_t need = (size_t)p.slots * 32 * bpt;
     if (need > b->partial_cap) {
@@ -428,6 +626,17 @@ static int batch_apply_plan(nb_batch *b, int wpb, int bpt, cudaStream_t s)
         if (e != cudaSuccess) return nb::cuda_error(e, "batched scratch allocation");
         b->partial_cap = need;
     }
+    if ((size_t)p.spart > b->spart_cap) {
+        cudaFree(b->spart);
+        b->spart = nullptr;
+        b->spart_cap = 0;
+        cudaError_t e = cudaMalloc((void **)&b->spart, (size_t)p.spart * sizeof(float4));
+        if (e != cudaSuccess) return nb::cuda_error(e, "batched source-side allocation");
+        b->spart_cap = (size_t)p.spart;
+    }
+    if (b->sym)
+        NB_CUDA(cudaMemcpyAsync(b->d_sp_off, sp_off.data(), sp_off.size() * sizeof(long long),
+                                cudaMemcpyHostToDevice, s));
     NB_CUDA(cudaMemcpyAsync(b->d_it_off, it_off.data(), it_off.size() * sizeof(long long),
                             cudaMemcpyHostToDevice, s));
     NB_CUDA(cudaMemcpyAsync(b->d_tb_off, tb_off.data(), tb_off.size() * sizeof(int),
@@ -453,6 +662,18 @@ static nb::BatchDev batch_dev(const nb_batch *b)
     return d;
 }
 
+static nb::BatchSymDev batch_sym_dev(const nb_batch *b)
+{
+    nb::BatchSymDev d;
+    d.sys_off = b->d_sys_off;
+    d.it_off = b->d_it_off;
+    d.row_off = b->d_tb_off;
+    d.sp_off = b->d_sp_off;
+    d.body_sys = b->d_body_sys;
+    d.nsys = b->nsys;
+    return d;
+}
+
 // One batched step from po into pn (vel in place); with acc_out the second
 // kernel writes the bare accelerations instead of integrating.
 static int batch_force_step(nb_batch *b, const float4 *po, float4 *pn, float4 *vel,
@@ -460,6 +681,17 @@ static int batch_force_step(nb_batch *b, const float4 *po, float4 *pn, float4 *v
 {
     const BatchPlan &p = b->plan;
     if (b->nbody == 0) return NB_OK;
+    if (b->sym) {
+        nb::bks_kernel_t k = nb::bks_kernel_for(p.wpb, p.bpt);
+        k<<<p.grid, 32 * p.wpb, 0, s>>>(po, batch_sym_dev(b), (float)b->p.eps2, b->partial, b->spart,
+                                        p.total, p.workers);
+        NB_LAUNCH_CHECK("bks_force_kernel launch");
+        nb::bks_integrate_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
+            po, pn, vel, b->partial, b->spart, batch_sym_dev(b), b->nbody, 32 * p.bpt, p.total,
+            p.workers, (float)b->p.damping, (float)b->p.dt, b->p.kick, (float)b->p.G, acc_out);
+        NB_LAUNCH_CHECK("bks_integrate_kernel launch");
+        return NB_OK;
+    }
     nb::bk_kernel_t k = nb::bk_kernel_for(p.wpb, p.bpt);
     k<<<p.grid, 32 * p.wpb, 0, s>>>(po, batch_dev(b), (float)b->p.eps2, b->partial, p.total, p.workers);
     NB_LAUNCH_CHECK("bk_force_kernel launch");
@@ -535,7 +767,10 @@ static void free_batch(nb_batch *b)
     cudaFree(b->pos[1]);
     cudaFree(b->vel);
     cudaFree(b->partial);
+    cudaFree(b->spart);
+    cudaFree(b->d_sp_off);
     cudaFree(b->sys_partial);
+    cudaFree(b->sys_spart);
     cudaFree(b->d_it_off_v);
     cudaFree(b->d_tb_off_v);
     cudaFree(b->vpartial);
@@ -558,8 +793,8 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
     if (!out) return set_error(NB_ERR_INVALID, "out is NULL");
     *out = nullptr;
     if (!p || nsys < 0 || (nsys > 0 && !sizes)) return set_error(NB_ERR_INVALID, "bad batch arguments");
-    if (p->precision != NB_F32 || p->algo != NB_ALGO_FAST)
-        return set_error(NB_ERR_UNSUPPORTED, "batches run the NB_F32 fast algorithm");
+    if (p->precision != NB_F32 || (p->algo != NB_ALGO_FAST && p->algo != NB_ALGO_SYM))
+        return set_error(NB_ERR_UNSUPPORTED, "batches run NB_F32 with the fast or symmetric algorithm");
     if (p->kick != NB_KICK_REFERENCE && p->kick != NB_KICK_PHYSICAL)
         return set_error(NB_ERR_INVALID, "unknown kick mode");
     long long nbody = 0;
@@ -573,6 +808,7 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
     b->nsys = nsys;
     b->nbody = (int)nbody;
     b->sizes.assign(sizes, sizes + nsys);
+    b->sym = p->algo == NB_ALGO_SYM;
     cudaError_t e = cudaGetDevice(&b->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
     if (e != cudaSuccess) {
@@ -596,6 +832,7 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
     NB_BALLOC(b->d_sys_off, sizeof(int) * (nsys + 1));
     NB_BALLOC(b->d_tb_off, sizeof(int) * (nsys + 1));
     NB_BALLOC(b->d_it_off, sizeof(long long) * (nsys + 1));
+    NB_BALLOC(b->d_sp_off, sizeof(long long) * (nsys + 1));
     NB_BALLOC(b->d_body_sys, sizeof(int) * (size_t)nbody);
     NB_BALLOC(b->pos[0], sb);
     NB_BALLOC(b->pos[1], sb);
@@ -608,8 +845,9 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
         free_batch(b);
         return nb::cuda_error(e, "batch tables");
     }
-    const int wpb = p->block ? p->block / 32 : 4;
-    const int bpt = p->bpt ? p->bpt : 4;
+    // defaults: symmetric one-warp workers x 16 targets; directed 4 x 4
+    const int wpb = p->block ? p->block / 32 : (b->sym ? 1 : 4);
+    const int bpt = p->bpt ? p->bpt : (b->sym ? 16 : 4);
     int st = batch_apply_plan(b, wpb, bpt, nullptr);
     if (st) {
         free_batch(b);
@@ -737,7 +975,8 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
     cudaDeviceProp prop;
     NB_CUDA(cudaGetDeviceProperties(&prop, b->device));
     std::ostringstream key;
-    key << prop.name << "|sms" << prop.multiProcessorCount << "|kick" << b->p.kick << "|";
+    key << prop.name << "|sms" << prop.multiProcessorCount << "|kick" << b->p.kick
+        << (b->sym ? "|sym" : "|dir") << "|";
     {
         std::map<int, int> hist;
         for (int n : b->sizes) {
@@ -776,14 +1015,20 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
         NB_CUDA(cudaMemcpyAsync(save_p, b->pos[b->cur], sb, cudaMemcpyDeviceToDevice, s));
         NB_CUDA(cudaMemcpyAsync(save_v, b->vel, sb, cudaMemcpyDeviceToDevice, s));
     }
-    const int cand[][2] = {{2, 4}, {2, 8}, {4, 2}, {4, 4}, {4, 8}, {8, 2}, {8, 4}, {8, 8}};
+    static const int cand_dir[][2] = {{2, 4}, {2, 8}, {4, 2}, {4, 4}, {4, 8}, {8, 2}, {8, 4}, {8, 8}};
+    static const int cand_sym[][2] = {{1, 8}, {1, 12}, {1, 16}, {2, 8}, {2, 16}, {4, 8}, {4, 16}};
+    std::vector<std::array<int, 2>> cands;
+    if (b->sym)
+        for (auto &c : cand_sym) cands.push_back({c[0], c[1]});
+    else
+        for (auto &c : cand_dir) cands.push_back({c[0], c[1]});
     float best = 1e30f;
     int bw = b->plan.wpb, bb = b->plan.bpt;
     cudaEvent_t e0, e1;
     NB_CUDA(cudaEventCreate(&e0));
     NB_CUDA(cudaEventCreate(&e1));
     int st = NB_OK;
-    for (auto &c : cand) {
+    for (auto &c : cands) {
         if ((st = batch_apply_plan(b, c[0], c[1], s))) break;
         if ((st = batch_step_once(b, s))) break;
         NB_CUDA(cudaEventRecord(e0, s));
@@ -821,35 +1066,79 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
     return NB_OK;
 }
 
-// The per-system baseline: every system stepped by its own plain stream-K
-// launches (force + integrate per system per step), as separate tasks would.
+}  // extern "C"
+
+// Plans of every system on its own (the per-system baselines): directed
+// stream-K plans, or symmetric plans for NB_ALGO_SYM batches, and the largest
+// scratch each kind needs.
+struct SysPlans {
+    std::vector<nb::SkPlan> dir;
+    std::vector<nb::SymPlan> sym;
+    size_t tpart = 1, spart = 1;  // float4 entries
+};
+
+static int sys_plans_for(nb_batch *b, SysPlans *out)
+{
+    SysPlans sp;
+    for (int i = 0; i < b->nsys; ++i) {
+        int st;
+        if (b->sym) {
+            nb::SymPlan q;
+            if ((st = nb::sym_plan(b->sizes[i], 0, 0, b->device, &q))) return st;
+            sp.tpart = std::max(sp.tpart, (size_t)q.slots * q.rb);
+            sp.spart = std::max(sp.spart, (size_t)q.spart_size);
+            sp.sym.push_back(q);
+        } else {
+            nb::SkPlan q;
+            if ((st = nb::fast_plan(b->sizes[i], 0, 0, 0, b->device, &q, 0))) return st;
+            sp.tpart = std::max(sp.tpart, (size_t)q.slots * q.tbsize);
+            sp.dir.push_back(q);
+        }
+    }
+    *out = std::move(sp);
+    return NB_OK;
+}
+
+// System i stepped on its own: force + integrate launches.
+static int sys_step(const nb_batch *b, const SysPlans &sp, int i, const float4 *po, float4 *pn,
+                    float4 *vel, float4 *tpart, float4 *spart, cudaStream_t s)
+{
+    const nb_params &p = b->p;
+    int st;
+    if (b->sym) {
+        if ((st = nb::sym_force(sp.sym[i], po, (float)p.eps2, tpart, spart, s))) return st;
+        return nb::sym_integrate(sp.sym[i], po, pn, vel, tpart, spart, (float)p.damping, (float)p.dt,
+                                 p.kick, (float)p.G, nullptr, s);
+    }
+    if ((st = nb::fast_force(sp.dir[i], po, (float)p.eps2, tpart, s, 0))) return st;
+    return nb::fast_integrate(sp.dir[i], po, pn, vel, tpart, (float)p.damping, (float)p.dt, p.kick,
+                              (float)p.G, nullptr, s);
+}
+
+extern "C" {
+
+// The per-system baseline: every system stepped by its own launches (force +
+// integrate per system per step, the batch's algorithm), as separate tasks
+// would, on one stream.
 int nb_batch_step_per_system(nb_batch *b, int steps, void *stream)
 {
     if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
     if (!b->has_state) return set_error(NB_ERR_STATE, "no state loaded");
     cudaStream_t s = (cudaStream_t)stream;
-    if (b->sys_plans.empty() && b->nsys) {
-        b->sys_plans.resize(b->nsys);
-        size_t need = 0;
-        for (int i = 0; i < b->nsys; ++i) {
-            int st = nb::fast_plan(b->sizes[i], 0, 0, 0, b->device, &b->sys_plans[i], 0);
-            if (st) return st;
-            need = std::max(need, (size_t)b->sys_plans[i].slots * b->sys_plans[i].tbsize);
-        }
-        NB_CUDA(cudaMalloc((void **)&b->sys_partial, std::max<size_t>(need, 1) * sizeof(float4)));
+    SysPlans sp;
+    int st = sys_plans_for(b, &sp);
+    if (st) return st;
+    if (!b->sys_partial) {
+        NB_CUDA(cudaMalloc((void **)&b->sys_partial, sp.tpart * sizeof(float4)));
+        NB_CUDA(cudaMalloc((void **)&b->sys_spart, sp.spart * sizeof(float4)));
     }
     std::vector<int> off(b->nsys + 1, 0);
     for (int i = 0; i < b->nsys; ++i) off[i + 1] = off[i] + b->sizes[i];
     for (int t = 0; t < steps; ++t) {
         for (int i = 0; i < b->nsys; ++i) {
-            const float4 *po = b->pos[b->cur] + off[i];
-            float4 *pn = b->pos[b->cur ^ 1] + off[i];
-            int st = nb::fast_force(b->sys_plans[i], po, (float)b->p.eps2, b->sys_partial, s, 0);
-            if (!st)
-                st = nb::fast_integrate(b->sys_plans[i], po, pn, b->vel + off[i], b->sys_partial,
-                                        (float)b->p.damping, (float)b->p.dt, b->p.kick, (float)b->p.G,
-                                        nullptr, s);
-            if (st) return st;
+            if ((st = sys_step(b, sp, i, b->pos[b->cur] + off[i], b->pos[b->cur ^ 1] + off[i],
+                               b->vel + off[i], b->sys_partial, b->sys_spart, s)))
+                return st;
         }
         b->cur ^= 1;
     }
@@ -870,17 +1159,14 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
     if (ntasks > b->nsys) ntasks = b->nsys > 0 ? b->nsys : 1;
     std::vector<int> off(b->nsys + 1, 0);
     for (int i = 0; i < b->nsys; ++i) off[i + 1] = off[i] + b->sizes[i];
-    std::vector<nb::SkPlan> plans(b->nsys);
-    size_t need = 1;
-    for (int i = 0; i < b->nsys; ++i) {
-        int st = nb::fast_plan(b->sizes[i], 0, 0, 0, b->device, &plans[i], 0);
-        if (st) return st;
-        need = std::max(need, (size_t)plans[i].slots * plans[i].tbsize);
-    }
-    std::vector<float4 *> scratch(ntasks, nullptr);
+    SysPlans sp;
+    int st0 = sys_plans_for(b, &sp);
+    if (st0) return st0;
+    std::vector<float4 *> tscratch(ntasks, nullptr), sscratch(ntasks, nullptr);
     std::vector<cudaStream_t> streams(ntasks, nullptr);
     for (int t = 0; t < ntasks; ++t) {
-        NB_CUDA(cudaMalloc((void **)&scratch[t], need * sizeof(float4)));
+        NB_CUDA(cudaMalloc((void **)&tscratch[t], sp.tpart * sizeof(float4)));
+        NB_CUDA(cudaMalloc((void **)&sscratch[t], sp.spart * sizeof(float4)));
         NB_CUDA(cudaStreamCreateWithFlags(&streams[t], cudaStreamNonBlocking));
     }
     const int cur = b->cur, dev = b->device;
@@ -892,13 +1178,8 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
             for (int i = t; i < b->nsys && status[t] == NB_OK; i += ntasks) {
                 int c = cur;
                 for (int k = 0; k < steps && status[t] == NB_OK; ++k) {
-                    const float4 *po = b->pos[c] + off[i];
-                    float4 *pn = b->pos[c ^ 1] + off[i];
-                    int st = nb::fast_force(plans[i], po, (float)b->p.eps2, scratch[t], streams[t], 0);
-                    if (!st)
-                        st = nb::fast_integrate(plans[i], po, pn, b->vel + off[i], scratch[t],
-                                                (float)b->p.damping, (float)b->p.dt, b->p.kick,
-                                                (float)b->p.G, nullptr, streams[t]);
+                    int st = sys_step(b, sp, i, b->pos[c] + off[i], b->pos[c ^ 1] + off[i], b->vel + off[i],
+                                      tscratch[t], sscratch[t], streams[t]);
                     if (!st && cudaStreamSynchronize(streams[t]) != cudaSuccess) st = NB_ERR_CUDA;
                     status[t] = st;
                     c ^= 1;
@@ -908,7 +1189,8 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
     }
     for (auto &w : workers) w.join();
     for (int t = 0; t < ntasks; ++t) {
-        cudaFree(scratch[t]);
+        cudaFree(tscratch[t]);
+        cudaFree(sscratch[t]);
         cudaStreamDestroy(streams[t]);
     }
     for (int t = 0; t < ntasks; ++t)

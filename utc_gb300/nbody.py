@@ -211,13 +211,15 @@ def probe_fma_peak(iters=20000, packed=True, stream=None):
 
 class NBodyBatch:
     """Many independent systems (sizes[s] bodies each) in one context; state
-    arrays are the systems' (n, 4) float32 arrays concatenated."""
+    arrays are the systems' (n, 4) float32 arrays concatenated.  algo "sym"
+    (each unordered pair once) or "fast" (directed)."""
 
     def __init__(self, sizes, kick="physical", eps2=1e-3, damping=1.0, dt=1e-3, G=1.0,
-                 warps_per_cta=0, bodies_per_lane=0):
+                 warps_per_cta=0, bodies_per_lane=0, algo="sym"):
         self.lib = N.lib()
         p = N.NbParams()
         self.lib.nb_params_default(C.byref(p))
+        p.algo = _ALGO[algo]
         p.kick = _KICK[kick]
         p.eps2, p.damping, p.dt, p.G = float(eps2), float(damping), float(dt), float(G)
         p.block = int(warps_per_cta) * 32
