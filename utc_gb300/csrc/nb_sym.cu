@@ -332,56 +332,51 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__re
     }
 }
 
-// Per body: target-side slots (CTA order) + source-side rows 0..I_b-1 (row
-// order), then the reference's kick / damping / drift (unfused, its order).
-__global__ void sym_integrate_kernel(const float4 *__restrict__ pos_old, float4 *__restrict__ pos_new,
-                                     float4 *__restrict__ vel, const float4 *__restrict__ tpart,
-                                     const float4 *__restrict__ spart, int n, int rb, int nc,
-                                     int nrb, long long total, int grid, float damping, float dt,
-                                     int kick, float G, float4 *__restrict__ acc_out)
+// Per body: target-side slots + source-side rows 0..I_b-1, then the
+// reference's kick / damping / drift (unfused, its order).  Four threads
+// share a body: thread q of the quad sums slots c0+q, c0+q+4, ... and rows
+// q, q+4, ... in order, and the quad combines its four sums as
+// (s0 + s1) + (s2 + s3) (fixed order: deterministic).  The row walk, up to
+// nrb - 1 entries for the last row block, is what bounds the kernel; split
+// four ways it is a quarter as long.
+constexpr int kSymIntegBlock = 256;
+
+__global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
+    const float4 *__restrict__ pos_old, float4 *__restrict__ pos_new, float4 *__restrict__ vel,
+    const float4 *__restrict__ tpart, const float4 *__restrict__ spart, int n, int rb, int nc, int nrb,
+    long long total, int grid, float damping, float dt, int kick, float G, float4 *__restrict__ acc_out)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int rc = rb / 32;
-    const int I = i / rb;
-    const long long first = sym_prefix(I, nc, rc);
-    const long long last = sym_prefix(I + 1, nc, rc) - 1;
-    const int c0 = sk_owner(first, total, grid);
-    const int c1 = sk_owner(last, total, grid);
-    const int li = i - I * rb;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)(t >> 2), q = (int)(t & 3);
+    const bool live = i < n;  // dead threads still take part in the shuffles
     float ax = 0.f, ay = 0.f, az = 0.f;
-    for (int c = c0; c <= c1; ++c) {
-        const float4 q = tpart[(size_t)(c + I) * rb + li];
-        ax = __fadd_rn(ax, q.x);
-        ay = __fadd_rn(ay, q.y);
-        az = __fadd_rn(az, q.z);
-    }
-    // rows 0..I-1 in order; entry of row r at soff(r) + i - (r + 1) rb, and
-    // consecutive rows are n - (r + 2) rb apart.  Eight loads are issued
-    // before their adds so the row walk is not one load latency per row.
-    long long off = (long long)i - rb;
-    int r = 0;
-    for (; r + 8 <= I; r += 8) {
-        float4 q[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            q[u] = spart[off];
-            off += (long long)n - (long long)(r + u + 2) * rb;
+    if (live) {
+        const int rc = rb / 32;
+        const int I = i / rb;
+        const int c0 = sk_owner(sym_prefix(I, nc, rc), total, grid);
+        const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1, total, grid);
+        const int li = i - I * rb;
+        for (int c = c0 + q; c <= c1; c += 4) {
+            const float4 v4 = tpart[(size_t)(c + I) * rb + li];
+            ax = __fadd_rn(ax, v4.x);
+            ay = __fadd_rn(ay, v4.y);
+            az = __fadd_rn(az, v4.z);
         }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            ax = __fadd_rn(ax, q[u].x);
-            ay = __fadd_rn(ay, q[u].y);
-            az = __fadd_rn(az, q[u].z);
+#pragma unroll 4
+        for (int r = q; r < I; r += 4) {
+            const float4 v4 = spart[sym_soff(r, n, rb) + (i - (long long)(r + 1) * rb)];
+            ax = __fadd_rn(ax, v4.x);
+            ay = __fadd_rn(ay, v4.y);
+            az = __fadd_rn(az, v4.z);
         }
     }
-    for (; r < I; ++r) {
-        const float4 q = spart[off];
-        off += (long long)n - (long long)(r + 2) * rb;
-        ax = __fadd_rn(ax, q.x);
-        ay = __fadd_rn(ay, q.y);
-        az = __fadd_rn(az, q.z);
-    }
+    ax = __fadd_rn(ax, __shfl_xor_sync(0xffffffffu, ax, 1));
+    ay = __fadd_rn(ay, __shfl_xor_sync(0xffffffffu, ay, 1));
+    az = __fadd_rn(az, __shfl_xor_sync(0xffffffffu, az, 1));
+    ax = __fadd_rn(ax, __shfl_xor_sync(0xffffffffu, ax, 2));
+    ay = __fadd_rn(ay, __shfl_xor_sync(0xffffffffu, ay, 2));
+    az = __fadd_rn(az, __shfl_xor_sync(0xffffffffu, az, 2));
+    if (!live || q != 0) return;
     if (acc_out) {
         acc_out[i] = make_float4(ax, ay, az, 0.f);
         return;
@@ -496,9 +491,10 @@ int sym_integrate(const SymPlan &p, const float4 *pos_old, float4 *pos_new, floa
                   float G, float4 *acc_out, cudaStream_t s)
 {
     if (p.n == 0) return NB_OK;
-    sym_integrate_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(pos_old, pos_new, vel, tpart, spart, p.n,
-                                                           p.rb, p.nc, p.nrb, p.total, p.grid,
-                                                           damping, dt, kick, G, acc_out);
+    const long long threads = 4ll * p.n;  // a quad of threads per body
+    sym_integrate_kernel<<<(unsigned)((threads + kSymIntegBlock - 1) / kSymIntegBlock), kSymIntegBlock, 0, s>>>(
+        pos_old, pos_new, vel, tpart, spart, p.n, p.rb, p.nc, p.nrb, p.total, p.grid, damping, dt, kick,
+        G, acc_out);
     NB_LAUNCH_CHECK("sym_integrate_kernel launch");
     return NB_OK;
 }
