@@ -232,7 +232,10 @@ int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void 
  * uniform cube, positions U[-1,1]^3, velocities U[-vmax,vmax]^3, masses
  * U[0.5,1.5]/n; kind 1: Plummer sphere of scale a, total mass M and
  * gravitational constant G (Aarseth, Henon & Wielen sampling), masses M/n,
- * centre of mass and momentum moved to zero.  pos/vel: device, n 4-vectors of
+ * centre of mass and momentum moved to zero; kinds 2, 3, 4: the reference
+ * app's random, shell and expand configurations with a = clusterScale and
+ * vmax = velocityScale, masses 1 (same distributions as randomizeBodies,
+ * not its rand() sequence).  pos/vel: device, n 4-vectors of
  * float (NB_F32) or double (NB_F64), vel.w = 1.  scratch_dev: device buffer of
  * nb_ics_scratch_bytes(n) bytes (Plummer only).  Replaces the host-side
  * randomizeBodies (benchapps/nbody/seq/nbody.h:89-250) for large synthetic

@@ -49,3 +49,32 @@ def test_plummer_profile_and_virial(cuda, precision):
         s.set_state(p.astype(np.float32), v.astype(np.float32))
         e = s.energy()
     assert abs(-e[0] / e[1] - 0.5) < 0.03
+
+
+@pytest.mark.parametrize("kind", ["random", "shell", "expand"])
+def test_reference_configurations(cuda, kind):
+    """The reference app's three initial configurations drawn on the GPU:
+    the support and structure of each distribution (randomizeBodies,
+    benchapps/nbody/seq/nbody.h:89-250), with clusterScale 1.54 and
+    velocityScale 8 (the app's first preset)."""
+    n, cs, vs = 5000, 1.54, 8.0
+    p, v = [t.cpu().numpy().astype(np.float64) for t in
+            gpu_initial_conditions(kind, n, seed=2, a=cs, vmax=vs)]
+    assert (p[:, 3] == 1.0).all() and (v[:, 3] == 1.0).all()
+    r = np.linalg.norm(p[:, :3], axis=1)
+    if kind == "random":
+        s = cs * max(1.0, n / 1024)
+        assert r.max() <= s * (1 + 1e-6)
+        assert np.linalg.norm(v[:, :3], axis=1).max() <= s * vs * (1 + 1e-6)
+        # uniform in the ball: the fraction inside half the radius is 1/8
+        assert abs((r < 0.5 * s).mean() - 0.125) < 0.02
+    elif kind == "shell":
+        assert r.min() >= 2.5 * cs * (1 - 1e-6) and r.max() <= 4.0 * cs * (1 + 1e-6)
+        # velocity = (pos x z) cs vs: perpendicular to z and to pos
+        assert np.abs(v[:, 2]).max() <= 1e-4 * np.abs(v[:, :3]).max()
+        assert np.abs((p[:, :3] * v[:, :3]).sum(1)).max() <= 1e-3 * (r * np.linalg.norm(v[:, :3], axis=1)).max()
+        assert np.allclose(v[:, 0], p[:, 1] * cs * vs, rtol=1e-5, atol=1e-5)
+    else:
+        s = cs * n / 1024
+        assert r.max() <= s * (1 + 1e-6)
+        assert np.allclose(v[:, :3], p[:, :3] * vs, rtol=1e-5, atol=1e-6)

@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(NT) vjp_pair_kernel(const float4 *__restrict__
     }
 }
 
-template <int W, int BPT, int MINB>
+template <int W, int BPT, int MINB, int U = 2>
 __global__ void __launch_bounds__(32 * W, MINB) sym_vjp_kernel(const float4 *__restrict__ pos,
                                                                const float4 *__restrict__ gbuf, int n,
                                                                float eps2, float4 *__restrict__ tpart,
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_vjp_kernel(const float4 *__r
                 // reaction on the rotating chunk body: P, q, Q of its own sum
                 // and its mass gradient w = sum inv^3 r.g_k
                 float rPx = 0.f, rPy = 0.f, rPz = 0.f, rq = 0.f, rQ0 = 0.f, rQ1 = 0.f, rQ2 = 0.f, rw = 0.f;
-#pragma unroll 2
+#pragma unroll(U)
                 for (int r = 0; r < 32; ++r) {
                     const int idx = (lane + r) & 31;
                     const float4 s = sC[idx];

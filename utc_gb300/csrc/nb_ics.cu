@@ -14,7 +14,17 @@
 //    with X uniform in (0, 0.999], speeds q * v_esc(r) with q drawn by
 //    rejection from q^2 (1 - q^2)^(7/2), isotropic directions, masses M/n;
 //    then the centre of mass and its velocity are moved to the origin
-//    (FP64 block sums reduced in order by one block: deterministic).
+//    (FP64 block sums reduced in order by one block: deterministic);
+//  * the reference app's own three configurations (randomizeBodies,
+//    benchapps/nbody/seq/nbody.h:89-250) with this generator in place of
+//    rand(), a = clusterScale, vmax = velocityScale, masses 1, vel.w = 1:
+//    random (positions uniform in the ball of radius s = a max(1, n/1024),
+//    velocities uniform in the ball of radius s vmax), shell (a unit
+//    direction drawn by rejection from the cube, each coordinate scaled by
+//    its own draw from [2.5a, 4a], velocity (pos x axis) a vmax with axis z,
+//    or (y, x, 1) normalised when the direction is within 1e-6 of z) and
+//    expand (positions uniform in the ball of radius s = a n/1024, or a when
+//    s < 1; velocity the same point times s vmax).
 #include <cmath>
 
 #include "nb_internal.cuh"
@@ -47,6 +57,25 @@ __device__ __forceinline__ V4 mk4(double x, double y, double z, double w)
     return r;
 }
 
+// A point uniform in the unit ball by rejection from the cube: tries use
+// streams k0, k0 + 1, ... (3 per try, 40 tries).  All 40 fail with
+// probability 0.476^40 ~ 1e-13; then the last candidate is pulled inside.
+__device__ __forceinline__ void ball_point(unsigned long long seed, unsigned long long id, unsigned k0,
+                                           double &x, double &y, double &z, double &len)
+{
+    for (unsigned t = 0; t < 40; ++t) {
+        x = 2.0 * u01(seed, id, k0 + 3 * t) - 1.0;
+        y = 2.0 * u01(seed, id, k0 + 3 * t + 1) - 1.0;
+        z = 2.0 * u01(seed, id, k0 + 3 * t + 2) - 1.0;
+        len = sqrt(x * x + y * y + z * z);
+        if (len <= 1.0) return;
+    }
+    x *= 0.5 / len;
+    y *= 0.5 / len;
+    z *= 0.5 / len;
+    len = 0.5;
+}
+
 template <typename V4>
 __global__ void ics_kernel(int kind, int n, unsigned long long seed, double a, double G, double M,
                            double vmax, V4 *__restrict__ pos, V4 *__restrict__ vel)
@@ -54,6 +83,47 @@ __global__ void ics_kernel(int kind, int n, unsigned long long seed, double a, d
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const unsigned long long id = (unsigned long long)i;
+    if (kind == 2 || kind == 4) {  // reference random / expand
+        double x, y, z, len;
+        ball_point(seed, id, 8, x, y, z, len);
+        double s = a * fmax(1.0, n / 1024.0);
+        if (kind == 4) {
+            s = a * (n / 1024.0);
+            if (s < 1.0) s = a;
+            pos[i] = mk4<V4>(x * s, y * s, z * s, 1.0);
+            vel[i] = mk4<V4>(x * s * vmax, y * s * vmax, z * s * vmax, 1.0);
+            return;
+        }
+        double vx, vy, vz, vlen;
+        ball_point(seed, id, 128, vx, vy, vz, vlen);
+        pos[i] = mk4<V4>(x * s, y * s, z * s, 1.0);
+        vel[i] = mk4<V4>(vx * s * vmax, vy * s * vmax, vz * s * vmax, 1.0);
+        return;
+    }
+    if (kind == 3) {  // reference shell
+        double x, y, z, len;
+        ball_point(seed, id, 8, x, y, z, len);
+        if (len > 1e-6) {
+            x /= len;
+            y /= len;
+            z /= len;
+        }
+        const double inner = 2.5 * a, outer = 4.0 * a;
+        const double px = x * (inner + (outer - inner) * u01(seed, id, 128));
+        const double py = y * (inner + (outer - inner) * u01(seed, id, 129));
+        const double pz = z * (inner + (outer - inner) * u01(seed, id, 130));
+        double ax = 0.0, ay = 0.0, az = 1.0;
+        if (1.0 - z < 1e-6) {
+            const double l = sqrt(y * y + x * x + 1.0);
+            ax = y / l;
+            ay = x / l;
+            az = 1.0 / l;
+        }
+        const double vs = a * vmax;
+        pos[i] = mk4<V4>(px, py, pz, 1.0);
+        vel[i] = mk4<V4>((py * az - pz * ay) * vs, (pz * ax - px * az) * vs, (px * ay - py * ax) * vs, 1.0);
+        return;
+    }
     if (kind == 0) {  // uniform cube
         pos[i] = mk4<V4>(2.0 * u01(seed, id, 0) - 1.0, 2.0 * u01(seed, id, 1) - 1.0,
                          2.0 * u01(seed, id, 2) - 1.0, (0.5 + u01(seed, id, 3)) / n);
@@ -172,7 +242,9 @@ extern "C" int nb_ics_generate(int kind, int n, unsigned long long seed, double 
                                double M, double vmax, int precision, void *pos_dev, void *vel_dev,
                                void *scratch_dev, void *stream)
 {
-    if (kind != 0 && kind != 1) return nb::set_error(NB_ERR_INVALID, "nb_ics_generate: kind is 0 (cube) or 1 (Plummer)");
+    if (kind < 0 || kind > 4)
+        return nb::set_error(NB_ERR_INVALID,
+                             "nb_ics_generate: kind is 0 (cube), 1 (Plummer), 2 (random), 3 (shell) or 4 (expand)");
     if (n < 0) return nb::set_error(NB_ERR_INVALID, "nb_ics_generate: n must be >= 0");
     if (precision != NB_F32 && precision != NB_F64)
         return nb::set_error(NB_ERR_INVALID, "nb_ics_generate: precision is NB_F32 or NB_F64");

@@ -330,8 +330,9 @@ class NBodyBatch:
 
 
 def gpu_initial_conditions(kind, n, seed=0, a=1.0, G=1.0, M=1.0, vmax=0.01, precision="f32", stream=None):
-    """Seeded bodies drawn on the GPU: kind "cube" or "plummer".  Returns
-    (pos, vel) torch CUDA tensors (n, 4)."""
+    """Seeded bodies drawn on the GPU: kind "cube", "plummer", or the
+    reference app's "random", "shell", "expand" (a = clusterScale, vmax =
+    velocityScale).  Returns (pos, vel) torch CUDA tensors (n, 4)."""
     torch = _torch()
     tdt = torch.float64 if precision == "f64" else torch.float32
     pos = torch.empty((max(n, 1), 4), dtype=tdt, device="cuda")
@@ -339,7 +340,8 @@ def gpu_initial_conditions(kind, n, seed=0, a=1.0, G=1.0, M=1.0, vmax=0.01, prec
     nbytes = N.lib().nb_ics_scratch_bytes(int(n))
     scratch = torch.empty((max(nbytes, 8) // 8,), dtype=torch.float64, device="cuda")
     s = current_stream_handle() if stream is None else stream
-    N.check(N.lib().nb_ics_generate({"cube": 0, "plummer": 1}[kind], int(n), int(seed), float(a), float(G),
+    kinds = {"cube": 0, "plummer": 1, "random": 2, "shell": 3, "expand": 4}
+    N.check(N.lib().nb_ics_generate(kinds[kind], int(n), int(seed), float(a), float(G),
                                     float(M), float(vmax), _PREC[precision], C.c_void_p(pos.data_ptr()),
                                     C.c_void_p(vel.data_ptr()), C.c_void_p(scratch.data_ptr()), C.c_void_p(s)),
             "nb_ics_generate")
