@@ -1,0 +1,119 @@
+"""Edge cases across every precision and algorithm: empty and one-body
+systems, invalid arguments answered with status codes (never a device
+fault), rejected combinations, and the batch API's argument checks."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from utc_gb300 import _native as N
+from utc_gb300 import ics
+from utc_gb300.nbody import NBodyBatch, NBodySystem
+
+pytestmark = pytest.mark.gpu
+
+MODES = [("f32", "fast"), ("f32", "sym"), ("f32", "exact"), ("f64", "exact"), ("f32comp", "fast"),
+         ("f32comp", "sym")]
+
+
+def dtype_of(prec):
+    return np.float64 if prec in ("f64", "f32comp") else np.float32
+
+
+@pytest.mark.parametrize("prec,algo", MODES)
+def test_empty_system_every_mode(cuda, prec, algo):
+    dt = dtype_of(prec)
+    with NBodySystem(0, prec, algo) as s:
+        s.set_state(np.zeros((0, 4), dt), np.zeros((0, 4), dt))
+        s.step(3)
+        p, v = s.get_state()
+        assert p.shape == (0, 4) and v.shape == (0, 4)
+        assert s.launches_per_step() == 0
+
+
+@pytest.mark.parametrize("prec,algo", MODES)
+def test_one_body_drifts_freely(cuda, prec, algo):
+    """A lone body feels no force (its self term is r = 0): after k steps of
+    the physical kick it has moved by k dt v exactly as the oracle says."""
+    dt_ = dtype_of(prec)
+    pos = np.array([[0.25, -0.5, 0.125, 2.0]], dt_)
+    vel = np.array([[0.5, 0.25, -1.0, 1.0]], dt_)
+    with NBodySystem(1, prec, algo, kick="physical", eps2=1e-2, damping=1.0, dt=1e-3) as s:
+        s.set_state(pos, vel)
+        s.step(5)
+        p, v = s.get_state()
+    want_p, want_v = oracle.step(pos.astype(np.float64), vel.astype(np.float64), 1e-2, 1.0, 1e-3, 5,
+                                 kick_mode=oracle.KICK_PHYSICAL)
+    assert np.allclose(p[:, :3], want_p[:, :3], rtol=1e-6, atol=1e-7)
+    assert np.allclose(v[:, :3], want_v[:, :3], rtol=1e-6, atol=1e-7)
+
+
+@pytest.mark.parametrize("prec,algo", MODES)
+def test_status_codes_every_mode(cuda, prec, algo):
+    with NBodySystem(64, prec, algo) as s:
+        assert s.lib.nb_step(s.handle, 1, None) == N.NB_ERR_STATE
+        assert s.lib.nb_accel(s.handle, None, None) == N.NB_ERR_STATE
+        assert s.lib.nb_step(s.handle, -1, None) == N.NB_ERR_INVALID
+        dt_ = dtype_of(prec)
+        p, v = ics.plummer(64, seed=1)
+        p, v = p.astype(dt_), v.astype(dt_)
+        s.set_state(p, v)
+        assert s.lib.nb_accel(s.handle, None, None) == N.NB_ERR_INVALID
+        assert s.lib.nb_set_state(s.handle, p.ctypes.data_as(C.c_void_p), None, 0, None) == N.NB_ERR_INVALID
+        assert s.lib.nb_set_state(s.handle, p.ctypes.data_as(C.c_void_p),
+                                  v.ctypes.data_as(C.c_void_p), 7, None) == N.NB_ERR_INVALID
+        s.step(1)  # the context is still usable after the refusals
+
+
+@pytest.mark.parametrize("prec,algo", [("f64", "sym"), ("f64", "fast"), ("f32comp", "exact")])
+def test_rejected_combinations(cuda, prec, algo):
+    with pytest.raises(N.NbError) as e:
+        NBodySystem(16, prec, algo)
+    assert e.value.status == N.NB_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("prec,algo", [("f32", "exact"), ("f64", "exact"), ("f32comp", "fast"),
+                                       ("f32comp", "sym")])
+def test_adjoint_needs_a_float_fast_context(cuda, prec, algo):
+    dt_ = dtype_of(prec)
+    p, v = ics.plummer(32, seed=2)
+    with NBodySystem(32, prec, algo) as s:
+        s.set_state(p.astype(dt_), v.astype(dt_))
+        assert s.lib.nb_adj_forward(s.handle, 4, 2, None) == N.NB_ERR_UNSUPPORTED
+
+
+def test_batch_argument_checks(cuda):
+    lib = N.lib()
+    prm = N.NbParams()
+    lib.nb_params_default(C.byref(prm))
+    h = C.c_void_p()
+    sizes = np.array([4, 0, 9], np.int32)  # a system without bodies
+    assert lib.nb_batch_create(C.byref(prm), 3, sizes.ctypes.data_as(C.c_void_p), C.byref(h)) == N.NB_ERR_INVALID
+    sizes = np.array([4, 9], np.int32)
+    prm.algo = N.NB_ALGO_EXACT
+    assert lib.nb_batch_create(C.byref(prm), 2, sizes.ctypes.data_as(C.c_void_p), C.byref(h)) == N.NB_ERR_UNSUPPORTED
+    prm.algo = N.NB_ALGO_SYM
+    prm.precision = N.NB_F64
+    assert lib.nb_batch_create(C.byref(prm), 2, sizes.ctypes.data_as(C.c_void_p), C.byref(h)) == N.NB_ERR_UNSUPPORTED
+    with NBodyBatch([4, 9]) as b:
+        assert b.lib.nb_batch_step(b.handle, 1, None) == N.NB_ERR_STATE
+        with pytest.raises(N.NbError):
+            b.set_shape(3, 5)  # shape not compiled
+
+
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_batch_of_single_bodies(cuda, algo):
+    """Systems of one body each: no forces, free drift, every system apart."""
+    sizes = [1] * 37
+    p, v = ics.uniform_cube(37, seed=4)
+    p32, v32 = ics.f32(p), ics.f32(v)
+    with NBodyBatch(sizes, eps2=np.float32(1e-3), dt=np.float32(1e-3), algo=algo) as b:
+        b.set_state(p32, v32)
+        b.step(4)
+        got, gv = b.get_state()
+    assert np.array_equal(gv, v32)
+    want = p32.copy()
+    for _ in range(4):
+        want[:, :3] = want[:, :3] + v32[:, :3] * np.float32(1e-3)
+    assert np.allclose(got, want, rtol=0, atol=1e-7)
