@@ -118,17 +118,18 @@ def test_fast_plain_cpu_scale_workload(cuda, kick):
     assert np.array_equal(p[:, 3], pos[:, 3]) and np.array_equal(v[:, 3], vel[:, 3])
 
 
-def test_fast_kat_within_reference_gpu_envelope(cuda):
-    """The golden scenario (SHELL, N=1024, 100 chaotic steps) on the fast
-    path stays within the envelope the reference's own GPU run shows around
-    the sequential frames."""
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_fast_kat_within_reference_gpu_envelope(cuda, algo):
+    """The golden scenario (SHELL, N=1024, 100 chaotic steps) on the directed
+    and symmetric paths stays within the envelope the reference's own GPU run
+    shows around the sequential frames."""
     kat = json.load(open(os.path.join(GOLD, "kat_shell_n1024.json")))
     env = kat["gpu_vs_seq_final_frame"]
     dt, cs, vs, soft, damp = oracle.demo_params(0, 1024)
     pos, vel = oracle.randomize(1, 1024, np.float32)
     eps2 = np.float32(soft) * np.float32(soft)
     want, _ = oracle.step(pos, vel, eps2, damp, dt, 100)
-    with NBodySystem(1024, "f32", "fast", eps2=eps2, damping=damp, dt=dt) as s:
+    with NBodySystem(1024, "f32", algo, eps2=eps2, damping=damp, dt=dt) as s:
         s.set_state(pos, vel)
         s.step(100)
         got, _ = s.get_state()
