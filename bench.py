@@ -670,6 +670,22 @@ def run_batched(args):
         b.step_tasks(steps, ntasks)
         t_tasks = (time.perf_counter() - t0) * 1e3
         pt, _ = b.get_state(stream=sh)
+        # batched adjoint: checkpointed forward (every 10 steps) and the
+        # reverse pass for all systems, against the plain batched forward
+        gx = torch.randn((b.nbody, 4), device="cuda", generator=torch.Generator("cuda").manual_seed(3)) * 1e-3
+        adj = {"forward_ckpt": [], "backward": []}
+        for _ in range(2):
+            b.set_state(pos, vel, stream=sh)
+            stream.synchronize()
+            for name, fn in (("forward_ckpt", lambda: b.adj_forward(steps, 10, stream=sh)),
+                             ("backward", lambda: b.adj_backward(gx, stream=sh))):
+                a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                c.record(stream)
+                c.synchronize()
+                adj[name].append(a.elapsed_time(c))
+        t_adjf, t_adjb = min(adj["forward_ckpt"]), min(adj["backward"])
     d = np.linalg.norm(pb[:, :3].astype(np.float64) - pr[:, :3], axis=1)
     w = np.linalg.norm(pr[:, :3].astype(np.float64), axis=1)
     out.update({
@@ -683,6 +699,10 @@ def run_batched(args):
         "G_interactions_per_s_per_system": pairs * steps / (t_base * 1e-3) / 1e9,
         "final_pos_rel_diff_max_vs_per_system": float((d / (w + 0.1)).max()),
         "tasks_equal_per_system_bitwise": bool(pt.tobytes() == pr.tobytes()),
+        "adjoint": {"ckpt_every": 10, "ms_forward_ckpt": t_adjf, "ms_backward": t_adjb,
+                    "backward_over_forward": t_adjb / t_launch,
+                    "note": "reverse pass over all systems (recompute + VJP) vs the batched forward "
+                            "launched step by step"},
     })
     out["other_algo"] = graph_and_per_system(other)
     out["speedup_vs_other_algo_per_system"] = out["other_algo"]["ms_per_system_launches"] / t_graph

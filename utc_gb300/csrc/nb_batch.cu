@@ -483,24 +483,215 @@ __global__ void bk_adj_update_kernel(const float4 *__restrict__ partial, BatchDe
         oz += qv.z;
         odm += qv.w;
     }
-    const float4 x = lx[i], v = lv[i];
-    const float mux = fmaf(dt, x.x, v.x), muy = fmaf(dt, x.y, v.y), muz = fmaf(dt, x.z, v.z);
-    float dmi = odm;
-    if (kick == NB_KICK_REFERENCE) {
-        const float4 a = acc[i];
-        dmi = fmaf(damping * dt, mux * a.x + muy * a.y + muz * a.z, dmi);
+    adj_body_update(i, ox, oy, oz, odm, pos, acc, lx, lv, gm, gbuf, damping, dt, kick, G, want_next_g);
+}
+
+// Symmetric batched VJP: sym_vjp_kernel's pair algebra (nb_adjoint.cu: each
+// unordered pair once, the chunk body's eight reaction sums rotating through
+// the warp) on the symmetric batched layout of bks_force_kernel.
+template <int WPB, int BPT>
+__global__ void __launch_bounds__(32 * WPB) bks_vjp_kernel(const float4 *__restrict__ pos,
+                                                           const float4 *__restrict__ gbuf, BatchSymDev bd,
+                                                           float eps2, float4 *__restrict__ tpart,
+                                                           float4 *__restrict__ spart, long long total,
+                                                           int workers)
+{
+    constexpr int RB = 32 * BPT;
+    constexpr int RC = BPT;
+    __shared__ __align__(16) float4 sC[WPB][32];
+    __shared__ __align__(16) float4 sG[WPB][32];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const int w = blockIdx.x * WPB + wid;
+    if (w >= workers) return;
+    long long it = sk_start(w, total, workers);
+    const long long end = sk_start(w + 1, total, workers);
+    if (it >= end) return;
+    const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    int s = find_sys(bd.it_off, bd.nsys, it);
+    while (it < end) {
+        while (it >= bd.it_off[s + 1]) ++s;
+        const int o = bd.sys_off[s];
+        const int ns = bd.sys_off[s + 1] - o;
+        const int nc = (ns + 31) / 32, nrb = (ns + RB - 1) / RB;
+        const long long base = bd.it_off[s];
+        const int I = sym_row_of(it - base, nc, RC, nrb);
+        const long long rfirst = base + sym_prefix(I, nc, RC);
+        const long long rend = base + sym_prefix(I + 1, nc, RC);
+        const long long seg_end = end < rend ? end : rend;
+        const int kc0 = I * RC + (int)(it - rfirst);
+        const int kc1 = I * RC + (int)(seg_end - rfirst);
+        const int tbase = I * RB;
+
+        // missing targets: zero mass and zero g, so every term they give is 0
+        float px[BPT], py[BPT], pz[BPT], pm[BPT], gx[BPT], gy[BPT], gz[BPT];
+        float Px[BPT], Py[BPT], Pz[BPT], Q0[BPT], Q1[BPT], Q2[BPT], q[BPT], dm[BPT];
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const int li = tbase + lane + 32 * k;
+            const float4 a = li < ns ? pos[o + li] : zero;
+            const float4 g = li < ns ? gbuf[o + li] : zero;
+            px[k] = a.x; py[k] = a.y; pz[k] = a.z; pm[k] = a.w;
+            gx[k] = g.x; gy[k] = g.y; gz[k] = g.z;
+            Px[k] = Py[k] = Pz[k] = Q0[k] = Q1[k] = Q2[k] = q[k] = dm[k] = 0.f;
+        }
+        for (int kc = kc0; kc < kc1; ++kc) {
+            const int jb = kc * 32;
+            __syncwarp();  // previous chunk's reads are done
+            sC[wid][lane] = (jb + lane < ns) ? pos[o + jb + lane] : pad;
+            sG[wid][lane] = (jb + lane < ns) ? gbuf[o + jb + lane] : zero;
+            __syncwarp();
+            if (kc < (I + 1) * RC) {
+                // chunk inside the own row block: directed, target side only
+#pragma unroll 2
+                for (int j = 0; j < 32; ++j) {
+                    const float4 sb = sC[wid][j];
+                    const float4 g = sG[wid][j];
+#pragma unroll
+                    for (int k = 0; k < BPT; ++k) {
+                        const float rx = sb.x - px[k], ry = sb.y - py[k], rz = sb.z - pz[k];
+                        float d2 = fmaf(rx, rx, eps2);
+                        d2 = fmaf(ry, ry, d2);
+                        d2 = fmaf(rz, rz, d2);
+                        const float inv = rsqrt_approx(d2);
+                        const float inv2 = inv * inv;
+                        const float inv3 = inv2 * inv;
+                        const float inv5 = inv3 * inv2;
+                        Px[k] = fmaf(inv3, g.x, Px[k]);
+                        Py[k] = fmaf(inv3, g.y, Py[k]);
+                        Pz[k] = fmaf(inv3, g.z, Pz[k]);
+                        q[k] = fmaf(inv3, sb.w, q[k]);
+                        const float rgj = fmaf(rz, g.z, fmaf(ry, g.y, rx * g.x));
+                        const float rgk = fmaf(rz, gz[k], fmaf(ry, gy[k], rx * gx[k]));
+                        const float cc = inv5 * fmaf(pm[k], rgj, -(sb.w * rgk));
+                        Q0[k] = fmaf(cc, rx, Q0[k]);
+                        Q1[k] = fmaf(cc, ry, Q1[k]);
+                        Q2[k] = fmaf(cc, rz, Q2[k]);
+                        dm[k] = fmaf(inv3, rgj, dm[k]);
+                    }
+                }
+            } else {
+                float rPx = 0.f, rPy = 0.f, rPz = 0.f, rq = 0.f, rQ0 = 0.f, rQ1 = 0.f, rQ2 = 0.f, rw = 0.f;
+#pragma unroll 2
+                for (int r = 0; r < 32; ++r) {
+                    const int idx = (lane + r) & 31;
+                    const float4 sb = sC[wid][idx];
+                    const float4 g = sG[wid][idx];
+#pragma unroll
+                    for (int k = 0; k < BPT; ++k) {
+                        const float rx = sb.x - px[k], ry = sb.y - py[k], rz = sb.z - pz[k];
+                        float d2 = fmaf(rx, rx, eps2);
+                        d2 = fmaf(ry, ry, d2);
+                        d2 = fmaf(rz, rz, d2);
+                        const float inv = rsqrt_approx(d2);
+                        const float inv2 = inv * inv;
+                        const float inv3 = inv2 * inv;
+                        const float inv5 = inv3 * inv2;
+                        const float rgj = fmaf(rz, g.z, fmaf(ry, g.y, rx * g.x));
+                        const float rgk = fmaf(rz, gz[k], fmaf(ry, gy[k], rx * gx[k]));
+                        const float cc = inv5 * fmaf(pm[k], rgj, -(sb.w * rgk));
+                        Px[k] = fmaf(inv3, g.x, Px[k]);
+                        Py[k] = fmaf(inv3, g.y, Py[k]);
+                        Pz[k] = fmaf(inv3, g.z, Pz[k]);
+                        q[k] = fmaf(inv3, sb.w, q[k]);
+                        Q0[k] = fmaf(cc, rx, Q0[k]);
+                        Q1[k] = fmaf(cc, ry, Q1[k]);
+                        Q2[k] = fmaf(cc, rz, Q2[k]);
+                        dm[k] = fmaf(inv3, rgj, dm[k]);
+                        rPx = fmaf(inv3, gx[k], rPx);
+                        rPy = fmaf(inv3, gy[k], rPy);
+                        rPz = fmaf(inv3, gz[k], rPz);
+                        rq = fmaf(inv3, pm[k], rq);
+                        rQ0 = fmaf(-cc, rx, rQ0);
+                        rQ1 = fmaf(-cc, ry, rQ1);
+                        rQ2 = fmaf(-cc, rz, rQ2);
+                        rw = fmaf(inv3, rgk, rw);
+                    }
+                    const int from = (lane + 1) & 31;
+                    rPx = __shfl_sync(0xffffffffu, rPx, from);
+                    rPy = __shfl_sync(0xffffffffu, rPy, from);
+                    rPz = __shfl_sync(0xffffffffu, rPz, from);
+                    rq = __shfl_sync(0xffffffffu, rq, from);
+                    rQ0 = __shfl_sync(0xffffffffu, rQ0, from);
+                    rQ1 = __shfl_sync(0xffffffffu, rQ1, from);
+                    rQ2 = __shfl_sync(0xffffffffu, rQ2, from);
+                    rw = __shfl_sync(0xffffffffu, rw, from);
+                }
+                // lane l holds chunk body l's reaction
+                if (jb + lane < ns) {
+                    const float4 sb = sC[wid][lane], gb = sG[wid][lane];
+                    const float ox = fmaf(sb.w, rPx, fmaf(-rq, gb.x, -3.f * rQ0));
+                    const float oy = fmaf(sb.w, rPy, fmaf(-rq, gb.y, -3.f * rQ1));
+                    const float oz = fmaf(sb.w, rPz, fmaf(-rq, gb.z, -3.f * rQ2));
+                    spart[bd.sp_off[s] + sym_soff(I, ns, RB) + (jb + lane - (I + 1) * RB)] =
+                        make_float4(ox, oy, oz, rw);
+                }
+            }
+        }
+        float4 *dst = tpart + ((long long)w + bd.row_off[s] + I) * RB;
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const float ox = fmaf(pm[k], Px[k], fmaf(-q[k], gx[k], -3.f * Q0[k]));
+            const float oy = fmaf(pm[k], Py[k], fmaf(-q[k], gy[k], -3.f * Q1[k]));
+            const float oz = fmaf(pm[k], Pz[k], fmaf(-q[k], gz[k], -3.f * Q2[k]));
+            dst[lane + 32 * k] = make_float4(ox, oy, oz, -dm[k]);
+        }
+        it = seg_end;
     }
-    gm[i] += dmi;
-    const float4 nx = make_float4(x.x + ox, x.y + oy, x.z + oz, 0.f);
-    const float4 nv = make_float4(damping * mux, damping * muy, damping * muz, 0.f);
-    lx[i] = nx;
-    lv[i] = nv;
-    if (want_next_g) {
-        const float kf = kick == NB_KICK_REFERENCE ? pos[i].w : G;
-        const float f = damping * dt * kf;
-        gbuf[i] = make_float4(f * fmaf(dt, nx.x, nv.x), f * fmaf(dt, nx.y, nv.y),
-                              f * fmaf(dt, nx.z, nv.z), 0.f);
+}
+
+// Symmetric batched reverse-step update: target-side slots (warp order) and
+// source-side rows (row order) of the body's system, then the per-body update.
+__global__ void bks_adj_update_kernel(const float4 *__restrict__ tpart, const float4 *__restrict__ spart,
+                                      BatchSymDev bd, int nbody, int rb, long long total, int workers,
+                                      const float4 *__restrict__ pos, const float4 *__restrict__ acc,
+                                      float4 *__restrict__ lx, float4 *__restrict__ lv,
+                                      float *__restrict__ gm, float4 *__restrict__ gbuf, float damping,
+                                      float dt, int kick, float G, int want_next_g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbody) return;
+    const int s = bd.body_sys[i];
+    const int o = bd.sys_off[s];
+    const int ns = bd.sys_off[s + 1] - o;
+    const int li = i - o;
+    const int rc = rb / 32;
+    const int nc = (ns + 31) / 32;
+    const int I = li / rb;
+    const long long base = bd.it_off[s];
+    const int c0 = sk_owner(base + sym_prefix(I, nc, rc), total, workers);
+    const int c1 = sk_owner(base + sym_prefix(I + 1, nc, rc) - 1, total, workers);
+    const long long grow = (long long)bd.row_off[s] + I;
+    const int lj = li - I * rb;
+    float ox = 0.f, oy = 0.f, oz = 0.f, odm = 0.f;
+    for (int c = c0; c <= c1; ++c) {
+        const float4 qv = tpart[(c + grow) * rb + lj];
+        ox += qv.x;
+        oy += qv.y;
+        oz += qv.z;
+        odm += qv.w;
     }
+    long long off = bd.sp_off[s] + li - rb;  // row r at soff(r) + li - (r + 1) rb
+    for (int r = 0; r < I; ++r) {
+        const float4 qv = spart[off];
+        off += (long long)ns - (long long)(r + 2) * rb;
+        ox += qv.x;
+        oy += qv.y;
+        oz += qv.z;
+        odm += qv.w;
+    }
+    adj_body_update(i, ox, oy, oz, odm, pos, acc, lx, lv, gm, gbuf, damping, dt, kick, G, want_next_g);
+}
+
+typedef void (*bks_vjp_t)(const float4 *, const float4 *, BatchSymDev, float, float4 *, float4 *, long long,
+                          int);
+
+static bks_vjp_t bks_vjp_for(int wpb, int bpt)
+{
+    if (wpb == 1 && bpt == 10) return bks_vjp_kernel<1, 10>;
+    if (wpb == 1 && bpt == 8) return bks_vjp_kernel<1, 8>;
+    return nullptr;
 }
 
 typedef void (*bk_vjp_t)(const float4 *, const float4 *, BatchDev, float, float4 *, long long, int);
@@ -564,6 +755,9 @@ struct nb_batch {
     long long *d_it_off_v = nullptr;
     int *d_tb_off_v = nullptr;
     float4 *vpartial = nullptr;
+    long long *d_sp_off_v = nullptr;  // symmetric VJP: source-side offsets
+    float4 *vspart = nullptr;         // and arrays
+    bool adj_live_last = false;       // last segment's states left by the forward
     int adj_steps = 0, adj_every = 0, adj_nckpt = 0, cap_ckpt = 0, cap_seg = 0;
     bool adj_ready = false;
     float4 *ckpt_pos = nullptr, *ckpt_vel = nullptr, *seg_pos = nullptr, *seg_acc = nullptr;
@@ -674,10 +868,8 @@ static nb::BatchSymDev batch_sym_dev(const nb_batch *b)
     return d;
 }
 
-// One batched step from po into pn (vel in place); with acc_out the second
-// kernel writes the bare accelerations instead of integrating.
-static int batch_force_step(nb_batch *b, const float4 *po, float4 *pn, float4 *vel,
-                            float4 *acc_out, cudaStream_t s)
+// The batched force pass at positions po (partials into the batch scratch).
+static int batch_force(nb_batch *b, const float4 *po, cudaStream_t s)
 {
     const BatchPlan &p = b->plan;
     if (b->nbody == 0) return NB_OK;
@@ -686,20 +878,42 @@ static int batch_force_step(nb_batch *b, const float4 *po, float4 *pn, float4 *v
         k<<<p.grid, 32 * p.wpb, 0, s>>>(po, batch_sym_dev(b), (float)b->p.eps2, b->partial, b->spart,
                                         p.total, p.workers);
         NB_LAUNCH_CHECK("bks_force_kernel launch");
+        return NB_OK;
+    }
+    nb::bk_kernel_t k = nb::bk_kernel_for(p.wpb, p.bpt);
+    k<<<p.grid, 32 * p.wpb, 0, s>>>(po, batch_dev(b), (float)b->p.eps2, b->partial, p.total, p.workers);
+    NB_LAUNCH_CHECK("bk_force_kernel launch");
+    return NB_OK;
+}
+
+// Sum the partials of the last force pass and integrate from po into pn (vel
+// in place), or with acc_out write the bare accelerations instead.
+static int batch_integrate(nb_batch *b, const float4 *po, float4 *pn, float4 *vel, float4 *acc_out,
+                           cudaStream_t s)
+{
+    const BatchPlan &p = b->plan;
+    if (b->nbody == 0) return NB_OK;
+    if (b->sym) {
         nb::bks_integrate_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
             po, pn, vel, b->partial, b->spart, batch_sym_dev(b), b->nbody, 32 * p.bpt, p.total,
             p.workers, (float)b->p.damping, (float)b->p.dt, b->p.kick, (float)b->p.G, acc_out);
         NB_LAUNCH_CHECK("bks_integrate_kernel launch");
         return NB_OK;
     }
-    nb::bk_kernel_t k = nb::bk_kernel_for(p.wpb, p.bpt);
-    k<<<p.grid, 32 * p.wpb, 0, s>>>(po, batch_dev(b), (float)b->p.eps2, b->partial, p.total, p.workers);
-    NB_LAUNCH_CHECK("bk_force_kernel launch");
     nb::bk_integrate_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
         po, pn, vel, b->partial, batch_dev(b), b->nbody, 32 * p.bpt, p.total, p.workers,
         (float)b->p.damping, (float)b->p.dt, b->p.kick, (float)b->p.G, acc_out);
     NB_LAUNCH_CHECK("bk_integrate_kernel launch");
     return NB_OK;
+}
+
+// One batched step from po into pn (vel in place); with acc_out the second
+// kernel writes the bare accelerations instead of integrating.
+static int batch_force_step(nb_batch *b, const float4 *po, float4 *pn, float4 *vel,
+                            float4 *acc_out, cudaStream_t s)
+{
+    int st = batch_force(b, po, s);
+    return st ? st : batch_integrate(b, po, pn, vel, acc_out, s);
 }
 
 static int batch_step_once(nb_batch *b, cudaStream_t s)
@@ -711,19 +925,22 @@ static int batch_step_once(nb_batch *b, cudaStream_t s)
     return NB_OK;
 }
 
-// VJP plan: its own (system, warp target block) tables for 32 * bpt targets
+// VJP plan: its own tables for 32 * bpt targets per warp block (directed:
+// (system, target block, source group) items; symmetric: (system, row,
+// chunk) items with the source-side offsets)
 static int batch_vplan_setup(nb_batch *b)
 {
     if (b->d_it_off_v) return NB_OK;
-    const int wpb = 4, bpt = 4, wtb = 32 * bpt;
-    nb::bk_vjp_t k = nb::bk_vjp_for(wpb, bpt);
-    std::vector<long long> it_off(b->nsys + 1, 0);
+    const int wpb = b->sym ? 1 : 4, bpt = b->sym ? 10 : 4, wtb = 32 * bpt;
+    const void *k = b->sym ? (const void *)nb::bks_vjp_for(wpb, bpt) : (const void *)nb::bk_vjp_for(wpb, bpt);
+    std::vector<long long> it_off(b->nsys + 1, 0), sp_off(b->nsys + 1, 0);
     std::vector<int> tb_off(b->nsys + 1, 0);
     for (int q = 0; q < b->nsys; ++q) {
         const long long n = b->sizes[q];
         const long long ntb = (n + wtb - 1) / wtb, ng = (n + nb::kGroup - 1) / nb::kGroup;
-        it_off[q + 1] = it_off[q] + ntb * ng;
+        it_off[q + 1] = it_off[q] + (b->sym ? nb::sym_prefix(ntb, (int)ng, bpt) : ntb * ng);
         tb_off[q + 1] = tb_off[q] + (int)ntb;
+        sp_off[q + 1] = sp_off[q] + (b->sym ? nb::sym_spart_entries((int)n, wtb) : 0);
     }
     int occ = 0;
     NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * wpb, 0));
@@ -733,6 +950,7 @@ static int batch_vplan_setup(nb_batch *b)
     p.bpt = bpt;
     p.total = it_off[b->nsys];
     p.total_wtb = tb_off[b->nsys];
+    p.spart = sp_off[b->nsys];
     long long workers = (long long)b->sms * occ * wpb;
     if (p.total > 0 && workers > p.total) workers = p.total;
     p.workers = p.total > 0 ? (int)workers : 0;
@@ -740,11 +958,15 @@ static int batch_vplan_setup(nb_batch *b)
     p.slots = p.total > 0 ? p.workers + p.total_wtb - 1 : 0;
     NB_CUDA(cudaMalloc((void **)&b->d_it_off_v, sizeof(long long) * (b->nsys + 1)));
     NB_CUDA(cudaMalloc((void **)&b->d_tb_off_v, sizeof(int) * (b->nsys + 1)));
+    NB_CUDA(cudaMalloc((void **)&b->d_sp_off_v, sizeof(long long) * (b->nsys + 1)));
     NB_CUDA(cudaMemcpy(b->d_it_off_v, it_off.data(), sizeof(long long) * (b->nsys + 1),
                        cudaMemcpyHostToDevice));
     NB_CUDA(cudaMemcpy(b->d_tb_off_v, tb_off.data(), sizeof(int) * (b->nsys + 1),
                        cudaMemcpyHostToDevice));
+    NB_CUDA(cudaMemcpy(b->d_sp_off_v, sp_off.data(), sizeof(long long) * (b->nsys + 1),
+                       cudaMemcpyHostToDevice));
     NB_CUDA(cudaMalloc((void **)&b->vpartial, std::max<size_t>((size_t)p.slots * wtb, 1) * sizeof(float4)));
+    NB_CUDA(cudaMalloc((void **)&b->vspart, std::max<size_t>((size_t)p.spart, 1) * sizeof(float4)));
     const size_t nb4 = std::max<size_t>((size_t)b->nbody, 1) * sizeof(float4);
     NB_CUDA(cudaMalloc((void **)&b->vel_tmp, nb4));
     NB_CUDA(cudaMalloc((void **)&b->lx, nb4));
@@ -774,6 +996,8 @@ static void free_batch(nb_batch *b)
     cudaFree(b->d_it_off_v);
     cudaFree(b->d_tb_off_v);
     cudaFree(b->vpartial);
+    cudaFree(b->d_sp_off_v);
+    cudaFree(b->vspart);
     cudaFree(b->ckpt_pos);
     cudaFree(b->ckpt_vel);
     cudaFree(b->seg_pos);
@@ -1234,6 +1458,12 @@ int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream)
         b->cap_seg = ckpt_every;
     }
     cudaStream_t s = (cudaStream_t)stream;
+    // as nb_adj_forward: the last segment's states (and reference-kick
+    // accelerations) stay in the segment buffers, so the reverse pass does
+    // not recompute that segment
+    const int t_last = (nckpt - 1) * ckpt_every;
+    b->adj_ready = false;
+    b->adj_live_last = false;
     for (int t = 0; t < steps; ++t) {
         if (t % ckpt_every == 0 && n) {
             const size_t k = (size_t)(t / ckpt_every) * n;
@@ -1242,12 +1472,24 @@ int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream)
             NB_CUDA(cudaMemcpyAsync(b->ckpt_vel + k, b->vel, n * sizeof(float4),
                                     cudaMemcpyDeviceToDevice, s));
         }
+        const bool keep = n && t >= t_last;
+        const size_t k = (size_t)(t - t_last);
+        if (keep && t == t_last)
+            NB_CUDA(cudaMemcpyAsync(b->seg_pos, b->pos[b->cur], n * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+        const float4 *xk = b->pos[b->cur];
         if ((st = batch_step_once(b, s))) return st;
+        if (!keep) continue;
+        if (b->p.kick == NB_KICK_REFERENCE &&
+            (st = batch_integrate(b, xk, nullptr, nullptr, b->seg_acc + k * n, s)))
+            return st;
+        NB_CUDA(cudaMemcpyAsync(b->seg_pos + (k + 1) * n, b->pos[b->cur], n * sizeof(float4),
+                                cudaMemcpyDeviceToDevice, s));
     }
     b->adj_steps = steps;
     b->adj_every = ckpt_every;
     b->adj_nckpt = nckpt;
     b->adj_ready = true;
+    b->adj_live_last = n > 0;
     return NB_OK;
 }
 
@@ -1265,8 +1507,13 @@ int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void 
     nb::BatchDev vd = batch_dev(b);
     vd.it_off = b->d_it_off_v;
     vd.tb_off = b->d_tb_off_v;
+    nb::BatchSymDev vsd = batch_sym_dev(b);
+    vsd.it_off = b->d_it_off_v;
+    vsd.row_off = b->d_tb_off_v;
+    vsd.sp_off = b->d_sp_off_v;
     const BatchPlan &vp = b->vplan;
-    nb::bk_vjp_t vk = nb::bk_vjp_for(vp.wpb, vp.bpt);
+    nb::bk_vjp_t vk = b->sym ? nullptr : nb::bk_vjp_for(vp.wpb, vp.bpt);
+    nb::bks_vjp_t vks = b->sym ? nb::bks_vjp_for(vp.wpb, vp.bpt) : nullptr;
     int st;
     NB_CUDA(cudaMemcpyAsync(b->lx, gx_T, n * sizeof(float4), cudaMemcpyDeviceToDevice, s));
     if (gv_T)
@@ -1278,11 +1525,15 @@ int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void 
     for (int seg = b->adj_nckpt - 1; seg >= 0; --seg) {
         const int t0 = seg * b->adj_every;
         const int len = (b->adj_steps - t0) < b->adj_every ? (b->adj_steps - t0) : b->adj_every;
-        NB_CUDA(cudaMemcpyAsync(b->seg_pos, b->ckpt_pos + (size_t)seg * n, n * sizeof(float4),
-                                cudaMemcpyDeviceToDevice, s));
-        NB_CUDA(cudaMemcpyAsync(b->vel_tmp, b->ckpt_vel + (size_t)seg * n, n * sizeof(float4),
-                                cudaMemcpyDeviceToDevice, s));
-        for (int k = 0; k < len; ++k) {
+        const bool recompute = !(seg == b->adj_nckpt - 1 && b->adj_live_last);
+        b->adj_live_last = false;  // the segment buffers are reused from here on
+        if (recompute) {
+            NB_CUDA(cudaMemcpyAsync(b->seg_pos, b->ckpt_pos + (size_t)seg * n, n * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, s));
+            NB_CUDA(cudaMemcpyAsync(b->vel_tmp, b->ckpt_vel + (size_t)seg * n, n * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, s));
+        }
+        for (int k = 0; recompute && k < len; ++k) {
             const float4 *xk = b->seg_pos + (size_t)k * n;
             if (p.kick == NB_KICK_REFERENCE &&
                 (st = batch_force_step(b, xk, nullptr, nullptr, b->seg_acc + (size_t)k * n, s)))
@@ -1296,11 +1547,23 @@ int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void 
                 if ((st = nb::adj_g(b->nbody, xk, b->lx, b->lv, b->gbuf, D, dt, p.kick, G, s))) return st;
                 have_g = true;
             }
+            const bool more = !(seg == 0 && k == 0);
+            if (b->sym) {
+                if (vp.total > 0) {
+                    vks<<<vp.grid, 32 * vp.wpb, 0, s>>>(xk, b->gbuf, vsd, eps2, b->vpartial, b->vspart,
+                                                         vp.total, vp.workers);
+                    NB_LAUNCH_CHECK("bks_vjp_kernel launch");
+                }
+                nb::bks_adj_update_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
+                    b->vpartial, b->vspart, vsd, b->nbody, 32 * vp.bpt, vp.total, vp.workers, xk,
+                    b->seg_acc + (size_t)k * n, b->lx, b->lv, b->gm, b->gbuf, D, dt, p.kick, G, more ? 1 : 0);
+                NB_LAUNCH_CHECK("bks_adj_update_kernel launch");
+                continue;
+            }
             if (vp.total > 0) {
                 vk<<<vp.grid, 32 * vp.wpb, 0, s>>>(xk, b->gbuf, vd, eps2, b->vpartial, vp.total, vp.workers);
                 NB_LAUNCH_CHECK("bk_vjp_kernel launch");
             }
-            const bool more = !(seg == 0 && k == 0);
             nb::bk_adj_update_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
                 b->vpartial, vd, b->nbody, 32 * vp.bpt, vp.total, vp.workers, xk,
                 b->seg_acc + (size_t)k * n, b->lx, b->lv, b->gm, b->gbuf, D, dt, p.kick, G, more ? 1 : 0);

@@ -213,6 +213,38 @@ int sym_comp_integrate(const SymPlan &p, const float4 *tpart, const float4 *spar
                        float4 *pos32, float4 *vhi, float4 *vlo, float damping, float dt,
                        double dt64, int kick, float G, double4 *acc_out, cudaStream_t s);
 
+// One reverse step's per-body update given the summed pair terms (o, odm):
+//   lx <- lx + out;  lv <- D mu;  gm += dm (+ D dt mu.a in reference mode)
+// and, when want_next_g, g for the next reverse step (at the previous state,
+// whose masses are the same).
+__device__ __forceinline__ void adj_body_update(int i, float ox, float oy, float oz, float odm,
+                                                const float4 *__restrict__ pos,
+                                                const float4 *__restrict__ acc,
+                                                float4 *__restrict__ lx, float4 *__restrict__ lv,
+                                                float *__restrict__ gm, float4 *__restrict__ gbuf,
+                                                float damping, float dt, int kick, float G,
+                                                int want_next_g)
+{
+    const float4 x = lx[i], v = lv[i];
+    const float mux = fmaf(dt, x.x, v.x), muy = fmaf(dt, x.y, v.y), muz = fmaf(dt, x.z, v.z);
+    float dmi = odm;
+    if (kick == NB_KICK_REFERENCE) {
+        const float4 a = acc[i];
+        dmi = fmaf(damping * dt, mux * a.x + muy * a.y + muz * a.z, dmi);
+    }
+    gm[i] += dmi;
+    const float4 nx = make_float4(x.x + ox, x.y + oy, x.z + oz, 0.f);
+    const float4 nv = make_float4(damping * mux, damping * muy, damping * muz, 0.f);
+    lx[i] = nx;
+    lv[i] = nv;
+    if (want_next_g) {
+        const float k = kick == NB_KICK_REFERENCE ? pos[i].w : G;
+        const float f = damping * dt * k;
+        gbuf[i] = make_float4(f * fmaf(dt, nx.x, nv.x), f * fmaf(dt, nx.y, nv.y),
+                              f * fmaf(dt, nx.z, nv.z), 0.f);
+    }
+}
+
 // Adjoint kernels (nb_adjoint.cu)
 int adj_plan(int n, int block, int bpt, int device, SkPlan *pl);
 int adj_g(int n, const float4 *pos, const float4 *lx, const float4 *lv, float4 *gbuf, float damping,
