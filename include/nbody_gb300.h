@@ -71,8 +71,10 @@ typedef enum {
     /* Each unordered pair evaluated once and applied to both bodies (the
      * pair term is odd in r): 16 FP32 operations and one rsqrt per two
      * interactions.  Same per-pair terms as NB_ALGO_FAST, different summation
-     * order; deterministic.  NB_F32 and NB_F32_COMP (compensated partial
-     * sums). */
+     * order; deterministic.  NB_F32, NB_F32_COMP (compensated partial sums)
+     * and NB_F64 (FP64 throughout, 1/sqrt from the FP64 approximation and two
+     * Newton steps: agrees with the FP64 reference to rounding, not bit for
+     * bit). */
     NB_ALGO_SYM = 2
 } nb_algo;
 

@@ -15,6 +15,7 @@ import os
 import oracle
 
 KERNEL_F32 = "_Z28_integrateNBodySystem_kernelIfEvPT_S1_S1_iS0_S0_S0_i"
+KERNEL_F64 = "_Z28_integrateNBodySystem_kernelIdEvPT_S1_S1_iS0_S0_S0_i"
 
 
 class RefKernel:
@@ -28,10 +29,23 @@ class RefKernel:
         self.cu.cuLaunchKernel.argtypes = [C.c_void_p] + [C.c_uint] * 6 + [C.c_uint, C.c_void_p,
                                                                             C.c_void_p, C.c_void_p]
         self.cu.cuModuleUnload.argtypes = [C.c_void_p]
+        # make the device's primary context (the one the runtime and torch
+        # use) current on this thread before loading the module
+        self.cu.cuDevicePrimaryCtxRetain.argtypes = [C.POINTER(C.c_void_p), C.c_int]
+        self.cu.cuCtxSetCurrent.argtypes = [C.c_void_p]
+        dev = C.c_int()
+        self._ok(self.cu.cuInit(0), "cuInit")
+        self._ok(self.cu.cuDeviceGet(C.byref(dev), 0), "cuDeviceGet")
+        self.ctx = C.c_void_p()
+        self._ok(self.cu.cuDevicePrimaryCtxRetain(C.byref(self.ctx), dev), "cuDevicePrimaryCtxRetain")
+        self._ok(self.cu.cuCtxSetCurrent(self.ctx), "cuCtxSetCurrent")
         self.mod = C.c_void_p()
         self._ok(self.cu.cuModuleLoad(C.byref(self.mod), path.encode()), "cuModuleLoad")
         self.fn = C.c_void_p()
         self._ok(self.cu.cuModuleGetFunction(C.byref(self.fn), self.mod, KERNEL_F32.encode()),
+                 "cuModuleGetFunction")
+        self.fn64 = C.c_void_p()
+        self._ok(self.cu.cuModuleGetFunction(C.byref(self.fn64), self.mod, KERNEL_F64.encode()),
                  "cuModuleGetFunction")
 
     @staticmethod
@@ -39,14 +53,18 @@ class RefKernel:
         if rc != 0:
             raise RuntimeError(f"{what} failed with CUresult {rc}")
 
-    def step(self, pos_old, pos_new, vel, n, dt, eps2, damping, block, stream):
-        """One reference step; pos/vel are device pointers (ints)."""
+    def step(self, pos_old, pos_new, vel, n, dt, eps2, damping, block, stream, double=False):
+        """One reference step; pos/vel are device pointers (ints) of float4
+        (or double4 with double=True)."""
         if n % block != 0 or block > 512:
             raise ValueError("the reference kernel needs n % block == 0 and block <= 512")
+        real = C.c_double if double else C.c_float
         args = [C.c_uint64(pos_old), C.c_uint64(pos_new), C.c_uint64(vel), C.c_int(n),
-                C.c_float(dt), C.c_float(eps2), C.c_float(damping), C.c_int(n // block)]
+                real(dt), real(eps2), real(damping), C.c_int(n // block)]
         params = (C.c_void_p * len(args))(*[C.addressof(a) for a in args])
-        self._ok(self.cu.cuLaunchKernel(self.fn, n // block, 1, 1, block, 1, 1, 0,
+        fn = self.fn64 if double else self.fn
+        # the kernel's shared tile is 4 T per thread (sharedPos[4][512] of T)
+        self._ok(self.cu.cuLaunchKernel(fn, n // block, 1, 1, block, 1, 1, 0,
                                         C.c_void_p(stream), params, None), "cuLaunchKernel")
 
     def close(self):

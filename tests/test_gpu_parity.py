@@ -260,12 +260,36 @@ def test_drop_in_task_f64_exact_matches_oracle(cuda):
     rt = (C.c_double * 4)()
     rc = N.task_lib().nbt_run_f64(n, eps2, float(np.float32(damp)), pos.ctypes.data_as(C.c_void_p),
                                   vel.ctypes.data_as(C.c_void_p), rt, loops, oi, 128,
-                                  float(np.float32(dt)), out.ctypes.data_as(C.c_void_p), 0, -1, 0)
+                                  float(np.float32(dt)), out.ctypes.data_as(C.c_void_p), 0, 1, 0)
     assert rc == 0
     p, v = pos, vel
     for k in range(loops // oi):
         p, v = oracle.step(p, v, eps2, float(np.float32(damp)), float(np.float32(dt)), oi)
         assert out[k].tobytes() == p.tobytes()
+
+
+def test_drop_in_task_f64_default_symmetric(cuda):
+    """The double task's default algorithm (FP64 symmetric) against the
+    FP64 oracle: positions within 1e-12 relative after the run."""
+    import ctypes as C
+
+    from utc_gb300 import _native as N
+
+    n, loops, oi = 1024, 8, 4
+    pos, vel = oracle.randomize(1, n, np.float64)
+    dt, _, _, soft, damp = oracle.demo_params(0, n)
+    eps2 = float(np.float32(soft)) ** 2
+    out = np.zeros((loops // oi, n, 4), np.float64)
+    rt = (C.c_double * 4)()
+    rc = N.task_lib().nbt_run_f64(n, eps2, float(np.float32(damp)), pos.ctypes.data_as(C.c_void_p),
+                                  vel.ctypes.data_as(C.c_void_p), rt, loops, oi, 128,
+                                  float(np.float32(dt)), out.ctypes.data_as(C.c_void_p), 0, -1, 0)
+    assert rc == 0
+    p, v = pos, vel
+    for k in range(loops // oi):
+        p, v = oracle.step(p, v, eps2, float(np.float32(damp)), float(np.float32(dt)), oi)
+        rel = np.linalg.norm(out[k][:, :3] - p[:, :3], axis=1) / (np.linalg.norm(p[:, :3], axis=1) + 1e-3)
+        assert rel.max() <= 1e-12
 
 
 def test_status_codes_on_device(cuda):

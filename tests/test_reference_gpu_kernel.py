@@ -125,3 +125,43 @@ def test_batch_vs_reference_kernel_per_system(ref_kernel, capsys):
         print(f"\n[batch baseline] {len(sizes)} systems, {steps} steps: reference kernel per system "
               f"{ms_ref:.1f} ms, batched launch {ms_b:.1f} ms, speed-up {ms_ref / ms_b:.1f}x")
     assert ms_b < ms_ref
+
+
+def test_reference_kernel_f64_vs_exact_f64(ref_kernel, capsys):
+    """The app's default state type is double: the reference's kernel in
+    double against the reference-exact FP64 kernel, same input, same update
+    rule (reference kick).  Agreement to FP64 rounding; both timed."""
+    import torch
+
+    n, steps, block = 16384, 3, 256
+    p64, v64 = ics.plummer(n, seed=3)
+    s = torch.cuda.current_stream()
+    bufs = [torch.from_numpy(p64).cuda(), torch.empty_like(torch.from_numpy(p64)).cuda()]
+    vt = torch.from_numpy(v64).cuda()
+    ref_kernel.step(bufs[0].data_ptr(), bufs[1].data_ptr(), vt.data_ptr(), n, 1e-4, 1e-4, 1.0, block,
+                    s.cuda_stream, double=True)  # warm-up
+    bufs[0].copy_(torch.from_numpy(p64))
+    vt.copy_(torch.from_numpy(v64))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for i in range(steps):
+        ref_kernel.step(bufs[i % 2].data_ptr(), bufs[(i + 1) % 2].data_ptr(), vt.data_ptr(), n, 1e-4, 1e-4,
+                        1.0, block, s.cuda_stream, double=True)
+    e1.record(s)
+    e1.synchronize()
+    ms_ref = e0.elapsed_time(e1)
+    p_ref = bufs[steps % 2].cpu().numpy()
+    r_ref = n * n * steps / (ms_ref * 1e-3) / 1e9
+    for algo in ("exact", "sym"):
+        with NBodySystem(n, "f64", algo, kick="reference", eps2=1e-4, damping=1.0, dt=1e-4) as sy:
+            sy.set_state(p64, v64)
+            sy.step(1)
+            sy.set_state(p64, v64)
+            f, g = sy.step_timed(steps)
+            p_ours, _ = sy.get_state()
+        assert np.abs(p_ours - p_ref).max() <= 1e-12 * np.abs(p_ref).max()
+        r_ours = n * n * steps / ((f + g) * 1e-3) / 1e9
+        with capsys.disabled():
+            print(f"\n[gpu baseline f64] N={n}: reference kernel (double, sm_103a build) {r_ref:.2f} "
+                  f"G interactions/s; {algo} FP64 kernel {r_ours:.2f} G interactions/s; "
+                  f"ratio {r_ours / r_ref:.2f}x")

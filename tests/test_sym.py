@@ -96,3 +96,33 @@ def test_sym_default_shape(cuda, n, shape):
     with NBodySystem(n, "f32", "sym") as s:
         info = s.plan_info()
     assert (info["block"], info["bpt"]) == shape
+
+
+@pytest.mark.parametrize("n", [1, 2, 33, 255, 256, 257, 1000, 2049, 5000])
+def test_sym_f64_accel_vs_oracle(cuda, n):
+    """FP64 symmetric kernel: accelerations within 1e-13 (|a| + mean|a|) of
+    the FP64 oracle (its 1/sqrt comes from the FP64 approximation refined by
+    two Newton steps; every other operation is FP64)."""
+    p, _ = ics.plummer(n, seed=n)
+    with NBodySystem(n, "f64", "sym", eps2=1e-3) as s:
+        s.set_state(p, np.zeros_like(p))
+        a = s.accel()
+    assert close(a, oracle.accel(p, 1e-3), tol=1e-13)
+
+
+@pytest.mark.parametrize("kick", ["reference", "physical"])
+def test_sym_f64_steps_vs_oracle(cuda, kick):
+    n, steps = 3000, 10
+    p, v = ics.uniform_cube(n, seed=1)
+    km = oracle.KICK_REFERENCE if kick == "reference" else oracle.KICK_PHYSICAL
+    with NBodySystem(n, "f64", "sym", kick=kick, eps2=1e-2, damping=0.999, dt=1e-3) as s:
+        s.set_state(p, v)
+        s.step(steps)
+        got, gv = s.get_state()
+        s.set_state(p, v)
+        s.step(steps)
+        again, _ = s.get_state()
+    want, wv = oracle.step(p, v, 1e-2, 0.999, 1e-3, steps, kick_mode=km)
+    rel = np.linalg.norm(got[:, :3] - want[:, :3], axis=1) / (np.linalg.norm(want[:, :3], axis=1) + 0.1)
+    assert rel.max() <= 1e-13
+    assert got.tobytes() == again.tobytes()

@@ -95,8 +95,6 @@ static int validate(const nb_params *p)
         return set_error(NB_ERR_INVALID, "unknown precision");
     if (p->algo != NB_ALGO_FAST && p->algo != NB_ALGO_EXACT && p->algo != NB_ALGO_SYM)
         return set_error(NB_ERR_INVALID, "unknown algo");
-    if (p->algo == NB_ALGO_SYM && p->precision == NB_F64)
-        return set_error(NB_ERR_UNSUPPORTED, "NB_ALGO_SYM runs on NB_F32 and NB_F32_COMP contexts");
     if (p->kick != NB_KICK_REFERENCE && p->kick != NB_KICK_PHYSICAL)
         return set_error(NB_ERR_INVALID, "unknown kick mode");
     if (p->memtype < NB_MEM_PAGEABLE || p->memtype > NB_MEM_UNIFIED)
@@ -105,7 +103,7 @@ static int validate(const nb_params *p)
         !std::isfinite(p->G))
         return set_error(NB_ERR_INVALID, "eps2, damping, dt and G must be finite");
     if (p->precision == NB_F64 && p->algo == NB_ALGO_FAST)
-        return set_error(NB_ERR_UNSUPPORTED, "NB_F64 runs the exact algorithm only");
+        return set_error(NB_ERR_UNSUPPORTED, "NB_F64 runs the exact or symmetric algorithm");
     if (p->precision == NB_F32_COMP && p->algo == NB_ALGO_EXACT)
         return set_error(NB_ERR_UNSUPPORTED,
                          "NB_F32_COMP runs the fast or symmetric (compensated) algorithms only");
@@ -172,6 +170,8 @@ static int dalloc(nb_ctx *c, void **p, size_t bytes)
 static bool uses_sym(const nb_ctx *c) { return c->p.precision == NB_F32 && c->p.algo == NB_ALGO_SYM; }
 // compensated context stepping with the compensated symmetric kernel
 static bool comp_sym(const nb_ctx *c) { return c->p.precision == NB_F32_COMP && c->p.algo == NB_ALGO_SYM; }
+// FP64 context stepping with the FP64 symmetric kernel
+static bool f64_sym(const nb_ctx *c) { return c->p.precision == NB_F64 && c->p.algo == NB_ALGO_SYM; }
 // the directed stream-K plan (c->plan) also serves the symmetric context's
 // energy pass and adjoint
 static bool uses_fast(const nb_ctx *c)
@@ -237,6 +237,15 @@ int nb_create(const nb_params *p, nb_ctx **out)
         }
     } else if ((st = dalloc(c, &c->pos[0], sb)) || (st = dalloc(c, &c->pos[1], sb)) ||
                (st = dalloc(c, &c->vel, sb))) {
+        free_ctx(c);
+        return st;
+    }
+    if (f64_sym(c) &&
+        ((st = nb::sym64_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan)) ||
+         (st = dev_alloc((void **)&c->sym_t, (size_t)c->splan.slots * c->splan.rb * sizeof(double4),
+                         "symmetric scratch allocation")) ||
+         (st = dev_alloc((void **)&c->sym_s, (size_t)c->splan.spart_size * sizeof(double4),
+                         "symmetric scratch allocation")))) {
         free_ctx(c);
         return st;
     }
@@ -377,7 +386,14 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[2], s));
         return st;  // positions are updated in place: no ping-pong
     }
-    if (p.precision == NB_F64) {
+    if (f64_sym(c)) {
+        st = nb::sym64_force(c->splan, (const double4 *)po, p.eps2, (double4 *)c->sym_t, (double4 *)c->sym_s, s);
+        if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
+        if (!st)
+            st = nb::sym64_integrate(c->splan, (const double4 *)po, (double4 *)pn, (double4 *)c->vel,
+                                     (const double4 *)c->sym_t, (const double4 *)c->sym_s, p.damping, p.dt,
+                                     p.kick, p.G, (double4 *)acc_out, s);
+    } else if (p.precision == NB_F64) {
         st = nb::exact_step_f64(p.n, (const double4 *)po, (double4 *)pn, (double4 *)c->vel, p.eps2,
                                 p.damping, p.dt, p.kick, p.G, (double4 *)acc_out, p.block, s);
     } else if (p.algo == NB_ALGO_EXACT) {
@@ -400,7 +416,7 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
                                     (float4 *)acc_out, s);
     }
     if (!st && ev) {
-        if (!uses_fast(c)) NB_CUDA(cudaEventRecord(ev[1], s));  // exact: one fused kernel
+        if (!uses_fast(c) && !f64_sym(c)) NB_CUDA(cudaEventRecord(ev[1], s));  // exact: one fused kernel
         NB_CUDA(cudaEventRecord(ev[2], s));
     }
     if (!st && !acc_out) c->cur ^= 1;
@@ -705,13 +721,13 @@ int nb_launches_per_step(nb_ctx *c)
 {
     if (!c) return -1;
     if (c->p.n == 0) return 0;
-    return (uses_fast(c) || is_comp(c)) ? 2 : 1;
+    return (uses_fast(c) || is_comp(c) || f64_sym(c)) ? 2 : 1;
 }
 
 int nb_plan_info(nb_ctx *c, int *info5)
 {
     if (!c || !info5) return set_error(NB_ERR_INVALID, "ctx/info is NULL");
-    if (uses_sym(c) || comp_sym(c)) {
+    if (uses_sym(c) || comp_sym(c) || f64_sym(c)) {
         info5[0] = c->splan.warps * 32;
         info5[1] = c->splan.bpt;
         info5[2] = c->splan.grid;

@@ -207,6 +207,14 @@ int sym_integrate(const SymPlan &p, const float4 *pos_old, float4 *pos_new, floa
                   const float4 *tpart, const float4 *spart, float damping, float dt, int kick,
                   float G, float4 *acc_out, cudaStream_t s);
 
+// FP64 symmetric path (nb_sym64.cu): tpart / spart hold double4 entries
+int sym64_plan(int n, int warps, int bpt, int device, SymPlan *pl);
+int sym64_force(const SymPlan &p, const double4 *pos, double eps2, double4 *tpart, double4 *spart,
+                cudaStream_t s);
+int sym64_integrate(const SymPlan &p, const double4 *pos_old, double4 *pos_new, double4 *vel,
+                    const double4 *tpart, const double4 *spart, double damping, double dt, int kick,
+                    double G, double4 *acc_out, cudaStream_t s);
+
 // Compensated kick / drift from compensated symmetric partials, or
 // (acc_out != nullptr) the bare FP64 accelerations (nb_precision.cu)
 int sym_comp_integrate(const SymPlan &p, const float4 *tpart, const float4 *spart, double4 *pos64,

@@ -31,7 +31,7 @@ void BodySystemGB300<T>::runImpl(double *runtime, int loops, int outInterval, in
     nb_params_default(&p);
     p.n = (int)m_numBodies;
     p.precision = std::is_same<T, double>::value ? NB_F64 : NB_F32;
-    p.algo = m_algo >= 0 ? m_algo : (std::is_same<T, double>::value ? NB_ALGO_EXACT : NB_ALGO_SYM);
+    p.algo = m_algo >= 0 ? m_algo : NB_ALGO_SYM;
     p.kick = m_kick;
     p.eps2 = (double)m_softeningSquared;
     p.damping = (double)m_damping;

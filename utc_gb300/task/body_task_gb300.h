@@ -12,9 +12,12 @@
  *     outbuffer + (step/outInterval - 1)*4N; runtime[] gets {total, kernel,
  *     copyin, copyout} seconds (body_task_sgpu.cu:40-137).
  * The work goes through the C ABI (include/nbody_gb300.h) on
- * UserTaskBase::__streamId.  T = float runs the symmetric fast kernel
- * (NB_ALGO_SYM) by default, T = double the reference-exact FP64 kernel.  `blocksize` is the CTA size
- * of the exact kernel; the fast kernel chooses its own launch shape.
+ * UserTaskBase::__streamId.  Both state types run the symmetric kernel
+ * (NB_ALGO_SYM) by default: in FP32 for T = float, in FP64 for T = double
+ * (FP64-accurate, not bit-identical to the sequential reference;
+ * setAlgo(NB_ALGO_EXACT) gives the reference-exact kernel).  `blocksize` is
+ * the CTA size of the exact kernel; the other kernels choose their own
+ * launch shape.
  * Errors do not stop the process: the message goes to stderr (as the
  * reference's checkCudaErr does) and lastStatus() keeps the code.
  */

@@ -8,7 +8,8 @@
  *   -b block size (exact kernel CTA size; N is rounded up to a multiple)
  * additions:
  *   -F  use float state (the reference fixes FTYPE=double at compile time)
- *   -a 0|1  force algorithm: 0 fast (float only), 1 reference-exact
+ *   -a 0|1|2  force algorithm: 0 directed fast (float only), 1 reference-exact,
+ *             2 symmetric (the default, float and double)
  *
  * Bodies come from NbodyInit (SHELL), run through Task<BodySystemGB300<T>>,
  * frames go through Task<Output<T>>; timers are printed as the reference
