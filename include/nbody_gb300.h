@@ -257,9 +257,10 @@ int nb_plan_info(nb_ctx *ctx, int *info5);
 /* Number of kernels nb_step launches per step for this context. */
 int nb_launches_per_step(nb_ctx *ctx);
 
-/* Peak FP32 FMA throughput probe: runs a kernel of independent packed-FMA
- * chains on all SMs for `iters` iterations; *flops receives the FP32
- * operations issued (2 per lane-FMA) and *ms the device time. */
+/* Peak FMA throughput probe: runs a kernel of independent FMA chains on all
+ * SMs for `iters` iterations (packed 0: scalar FP32 FFMA, 1: packed FP32
+ * FFMA2, 2: FP64 DFMA); *flops receives the operations issued (2 per
+ * lane-FMA) and *ms the device time. */
 int nb_probe_fma_peak(int iters, int packed, double *flops, float *ms, void *stream);
 
 const char *nb_last_error(void);

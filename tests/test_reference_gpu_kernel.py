@@ -165,3 +165,9 @@ def test_reference_kernel_f64_vs_exact_f64(ref_kernel, capsys):
             print(f"\n[gpu baseline f64] N={n}: reference kernel (double, sm_103a build) {r_ref:.2f} "
                   f"G interactions/s; {algo} FP64 kernel {r_ours:.2f} G interactions/s; "
                   f"ratio {r_ours / r_ref:.2f}x")
+    from utc_gb300.nbody import probe_fma_peak
+
+    peak64, _ = probe_fma_peak(2000, packed=2)
+    with capsys.disabled():
+        print(f"[gpu baseline f64] measured FP64 DFMA peak {peak64 / 1e12:.3f} TFLOP/s")
+    assert peak64 > 0

@@ -342,13 +342,31 @@ __global__ void __launch_bounds__(256) probe_fma1_kernel(float *out, int iters)
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+__global__ void __launch_bounds__(256) probe_dfma_kernel(float *out, int iters)
+{
+    const double base = 1.0 + 1e-9 * (double)threadIdx.x;
+    double a[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) a[k] = base + k;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) a[k] = fma(a[k], 0.999999999, 1e-10);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) s += a[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = (float)s;
+}
+
+// packed: 0 scalar FFMA, 1 packed FFMA2, 2 FP64 DFMA
 int probe_fma(int iters, int packed, double *flops, float *ms, cudaStream_t s)
 {
     if (iters <= 0 || !flops || !ms) return set_error(NB_ERR_INVALID, "probe_fma arguments");
     int dev = 0, sms = 0, occ = 0;
     NB_CUDA(cudaGetDevice(&dev));
     NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    auto kern = packed ? probe_fma2_kernel : probe_fma1_kernel;
+    if (packed < 0 || packed > 2) return set_error(NB_ERR_INVALID, "probe_fma: packed is 0, 1 or 2");
+    auto kern = packed == 2 ? probe_dfma_kernel : packed ? probe_fma2_kernel : probe_fma1_kernel;
     NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, 0));
     const int grid = sms * std::max(occ, 1);
     float *out = nullptr;

@@ -201,10 +201,11 @@ class NBodySystem:
 
 
 def probe_fma_peak(iters=20000, packed=True, stream=None):
-    """Measured FP32 FMA peak in FLOP/s on the current device."""
+    """Measured FMA peak in FLOP/s on the current device: FP32 (packed True or
+    False) or FP64 (packed=2)."""
     flops, ms = C.c_double(), C.c_float()
     s = current_stream_handle() if stream is None else stream
-    N.check(N.lib().nb_probe_fma_peak(int(iters), int(bool(packed)), C.byref(flops), C.byref(ms),
+    N.check(N.lib().nb_probe_fma_peak(int(iters), 2 if packed == 2 else int(bool(packed)), C.byref(flops), C.byref(ms),
                                       C.c_void_p(s)), "nb_probe_fma_peak")
     return flops.value / (ms.value * 1e-3), ms.value
 
