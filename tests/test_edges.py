@@ -117,3 +117,56 @@ def test_batch_of_single_bodies(cuda, algo):
     for _ in range(4):
         want[:, :3] = want[:, :3] + v32[:, :3] * np.float32(1e-3)
     assert np.allclose(got, want, rtol=0, atol=1e-7)
+
+
+@pytest.mark.parametrize("prec,algo", MODES)
+def test_graph_replay_equals_single_steps(cuda, prec, algo):
+    """nb_step on a non-default stream replays a captured graph of steps; the
+    result must equal stepping one launch pair at a time, from either
+    ping-pong buffer."""
+    import torch
+
+    dt_ = dtype_of(prec)
+    n = 700
+    p, v = ics.plummer(n, seed=5)
+    p, v = p.astype(dt_), v.astype(dt_)
+    side = torch.cuda.Stream()
+    with NBodySystem(n, prec, algo, kick="physical", eps2=1e-3, damping=1.0, dt=1e-3) as s:
+        s.set_state(p, v)
+        for _ in range(71):
+            s.step(1)
+        want = s.get_state()
+        s.set_state(p, v)
+        s.step(1)  # odd start: the graph begins from the second buffer
+        torch.cuda.synchronize()
+        with torch.cuda.stream(side):
+            s.step(70, stream=side.cuda_stream)
+            side.synchronize()
+        got = s.get_state()
+    assert got[0].tobytes() == want[0].tobytes() and got[1].tobytes() == want[1].tobytes()
+
+
+def test_graph_replay_speeds_up_small_systems(cuda, capsys):
+    import torch
+
+    n, steps = 1024, 320
+    p, v = ics.plummer(n, seed=6)
+    side = torch.cuda.Stream()
+    with NBodySystem(n, "f32", "sym", kick="physical", eps2=np.float32(1e-3), dt=np.float32(1e-3)) as s:
+        s.set_state(ics.f32(p), ics.f32(v))
+        times = {}
+        for name, st in (("launches", None), ("graph", side.cuda_stream)):
+            with torch.cuda.stream(side if st else torch.cuda.current_stream()):
+                cur = torch.cuda.current_stream()
+                s.step(steps, stream=cur.cuda_stream if st else 0)  # warm-up (captures the graph)
+                cur.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(cur)
+                s.step(steps, stream=cur.cuda_stream if st else 0)
+                b.record(cur)
+                b.synchronize()
+                times[name] = a.elapsed_time(b) / steps
+    with capsys.disabled():
+        print(f"\n[small N] N={n}: {times['launches'] * 1e3:.1f} us/step launched, "
+              f"{times['graph'] * 1e3:.1f} us/step from the graph")
+    assert times["graph"] < times["launches"]

@@ -21,8 +21,8 @@ def close(got, want, tol=2e-5):
 
 
 @pytest.mark.parametrize("n", [1, 2, 31, 33, 255, 256, 257, 1000, 2047, 2048, 2049, 4097, 9000])
-@pytest.mark.parametrize("shape", [(0, 0), (32, 16), (32, 20), (64, 16), (128, 20), (256, 24), (256, 8),
-                                   (256, 4), (128, 8), (256, -8), (128, -8), (256, -4)])
+@pytest.mark.parametrize("shape", [(0, 0), (32, 16), (32, 20), (32, 8), (32, 4), (64, 16), (128, 20),
+                                   (256, 24), (256, 8), (256, 4), (128, 8), (256, -8), (128, -8), (256, -4)])
 def test_sym_accel_vs_fp64(cuda, n, shape):
     p, _ = ics.plummer(n, seed=n)
     pos = ics.f32(p)
@@ -89,10 +89,13 @@ def test_sym_adjoint_matches_directed_adjoint(cuda):
         assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("n,shape", [(65536, (32, 16)), (1048576, (128, 20))])
+@pytest.mark.parametrize("n,shape", [(65536, (32, 16)), (1048576, (128, 20)), (1024, (32, 4)),
+                                     (4096, (32, 8)), (16384, (32, 16))])
 def test_sym_default_shape(cuda, n, shape):
     """One-warp CTAs x 16 targets unless the source-side array (about
-    N^2 / (2 rb) float4) would pass 8 GiB; then 4 warps x 20 targets."""
+    N^2 / (2 rb) float4) would pass 8 GiB, then 4 warps x 20 targets; small
+    systems drop to 8 or 4 targets per lane to keep four (row, chunk) items
+    per SM."""
     with NBodySystem(n, "f32", "sym") as s:
         info = s.plan_info()
     assert (info["block"], info["bpt"]) == shape

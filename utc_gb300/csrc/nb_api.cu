@@ -62,6 +62,10 @@ struct nb_ctx {
     // symmetric algorithm: plan and its two partial arrays
     nb::SymPlan splan;
     float4 *sym_t = nullptr, *sym_s = nullptr;
+    // nb_step on a capturable stream replays a CUDA graph of kGraphSteps
+    // steps (one per starting ping-pong buffer): small systems are otherwise
+    // bound by the per-kernel launch cost
+    cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
     // adjoint: checkpoints of the last nb_adj_forward and reverse-pass buffers
     struct Adj {
         int steps = 0, every = 0, nckpt = 0;
@@ -114,6 +118,8 @@ static int validate(const nb_params *p)
 
 static void free_ctx(nb_ctx *c)
 {
+    for (auto &g : c->step_graph)
+        if (g) cudaGraphExecDestroy(g);
     if (!c) return;
     cudaFree(c->pos[0]);
     cudaFree(c->pos[1]);
@@ -423,15 +429,55 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
     return st;
 }
 
+}  // extern "C"
+
+// Steps per replayed graph: even, so that the ping-pong buffers are back in
+// place after a replay and the graph can be replayed again.
+constexpr int kGraphSteps = 16;
+
+// Capture kGraphSteps steps from the current buffer into a graph.  The
+// kernels' arguments (buffers, plans, parameters) are fixed for the
+// context's lifetime, so the graph stays valid.
+static int capture_step_graph(nb_ctx *c, cudaStream_t s, cudaGraphExec_t *out)
+{
+    const int cur0 = c->cur;
+    cudaGraph_t g = nullptr;
+    NB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int st = NB_OK;
+    for (int i = 0; i < kGraphSteps && !st; ++i) st = step_once(c, s, nullptr);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    c->cur = cur0;
+    if (st) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return nb::cuda_error(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return nb::cuda_error(e, "cudaGraphInstantiate");
+    return NB_OK;
+}
+
+extern "C" {
+
 int nb_step(nb_ctx *c, int steps, void *stream)
 {
     if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
     if (steps < 0) return set_error(NB_ERR_INVALID, "steps must be >= 0");
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
-    for (int i = 0; i < steps; ++i) {
-        int st = step_once(c, (cudaStream_t)stream, nullptr);
-        if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    int st;
+    // the legacy default stream cannot be captured: launch step by step there
+    const bool graphs = s != nullptr && s != cudaStreamLegacy && c->p.n > 0;
+    if (graphs && steps >= 2 * kGraphSteps) {
+        for (; steps >= kGraphSteps; steps -= kGraphSteps) {
+            cudaGraphExec_t &g = c->step_graph[c->cur];
+            if (!g && (st = capture_step_graph(c, s, &g))) return st;
+            NB_CUDA(cudaGraphLaunch(g, s));
+        }
     }
+    for (; steps > 0; --steps)
+        if ((st = step_once(c, s, nullptr))) return st;
     return NB_OK;
 }
 

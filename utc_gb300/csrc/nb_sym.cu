@@ -415,6 +415,8 @@ static sym_kernel_t sym_kernel_for(int w, int bpt, int comp)
         return nullptr;
     }
     if (w == 1 && bpt == 16) return sym_force_kernel<1, 16, 8, false>;
+    if (w == 1 && bpt == 8) return sym_force_kernel<1, 8, 8, false>;
+    if (w == 1 && bpt == 4) return sym_force_kernel<1, 4, 8, false>;
     if (w == 1 && bpt == 20) return sym_force_kernel<1, 20, 8, false>;
     if (w == 2 && bpt == 16) return sym_force_kernel<2, 16, 4, false>;
     if (w == 4 && bpt == 20) return sym_force_kernel<4, 20, 2, false>;
@@ -446,6 +448,19 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp)
             ++s;
         warps = shapes[s][0];
         bpt = shapes[s][1];
+        // small systems: fewer targets per lane until there are at least
+        // four (row, chunk) items per resident warp slot of an SM, so the
+        // launch is not a few long items (at N=1024, 16 targets per lane give
+        // 48 items)
+        if (!comp && warps == 1) {
+            int sms = 0;
+            NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+            while (bpt > 4 && n > 0) {
+                const int rb = 32 * bpt, nrb = (n + rb - 1) / rb, nc = (n + 31) / 32;
+                if (sym_prefix(nrb, nc, bpt) >= 4ll * sms) break;
+                bpt /= 2;
+            }
+        }
     }
     if (warps == 0) warps = 8;
     if (bpt == 0) bpt = 8;

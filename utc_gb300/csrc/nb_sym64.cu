@@ -223,6 +223,14 @@ int sym64_plan(int n, int warps, int bpt, int device, SymPlan *pl)
             ++s;
         warps = shapes[s][0];
         bpt = shapes[s][1];
+        // small systems: 4 targets per lane when 8 give fewer than four
+        // (row, chunk) items per SM
+        if (warps == 1 && n > 0) {
+            int sms = 0;
+            NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+            const int rb = 32 * bpt, nrb = (n + rb - 1) / rb, nc = (n + 31) / 32;
+            if (sym_prefix(nrb, nc, bpt) < 4ll * sms) bpt = 4;
+        }
     }
     sym64_kernel_t k = sym64_kernel_for(warps, bpt);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "FP64 symmetric kernel shape not compiled");
