@@ -129,3 +129,29 @@ def test_sym_f64_steps_vs_oracle(cuda, kick):
     rel = np.linalg.norm(got[:, :3] - want[:, :3], axis=1) / (np.linalg.norm(want[:, :3], axis=1) + 0.1)
     assert rel.max() <= 1e-13
     assert got.tobytes() == again.tobytes()
+
+
+def test_gpu_scale_positions_after_100_steps_vs_fp64(cuda):
+    """The GPU-scale workload as the bench runs it (N=65536 Plummer,
+    eps2 = dt = 1e-4, 100 leapfrog steps): float positions from the symmetric
+    and directed kernels within 1e-5 (|x| + 0.1) of an FP64 run of the same
+    float-rounded start.  The FP64 run is the FP64 symmetric kernel, itself
+    held to 1e-13 of the FP64 oracle (test_sym_f64_*); the CPU oracle would
+    need minutes for this size."""
+    n, steps = 65536, 100
+    p, v = ics.plummer(n, seed=0)
+    p32, v32 = ics.f32(p), ics.f32(v)
+    with NBodySystem(n, "f64", "sym", kick="physical", eps2=float(np.float32(1e-4)), damping=1.0,
+                     dt=float(np.float32(1e-4))) as s:
+        s.set_state(p32.astype(np.float64), v32.astype(np.float64))
+        s.step(steps)
+        want, _ = s.get_state()
+    scale = np.linalg.norm(want[:, :3], axis=1) + 0.1
+    for algo in ("sym", "fast"):
+        with NBodySystem(n, "f32", algo, kick="physical", eps2=np.float32(1e-4), damping=1.0,
+                         dt=np.float32(1e-4)) as s:
+            s.set_state(p32, v32)
+            s.step(steps)
+            got, _ = s.get_state()
+        rel = np.linalg.norm(got[:, :3].astype(np.float64) - want[:, :3], axis=1) / scale
+        assert rel.max() <= 1e-5, (algo, rel.max())
