@@ -430,6 +430,7 @@ def run_precision(args):
     # unordered pair once
     modes = {"f32": ("f32", "fast"), "f32sym": ("f32", "sym"), "f32comp": ("f32comp", "fast"),
              "f32comp_sym": ("f32comp", "sym")}
+    final_pos = {}
     for mode, (prec, algo) in modes.items():
         sysm = NBodySystem(n, prec, algo, kick="physical", eps2=np.float32(eps2), damping=1.0,
                            dt=np.float32(dt))
@@ -463,6 +464,7 @@ def run_precision(args):
             if t < steps:
                 f, g = sysm.step_timed(1)
                 force_ms += f
+        final_pos[mode] = np.asarray(pos, np.float64)[:, :3]
         rate = float(n) ** 2 * steps / (force_ms * 1e-3) / 1e9
         out["modes"][mode] = {
             "force_kernel_G_interactions_per_s": rate,
@@ -473,6 +475,13 @@ def run_precision(args):
             "per_step": per_step,
         }
         sysm.close()
+    # final positions against the compensated symmetric run (FP64 positions,
+    # forces within 1.7e-6 of FP64): |dx| / (|x| + 0.1), max over bodies
+    ref = final_pos["f32comp_sym"]
+    scale = np.linalg.norm(ref, axis=1) + 0.1
+    for mode in modes:
+        out["modes"][mode]["pos_rel_max_vs_compensated_symmetric"] = float(
+            (np.linalg.norm(final_pos[mode] - ref, axis=1) / scale).max())
     peak, _ = probe_fma_peak(20000, True)
     out["forward_N1M"] = {}
     for mode in modes:
