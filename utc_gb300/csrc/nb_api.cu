@@ -251,7 +251,7 @@ int nb_create(const nb_params *p, nb_ctx **out)
          (st = dev_alloc((void **)&c->sym_t, (size_t)c->splan.slots * c->splan.rb * sizeof(double4),
                          "symmetric scratch allocation")) ||
          (st = dev_alloc((void **)&c->sym_s, (size_t)c->splan.spart_size * sizeof(double4),
-                         "symmetric source-side array (about N^2/(2 rb) entries; NB_ALGO_FAST needs O(N) scratch)")))) {
+                         "symmetric source-side array (about N^2/(2 rb) entries; NB_ALGO_EXACT needs none)")))) {
         free_ctx(c);
         return st;
     }
