@@ -1,7 +1,7 @@
 """Fixed small runs of the kernels for profilers.
 
     python -m utc_gb300.profile_case --n 65536 --steps 4 [--algo fast|sym|exact]
-        [--precision f32|f32comp] [--case step|adjoint|batch]
+        [--precision f32|f32comp|f64] [--case step|adjoint|batch]
         [--block B --bpt K] [--kick physical|reference] [--systems S]
 
 case step:    `steps` steps of a seeded Plummer sphere (eps2=1e-4, dt=1e-4)
@@ -23,7 +23,7 @@ def main():
     ap.add_argument("--n", type=int, default=65536)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--algo", default="fast")
-    ap.add_argument("--precision", default="f32", choices=["f32", "f32comp"])
+    ap.add_argument("--precision", default="f32", choices=["f32", "f32comp", "f64"])
     ap.add_argument("--case", default="step", choices=["step", "adjoint", "batch"])
     ap.add_argument("--kick", default="physical")
     ap.add_argument("--block", type=int, default=0)
@@ -61,10 +61,10 @@ def main():
             print("ok", "adjoint", a.n, a.steps, s.plan_info())
         return
     p, v = ics.plummer(a.n, seed=0)
-    eps2 = 1e-4 if a.precision == "f32comp" else np.float32(1e-4)
+    eps2 = 1e-4 if a.precision in ("f32comp", "f64") else np.float32(1e-4)
     with NBodySystem(a.n, a.precision, a.algo, kick=a.kick, eps2=eps2, damping=1.0,
                      dt=np.float32(1e-4), block=a.block, bpt=a.bpt) as s:
-        if a.precision == "f32comp":
+        if a.precision in ("f32comp", "f64"):
             s.set_state(p, v)
         else:
             s.set_state(ics.f32(p), ics.f32(v))
