@@ -122,8 +122,17 @@ int nb_set_state(nb_ctx *ctx, const void *pos, const void *vel, int where, void 
 int nb_get_state(nb_ctx *ctx, void *pos, void *vel, int where, void *stream);
 
 /* Advance `steps` steps on `stream` (asynchronous).  Replaces the launch
- * loop of BodySystemSGPU::runImpl, body_task_sgpu.cu:85-127. */
+ * loop of BodySystemSGPU::runImpl, body_task_sgpu.cu:85-127.  On a stream
+ * other than the legacy default stream, bulk steps replay a captured CUDA
+ * graph. */
 int nb_step(nb_ctx *ctx, int steps, void *stream);
+
+/* Change eps2 (the softening squared), damping, dt and G of a context (or of
+ * a batch).  Replaces BodySystem<T>::setSoftening (which stores the square),
+ * setDamping and the per-call deltaTime of update(deltaTime)
+ * (benchapps/nbody/seq/bodysystem.h:19-29).  Takes effect for the next step;
+ * drops captured step graphs and a recorded adjoint forward pass. */
+int nb_set_params(nb_ctx *ctx, double eps2, double damping, double dt, double G);
 
 /* nb_step with a CUDA event pair around every kernel it launches, on the
  * same stream.  Adds the summed device milliseconds of the force kernel and
@@ -225,6 +234,7 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks);
 /* Adjoint of `steps` batched steps, same contract as nb_adj_forward /
  * nb_adj_backward over the concatenated bodies of all systems (no
  * counterpart in the reference). */
+int nb_batch_set_params(nb_batch *b, double eps2, double damping, double dt, double G);
 int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream);
 int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void *gx0, void *gv0,
                           void *gm, void *stream);

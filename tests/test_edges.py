@@ -170,3 +170,69 @@ def test_graph_replay_speeds_up_small_systems(cuda, capsys):
         print(f"\n[small N] N={n}: {times['launches'] * 1e3:.1f} us/step launched, "
               f"{times['graph'] * 1e3:.1f} us/step from the graph")
     assert times["graph"] < times["launches"]
+
+
+@pytest.mark.parametrize("prec,algo", MODES)
+def test_set_params_equals_a_fresh_context(cuda, prec, algo):
+    """nb_set_params (setSoftening / setDamping / update(dt)) mid-run: the
+    steps after it equal those of a context created with the new values,
+    also through a graph captured before the change."""
+    import torch
+
+    dt_ = dtype_of(prec)
+    n = 500
+    p, v = ics.plummer(n, seed=8)
+    p, v = p.astype(dt_), v.astype(dt_)
+    side = torch.cuda.Stream()
+    kw = dict(kick="physical", eps2=1e-3, damping=1.0, dt=1e-3)
+    with NBodySystem(n, prec, algo, **kw) as s:
+        s.set_state(p, v)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(side):
+            s.step(40, stream=side.cuda_stream)  # captures a graph with the old values
+            side.synchronize()
+        mid = s.get_state()
+        s.set_params(2e-3, 0.99, 5e-4)
+        with torch.cuda.stream(side):
+            s.step(40, stream=side.cuda_stream)
+            side.synchronize()
+        got = s.get_state()
+    with NBodySystem(n, prec, algo, kick="physical", eps2=2e-3, damping=0.99, dt=5e-4) as f:
+        f.set_state(*mid)
+        for _ in range(40):
+            f.step(1)
+        want = f.get_state()
+    assert got[0].tobytes() == want[0].tobytes() and got[1].tobytes() == want[1].tobytes()
+
+
+def test_set_params_rejects_non_finite(cuda):
+    with NBodySystem(16, "f32", "sym") as s:
+        assert s.lib.nb_set_params(s.handle, float("nan"), 1.0, 1e-3, 1.0) == N.NB_ERR_INVALID
+        assert s.lib.nb_set_params(None, 1e-3, 1.0, 1e-3, 1.0) == N.NB_ERR_INVALID
+
+
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_batch_set_params(cuda, algo):
+    import torch
+
+    sizes = [5, 300, 64]
+    p, v = ics.uniform_cube(369, seed=3)
+    p32, v32 = ics.f32(p), ics.f32(v)
+    side = torch.cuda.Stream()
+    with NBodyBatch(sizes, eps2=np.float32(1e-3), dt=np.float32(1e-3), algo=algo) as b:
+        b.set_state(p32, v32)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(side):
+            b.run(6, side.cuda_stream)
+            side.synchronize()
+        mid = b.get_state()
+        b.set_params(np.float32(2e-3), 1.0, np.float32(5e-4))
+        with torch.cuda.stream(side):
+            b.run(6, side.cuda_stream)  # the old graph was dropped
+            side.synchronize()
+        got = b.get_state()
+    with NBodyBatch(sizes, eps2=np.float32(2e-3), dt=np.float32(5e-4), algo=algo) as f:
+        f.set_state(*mid)
+        f.step(6)
+        want = f.get_state()
+    assert got[0].tobytes() == want[0].tobytes()

@@ -52,6 +52,7 @@ def _declare(lib):
         "nb_set_state": (I, [vp, vp, vp, I, vp]),
         "nb_get_state": (I, [vp, vp, vp, I, vp]),
         "nb_step": (I, [vp, I, vp]),
+        "nb_set_params": (I, [vp, D, D, D, D]),
         "nb_accel": (I, [vp, vp, vp]),
         "nb_step_timed": (I, [vp, I, P(C.c_float), P(C.c_float), vp]),
         "nb_energy": (I, [vp, P(D), vp, vp]),
@@ -68,6 +69,7 @@ def _declare(lib):
         "nb_batch_set_state": (I, [vp, vp, vp, I, vp]),
         "nb_batch_get_state": (I, [vp, vp, vp, I, vp]),
         "nb_batch_step": (I, [vp, I, vp]),
+        "nb_batch_set_params": (I, [vp, D, D, D, D]),
         "nb_batch_run": (I, [vp, I, vp]),
         "nb_batch_autotune": (I, [vp, I, C.c_char_p, vp, P(I)]),
         "nb_batch_set_shape": (I, [vp, I, I]),

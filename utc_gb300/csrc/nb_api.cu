@@ -481,6 +481,26 @@ int nb_step(nb_ctx *c, int steps, void *stream)
     return NB_OK;
 }
 
+int nb_set_params(nb_ctx *c, double eps2, double damping, double dt, double G)
+{
+    if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
+    if (!std::isfinite(eps2) || !std::isfinite(damping) || !std::isfinite(dt) || !std::isfinite(G))
+        return set_error(NB_ERR_INVALID, "eps2, damping, dt and G must be finite");
+    // captured graphs hold the old values as kernel arguments
+    for (auto &g : c->step_graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    c->p.eps2 = eps2;
+    c->p.damping = damping;
+    c->p.dt = dt;
+    c->p.G = G;
+    c->adj.ready = false;  // a recorded forward pass used the old values
+    c->adj.live_last = false;
+    return NB_OK;
+}
+
 int nb_step_timed(nb_ctx *c, int steps, float *ms_force, float *ms_integrate, void *stream)
 {
     if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");

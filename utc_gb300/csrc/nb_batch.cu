@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <array>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -1164,6 +1165,25 @@ int nb_batch_run(nb_batch *b, int steps, void *stream)
     }
     NB_CUDA(cudaGraphLaunch(b->graph, s));
     if (steps % 2) b->cur ^= 1;
+    return NB_OK;
+}
+
+int nb_batch_set_params(nb_batch *b, double eps2, double damping, double dt, double G)
+{
+    if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
+    if (!std::isfinite(eps2) || !std::isfinite(damping) || !std::isfinite(dt) || !std::isfinite(G))
+        return set_error(NB_ERR_INVALID, "eps2, damping, dt and G must be finite");
+    if (b->graph) {  // it holds the old values as kernel arguments
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        b->graph_cur = -1;
+    }
+    b->p.eps2 = eps2;
+    b->p.damping = damping;
+    b->p.dt = dt;
+    b->p.G = G;
+    b->adj_ready = false;
+    b->adj_live_last = false;
     return NB_OK;
 }
 

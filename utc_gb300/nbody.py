@@ -111,6 +111,12 @@ class NBodySystem:
         s = current_stream_handle() if stream is None else stream
         N.check(self.lib.nb_step(self.handle, int(steps), C.c_void_p(s)), "nb_step")
 
+    def set_params(self, eps2, damping, dt, G=1.0):
+        """New eps2 (softening squared), damping, dt and G for the next steps
+        (BodySystem<T>::setSoftening / setDamping / update(dt))."""
+        N.check(self.lib.nb_set_params(self.handle, float(eps2), float(damping), float(dt), float(G)),
+                "nb_set_params")
+
     def step_timed(self, steps=1, stream=None):
         """Step with per-kernel CUDA events; returns (force_ms, integrate_ms) summed."""
         f, g = C.c_float(0.0), C.c_float(0.0)
@@ -276,6 +282,10 @@ class NBodyBatch:
     def step(self, steps=1, stream=None):
         s = current_stream_handle() if stream is None else stream
         N.check(self.lib.nb_batch_step(self.handle, int(steps), C.c_void_p(s)), "nb_batch_step")
+
+    def set_params(self, eps2, damping, dt, G=1.0):
+        N.check(self.lib.nb_batch_set_params(self.handle, float(eps2), float(damping), float(dt), float(G)),
+                "nb_batch_set_params")
 
     def run(self, steps, stream):
         """`steps` steps as one CUDA graph on a non-default stream handle."""
