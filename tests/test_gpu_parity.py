@@ -316,3 +316,33 @@ def test_empty_system(cuda):
         p, v = s.get_state()
         assert p.shape == (0, 4)
         assert s.launches_per_step() == 0
+
+
+def test_app_driver_reproduces_golden_file(cuda, tmp_path):
+    """The app driver (the reference's flags; bodies from NbodyInit's SHELL
+    initialiser on rand(); Task<BodySystemGB300<float>> with the exact
+    algorithm; frames through Task<Output<float>>) writes the reference's
+    golden output file byte for byte."""
+    import hashlib
+    import subprocess
+
+    kat = json.load(open(os.path.join(GOLD, "kat_shell_n1024.json")))
+    app = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "utc_gb300", "nbody_main")
+    out = tmp_path / "outpos.txt"
+    r = subprocess.run([app, "-F", "-a", "1", "-n", "1024", "-i", "0", "-l", "100", "-o", "100",
+                        "-O", str(out)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    data = out.read_bytes()
+    assert len(data) == kat["seq_outpos_bytes"]
+    assert hashlib.sha256(data).hexdigest() == kat["seq_outpos_sha256"]
+    # the default (symmetric) run of the same scenario stays within the
+    # envelope of the reference's own GPU run
+    out2 = tmp_path / "outpos_sym.txt"
+    r = subprocess.run([app, "-F", "-n", "1024", "-i", "0", "-l", "100", "-o", "100", "-O", str(out2)],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    a = np.array(data.decode().split(), dtype=np.float64)
+    b = np.array(out2.read_text().split(), dtype=np.float64)
+    assert a.shape == b.shape
+    d = np.abs(a - b)
+    assert d.max() <= 10 * kat["gpu_vs_seq_final_frame"]["max_abs"]

@@ -85,7 +85,10 @@ def build(force: bool = False, verbose: bool = False) -> None:
     task_srcs = [os.path.join(TASK, "body_task_gb300.cc")]
     task_hdrs = glob.glob(os.path.join(TASK, "*.h")) + [os.path.join(INCLUDE, "nbody_gb300.h")]
     cxx = os.environ.get("CXX", "g++")
-    common = ["-std=c++17", "-O2", "-fPIC", "-I", INCLUDE, "-I", TASK,
+    # -ffp-contract=off: NbodyInit restates the reference's float arithmetic,
+    # which its x86-64 build evaluates without FMA; aarch64 g++ would contract
+    # a*b+c and change the initial bodies' bits
+    common = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-I", INCLUDE, "-I", TASK,
               "-I", os.path.join(home, "include")]
     libs = ["-L", PKG, "-lnbody_gb300", "-Wl,-rpath,$ORIGIN",
             "-L", os.path.join(home, "lib64"), "-lcudart_static", "-ldl", "-lrt", "-lpthread"]
