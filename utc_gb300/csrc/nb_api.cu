@@ -436,8 +436,8 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
 constexpr int kGraphSteps = 16;
 
 // Capture kGraphSteps steps from the current buffer into a graph.  The
-// kernels' arguments (buffers, plans, parameters) are fixed for the
-// context's lifetime, so the graph stays valid.
+// kernels' arguments (buffers, plans, parameters) stay fixed until
+// nb_set_params, which destroys the captured graphs.
 static int capture_step_graph(nb_ctx *c, cudaStream_t s, cudaGraphExec_t *out)
 {
     const int cur0 = c->cur;
