@@ -147,10 +147,12 @@ int nb_accel(nb_ctx *ctx, void *acc_dev, void *stream);
 /* Total energy and momentum of the current state, reduced in FP64 on the
  * GPU: out5 = {kinetic sum 0.5 m |v|^2, potential -0.5 G sum_i sum_{j!=i}
  * m_i m_j / sqrt(r^2 + eps2), momentum x, y, z}.  The pair terms are FP32
- * (compensated in NB_F32_COMP).  accphi_dev (may be NULL) receives per body
- * the bare acceleration and, in w, the potential sum over j != i, as n
- * float4 (NB_F32) or double4 (NB_F32_COMP).  Needs eps2 > 0.  Synchronises
- * `stream`.  No counterpart in the reference (used by the precision study). */
+ * (compensated in NB_F32_COMP) or FP64 (NB_F64, any algorithm).  accphi_dev
+ * (may be NULL) receives per body the bare acceleration and, in w, the
+ * potential sum over j != i, as n float4 (NB_F32) or double4 (NB_F32_COMP,
+ * NB_F64).  NB_F32 needs the fast or symmetric algorithm.  Needs eps2 > 0.
+ * Synchronises `stream`.  No counterpart in the reference (used by the
+ * precision study). */
 int nb_energy(nb_ctx *ctx, double *out5, void *accphi_dev, void *stream);
 
 /* Adjoint (reverse mode) of `steps` steps; no counterpart in the reference.

@@ -84,28 +84,31 @@ def test_compensated_steps_vs_fp64_oracle(cuda, algo):
     assert dv.max() <= 1e-6, dv.max()
 
 
-@pytest.mark.parametrize("precision", ["f32", "f32comp"])
-def test_energy_momentum_vs_fp64(cuda, precision):
+@pytest.mark.parametrize("precision,algo", [("f32", "fast"), ("f32", "sym"), ("f32comp", "fast"),
+                                            ("f32comp", "sym"), ("f64", "sym"), ("f64", "exact")])
+def test_energy_momentum_vs_fp64(cuda, precision, algo):
     n = 4096
     p, v = ics.plummer(n, seed=4)
     if precision == "f32":
         p, v = p.astype(np.float32), v.astype(np.float32)
     eps2 = np.float32(1e-3)
-    with NBodySystem(n, precision, "fast", kick="physical", eps2=eps2) as s:
+    with NBodySystem(n, precision, algo, kick="physical", eps2=eps2) as s:
         s.set_state(p, v)
         e, bodies = s.energy(with_bodies=True)
     p64 = np.asarray(p, np.float64)
     if precision == "f32comp":
         p64 = p64.astype(np.float32).astype(np.float64)  # pair terms read float positions
     ref = oracle.energy(p64, np.asarray(v, np.float64), float(eps2))
-    tol = 1e-6 if precision == "f32comp" else 2e-5
+    tol = {"f32comp": 1e-6, "f32": 2e-5, "f64": 1e-12}[precision]
     assert abs(e[0] - ref[0]) <= 1e-12 * abs(ref[0]) + 1e-300
     assert abs(e[1] - ref[1]) <= tol * abs(ref[1])
     pmag = np.abs(p64[:, 3] * np.linalg.norm(v[:, :3], axis=1)).sum()
     assert np.abs(e[2:] - ref[2:]).max() <= 1e-12 * pmag
     tidx = np.arange(0, n, 16, dtype=np.int32)
-    _, phi = oracle.accel_phi_subset_f64(p64, tidx, float(eps2))
+    acc, phi = oracle.accel_phi_subset_f64(p64, tidx, float(eps2))
     assert np.abs(bodies[tidx, 3] - phi).max() <= tol * np.abs(phi).max()
+    if precision == "f64":
+        assert np.abs(bodies[tidx, :3] - acc).max() <= 1e-12 * np.abs(acc).max()
 
 
 @pytest.mark.parametrize("algo", ["fast", "sym"])

@@ -246,6 +246,14 @@ int nb_create(const nb_params *p, nb_ctx **out)
         free_ctx(c);
         return st;
     }
+    if (p->precision == NB_F64 &&
+        ((st = dev_alloc(&c->acc_tmp, n * sizeof(double4), "energy scratch allocation")) ||
+         (st = dev_alloc((void **)&c->e_blocks, (size_t)(nb::energy_blocks(p->n) + 1) * 5 * sizeof(double),
+                         "energy scratch allocation")) ||
+         (st = dev_alloc((void **)&c->e_out, 8 * sizeof(double), "energy scratch allocation")))) {
+        free_ctx(c);
+        return st;
+    }
     if (f64_sym(c) &&
         ((st = nb::sym64_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan)) ||
          (st = dev_alloc((void **)&c->sym_t, (size_t)c->splan.slots * c->splan.rb * sizeof(double4),
@@ -545,13 +553,21 @@ int nb_energy(nb_ctx *c, double *out5, void *accphi_dev, void *stream)
 {
     if (!c || !out5) return set_error(NB_ERR_INVALID, "ctx/out is NULL");
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
-    if (!(uses_fast(c) || is_comp(c)))
-        return set_error(NB_ERR_UNSUPPORTED, "nb_energy needs an NB_F32 fast or NB_F32_COMP context");
+    if (!(uses_fast(c) || is_comp(c) || c->p.precision == NB_F64))
+        return set_error(NB_ERR_UNSUPPORTED,
+                         "nb_energy needs an NB_F32 fast or symmetric, NB_F32_COMP or NB_F64 context");
     if (!(c->p.eps2 > 0.0)) return set_error(NB_ERR_INVALID, "nb_energy needs eps2 > 0");
     cudaStream_t s = (cudaStream_t)stream;
     const nb_params &p = c->p;
     int st;
-    if (is_comp(c)) {
+    if (p.precision == NB_F64) {
+        const double4 *pos = (const double4 *)c->pos[c->cur];
+        st = nb::energy_phi_f64(p.n, pos, p.eps2, (double4 *)c->acc_tmp, s);
+        if (!st)
+            st = nb::energy_reduce(p.n, nullptr, pos, nullptr, nullptr, nullptr,
+                                   (const double4 *)c->acc_tmp, p.G, c->e_blocks, c->e_out, s,
+                                   (const double4 *)c->vel);
+    } else if (is_comp(c)) {
         st = nb::fast_force(c->eplan, c->pos32, (float)p.eps2, c->partial, s, nb::SK_COMP | nb::SK_PHI);
         if (!st)
             st = nb::fast_reduce(c->eplan, c->partial, 1, c->pos32, (float)p.eps2, nullptr,
@@ -574,7 +590,7 @@ int nb_energy(nb_ctx *c, double *out5, void *accphi_dev, void *stream)
     if (st) return st;
     if (accphi_dev && p.n)
         NB_CUDA(cudaMemcpyAsync(accphi_dev, c->acc_tmp,
-                                (size_t)p.n * (is_comp(c) ? sizeof(double4) : sizeof(float4)),
+                                (size_t)p.n * (c->elem == 8 ? sizeof(double4) : sizeof(float4)),
                                 cudaMemcpyDeviceToDevice, s));
     NB_CUDA(cudaMemcpyAsync(out5, c->e_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
     NB_CUDA(cudaStreamSynchronize(s));

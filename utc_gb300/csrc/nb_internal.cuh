@@ -74,6 +74,20 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
     const float bb = __fsub_rn(s, a);
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
+// 1/sqrt(x) in FP64: the FP64 approximate reciprocal square root refined by
+// two Newton-Raphson steps, y <- y + (y/2)(1 - x y^2), each squaring the
+// relative error.  x must be a normal positive FP64 number.
+__device__ __forceinline__ double rsqrt64(double x)
+{
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const double r = fma(-x, y * y, 1.0);  // 1 - x y^2
+        y = fma(0.5 * y, r, y);
+    }
+    return y;
+}
 __device__ __forceinline__ float rsqrt_approx(float x)
 {
     float r;
@@ -148,9 +162,16 @@ int comp_integrate(const SkPlan &p, const float4 *partial, double4 *pos64, float
                    float4 *vhi, float4 *vlo, float damping, float dt, double dt64, int kick,
                    float G, cudaStream_t s);
 int energy_blocks(int n);
+// FP64 accelerations and potentials over j != i of an NB_F64 state, into
+// out (ax, ay, az, phi) (nb_precision.cu)
+int energy_phi_f64(int n, const double4 *pos, double eps2, double4 *out, cudaStream_t s);
+// Energy and momentum in FP64 from the state (masses from pos64 if given,
+// else pos32; velocities from vel64 if given, else vel32 + vlo) and the
+// per-body potentials (phi64 if given, else phi32).
 int energy_reduce(int n, const float4 *pos32, const double4 *pos64, const float4 *vel32,
                   const float4 *vlo, const float4 *phi32, const double4 *phi64, double G,
-                  double *block_tmp, double *out_dev, cudaStream_t s);
+                  double *block_tmp, double *out_dev, cudaStream_t s,
+                  const double4 *vel64 = nullptr);
 
 // Symmetric force kernel (nb_sym.cu)
 // Work layout of the symmetric kernels (nb_sym.cu, nb_adjoint.cu): row

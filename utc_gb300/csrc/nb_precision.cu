@@ -208,15 +208,24 @@ __global__ void energy_partial_kernel(int n, const float4 *__restrict__ pos32,
                                       const float4 *__restrict__ vlo,
                                       const float4 *__restrict__ phi32,
                                       const double4 *__restrict__ phi64, double G,
-                                      double *__restrict__ block_out)
+                                      double *__restrict__ block_out,
+                                      const double4 *__restrict__ vel64)
 {
     __shared__ double red[5][kEnergyBlock];
     const int i = blockIdx.x * kEnergyBlock + threadIdx.x;
     double ke = 0, pe = 0, px = 0, py = 0, pz = 0;
     if (i < n) {
-        const float m32 = pos32[i].w;
-        const double m = pos64 ? pos64[i].w : (double)m32;
-        double vx = vel32[i].x, vy = vel32[i].y, vz = vel32[i].z;
+        const double m = pos64 ? pos64[i].w : (double)pos32[i].w;
+        double vx, vy, vz;
+        if (vel64) {
+            vx = vel64[i].x;
+            vy = vel64[i].y;
+            vz = vel64[i].z;
+        } else {
+            vx = vel32[i].x;
+            vy = vel32[i].y;
+            vz = vel32[i].z;
+        }
         if (vlo) {
             vx += (double)vlo[i].x;
             vy += (double)vlo[i].y;
@@ -310,14 +319,58 @@ int sym_comp_integrate(const SymPlan &p, const float4 *tpart, const float4 *spar
 
 int energy_blocks(int n) { return (n + kEnergyBlock - 1) / kEnergyBlock; }
 
+// FP64 forces and potentials of an NB_F64 state for the energy pass: one
+// thread per target, sources in index order through shared memory, j == i
+// left out.  Not a throughput path: it runs only when the energy is asked for.
+constexpr int kPhi64Block = 256;
+
+__global__ void __launch_bounds__(kPhi64Block) phi64_kernel(const double4 *__restrict__ pos, int n,
+                                                            double eps2, double4 *__restrict__ out)
+{
+    __shared__ double4 sp[kPhi64Block];
+    const int i = blockIdx.x * kPhi64Block + threadIdx.x;
+    const double4 pi = i < n ? pos[i] : make_double4(0.0, 0.0, 0.0, 0.0);
+    double ax = 0.0, ay = 0.0, az = 0.0, phi = 0.0;
+    for (int jt = 0; jt < n; jt += kPhi64Block) {
+        __syncthreads();
+        if (jt + (int)threadIdx.x < n) sp[threadIdx.x] = pos[jt + threadIdx.x];
+        __syncthreads();
+        const int cnt = min(kPhi64Block, n - jt);
+        for (int j = 0; j < cnt; ++j) {
+            if (jt + j == i) continue;
+            const double4 q = sp[j];
+            const double rx = q.x - pi.x, ry = q.y - pi.y, rz = q.z - pi.z;
+            double d2 = fma(rx, rx, eps2);
+            d2 = fma(ry, ry, d2);
+            d2 = fma(rz, rz, d2);
+            const double inv = rsqrt64(d2);
+            const double mi = q.w * inv;
+            const double sc = mi * (inv * inv);
+            ax = fma(rx, sc, ax);
+            ay = fma(ry, sc, ay);
+            az = fma(rz, sc, az);
+            phi += mi;
+        }
+    }
+    if (i < n) out[i] = make_double4(ax, ay, az, phi);
+}
+
+int energy_phi_f64(int n, const double4 *pos, double eps2, double4 *out, cudaStream_t s)
+{
+    if (n == 0) return NB_OK;
+    phi64_kernel<<<(n + kPhi64Block - 1) / kPhi64Block, kPhi64Block, 0, s>>>(pos, n, eps2, out);
+    NB_LAUNCH_CHECK("phi64_kernel launch");
+    return NB_OK;
+}
+
 int energy_reduce(int n, const float4 *pos32, const double4 *pos64, const float4 *vel32,
                   const float4 *vlo, const float4 *phi32, const double4 *phi64, double G,
-                  double *block_tmp, double *out_dev, cudaStream_t s)
+                  double *block_tmp, double *out_dev, cudaStream_t s, const double4 *vel64)
 {
     const int nb = energy_blocks(n);
     if (nb > 0) {
         energy_partial_kernel<<<nb, kEnergyBlock, 0, s>>>(n, pos32, pos64, vel32, vlo, phi32, phi64,
-                                                          G, block_tmp);
+                                                          G, block_tmp, vel64);
         NB_LAUNCH_CHECK("energy_partial_kernel launch");
     }
     energy_final_kernel<<<1, 32, 0, s>>>(block_tmp, nb, out_dev);

@@ -21,18 +21,6 @@
 
 namespace nb {
 
-__device__ __forceinline__ double rsqrt64(double x)
-{
-    double y;
-    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-#pragma unroll
-    for (int it = 0; it < 2; ++it) {
-        const double r = fma(-x, y * y, 1.0);  // 1 - x y^2
-        y = fma(0.5 * y, r, y);
-    }
-    return y;
-}
-
 template <int W, int BPT, int MINB>
 __global__ void __launch_bounds__(32 * W, MINB) sym64_force_kernel(const double4 *__restrict__ pos, int n,
                                                                    double eps2, double4 *__restrict__ tpart,

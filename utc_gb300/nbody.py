@@ -143,7 +143,7 @@ class NBodySystem:
         s = current_stream_handle() if stream is None else stream
         buf = None
         if with_bodies:
-            tdt = torch.float64 if self.precision == "f32comp" else torch.float32
+            tdt = torch.float64 if self.precision in ("f32comp", "f64") else torch.float32
             buf = torch.zeros((max(self.n, 1), 4), dtype=tdt, device="cuda")
         N.check(self.lib.nb_energy(self.handle, out, C.c_void_p(buf.data_ptr() if buf is not None else 0),
                                    C.c_void_p(s)), "nb_energy")
