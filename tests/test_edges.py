@@ -236,3 +236,29 @@ def test_batch_set_params(cuda, algo):
         f.step(6)
         want = f.get_state()
     assert got[0].tobytes() == want[0].tobytes()
+
+
+def test_step_inside_a_callers_graph_capture(cuda):
+    """A caller capturing its own stream into a CUDA graph can put nb_step in
+    it: nb_step then launches step by step into that capture instead of
+    capturing a graph of its own."""
+    import torch
+
+    n = 300
+    p, v = ics.plummer(n, seed=9)
+    p32, v32 = ics.f32(p), ics.f32(v)
+    side = torch.cuda.Stream()
+    with NBodySystem(n, "f32", "sym", kick="physical", eps2=np.float32(1e-3), dt=np.float32(1e-3)) as s:
+        s.set_state(p32, v32)
+        for _ in range(40):
+            s.step(1)
+        want = s.get_state()
+        s.set_state(p32, v32)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            s.step(40, stream=torch.cuda.current_stream().cuda_stream)
+        g.replay()
+        torch.cuda.synchronize()
+        got = s.get_state()
+    assert got[0].tobytes() == want[0].tobytes() and got[1].tobytes() == want[1].tobytes()

@@ -475,8 +475,15 @@ int nb_step(nb_ctx *c, int steps, void *stream)
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
     cudaStream_t s = (cudaStream_t)stream;
     int st;
-    // the legacy default stream cannot be captured: launch step by step there
-    const bool graphs = s != nullptr && s != cudaStreamLegacy && c->p.n > 0;
+    // the legacy default stream cannot be captured: launch step by step there,
+    // and also on a stream the caller is capturing into a graph of its own
+    // (the launches then go into the caller's graph)
+    bool graphs = s != nullptr && s != cudaStreamLegacy && c->p.n > 0;
+    if (graphs) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        NB_CUDA(cudaStreamIsCapturing(s, &cs));
+        graphs = cs == cudaStreamCaptureStatusNone;
+    }
     if (graphs && steps >= 2 * kGraphSteps) {
         for (; steps >= kGraphSteps; steps -= kGraphSteps) {
             cudaGraphExec_t &g = c->step_graph[c->cur];
