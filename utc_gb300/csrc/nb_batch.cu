@@ -1140,6 +1140,19 @@ int nb_batch_run(nb_batch *b, int steps, void *stream)
     if (steps == 0 || b->nbody == 0) return NB_OK;
     cudaStream_t s = (cudaStream_t)stream;
     if (s == nullptr) return set_error(NB_ERR_INVALID, "nb_batch_run needs a non-default stream");
+    {
+        // inside the caller's own capture of this stream: launch the steps
+        // into that capture instead of nesting one
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        NB_CUDA(cudaStreamIsCapturing(s, &cs));
+        if (cs != cudaStreamCaptureStatusNone) {
+            for (int i = 0; i < steps; ++i) {
+                int st = batch_step_once(b, s);
+                if (st) return st;
+            }
+            return NB_OK;
+        }
+    }
     if (!b->graph || b->graph_steps != steps || b->graph_cur != b->cur) {
         if (b->graph) {
             cudaGraphExecDestroy(b->graph);
