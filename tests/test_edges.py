@@ -262,3 +262,26 @@ def test_step_inside_a_callers_graph_capture(cuda):
         torch.cuda.synchronize()
         got = s.get_state()
     assert got[0].tobytes() == want[0].tobytes() and got[1].tobytes() == want[1].tobytes()
+
+
+@pytest.mark.parametrize("algo", ["fast", "sym"])
+def test_batch_run_inside_a_callers_graph_capture(cuda, algo):
+    import torch
+
+    sizes = [3, 250, 64]
+    p, v = ics.uniform_cube(317, seed=11)
+    p32, v32 = ics.f32(p), ics.f32(v)
+    side = torch.cuda.Stream()
+    with NBodyBatch(sizes, eps2=np.float32(1e-3), dt=np.float32(1e-3), algo=algo) as b:
+        b.set_state(p32, v32)
+        b.step(6)
+        want = b.get_state()
+        b.set_state(p32, v32)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            b.run(6, torch.cuda.current_stream().cuda_stream)
+        g.replay()
+        torch.cuda.synchronize()
+        got = b.get_state()
+    assert got[0].tobytes() == want[0].tobytes()

@@ -335,39 +335,53 @@ __global__ void adj_update_kernel(const float4 *__restrict__ partial, int n, int
     adj_body_update(i, ox, oy, oz, odm, pos, acc, lx, lv, gm, gbuf, damping, dt, kick, G, want_next_g);
 }
 
-// Symmetric layout: target-side slots (CTA order), then the source-side
-// entries of rows 0..I-1 (row order), then update.
-__global__ void adj_update_sym_kernel(const float4 *__restrict__ tpart, const float4 *__restrict__ spart,
-                                      int n, int rb, int nc, int nrb, long long total, int grid,
-                                      const float4 *__restrict__ pos, const float4 *__restrict__ acc,
-                                      float4 *__restrict__ lx, float4 *__restrict__ lv,
-                                      float *__restrict__ gm, float4 *__restrict__ gbuf, float damping,
-                                      float dt, int kick, float G, int want_next_g)
+// Symmetric layout: target-side slots and the source-side entries of rows
+// 0..I-1, then the per-body update.  Four threads share a body (thread q of
+// the quad sums slots c0+q, c0+q+4, ... and rows q, q+4, ..., the quad
+// combines its sums as (s0 + s1) + (s2 + s3), a fixed order): the row walk of
+// the last row blocks is what bounds this kernel.
+constexpr int kAdjUpdBlock = 256;
+
+__global__ void __launch_bounds__(kAdjUpdBlock) adj_update_sym_kernel(
+    const float4 *__restrict__ tpart, const float4 *__restrict__ spart, int n, int rb, int nc, int nrb,
+    long long total, int grid, const float4 *__restrict__ pos, const float4 *__restrict__ acc,
+    float4 *__restrict__ lx, float4 *__restrict__ lv, float *__restrict__ gm, float4 *__restrict__ gbuf,
+    float damping, float dt, int kick, float G, int want_next_g)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int rc = rb / 32;
-    const int I = i / rb;
-    const int c0 = sk_owner(sym_prefix(I, nc, rc), total, grid);
-    const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1, total, grid);
-    const int li = i - I * rb;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)(t >> 2), q = (int)(t & 3);
+    const bool live = i < n;  // dead threads still take part in the shuffles
     float ox = 0.f, oy = 0.f, oz = 0.f, odm = 0.f;
-    for (int c = c0; c <= c1; ++c) {
-        const float4 q = tpart[(size_t)(c + I) * rb + li];
-        ox += q.x;
-        oy += q.y;
-        oz += q.z;
-        odm += q.w;
+    if (live) {
+        const int rc = rb / 32;
+        const int I = i / rb;
+        const int c0 = sk_owner(sym_prefix(I, nc, rc), total, grid);
+        const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1, total, grid);
+        const int li = i - I * rb;
+        for (int c = c0 + q; c <= c1; c += 4) {
+            const float4 v4 = tpart[(size_t)(c + I) * rb + li];
+            ox += v4.x;
+            oy += v4.y;
+            oz += v4.z;
+            odm += v4.w;
+        }
+#pragma unroll 4
+        for (int r = q; r < I; r += 4) {
+            const float4 v4 = spart[sym_soff(r, n, rb) + (i - (long long)(r + 1) * rb)];
+            ox += v4.x;
+            oy += v4.y;
+            oz += v4.z;
+            odm += v4.w;
+        }
     }
-    long long off = (long long)i - rb;  // row r at soff(r) + i - (r + 1) rb
-    for (int r = 0; r < I; ++r) {
-        const float4 q = spart[off];
-        off += (long long)n - (long long)(r + 2) * rb;
-        ox += q.x;
-        oy += q.y;
-        oz += q.z;
-        odm += q.w;
+#pragma unroll
+    for (int m = 1; m <= 2; m <<= 1) {
+        ox += __shfl_xor_sync(0xffffffffu, ox, m);
+        oy += __shfl_xor_sync(0xffffffffu, oy, m);
+        oz += __shfl_xor_sync(0xffffffffu, oz, m);
+        odm += __shfl_xor_sync(0xffffffffu, odm, m);
     }
+    if (!live || q != 0) return;
     adj_body_update(i, ox, oy, oz, odm, pos, acc, lx, lv, gm, gbuf, damping, dt, kick, G, want_next_g);
 }
 
@@ -506,9 +520,10 @@ int adj_update_sym(const SymPlan &p, const float4 *tpart, const float4 *spart, c
                    float dt, int kick, float G, int want_next_g, cudaStream_t s)
 {
     if (p.n == 0) return NB_OK;
-    adj_update_sym_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(tpart, spart, p.n, p.rb, p.nc, p.nrb,
-                                                           p.total, p.grid, pos_prev, acc, lx, lv, gm,
-                                                           gbuf, damping, dt, kick, G, want_next_g);
+    const long long threads = 4ll * p.n;  // a quad of threads per body
+    adj_update_sym_kernel<<<(unsigned)((threads + kAdjUpdBlock - 1) / kAdjUpdBlock), kAdjUpdBlock, 0, s>>>(
+        tpart, spart, p.n, p.rb, p.nc, p.nrb, p.total, p.grid, pos_prev, acc, lx, lv, gm, gbuf, damping, dt,
+        kick, G, want_next_g);
     NB_LAUNCH_CHECK("adj_update_sym_kernel launch");
     return NB_OK;
 }
