@@ -84,6 +84,11 @@ struct nb_ctx {
         bool ready = false;
         // the forward pass left the last segment's states in seg_pos/seg_acc
         bool live_last = false;
+        // second segment buffer: segment s-1 is recomputed on rstream while
+        // the reverse pass runs through segment s on the caller's stream
+        float4 *seg_pos2 = nullptr, *seg_acc2 = nullptr, *vel_tmp2 = nullptr;
+        cudaStream_t rstream = nullptr;
+        cudaEvent_t ev_rec[2] = {nullptr, nullptr}, ev_go = nullptr;
     } adj;
 };
 
@@ -148,6 +153,13 @@ static void free_ctx(nb_ctx *c)
     cudaFree(c->adj.partial);
     cudaFree(c->adj.sym_t);
     cudaFree(c->adj.sym_s);
+    cudaFree(c->adj.seg_pos2);
+    cudaFree(c->adj.seg_acc2);
+    cudaFree(c->adj.vel_tmp2);
+    if (c->adj.rstream) cudaStreamDestroy(c->adj.rstream);
+    for (auto &e : c->adj.ev_rec)
+        if (e) cudaEventDestroy(e);
+    if (c->adj.ev_go) cudaEventDestroy(c->adj.ev_go);
     cudaFree(c->sym_t);
     cudaFree(c->sym_s);
     for (int k = 0; k < 2; ++k) {
@@ -618,7 +630,8 @@ static int adj_reserve(nb_ctx *c, int nckpt, int every)
         cudaFree(A.sym_s);
         cudaFree(A.partial);
         cudaFree(A.vel_tmp);
-        A.sym_t = A.sym_s = A.partial = A.vel_tmp = nullptr;
+        cudaFree(A.vel_tmp2);
+        A.sym_t = A.sym_s = A.partial = A.vel_tmp = A.vel_tmp2 = nullptr;
         A.sym = uses_sym(c);
         if (A.sym) {
             if ((st = nb::sym_vjp_plan(c->p.n, 0, 0, c->device, &A.splan)) ||
@@ -635,6 +648,7 @@ static int adj_reserve(nb_ctx *c, int nckpt, int every)
                 return st;
         }
         if ((st = dev_alloc((void **)&A.vel_tmp, n * sizeof(float4), "adjoint allocation")) ||
+            (st = dev_alloc((void **)&A.vel_tmp2, n * sizeof(float4), "adjoint allocation")) ||
             (st = dev_alloc((void **)&A.lx, n * sizeof(float4), "adjoint allocation")) ||
             (st = dev_alloc((void **)&A.lv, n * sizeof(float4), "adjoint allocation")) ||
             (st = dev_alloc((void **)&A.gbuf, n * sizeof(float4), "adjoint allocation")) ||
@@ -654,10 +668,14 @@ static int adj_reserve(nb_ctx *c, int nckpt, int every)
     if (every > A.cap_seg) {
         cudaFree(A.seg_pos);
         cudaFree(A.seg_acc);
-        A.seg_pos = A.seg_acc = nullptr;
+        cudaFree(A.seg_pos2);
+        cudaFree(A.seg_acc2);
+        A.seg_pos = A.seg_acc = A.seg_pos2 = A.seg_acc2 = nullptr;
         A.cap_seg = 0;
         if ((st = dev_alloc((void **)&A.seg_pos, n * (every + 1) * sizeof(float4), "segment allocation")) ||
-            (st = dev_alloc((void **)&A.seg_acc, n * every * sizeof(float4), "segment allocation")))
+            (st = dev_alloc((void **)&A.seg_acc, n * every * sizeof(float4), "segment allocation")) ||
+            (st = dev_alloc((void **)&A.seg_pos2, n * (every + 1) * sizeof(float4), "segment allocation")) ||
+            (st = dev_alloc((void **)&A.seg_acc2, n * every * sizeof(float4), "segment allocation")))
             return st;
         A.cap_seg = every;
     }
@@ -742,46 +760,72 @@ int nb_adj_backward(nb_ctx *c, const void *gx_T, const void *gv_T, void *gx0, vo
     else
         NB_CUDA(cudaMemsetAsync(A.lv, 0, n * sizeof(float4), s));
     NB_CUDA(cudaMemsetAsync(A.gm, 0, n * sizeof(float), s));
-    bool have_g = false;
-    for (int seg = A.nckpt - 1; seg >= 0; --seg) {
+    // Recompute segment `seg` from its checkpoint into segment buffer b on
+    // stream rs, with the algorithm of the forward pass (same bits).
+    auto recompute = [&](int seg, int b, cudaStream_t rs) -> int {
+        float4 *sp = b ? A.seg_pos2 : A.seg_pos, *sa = b ? A.seg_acc2 : A.seg_acc;
+        float4 *vt = b ? A.vel_tmp2 : A.vel_tmp;
         const int t0 = seg * A.every;
         const int len = (A.steps - t0) < A.every ? (A.steps - t0) : A.every;
-        // recompute the segment's positions (and accelerations) from its
-        // checkpoint, unless the forward pass left them in place
-        const bool recompute = !(seg == A.nckpt - 1 && A.live_last);
-        A.live_last = false;  // the buffers are reused from here on
-        if (recompute) {
-            NB_CUDA(cudaMemcpyAsync(A.seg_pos, A.ckpt_pos + (size_t)seg * n, n * sizeof(float4),
-                                    cudaMemcpyDeviceToDevice, s));
-            NB_CUDA(cudaMemcpyAsync(A.vel_tmp, A.ckpt_vel + (size_t)seg * n, n * sizeof(float4),
-                                    cudaMemcpyDeviceToDevice, s));
-        }
-        for (int k = 0; recompute && k < len; ++k) {
-            const float4 *xk = A.seg_pos + (size_t)k * n;
+        NB_CUDA(cudaMemcpyAsync(sp, A.ckpt_pos + (size_t)seg * n, n * sizeof(float4), cudaMemcpyDeviceToDevice, rs));
+        NB_CUDA(cudaMemcpyAsync(vt, A.ckpt_vel + (size_t)seg * n, n * sizeof(float4), cudaMemcpyDeviceToDevice, rs));
+        int st2;
+        for (int k = 0; k < len; ++k) {
+            const float4 *xk = sp + (size_t)k * n;
+            float4 *xn = sp + (size_t)(k + 1) * n;
             if (uses_sym(c)) {
-                // recompute with the algorithm of the forward pass: same bits
-                if ((st = nb::sym_force(c->splan, xk, eps2, c->sym_t, c->sym_s, s))) return st;
+                if ((st2 = nb::sym_force(c->splan, xk, eps2, c->sym_t, c->sym_s, rs))) return st2;
                 if (p.kick == NB_KICK_REFERENCE &&
-                    (st = nb::sym_integrate(c->splan, xk, nullptr, nullptr, c->sym_t, c->sym_s, D,
-                                            dt, p.kick, G, A.seg_acc + (size_t)k * n, s)))
-                    return st;
-                if ((st = nb::sym_integrate(c->splan, xk, A.seg_pos + (size_t)(k + 1) * n, A.vel_tmp,
-                                            c->sym_t, c->sym_s, D, dt, p.kick, G, nullptr, s)))
-                    return st;
+                    (st2 = nb::sym_integrate(c->splan, xk, nullptr, nullptr, c->sym_t, c->sym_s, D, dt,
+                                             p.kick, G, sa + (size_t)k * n, rs)))
+                    return st2;
+                if ((st2 = nb::sym_integrate(c->splan, xk, xn, vt, c->sym_t, c->sym_s, D, dt, p.kick, G,
+                                             nullptr, rs)))
+                    return st2;
                 continue;
             }
-            if ((st = nb::fast_force(c->plan, xk, eps2, c->partial, s))) return st;
+            if ((st2 = nb::fast_force(c->plan, xk, eps2, c->partial, rs))) return st2;
             if (p.kick == NB_KICK_REFERENCE &&
-                (st = nb::fast_reduce(c->plan, c->partial, 0, xk, eps2, A.seg_acc + (size_t)k * n,
-                                      nullptr, s)))
-                return st;
-            if ((st = nb::fast_integrate(c->plan, xk, A.seg_pos + (size_t)(k + 1) * n, A.vel_tmp,
-                                         c->partial, D, dt, p.kick, G, nullptr, s)))
-                return st;
+                (st2 = nb::fast_reduce(c->plan, c->partial, 0, xk, eps2, sa + (size_t)k * n, nullptr, rs)))
+                return st2;
+            if ((st2 = nb::fast_integrate(c->plan, xk, xn, vt, c->partial, D, dt, p.kick, G, nullptr, rs)))
+                return st2;
         }
+        return NB_OK;
+    };
+    // Segments alternate between the two buffers, the last one in buffer 0
+    // (where the forward pass leaves it).  While the reverse pass runs through
+    // segment seg on `s`, segment seg-1 is recomputed on rstream into the
+    // other buffer; each side waits on an event for the other.
+    const int last = A.nckpt - 1;
+    auto buf_of = [&](int seg) { return (last - seg) & 1; };
+    const bool live = A.live_last;
+    A.live_last = false;  // the buffers are reused from here on
+    if (last > 0 && !A.rstream) {
+        NB_CUDA(cudaStreamCreateWithFlags(&A.rstream, cudaStreamNonBlocking));
+        for (auto &e : A.ev_rec) NB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        NB_CUDA(cudaEventCreateWithFlags(&A.ev_go, cudaEventDisableTiming));
+    }
+    if (!live && (st = recompute(last, buf_of(last), s))) return st;
+    bool have_g = false;
+    for (int seg = last; seg >= 0; --seg) {
+        const int b = buf_of(seg);
+        if (seg < last) NB_CUDA(cudaStreamWaitEvent(s, A.ev_rec[b], 0));
+        if (seg > 0) {
+            // everything enqueued on s so far (the reverse of seg+1, which
+            // used the other buffer, and any recompute on s) precedes it
+            NB_CUDA(cudaEventRecord(A.ev_go, s));
+            NB_CUDA(cudaStreamWaitEvent(A.rstream, A.ev_go, 0));
+            if ((st = recompute(seg - 1, buf_of(seg - 1), A.rstream))) return st;
+            NB_CUDA(cudaEventRecord(A.ev_rec[buf_of(seg - 1)], A.rstream));
+        }
+        const float4 *sp = b ? A.seg_pos2 : A.seg_pos, *sa = b ? A.seg_acc2 : A.seg_acc;
+        const int t0 = seg * A.every;
+        const int len = (A.steps - t0) < A.every ? (A.steps - t0) : A.every;
         // reverse through the segment
         for (int k = len - 1; k >= 0; --k) {
-            const float4 *xk = A.seg_pos + (size_t)k * n;
+            const float4 *xk = sp + (size_t)k * n;
+            const float4 *ak = sa + (size_t)k * n;
             if (!have_g) {
                 if ((st = nb::adj_g(p.n, xk, A.lx, A.lv, A.gbuf, D, dt, p.kick, G, s))) return st;
                 have_g = true;
@@ -789,14 +833,14 @@ int nb_adj_backward(nb_ctx *c, const void *gx_T, const void *gv_T, void *gx0, vo
             const bool more = !(seg == 0 && k == 0);
             if (A.sym) {
                 if ((st = nb::sym_vjp(A.splan, xk, A.gbuf, eps2, A.sym_t, A.sym_s, s)) ||
-                    (st = nb::adj_update_sym(A.splan, A.sym_t, A.sym_s, xk, A.seg_acc + (size_t)k * n,
-                                             A.lx, A.lv, A.gm, A.gbuf, D, dt, p.kick, G, more ? 1 : 0, s)))
+                    (st = nb::adj_update_sym(A.splan, A.sym_t, A.sym_s, xk, ak, A.lx, A.lv, A.gm, A.gbuf, D,
+                                             dt, p.kick, G, more ? 1 : 0, s)))
                     return st;
                 continue;
             }
             if ((st = nb::adj_vjp(A.plan, xk, A.gbuf, eps2, A.partial, s))) return st;
-            if ((st = nb::adj_update(A.plan, A.partial, xk, A.seg_acc + (size_t)k * n, A.lx, A.lv,
-                                     A.gm, A.gbuf, D, dt, p.kick, G, more ? 1 : 0, s)))
+            if ((st = nb::adj_update(A.plan, A.partial, xk, ak, A.lx, A.lv, A.gm, A.gbuf, D, dt, p.kick, G,
+                                     more ? 1 : 0, s)))
                 return st;
         }
     }
