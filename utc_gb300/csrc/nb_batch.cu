@@ -762,6 +762,11 @@ struct nb_batch {
     int adj_steps = 0, adj_every = 0, adj_nckpt = 0, cap_ckpt = 0, cap_seg = 0;
     bool adj_ready = false;
     float4 *ckpt_pos = nullptr, *ckpt_vel = nullptr, *seg_pos = nullptr, *seg_acc = nullptr;
+    // second segment buffer and stream: segment s-1 is recomputed on rstream
+    // while the reverse pass runs through segment s
+    float4 *seg_pos2 = nullptr, *seg_acc2 = nullptr, *vel_tmp2 = nullptr;
+    cudaStream_t rstream = nullptr;
+    cudaEvent_t ev_rec[2] = {nullptr, nullptr}, ev_go = nullptr;
     float4 *vel_tmp = nullptr, *lx = nullptr, *lv = nullptr, *gbuf = nullptr;
     float *gm = nullptr;
 };
@@ -970,6 +975,7 @@ static int batch_vplan_setup(nb_batch *b)
     NB_CUDA(cudaMalloc((void **)&b->vspart, std::max<size_t>((size_t)p.spart, 1) * sizeof(float4)));
     const size_t nb4 = std::max<size_t>((size_t)b->nbody, 1) * sizeof(float4);
     NB_CUDA(cudaMalloc((void **)&b->vel_tmp, nb4));
+    NB_CUDA(cudaMalloc((void **)&b->vel_tmp2, nb4));
     NB_CUDA(cudaMalloc((void **)&b->lx, nb4));
     NB_CUDA(cudaMalloc((void **)&b->lv, nb4));
     NB_CUDA(cudaMalloc((void **)&b->gbuf, nb4));
@@ -1004,6 +1010,13 @@ static void free_batch(nb_batch *b)
     cudaFree(b->seg_pos);
     cudaFree(b->seg_acc);
     cudaFree(b->vel_tmp);
+    cudaFree(b->seg_pos2);
+    cudaFree(b->seg_acc2);
+    cudaFree(b->vel_tmp2);
+    if (b->rstream) cudaStreamDestroy(b->rstream);
+    for (auto &e : b->ev_rec)
+        if (e) cudaEventDestroy(e);
+    if (b->ev_go) cudaEventDestroy(b->ev_go);
     cudaFree(b->lx);
     cudaFree(b->lv);
     cudaFree(b->gbuf);
@@ -1484,10 +1497,14 @@ int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream)
     if (ckpt_every > b->cap_seg) {
         cudaFree(b->seg_pos);
         cudaFree(b->seg_acc);
-        b->seg_pos = b->seg_acc = nullptr;
+        cudaFree(b->seg_pos2);
+        cudaFree(b->seg_acc2);
+        b->seg_pos = b->seg_acc = b->seg_pos2 = b->seg_acc2 = nullptr;
         b->cap_seg = 0;
         NB_CUDA(cudaMalloc((void **)&b->seg_pos, std::max<size_t>(n * (ckpt_every + 1), 1) * sizeof(float4)));
         NB_CUDA(cudaMalloc((void **)&b->seg_acc, std::max<size_t>(n * ckpt_every, 1) * sizeof(float4)));
+        NB_CUDA(cudaMalloc((void **)&b->seg_pos2, std::max<size_t>(n * (ckpt_every + 1), 1) * sizeof(float4)));
+        NB_CUDA(cudaMalloc((void **)&b->seg_acc2, std::max<size_t>(n * ckpt_every, 1) * sizeof(float4)));
         b->cap_seg = ckpt_every;
     }
     cudaStream_t s = (cudaStream_t)stream;
@@ -1554,28 +1571,56 @@ int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void 
     else
         NB_CUDA(cudaMemsetAsync(b->lv, 0, n * sizeof(float4), s));
     NB_CUDA(cudaMemsetAsync(b->gm, 0, n * sizeof(float), s));
-    bool have_g = false;
-    for (int seg = b->adj_nckpt - 1; seg >= 0; --seg) {
+    // Recompute segment `seg` from its checkpoint into buffer k on stream rs
+    // (one force pass per step; with the reference kick its partials also
+    // give the accelerations).  Same kernels, same bits as the forward pass.
+    auto recompute = [&](int seg, int kb, cudaStream_t rs) -> int {
+        float4 *sp = kb ? b->seg_pos2 : b->seg_pos, *sa = kb ? b->seg_acc2 : b->seg_acc;
+        float4 *vt = kb ? b->vel_tmp2 : b->vel_tmp;
         const int t0 = seg * b->adj_every;
         const int len = (b->adj_steps - t0) < b->adj_every ? (b->adj_steps - t0) : b->adj_every;
-        const bool recompute = !(seg == b->adj_nckpt - 1 && b->adj_live_last);
-        b->adj_live_last = false;  // the segment buffers are reused from here on
-        if (recompute) {
-            NB_CUDA(cudaMemcpyAsync(b->seg_pos, b->ckpt_pos + (size_t)seg * n, n * sizeof(float4),
-                                    cudaMemcpyDeviceToDevice, s));
-            NB_CUDA(cudaMemcpyAsync(b->vel_tmp, b->ckpt_vel + (size_t)seg * n, n * sizeof(float4),
-                                    cudaMemcpyDeviceToDevice, s));
-        }
-        for (int k = 0; recompute && k < len; ++k) {
-            const float4 *xk = b->seg_pos + (size_t)k * n;
+        NB_CUDA(cudaMemcpyAsync(sp, b->ckpt_pos + (size_t)seg * n, n * sizeof(float4), cudaMemcpyDeviceToDevice, rs));
+        NB_CUDA(cudaMemcpyAsync(vt, b->ckpt_vel + (size_t)seg * n, n * sizeof(float4), cudaMemcpyDeviceToDevice, rs));
+        int st2;
+        for (int k = 0; k < len; ++k) {
+            const float4 *xk = sp + (size_t)k * n;
+            if ((st2 = batch_force(b, xk, rs))) return st2;
             if (p.kick == NB_KICK_REFERENCE &&
-                (st = batch_force_step(b, xk, nullptr, nullptr, b->seg_acc + (size_t)k * n, s)))
-                return st;
-            if ((st = batch_force_step(b, xk, b->seg_pos + (size_t)(k + 1) * n, b->vel_tmp, nullptr, s)))
-                return st;
+                (st2 = batch_integrate(b, xk, nullptr, nullptr, sa + (size_t)k * n, rs)))
+                return st2;
+            if ((st2 = batch_integrate(b, xk, sp + (size_t)(k + 1) * n, vt, nullptr, rs))) return st2;
         }
+        return NB_OK;
+    };
+    // As in nb_adj_backward: segments alternate between the two buffers (the
+    // last one in buffer 0, where the forward pass leaves it), and segment
+    // seg-1 is recomputed on rstream while the reverse pass runs through seg.
+    const int last = b->adj_nckpt - 1;
+    auto buf_of = [&](int seg) { return (last - seg) & 1; };
+    const bool live = b->adj_live_last;
+    b->adj_live_last = false;  // the segment buffers are reused from here on
+    if (last > 0 && !b->rstream) {
+        NB_CUDA(cudaStreamCreateWithFlags(&b->rstream, cudaStreamNonBlocking));
+        for (auto &e : b->ev_rec) NB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        NB_CUDA(cudaEventCreateWithFlags(&b->ev_go, cudaEventDisableTiming));
+    }
+    if (!live && (st = recompute(last, buf_of(last), s))) return st;
+    bool have_g = false;
+    for (int seg = last; seg >= 0; --seg) {
+        const int kb = buf_of(seg);
+        if (seg < last) NB_CUDA(cudaStreamWaitEvent(s, b->ev_rec[kb], 0));
+        if (seg > 0) {
+            NB_CUDA(cudaEventRecord(b->ev_go, s));
+            NB_CUDA(cudaStreamWaitEvent(b->rstream, b->ev_go, 0));
+            if ((st = recompute(seg - 1, buf_of(seg - 1), b->rstream))) return st;
+            NB_CUDA(cudaEventRecord(b->ev_rec[buf_of(seg - 1)], b->rstream));
+        }
+        const float4 *sp = kb ? b->seg_pos2 : b->seg_pos, *sa = kb ? b->seg_acc2 : b->seg_acc;
+        const int t0 = seg * b->adj_every;
+        const int len = (b->adj_steps - t0) < b->adj_every ? (b->adj_steps - t0) : b->adj_every;
         for (int k = len - 1; k >= 0; --k) {
-            const float4 *xk = b->seg_pos + (size_t)k * n;
+            const float4 *xk = sp + (size_t)k * n;
+            const float4 *ak = sa + (size_t)k * n;
             if (!have_g) {
                 if ((st = nb::adj_g(b->nbody, xk, b->lx, b->lv, b->gbuf, D, dt, p.kick, G, s))) return st;
                 have_g = true;
@@ -1588,8 +1633,8 @@ int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void 
                     NB_LAUNCH_CHECK("bks_vjp_kernel launch");
                 }
                 nb::bks_adj_update_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
-                    b->vpartial, b->vspart, vsd, b->nbody, 32 * vp.bpt, vp.total, vp.workers, xk,
-                    b->seg_acc + (size_t)k * n, b->lx, b->lv, b->gm, b->gbuf, D, dt, p.kick, G, more ? 1 : 0);
+                    b->vpartial, b->vspart, vsd, b->nbody, 32 * vp.bpt, vp.total, vp.workers, xk, ak, b->lx,
+                    b->lv, b->gm, b->gbuf, D, dt, p.kick, G, more ? 1 : 0);
                 NB_LAUNCH_CHECK("bks_adj_update_kernel launch");
                 continue;
             }
@@ -1598,8 +1643,8 @@ int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void 
                 NB_LAUNCH_CHECK("bk_vjp_kernel launch");
             }
             nb::bk_adj_update_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
-                b->vpartial, vd, b->nbody, 32 * vp.bpt, vp.total, vp.workers, xk,
-                b->seg_acc + (size_t)k * n, b->lx, b->lv, b->gm, b->gbuf, D, dt, p.kick, G, more ? 1 : 0);
+                b->vpartial, vd, b->nbody, 32 * vp.bpt, vp.total, vp.workers, xk, ak, b->lx, b->lv, b->gm,
+                b->gbuf, D, dt, p.kick, G, more ? 1 : 0);
             NB_LAUNCH_CHECK("bk_adj_update_kernel launch");
         }
     }
