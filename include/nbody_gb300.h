@@ -161,8 +161,10 @@ int nb_energy(nb_ctx *ctx, double *out5, void *accphi_dev, void *stream);
  * takes the cotangents of the final positions gx_T and velocities gv_T
  * (device, n float4, xyz used; gv_T may be NULL for zero) and writes
  * dL/dx0, dL/dv0 (device n float4, w = 0) and dL/dm (device n float),
- * recomputing each segment's trajectory from its checkpoint.  NB_F32 fast
- * contexts only; both kick modes. */
+ * recomputing each segment's trajectory from its checkpoint.  The recompute
+ * of the next segment runs on a stream of the context's own, ordered against
+ * `stream` by events: the results are complete once `stream` has reached the
+ * end of the call.  NB_F32 fast or symmetric contexts; both kick modes. */
 int nb_adj_forward(nb_ctx *ctx, int steps, int ckpt_every, void *stream);
 int nb_adj_backward(nb_ctx *ctx, const void *gx_T, const void *gv_T, void *gx0, void *gv0,
                     void *gm, void *stream);
