@@ -191,9 +191,10 @@ int nb_run_host(nb_ctx *ctx, const void *pos, const void *vel, int loops,
  * pos_new (written, distinct from pos_old) and vel (updated in place).
  * The partial-force scratch is a 16 MiB array compiled into the library
  * (present on every GPU that loads it until exit), which limits n to
- * 262,144; larger n returns NB_ERR_INVALID.  The first call on a device
- * looks up that array's device address, so make it before any stream
- * capture on that device.  All calls share the array: calls whose kernels
+ * 262,144; larger n returns NB_ERR_INVALID.  The first call in each CUDA
+ * context looks up that array's device address (again after cudaDeviceReset
+ * or in a driver-API context of the caller's), so make it before any stream
+ * capture in that context.  All calls share the array: calls whose kernels
  * overlap on the GPU race and must be serialised. */
 int nb_step_f32_noalloc(const float *pos_old, float *pos_new, float *vel, int n, float eps2,
                         float damping, float dt, int kick, float G, void *stream);

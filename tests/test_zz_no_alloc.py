@@ -63,3 +63,78 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(cuda):
                                  N.NB_KICK_PHYSICAL, 1.0, None)
     assert rc == N.NB_ERR_INVALID
     assert b"262144" in lib.nb_last_error()
+
+
+def _driver():
+    """The CUDA driver API through ctypes (only what the next test uses)."""
+    cu = C.CDLL("libcuda.so.1")
+    u64, vp = C.c_uint64, C.c_void_p
+    for name, args in [("cuInit", [C.c_uint]), ("cuDeviceGet", [C.POINTER(C.c_int), C.c_int]),
+                       ("cuCtxCreate_v4", [C.POINTER(vp), vp, C.c_uint, C.c_int]),
+                       ("cuCtxPopCurrent_v2", [C.POINTER(vp)]), ("cuCtxDestroy_v2", [vp]),
+                       ("cuCtxSynchronize", []), ("cuMemAlloc_v2", [C.POINTER(u64), C.c_size_t]),
+                       ("cuMemFree_v2", [u64]), ("cuMemcpyHtoD_v2", [u64, vp, C.c_size_t]),
+                       ("cuMemcpyDtoH_v2", [vp, u64, C.c_size_t])]:
+        f = getattr(cu, name)
+        f.argtypes, f.restype = args, C.c_int
+    return cu
+
+
+def test_noalloc_in_a_driver_api_context(cuda):
+    """The scratch array's address belongs to a CUDA context: a call made
+    while a caller's own driver-API context is current looks it up in that
+    context, and the next call in the primary context uses the primary
+    context's address again.  Both give the step bit for bit."""
+    import torch
+
+    n = 3000
+    p64, v64 = ics.plummer(n, seed=5)
+    pos, vel = ics.f32(p64), ics.f32(v64)
+    lib = N.lib()
+    eps2, dt = np.float32(1e-4), np.float32(1e-4)
+
+    def step_in_primary():
+        p0, p1 = torch.from_numpy(pos).cuda(), torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+        v = torch.from_numpy(vel).cuda()
+        rc = lib.nb_step_f32_noalloc(C.c_void_p(p0.data_ptr()), C.c_void_p(p1.data_ptr()),
+                                     C.c_void_p(v.data_ptr()), n, eps2, 1.0, dt, N.NB_KICK_PHYSICAL, 1.0,
+                                     C.c_void_p(current_stream_handle()))
+        assert rc == N.NB_OK, lib.nb_last_error()
+        torch.cuda.synchronize()
+        return p1.cpu().numpy(), v.cpu().numpy()
+
+    want_p, want_v = step_in_primary()
+
+    cu = _driver()
+    assert cu.cuInit(0) == 0
+    dev = C.c_int()
+    assert cu.cuDeviceGet(C.byref(dev), torch.cuda.current_device()) == 0
+    ctx = C.c_void_p()
+    assert cu.cuCtxCreate_v4(C.byref(ctx), None, 0, dev) == 0  # current from here on
+    nbytes = n * 16
+    ptrs = []
+    try:
+        for _ in range(3):
+            d = C.c_uint64()
+            assert cu.cuMemAlloc_v2(C.byref(d), nbytes) == 0
+            ptrs.append(d.value)
+        p0, p1, v = ptrs
+        assert cu.cuMemcpyHtoD_v2(p0, pos.ctypes.data, nbytes) == 0
+        assert cu.cuMemcpyHtoD_v2(v, vel.ctypes.data, nbytes) == 0
+        rc = lib.nb_step_f32_noalloc(C.c_void_p(p0), C.c_void_p(p1), C.c_void_p(v), n, eps2, 1.0, dt,
+                                     N.NB_KICK_PHYSICAL, 1.0, None)
+        assert rc == N.NB_OK, lib.nb_last_error()
+        assert cu.cuCtxSynchronize() == 0
+        got_p, got_v = np.empty_like(pos), np.empty_like(vel)
+        assert cu.cuMemcpyDtoH_v2(got_p.ctypes.data, p1, nbytes) == 0
+        assert cu.cuMemcpyDtoH_v2(got_v.ctypes.data, v, nbytes) == 0
+    finally:
+        for d in ptrs:
+            cu.cuMemFree_v2(d)
+        popped = C.c_void_p()
+        cu.cuCtxPopCurrent_v2(C.byref(popped))
+        cu.cuCtxDestroy_v2(ctx)
+    assert np.array_equal(got_p, want_p) and np.array_equal(got_v, want_v)
+
+    again_p, again_v = step_in_primary()
+    assert np.array_equal(again_p, want_p) and np.array_equal(again_v, want_v)

@@ -17,15 +17,22 @@
 // Host code never hands the array's name to a kernel: on the host that name
 // is only a stand-in for the device symbol (using it as a pointer would fault,
 // or on a GPU that can reach host memory silently use the wrong memory).  The
-// first call on each device looks up the array's device address with
-// cudaGetSymbolAddress, with that device current, and caches it; that first
-// call should therefore come before any stream capture on that device.
+// array's device address belongs to a CUDA context, not to a device: the
+// first call in each context looks it up with cudaGetSymbolAddress and caches
+// it beside the context's unique ID (cuCtxGetId), one entry per device.  A
+// call in another context on that device -- the primary context re-created
+// after cudaDeviceReset, or a driver-API context the caller made current --
+// sees a different ID and looks the address up again instead of using one
+// that is no longer mapped.  The lookup should come before any stream capture
+// in that context.
 //
 // All calls share the one array and it keeps what the last call wrote.
 // Nothing in it has to start at zero: each call writes every scratch entry
 // it later reads.  Calls whose kernels overlap on the GPU (for example on two
 // streams at once) race on the array and corrupt each other's results;
 // serialise them.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "nb_internal.cuh"
@@ -40,25 +47,72 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) float4 g_noalloc_scratch[kNoAllocScratchFloat4];
 
+struct ScratchAddress {
+    unsigned long long ctx_id;  // cuCtxGetId of the context it was looked up in
+    float4 *ptr;
+};
 std::mutex g_scratch_mu;
-float4 *g_scratch_ptr[kMaxDevices] = {};
+ScratchAddress g_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device (looked up once
-// per device, with that device current).
-int scratch_for_current_device(float4 **out)
+// The two driver calls, found through the runtime (the library does not link
+// the driver library itself).  Resolved once, under g_scratch_mu.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+int resolve_driver_calls()
 {
-    int dev = 0;
-    NB_CUDA(cudaGetDevice(&dev));
+    if (g_ctx_get_current && g_ctx_get_id) return NB_OK;
+    void *f0 = nullptr, *f1 = nullptr;
+    cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = q0;
+    NB_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0));
+    NB_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1));
+    if (q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+        return nb::set_error(NB_ERR_CUDA, "nb_step_f32_noalloc: driver has no cuCtxGetCurrent/cuCtxGetId");
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f1);
+    return NB_OK;
+}
+
+// Unique ID of the calling thread's current CUDA context; 0 if none is
+// current yet (the runtime binds one on its first call that needs it).
+int current_context_id(unsigned long long *id)
+{
+    *id = 0;
+    int st = resolve_driver_calls();
+    if (st) return st;
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS)
+        return nb::set_error(NB_ERR_CUDA, "nb_step_f32_noalloc: cuCtxGetCurrent failed");
+    if (ctx && g_ctx_get_id(ctx, id) != CUDA_SUCCESS)
+        return nb::set_error(NB_ERR_CUDA, "nb_step_f32_noalloc: cuCtxGetId failed");
+    return NB_OK;
+}
+
+// Device address of g_noalloc_scratch in the current context of device dev
+// (looked up again whenever the context differs from the cached one).
+int scratch_for_current_context(int dev, float4 **out)
+{
     if (dev < 0 || dev >= kMaxDevices)
         return nb::set_error(NB_ERR_UNSUPPORTED, "nb_step_f32_noalloc: device ordinal out of range");
     std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    unsigned long long id = 0;
+    int st = current_context_id(&id);
+    if (st) return st;
+    ScratchAddress &a = g_scratch_addr[dev];
+    if (id == 0 || !a.ptr || a.ctx_id != id) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return nb::cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-        g_scratch_ptr[dev] = static_cast<float4 *>(p);
+        if (id == 0) {  // the lookup bound the runtime's context: cache under it
+            st = current_context_id(&id);
+            if (st) return st;
+        }
+        a.ctx_id = id;  // 0 still: not cached, looked up again next time
+        a.ptr = static_cast<float4 *>(p);
     }
-    *out = g_scratch_ptr[dev];
+    *out = a.ptr;
     return NB_OK;
 }
 
@@ -79,11 +133,11 @@ extern "C" int nb_step_f32_noalloc(const float *pos_old, float *pos_new, float *
         return nb::set_error(NB_ERR_INVALID, "nb_step_f32_noalloc: NULL buffer");
     if (pos_old == pos_new)
         return nb::set_error(NB_ERR_INVALID, "nb_step_f32_noalloc: pos_old and pos_new must differ");
-    float4 *scratch = nullptr;
-    int st = scratch_for_current_device(&scratch);
-    if (st) return st;
     int dev = 0;
     NB_CUDA(cudaGetDevice(&dev));
+    float4 *scratch = nullptr;
+    int st = scratch_for_current_context(dev, &scratch);
+    if (st) return st;
     nb::SkPlan plan;
     st = nb::fast_plan(n, kNoAllocBlock, kNoAllocBpt, 0, dev, &plan);
     if (st) return st;
