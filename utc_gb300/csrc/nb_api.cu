@@ -123,9 +123,9 @@ static int validate(const nb_params *p)
 
 static void free_ctx(nb_ctx *c)
 {
+    if (!c) return;
     for (auto &g : c->step_graph)
         if (g) cudaGraphExecDestroy(g);
-    if (!c) return;
     cudaFree(c->pos[0]);
     cudaFree(c->pos[1]);
     cudaFree(c->vel);

@@ -1399,8 +1399,16 @@ int nb_batch_step_per_system(nb_batch *b, int steps, void *stream)
     int st = sys_plans_for(b, &sp);
     if (st) return st;
     if (!b->sys_partial) {
-        NB_CUDA(cudaMalloc((void **)&b->sys_partial, sp.tpart * sizeof(float4)));
-        NB_CUDA(cudaMalloc((void **)&b->sys_spart, sp.spart * sizeof(float4)));
+        // both or neither: a failure leaves no half-allocated pair behind
+        float4 *t = nullptr, *u = nullptr;
+        cudaError_t e = cudaMalloc((void **)&t, sp.tpart * sizeof(float4));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&u, sp.spart * sizeof(float4));
+        if (e != cudaSuccess) {
+            cudaFree(t);
+            return nb::cuda_error(e, "per-system baseline scratch allocation");
+        }
+        b->sys_partial = t;
+        b->sys_spart = u;
     }
     std::vector<int> off(b->nsys + 1, 0);
     for (int i = 0; i < b->nsys; ++i) off[i + 1] = off[i] + b->sizes[i];
@@ -1434,10 +1442,21 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
     if (st0) return st0;
     std::vector<float4 *> tscratch(ntasks, nullptr), sscratch(ntasks, nullptr);
     std::vector<cudaStream_t> streams(ntasks, nullptr);
+    auto release = [&] {
+        for (int t = 0; t < ntasks; ++t) {
+            cudaFree(tscratch[t]);
+            cudaFree(sscratch[t]);
+            if (streams[t]) cudaStreamDestroy(streams[t]);
+        }
+    };
     for (int t = 0; t < ntasks; ++t) {
-        NB_CUDA(cudaMalloc((void **)&tscratch[t], sp.tpart * sizeof(float4)));
-        NB_CUDA(cudaMalloc((void **)&sscratch[t], sp.spart * sizeof(float4)));
-        NB_CUDA(cudaStreamCreateWithFlags(&streams[t], cudaStreamNonBlocking));
+        cudaError_t e = cudaMalloc((void **)&tscratch[t], sp.tpart * sizeof(float4));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&sscratch[t], sp.spart * sizeof(float4));
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&streams[t], cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            release();
+            return nb::cuda_error(e, "per-system task baseline setup");
+        }
     }
     const int cur = b->cur, dev = b->device;
     std::vector<int> status(ntasks, NB_OK);
@@ -1458,11 +1477,7 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
         });
     }
     for (auto &w : workers) w.join();
-    for (int t = 0; t < ntasks; ++t) {
-        cudaFree(tscratch[t]);
-        cudaFree(sscratch[t]);
-        cudaStreamDestroy(streams[t]);
-    }
+    release();
     for (int t = 0; t < ntasks; ++t)
         if (status[t]) return set_error(status[t], "per-system task baseline failed");
     if (steps % 2) b->cur ^= 1;
