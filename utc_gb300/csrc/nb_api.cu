@@ -25,6 +25,25 @@ int cuda_error(cudaError_t e, const char *what)
                              cudaGetErrorString(e) + ")");
 }
 
+int create_recompute_stream(cudaStream_t *stream, cudaEvent_t ev_rec[2], cudaEvent_t *ev_go)
+{
+    cudaStream_t rs = nullptr;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    cudaError_t e = cudaStreamCreateWithFlags(&rs, cudaStreamNonBlocking);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        if (rs) cudaStreamDestroy(rs);
+        return cuda_error(e, "adjoint recompute stream setup");
+    }
+    ev_rec[0] = ev[0];
+    ev_rec[1] = ev[1];
+    *ev_go = ev[2];
+    *stream = rs;
+    return NB_OK;
+}
+
 }  // namespace nb
 
 struct nb_ctx {
@@ -801,11 +820,9 @@ int nb_adj_backward(nb_ctx *c, const void *gx_T, const void *gv_T, void *gx0, vo
     auto buf_of = [&](int seg) { return (last - seg) & 1; };
     const bool live = A.live_last;
     A.live_last = false;  // the buffers are reused from here on
-    if (last > 0 && !A.rstream) {
-        NB_CUDA(cudaStreamCreateWithFlags(&A.rstream, cudaStreamNonBlocking));
-        for (auto &e : A.ev_rec) NB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        NB_CUDA(cudaEventCreateWithFlags(&A.ev_go, cudaEventDisableTiming));
-    }
+    if (last > 0 && !A.rstream &&
+        (st = nb::create_recompute_stream(&A.rstream, A.ev_rec, &A.ev_go)))
+        return st;
     if (!live && (st = recompute(last, buf_of(last), s))) return st;
     bool have_g = false;
     for (int seg = last; seg >= 0; --seg) {
@@ -890,9 +907,17 @@ int nb_run_host(nb_ctx *c, const void *pos, const void *vel, int loops, int out_
     const auto t_start = std::chrono::steady_clock::now();
     const bool pinned = c->p.memtype == NB_MEM_PINNED && sb > 0;
     if (pinned && !c->stage_pos) {
-        NB_CUDA(cudaMallocHost(&c->stage_pos, sb));
-        NB_CUDA(cudaMallocHost(&c->stage_vel, sb));
-        NB_CUDA(cudaMallocHost(&c->stage_out, sb));
+        // all three or none: a failed call leaves nothing half set up
+        void *b3[3] = {nullptr, nullptr, nullptr};
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMallocHost(&b3[k], sb);
+        if (e != cudaSuccess) {
+            for (void *q : b3) cudaFreeHost(q);
+            return nb::cuda_error(e, "pinned staging allocation");
+        }
+        c->stage_pos = b3[0];
+        c->stage_vel = b3[1];
+        c->stage_out = b3[2];
     }
     cudaEvent_t ev[2];
     for (int k = 0; k < 2; ++k) NB_CUDA(cudaEventCreate(&ev[k]));
@@ -923,14 +948,37 @@ int nb_run_host(nb_ctx *c, const void *pos, const void *vel, int loops, int out_
     // frames: snapshot on the compute stream, D2H on the copy stream
     const int frames = loops / out_interval;
     if (frames > 0 && sb && !c->copy_stream) {
-        NB_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-        for (int k = 0; k < 2; ++k) {
-            NB_CUDA(cudaMalloc(&c->snap[k], sb));
-            NB_CUDA(cudaMallocHost(&c->stage[k], sb));
-            NB_CUDA(cudaEventCreate(&c->ev_snap[k]));
-            NB_CUDA(cudaEventCreate(&c->ev_c0[k]));
-            NB_CUDA(cudaEventCreate(&c->ev_c1[k]));
+        // the copy stream is set last: a failed call leaves nothing half set up
+        cudaStream_t cs = nullptr;
+        void *snap[2] = {nullptr, nullptr}, *stage[2] = {nullptr, nullptr};
+        cudaEvent_t es[2] = {nullptr, nullptr}, e0[2] = {nullptr, nullptr}, e1[2] = {nullptr, nullptr};
+        cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+            e = cudaMalloc(&snap[k], sb);
+            if (e == cudaSuccess) e = cudaMallocHost(&stage[k], sb);
+            if (e == cudaSuccess) e = cudaEventCreate(&es[k]);
+            if (e == cudaSuccess) e = cudaEventCreate(&e0[k]);
+            if (e == cudaSuccess) e = cudaEventCreate(&e1[k]);
         }
+        if (e != cudaSuccess) {
+            for (int k = 0; k < 2; ++k) {
+                cudaFree(snap[k]);
+                cudaFreeHost(stage[k]);
+                if (es[k]) cudaEventDestroy(es[k]);
+                if (e0[k]) cudaEventDestroy(e0[k]);
+                if (e1[k]) cudaEventDestroy(e1[k]);
+            }
+            if (cs) cudaStreamDestroy(cs);
+            return nb::cuda_error(e, "frame copy-out setup");
+        }
+        for (int k = 0; k < 2; ++k) {
+            c->snap[k] = snap[k];
+            c->stage[k] = stage[k];
+            c->ev_snap[k] = es[k];
+            c->ev_c0[k] = e0[k];
+            c->ev_c1[k] = e1[k];
+        }
+        c->copy_stream = cs;
     }
     const int nstretch = (loops + out_interval - 1) / out_interval;
     while (c->events.size() < 2 * (size_t)nstretch) {

@@ -962,25 +962,37 @@ static int batch_vplan_setup(nb_batch *b)
     p.workers = p.total > 0 ? (int)workers : 0;
     p.grid = (p.workers + wpb - 1) / wpb;
     p.slots = p.total > 0 ? p.workers + p.total_wtb - 1 : 0;
-    NB_CUDA(cudaMalloc((void **)&b->d_it_off_v, sizeof(long long) * (b->nsys + 1)));
-    NB_CUDA(cudaMalloc((void **)&b->d_tb_off_v, sizeof(int) * (b->nsys + 1)));
-    NB_CUDA(cudaMalloc((void **)&b->d_sp_off_v, sizeof(long long) * (b->nsys + 1)));
-    NB_CUDA(cudaMemcpy(b->d_it_off_v, it_off.data(), sizeof(long long) * (b->nsys + 1),
-                       cudaMemcpyHostToDevice));
-    NB_CUDA(cudaMemcpy(b->d_tb_off_v, tb_off.data(), sizeof(int) * (b->nsys + 1),
-                       cudaMemcpyHostToDevice));
-    NB_CUDA(cudaMemcpy(b->d_sp_off_v, sp_off.data(), sizeof(long long) * (b->nsys + 1),
-                       cudaMemcpyHostToDevice));
-    NB_CUDA(cudaMalloc((void **)&b->vpartial, std::max<size_t>((size_t)p.slots * wtb, 1) * sizeof(float4)));
-    NB_CUDA(cudaMalloc((void **)&b->vspart, std::max<size_t>((size_t)p.spart, 1) * sizeof(float4)));
+    // d_it_off_v, which marks the setup as done, is set last: a failed call
+    // frees what it made and leaves nothing half set up
     const size_t nb4 = std::max<size_t>((size_t)b->nbody, 1) * sizeof(float4);
-    NB_CUDA(cudaMalloc((void **)&b->vel_tmp, nb4));
-    NB_CUDA(cudaMalloc((void **)&b->vel_tmp2, nb4));
-    NB_CUDA(cudaMalloc((void **)&b->lx, nb4));
-    NB_CUDA(cudaMalloc((void **)&b->lv, nb4));
-    NB_CUDA(cudaMalloc((void **)&b->gbuf, nb4));
-    NB_CUDA(cudaMalloc((void **)&b->gm, std::max<size_t>((size_t)b->nbody, 1) * sizeof(float)));
+    const size_t ns = (size_t)b->nsys + 1;
+    void *m[11] = {};
+    const size_t bytes[11] = {sizeof(long long) * ns, sizeof(int) * ns, sizeof(long long) * ns,
+                              std::max<size_t>((size_t)p.slots * wtb, 1) * sizeof(float4),
+                              std::max<size_t>((size_t)p.spart, 1) * sizeof(float4),
+                              nb4, nb4, nb4, nb4, nb4,
+                              std::max<size_t>((size_t)b->nbody, 1) * sizeof(float)};
+    cudaError_t e = cudaSuccess;
+    for (int q = 0; q < 11 && e == cudaSuccess; ++q) e = cudaMalloc(&m[q], bytes[q]);
+    if (e == cudaSuccess) e = cudaMemcpy(m[0], it_off.data(), bytes[0], cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(m[1], tb_off.data(), bytes[1], cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(m[2], sp_off.data(), bytes[2], cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        for (void *q : m) cudaFree(q);
+        return nb::cuda_error(e, "batched adjoint allocation");
+    }
+    b->d_tb_off_v = (int *)m[1];
+    b->d_sp_off_v = (long long *)m[2];
+    b->vpartial = (float4 *)m[3];
+    b->vspart = (float4 *)m[4];
+    b->vel_tmp = (float4 *)m[5];
+    b->vel_tmp2 = (float4 *)m[6];
+    b->lx = (float4 *)m[7];
+    b->lv = (float4 *)m[8];
+    b->gbuf = (float4 *)m[9];
+    b->gm = (float *)m[10];
     b->vplan = p;
+    b->d_it_off_v = (long long *)m[0];
     return NB_OK;
 }
 
@@ -1279,11 +1291,26 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
     }
     const size_t sb = (size_t)b->nbody * sizeof(float4);
     float4 *save_p = nullptr, *save_v = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto release = [&] {
+        cudaFree(save_p);
+        cudaFree(save_v);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    cudaError_t ce = cudaSuccess;
     if (sb) {
-        NB_CUDA(cudaMalloc((void **)&save_p, sb));
-        NB_CUDA(cudaMalloc((void **)&save_v, sb));
-        NB_CUDA(cudaMemcpyAsync(save_p, b->pos[b->cur], sb, cudaMemcpyDeviceToDevice, s));
-        NB_CUDA(cudaMemcpyAsync(save_v, b->vel, sb, cudaMemcpyDeviceToDevice, s));
+        ce = cudaMalloc((void **)&save_p, sb);
+        if (ce == cudaSuccess) ce = cudaMalloc((void **)&save_v, sb);
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(save_p, b->pos[b->cur], sb, cudaMemcpyDeviceToDevice, s);
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(save_v, b->vel, sb, cudaMemcpyDeviceToDevice, s);
+    }
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        cudaStreamSynchronize(s);  // a copy may be in flight
+        release();
+        return nb::cuda_error(ce, "autotune setup");
     }
     static const int cand_dir[][2] = {{2, 4}, {2, 8}, {4, 2}, {4, 4}, {4, 8}, {8, 2}, {8, 4}, {8, 8}};
     static const int cand_sym[][2] = {{1, 8}, {1, 12}, {1, 16}, {2, 8}, {2, 16}, {4, 8}, {4, 16}};
@@ -1294,36 +1321,35 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
         for (auto &c : cand_dir) cands.push_back({c[0], c[1]});
     float best = 1e30f;
     int bw = b->plan.wpb, bb = b->plan.bpt;
-    cudaEvent_t e0, e1;
-    NB_CUDA(cudaEventCreate(&e0));
-    NB_CUDA(cudaEventCreate(&e1));
     int st = NB_OK;
     for (auto &c : cands) {
         if ((st = batch_apply_plan(b, c[0], c[1], s))) break;
         if ((st = batch_step_once(b, s))) break;
-        NB_CUDA(cudaEventRecord(e0, s));
-        for (int r = 0; r < reps && !st; ++r) st = batch_step_once(b, s);
-        NB_CUDA(cudaEventRecord(e1, s));
-        NB_CUDA(cudaEventSynchronize(e1));
+        cudaError_t te = cudaEventRecord(e0, s);
+        for (int r = 0; r < reps && !st && te == cudaSuccess; ++r) st = batch_step_once(b, s);
+        if (st) break;
+        if (te == cudaSuccess) te = cudaEventRecord(e1, s);
+        if (te == cudaSuccess) te = cudaEventSynchronize(e1);
         float ms = 0;
-        NB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (te == cudaSuccess) te = cudaEventElapsedTime(&ms, e0, e1);
+        if (te != cudaSuccess) {
+            st = nb::cuda_error(te, "autotune timing");
+            break;
+        }
         if (ms < best) {
             best = ms;
             bw = c[0];
             bb = c[1];
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     if (!st) st = batch_apply_plan(b, bw, bb, s);
-    if (sb) {
+    if (sb) {  // the candidates' steps are undone
         b->cur = 0;
         cudaMemcpyAsync(b->pos[0], save_p, sb, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(b->vel, save_v, sb, cudaMemcpyDeviceToDevice, s);
-        cudaStreamSynchronize(s);
-        cudaFree(save_p);
-        cudaFree(save_v);
     }
+    cudaStreamSynchronize(s);
+    release();
     if (st) return st;
     if (cache_path) {
         std::ofstream outf(cache_path, std::ios::app);
@@ -1614,11 +1640,9 @@ int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void 
     auto buf_of = [&](int seg) { return (last - seg) & 1; };
     const bool live = b->adj_live_last;
     b->adj_live_last = false;  // the segment buffers are reused from here on
-    if (last > 0 && !b->rstream) {
-        NB_CUDA(cudaStreamCreateWithFlags(&b->rstream, cudaStreamNonBlocking));
-        for (auto &e : b->ev_rec) NB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        NB_CUDA(cudaEventCreateWithFlags(&b->ev_go, cudaEventDisableTiming));
-    }
+    if (last > 0 && !b->rstream &&
+        (st = nb::create_recompute_stream(&b->rstream, b->ev_rec, &b->ev_go)))
+        return st;
     if (!live && (st = recompute(last, buf_of(last), s))) return st;
     bool have_g = false;
     for (int seg = last; seg >= 0; --seg) {

@@ -370,20 +370,27 @@ int probe_fma(int iters, int packed, double *flops, float *ms, cudaStream_t s)
     NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, 0));
     const int grid = sms * std::max(occ, 1);
     float *out = nullptr;
-    NB_CUDA(cudaMallocAsync((void **)&out, sizeof(float) * grid * 256, s));
-    cudaEvent_t e0, e1;
-    NB_CUDA(cudaEventCreate(&e0));
-    NB_CUDA(cudaEventCreate(&e1));
-    kern<<<grid, 256, 0, s>>>(out, 16);  // warm-up
-    NB_CUDA(cudaEventRecord(e0, s));
-    kern<<<grid, 256, 0, s>>>(out, iters);
-    NB_CUDA(cudaEventRecord(e1, s));
-    NB_CUDA(cudaEventSynchronize(e1));
-    NB_CUDA(cudaEventElapsedTime(ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    NB_CUDA(cudaFreeAsync(out, s));
-    NB_CUDA(cudaStreamSynchronize(s));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMalloc((void **)&out, sizeof(float) * grid * 256);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) {
+        kern<<<grid, 256, 0, s>>>(out, 16);  // warm-up
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+    if (e == cudaSuccess) {
+        kern<<<grid, 256, 0, s>>>(out, iters);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    cudaStreamSynchronize(s);  // nothing of the probe is in flight below
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess) return cuda_error(e, "probe_fma");
     // 16 lane-FMAs per thread per iteration either way, 2 FLOP each
     *flops = 2.0 * 16.0 * (double)iters * (double)grid * 256.0;
     return NB_OK;

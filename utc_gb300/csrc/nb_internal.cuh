@@ -303,4 +303,9 @@ int exact_step_f64(int n, const double4 *pos_old, double4 *pos_new, double4 *vel
 // FMA peak probe (nb_fast.cu)
 int probe_fma(int iters, int packed, double *flops, float *ms, cudaStream_t s);
 
+// The adjoint's recompute stream and its three events (two "segment
+// recomputed", one "buffer free"), created together or not at all
+// (nb_api.cu).
+int create_recompute_stream(cudaStream_t *stream, cudaEvent_t ev_rec[2], cudaEvent_t *ev_go);
+
 }  // namespace nb
