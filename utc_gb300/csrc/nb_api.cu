@@ -643,14 +643,18 @@ static int adj_reserve(nb_ctx *c, int nckpt, int every)
     const size_t n = (size_t)c->p.n;
     auto &A = c->adj;
     int st;
-    if (!A.lx) {
-        // a retry after a failed allocation starts from nothing
+    if (!A.gm) {
+        // gm is allocated last: without it, a retry after a failed
+        // allocation starts from nothing
         cudaFree(A.sym_t);
         cudaFree(A.sym_s);
         cudaFree(A.partial);
         cudaFree(A.vel_tmp);
         cudaFree(A.vel_tmp2);
-        A.sym_t = A.sym_s = A.partial = A.vel_tmp = A.vel_tmp2 = nullptr;
+        cudaFree(A.lx);
+        cudaFree(A.lv);
+        cudaFree(A.gbuf);
+        A.sym_t = A.sym_s = A.partial = A.vel_tmp = A.vel_tmp2 = A.lx = A.lv = A.gbuf = nullptr;
         A.sym = uses_sym(c);
         if (A.sym) {
             if ((st = nb::sym_vjp_plan(c->p.n, 0, 0, c->device, &A.splan)) ||
