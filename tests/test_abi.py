@@ -61,6 +61,24 @@ def test_create_rejects_bad_params(built, kw, status):
     assert N.lib().nb_last_error()
 
 
+@pytest.mark.parametrize("kw,status", [
+    (dict(eps2=float("inf")), N.NB_ERR_INVALID),
+    (dict(dt=float("nan")), N.NB_ERR_INVALID),
+    (dict(kick=3), N.NB_ERR_INVALID),
+    (dict(precision=N.NB_F64), N.NB_ERR_UNSUPPORTED),
+    (dict(algo=N.NB_ALGO_EXACT), N.NB_ERR_UNSUPPORTED),
+])
+def test_batch_create_rejects_bad_params(built, kw, status):
+    """Checked before any CUDA call, so this runs without a GPU."""
+    p = _params(**kw)
+    sizes = (C.c_int * 2)(16, 40)
+    h = C.c_void_p()
+    rc = N.lib().nb_batch_create(C.byref(p), 2, sizes, C.byref(h))
+    assert rc == status
+    assert h.value is None
+    assert N.lib().nb_last_error()
+
+
 def test_null_handles_are_rejected(built):
     lib = N.lib()
     assert lib.nb_step(None, 1, None) == N.NB_ERR_INVALID

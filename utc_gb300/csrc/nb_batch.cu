@@ -751,6 +751,9 @@ struct nb_batch {
     int graph_steps = 0, graph_cur = -1;
     // scratch of the per-system baseline (target-side and source-side)
     float4 *sys_partial = nullptr, *sys_spart = nullptr;
+    // plan, scratch and device tables agree; false after a failed plan change
+    // (launches then refuse to run rather than use a stale or NULL scratch)
+    bool plan_ok = false;
     // adjoint: VJP plan (own iteration tables), checkpoints, reverse buffers
     BatchPlan vplan;
     long long *d_it_off_v = nullptr;
@@ -817,6 +820,14 @@ static int batch_apply_plan(nb_batch *b, int wpb, int bpt, cudaStream_t s)
     std::vector<int> tb_off;
     int st = batch_plan_for(b, wpb, bpt, &p, &it_off, &tb_off, &sp_off);
     if (st) return st;
+    // from here on the scratch, the tables or both change: the captured graph
+    // (its arguments) and the old plan are void until this call succeeds
+    b->plan_ok = false;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        b->graph_cur = -1;
+    }
     const size_t need = (size_t)p.slots * 32 * bpt;
     if (need > b->partial_cap) {
         cudaFree(b->partial);
@@ -843,11 +854,7 @@ static int batch_apply_plan(nb_batch *b, int wpb, int bpt, cudaStream_t s)
                             cudaMemcpyHostToDevice, s));
     NB_CUDA(cudaStreamSynchronize(s));
     b->plan = p;
-    if (b->graph) {
-        cudaGraphExecDestroy(b->graph);
-        b->graph = nullptr;
-        b->graph_cur = -1;
-    }
+    b->plan_ok = true;
     return NB_OK;
 }
 
@@ -879,6 +886,8 @@ static int batch_force(nb_batch *b, const float4 *po, cudaStream_t s)
 {
     const BatchPlan &p = b->plan;
     if (b->nbody == 0) return NB_OK;
+    if (!b->plan_ok)
+        return set_error(NB_ERR_STATE, "batch has no valid launch plan (a plan change or autotune failed)");
     if (b->sym) {
         nb::bks_kernel_t k = nb::bks_kernel_for(p.wpb, p.bpt);
         k<<<p.grid, 32 * p.wpb, 0, s>>>(po, batch_sym_dev(b), (float)b->p.eps2, b->partial, b->spart,
@@ -899,6 +908,8 @@ static int batch_integrate(nb_batch *b, const float4 *po, float4 *pn, float4 *ve
 {
     const BatchPlan &p = b->plan;
     if (b->nbody == 0) return NB_OK;
+    if (!b->plan_ok)
+        return set_error(NB_ERR_STATE, "batch has no valid launch plan (a plan change or autotune failed)");
     if (b->sym) {
         nb::bks_integrate_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
             po, pn, vel, b->partial, b->spart, batch_sym_dev(b), b->nbody, 32 * p.bpt, p.total,
@@ -1047,6 +1058,8 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
         return set_error(NB_ERR_UNSUPPORTED, "batches run NB_F32 with the fast or symmetric algorithm");
     if (p->kick != NB_KICK_REFERENCE && p->kick != NB_KICK_PHYSICAL)
         return set_error(NB_ERR_INVALID, "unknown kick mode");
+    if (!std::isfinite(p->eps2) || !std::isfinite(p->damping) || !std::isfinite(p->dt) || !std::isfinite(p->G))
+        return set_error(NB_ERR_INVALID, "eps2, damping, dt and G must be finite");
     long long nbody = 0;
     for (int s = 0; s < nsys; ++s) {
         if (sizes[s] < 1) return set_error(NB_ERR_INVALID, "every system needs at least one body");
@@ -1263,7 +1276,7 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
         std::map<int, int> hist;
         for (int n : b->sizes) {
             int lg = 0;
-            while ((1 << (lg + 1)) <= n) ++lg;
+            while ((2LL << lg) <= n) ++lg;
             hist[lg]++;
         }
         for (auto &h : hist) key << h.first << ":" << h.second << ",";
@@ -1320,7 +1333,8 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
     else
         for (auto &c : cand_dir) cands.push_back({c[0], c[1]});
     float best = 1e30f;
-    int bw = b->plan.wpb, bb = b->plan.bpt;
+    const int w0 = b->plan.wpb, b0 = b->plan.bpt;
+    int bw = w0, bb = b0;
     int st = NB_OK;
     for (auto &c : cands) {
         if ((st = batch_apply_plan(b, c[0], c[1], s))) break;
@@ -1343,6 +1357,7 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
         }
     }
     if (!st) st = batch_apply_plan(b, bw, bb, s);
+    if (st) batch_apply_plan(b, w0, b0, s);  // back to the plan from before, if it still fits
     if (sb) {  // the candidates' steps are undone
         b->cur = 0;
         cudaMemcpyAsync(b->pos[0], save_p, sb, cudaMemcpyDeviceToDevice, s);
