@@ -285,3 +285,43 @@ def test_batch_run_inside_a_callers_graph_capture(cuda, algo):
         torch.cuda.synchronize()
         got = b.get_state()
     assert got[0].tobytes() == want[0].tobytes()
+
+
+def test_python_layer_checks_device_buffers(cuda):
+    """Device tensors of the wrong shape are refused before any copy (the C
+    ABI copies whole buffers by the context's size); a tensor of another
+    dtype is converted and gives the same state as the exact dtype."""
+    import torch
+
+    n = 300
+    p64, v64 = ics.plummer(n, seed=11)
+    with NBodySystem(n, "f64", "sym", kick="physical", eps2=1e-3, damping=1.0, dt=1e-3) as s:
+        s.set_state(torch.from_numpy(p64).cuda(), torch.from_numpy(v64).cuda())
+        want = s.get_state()
+        s.set_state(torch.from_numpy(p64).float().cuda(), torch.from_numpy(v64).float().cuda())
+        got = s.get_state()
+        assert np.array_equal(got[0], p64.astype(np.float32).astype(np.float64))
+        with pytest.raises(ValueError):
+            s.set_state(torch.zeros((n - 1, 4), dtype=torch.float64, device="cuda"),
+                        torch.zeros((n - 1, 4), dtype=torch.float64, device="cuda"))
+        with pytest.raises(ValueError):
+            s.get_state_device(torch.empty((n, 4), dtype=torch.float32, device="cuda"),
+                               torch.empty((n, 4), dtype=torch.float32, device="cuda"))
+        pt = torch.empty((n, 4), dtype=torch.float64, device="cuda")
+        vt = torch.empty_like(pt)
+        s.set_state(torch.from_numpy(p64).cuda(), torch.from_numpy(v64).cuda())
+        s.get_state_device(pt, vt)
+        torch.cuda.synchronize()
+        assert np.array_equal(pt.cpu().numpy(), want[0])
+    with NBodySystem(n, "f32", "sym", kick="physical", eps2=np.float32(1e-3), damping=1.0,
+                     dt=np.float32(1e-3)) as s:
+        s.set_state(ics.f32(p64), ics.f32(v64))
+        s.adj_forward(4, 2)
+        g = torch.randn((n, 4), device="cuda") * 1e-3
+        a = [t.clone() for t in s.adj_backward(g)]
+        b = s.adj_backward(g.double())
+        assert all(torch.equal(x, y) for x, y in zip(a, b))
+        with pytest.raises(ValueError):
+            s.adj_backward(torch.zeros((n, 3), device="cuda"))
+        with pytest.raises(ValueError):
+            s.adj_backward(g.cpu())

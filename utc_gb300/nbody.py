@@ -36,6 +36,19 @@ def _is_torch(x):
     return type(x).__module__.startswith("torch")
 
 
+def _device_buffer(x, shape, dtype, name):
+    """x as a contiguous CUDA tensor of exactly `shape` and `dtype` (converted
+    if only the dtype or the layout differ).  The C ABI copies whole buffers
+    by the context's size: a tensor of another size would be read or written
+    past its end, so that is refused here."""
+    torch = _torch()
+    if not _is_torch(x) or not x.is_cuda:
+        raise ValueError(f"{name}: needs a CUDA tensor")
+    if tuple(x.shape) != tuple(shape):
+        raise ValueError(f"{name}: needs shape {tuple(shape)}, got {tuple(x.shape)}")
+    return x.to(dtype).contiguous()
+
+
 class NBodySystem:
     def __init__(self, n, precision="f32", algo="fast", kick="reference", eps2=0.00125,
                  damping=0.995, dt=0.016, G=1.0, block=0, bpt=0, ctas_per_sm=0,
@@ -77,19 +90,26 @@ class NBodySystem:
         self.close()
 
     # ------------------------------------------------------------------
-    def _buf(self, x):
+    def _torch_dtype(self):
+        torch = _torch()
+        return torch.float64 if self.dtype == np.float64 else torch.float32
+
+    def _buf(self, x, name):
         if _is_torch(x):
-            assert x.is_cuda and x.is_contiguous() and x.shape == (self.n, 4)
-            return C.c_void_p(x.data_ptr()), N.NB_DEVICE, x
+            t = _device_buffer(x, (self.n, 4), self._torch_dtype(), name)
+            return C.c_void_p(t.data_ptr()), N.NB_DEVICE, t
         a = np.ascontiguousarray(x, dtype=self.dtype).reshape(self.n, 4)
         return a.ctypes.data_as(C.c_void_p), N.NB_HOST, a
 
     def set_state(self, pos, vel, stream=None):
-        pp, wp, keep_p = self._buf(pos)
-        vp, wv, keep_v = self._buf(vel)
-        assert wp == wv, "pos and vel must both be host or both be device buffers"
+        pp, wp, keep_p = self._buf(pos, "pos")
+        vp, wv, keep_v = self._buf(vel, "vel")
+        if wp != wv:
+            raise ValueError("pos and vel must both be host or both be device buffers")
         s = current_stream_handle() if stream is None else stream
         N.check(self.lib.nb_set_state(self.handle, pp, vp, wp, C.c_void_p(s)), "nb_set_state")
+        if wp == N.NB_DEVICE and (keep_p is not pos or keep_v is not vel):
+            _torch().cuda.synchronize()  # the copies read converted temporaries
         del keep_p, keep_v
 
     def get_state(self, stream=None):
@@ -102,6 +122,13 @@ class NBodySystem:
         return pos, vel
 
     def get_state_device(self, pos_t, vel_t, stream=None):
+        """Copy the state into the CUDA tensors pos_t, vel_t ((n, 4), the
+        context's host dtype, contiguous: they are written in place)."""
+        for t, name in ((pos_t, "pos_t"), (vel_t, "vel_t")):
+            if not (_is_torch(t) and t.is_cuda and t.is_contiguous() and tuple(t.shape) == (self.n, 4)
+                    and t.dtype == self._torch_dtype()):
+                raise ValueError(f"{name}: needs a contiguous CUDA tensor of shape ({self.n}, 4) "
+                                 f"and dtype {self._torch_dtype()}")
         s = current_stream_handle() if stream is None else stream
         N.check(self.lib.nb_get_state(self.handle, C.c_void_p(pos_t.data_ptr()),
                                       C.c_void_p(vel_t.data_ptr()), N.NB_DEVICE, C.c_void_p(s)),
@@ -167,21 +194,21 @@ class NBodySystem:
         gv0 = torch.zeros((self.n, 4), dtype=torch.float32, device="cuda")
         gm = torch.zeros((self.n,), dtype=torch.float32, device="cuda")
         s = current_stream_handle() if stream is None else stream
-        gx_T = gx_T.contiguous()
-        gv_ptr = C.c_void_p(gv_T.contiguous().data_ptr()) if gv_T is not None else C.c_void_p(0)
-        keep = gv_T.contiguous() if gv_T is not None else None
-        if keep is not None:
-            gv_ptr = C.c_void_p(keep.data_ptr())
-        N.check(self.lib.nb_adj_backward(self.handle, C.c_void_p(gx_T.data_ptr()), gv_ptr,
+        gx = _device_buffer(gx_T, (self.n, 4), torch.float32, "gx_T")
+        gv = _device_buffer(gv_T, (self.n, 4), torch.float32, "gv_T") if gv_T is not None else None
+        gv_ptr = C.c_void_p(gv.data_ptr()) if gv is not None else C.c_void_p(0)
+        N.check(self.lib.nb_adj_backward(self.handle, C.c_void_p(gx.data_ptr()), gv_ptr,
                                          C.c_void_p(gx0.data_ptr()), C.c_void_p(gv0.data_ptr()),
                                          C.c_void_p(gm.data_ptr()), C.c_void_p(s)),
                 "nb_adj_backward")
+        if gx is not gx_T or (gv is not None and gv is not gv_T):
+            torch.cuda.synchronize()  # the pass read converted temporaries
         return gx0, gv0, gm
 
     def run_host(self, pos, vel, loops, out_interval, stream=None):
         """Task-style run with host buffers; returns (frames (k, n, 4), timings[4])."""
-        pos = np.ascontiguousarray(pos, dtype=self.dtype)
-        vel = np.ascontiguousarray(vel, dtype=self.dtype)
+        pos = np.ascontiguousarray(pos, dtype=self.dtype).reshape(self.n, 4)
+        vel = np.ascontiguousarray(vel, dtype=self.dtype).reshape(self.n, 4)
         k = loops // out_interval if out_interval > 0 else 0
         out = np.zeros((max(k, 1), self.n, 4), self.dtype)
         t = (C.c_double * 4)()
@@ -259,10 +286,15 @@ class NBodyBatch:
 
     def set_state(self, pos, vel, stream=None):
         s = current_stream_handle() if stream is None else stream
-        if _is_torch(pos):
-            N.check(self.lib.nb_batch_set_state(self.handle, C.c_void_p(pos.data_ptr()),
-                                                C.c_void_p(vel.data_ptr()), N.NB_DEVICE, C.c_void_p(s)),
+        if _is_torch(pos) or _is_torch(vel):
+            torch = _torch()
+            p = _device_buffer(pos, (self.nbody, 4), torch.float32, "pos")
+            v = _device_buffer(vel, (self.nbody, 4), torch.float32, "vel")
+            N.check(self.lib.nb_batch_set_state(self.handle, C.c_void_p(p.data_ptr()),
+                                                C.c_void_p(v.data_ptr()), N.NB_DEVICE, C.c_void_p(s)),
                     "nb_batch_set_state")
+            if p is not pos or v is not vel:
+                torch.cuda.synchronize()  # the copies read converted temporaries
             return
         pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(self.nbody, 4)
         vel = np.ascontiguousarray(vel, dtype=np.float32).reshape(self.nbody, 4)
@@ -320,13 +352,15 @@ class NBodyBatch:
         gv0 = torch.zeros((self.nbody, 4), dtype=torch.float32, device="cuda")
         gm = torch.zeros((self.nbody,), dtype=torch.float32, device="cuda")
         s = current_stream_handle() if stream is None else stream
-        gx_T = gx_T.contiguous()
-        gv_keep = gv_T.contiguous() if gv_T is not None else None
+        gx = _device_buffer(gx_T, (self.nbody, 4), torch.float32, "gx_T")
+        gv = _device_buffer(gv_T, (self.nbody, 4), torch.float32, "gv_T") if gv_T is not None else None
         N.check(self.lib.nb_batch_adj_backward(
-            self.handle, C.c_void_p(gx_T.data_ptr()),
-            C.c_void_p(gv_keep.data_ptr() if gv_keep is not None else 0),
+            self.handle, C.c_void_p(gx.data_ptr()),
+            C.c_void_p(gv.data_ptr() if gv is not None else 0),
             C.c_void_p(gx0.data_ptr()), C.c_void_p(gv0.data_ptr()), C.c_void_p(gm.data_ptr()),
             C.c_void_p(s)), "nb_batch_adj_backward")
+        if gx is not gx_T or (gv is not None and gv is not gv_T):
+            torch.cuda.synchronize()  # the pass read converted temporaries
         return gx0, gv0, gm
 
     def set_shape(self, warps_per_cta, bodies_per_lane):
