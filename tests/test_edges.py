@@ -325,3 +325,40 @@ def test_python_layer_checks_device_buffers(cuda):
             s.adj_backward(torch.zeros((n, 3), device="cuda"))
         with pytest.raises(ValueError):
             s.adj_backward(g.cpu())
+
+
+@pytest.mark.parametrize("prec,algo", MODES)
+def test_coincident_bodies_every_mode(cuda, prec, algo):
+    """Bodies at the same point (every body has a twin, three share one
+    point): with eps2 > 0 their pair terms are exactly 0 (r = 0) and every
+    acceleration stays finite and equal to the oracle's."""
+    base, _ = ics.plummer(300, seed=21)
+    pos = np.concatenate([base, base])
+    pos[7, :3] = pos[8, :3] = pos[9, :3]
+    pos[:, 3] = 1.0 / pos.shape[0]
+    dt = dtype_of(prec)
+    host = pos.astype(dt)
+    eps2 = 1e-3 if dt == np.float64 else np.float32(1e-3)
+    with NBodySystem(pos.shape[0], prec, algo, kick="physical", eps2=eps2, damping=1.0) as s:
+        s.set_state(host, np.zeros_like(host))
+        a = s.accel().astype(np.float64)
+    want = oracle.accel(host.astype(np.float64), float(eps2))
+    assert np.isfinite(a).all()
+    tol = 1e-12 if prec == "f64" else 1e-5
+    d = np.linalg.norm(a - want, axis=1)
+    w = np.linalg.norm(want, axis=1)
+    assert (d <= tol * (w + w.mean())).all()
+
+
+@pytest.mark.parametrize("prec,algo", MODES)
+def test_zero_softening_is_nan_like_the_reference(cuda, prec, algo):
+    """The reference sums over every j including i (bodysystem.cc:115-125,
+    bodysystem_kernel.cu:60-85), so with eps2 = 0 the self term is 0 * inf
+    and every acceleration is NaN; each mode gives the same."""
+    p, _ = ics.plummer(64, seed=1)
+    dt = dtype_of(prec)
+    host = p.astype(dt)
+    assert np.isnan(oracle.accel(host, 0.0)).all()
+    with NBodySystem(64, prec, algo, kick="physical", eps2=0.0, damping=1.0) as s:
+        s.set_state(host, np.zeros_like(host))
+        assert np.isnan(s.accel()).all()
