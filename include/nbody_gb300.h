@@ -41,6 +41,9 @@ extern "C" {
 
 #define NB_ABI_VERSION 1
 
+/* Largest system (and batch) size: indices stay within 32-bit arithmetic. */
+#define NB_MAX_BODIES (1 << 30)
+
 typedef enum {
     NB_OK = 0,
     NB_ERR_INVALID = 1,     /* bad argument */
@@ -88,7 +91,7 @@ typedef enum { NB_HOST = 0, NB_DEVICE = 1 } nb_where;
 typedef enum { NB_MEM_PAGEABLE = 0, NB_MEM_PINNED = 1, NB_MEM_UNIFIED = 2 } nb_memtype;
 
 typedef struct nb_params {
-    int n;            /* bodies, >= 0 */
+    int n;            /* bodies, 0 <= n <= 2^30 (NB_MAX_BODIES) */
     int precision;    /* nb_precision */
     int algo;         /* nb_algo */
     int kick;         /* nb_kick */

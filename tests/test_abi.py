@@ -45,6 +45,7 @@ def _params(**kw):
 
 @pytest.mark.parametrize("kw,status", [
     (dict(n=-1), N.NB_ERR_INVALID),
+    (dict(n=(1 << 30) + 1), N.NB_ERR_INVALID),
     (dict(n=8, precision=7), N.NB_ERR_INVALID),
     (dict(n=8, algo=9), N.NB_ERR_INVALID),
     (dict(n=8, kick=3), N.NB_ERR_INVALID),

@@ -118,7 +118,8 @@ static size_t state_bytes(const nb_ctx *c) { return (size_t)c->p.n * 4 * c->elem
 static int validate(const nb_params *p)
 {
     if (!p) return set_error(NB_ERR_INVALID, "params is NULL");
-    if (p->n < 0) return set_error(NB_ERR_INVALID, "n must be >= 0");
+    if (p->n < 0 || p->n > NB_MAX_BODIES)
+        return set_error(NB_ERR_INVALID, "n must be in [0, 2^30]");
     if (p->precision != NB_F32 && p->precision != NB_F64 && p->precision != NB_F32_COMP)
         return set_error(NB_ERR_INVALID, "unknown precision");
     if (p->algo != NB_ALGO_FAST && p->algo != NB_ALGO_EXACT && p->algo != NB_ALGO_SYM)

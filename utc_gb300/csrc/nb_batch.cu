@@ -1065,7 +1065,7 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
         if (sizes[s] < 1) return set_error(NB_ERR_INVALID, "every system needs at least one body");
         nbody += sizes[s];
     }
-    if (nbody > (1LL << 30)) return set_error(NB_ERR_INVALID, "batch too large");
+    if (nbody > NB_MAX_BODIES) return set_error(NB_ERR_INVALID, "batch too large (more than 2^30 bodies)");
     nb_batch *b = new nb_batch();
     b->p = *p;
     b->nsys = nsys;

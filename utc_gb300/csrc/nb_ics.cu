@@ -245,7 +245,7 @@ extern "C" int nb_ics_generate(int kind, int n, unsigned long long seed, double 
     if (kind < 0 || kind > 4)
         return nb::set_error(NB_ERR_INVALID,
                              "nb_ics_generate: kind is 0 (cube), 1 (Plummer), 2 (random), 3 (shell) or 4 (expand)");
-    if (n < 0) return nb::set_error(NB_ERR_INVALID, "nb_ics_generate: n must be >= 0");
+    if (n < 0 || n > NB_MAX_BODIES) return nb::set_error(NB_ERR_INVALID, "nb_ics_generate: n must be in [0, 2^30]");
     if (precision != NB_F32 && precision != NB_F64)
         return nb::set_error(NB_ERR_INVALID, "nb_ics_generate: precision is NB_F32 or NB_F64");
     if (n == 0) return NB_OK;
