@@ -75,10 +75,18 @@ typedef enum {
      * pair term is odd in r): 16 FP32 operations and one rsqrt per two
      * interactions.  Same per-pair terms as NB_ALGO_FAST, different summation
      * order; deterministic.  NB_F32, NB_F32_COMP (compensated partial sums)
-     * and NB_F64 (FP64 throughout, 1/sqrt from the FP64 approximation and two
-     * Newton steps: agrees with the FP64 reference to rounding, not bit for
-     * bit). */
-    NB_ALGO_SYM = 2
+     * and NB_F64: pair terms in float-float arithmetic on the FP32 pipe
+     * (positions scaled by powers of two and split exactly into three
+     * floats, error-free sums and products, one Halley step on the FP32
+     * rsqrt; chunk sums folded into FP64), within a few 1e-15 of the FP64
+     * reference, not bit for bit.  Range for NB_F64: eps2 >= 2^-100 max|x|^2
+     * and masses >= 2^-100 of the largest. */
+    NB_ALGO_SYM = 2,
+    /* NB_F64 only: the symmetric algorithm in FP64 arithmetic throughout
+     * (1/sqrt from the FP64 approximation and two Newton steps), within a
+     * few 1e-16 of the FP64 reference, any range; about 1/5.7 the speed of
+     * NB_ALGO_SYM on GB300's narrow FP64 pipe. */
+    NB_ALGO_SYM_FP64 = 3
 } nb_algo;
 
 typedef enum { NB_KICK_REFERENCE = 0, NB_KICK_PHYSICAL = 1 } nb_kick;

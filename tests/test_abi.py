@@ -52,6 +52,7 @@ def _params(**kw):
     (dict(n=8, memtype=5), N.NB_ERR_INVALID),
     (dict(n=8, dt=float("nan")), N.NB_ERR_INVALID),
     (dict(n=8, precision=N.NB_F64, algo=N.NB_ALGO_FAST), N.NB_ERR_UNSUPPORTED),
+    (dict(n=8, precision=N.NB_F32, algo=N.NB_ALGO_SYM_FP64), N.NB_ERR_UNSUPPORTED),
 ])
 def test_create_rejects_bad_params(built, kw, status):
     p = _params(**kw)

@@ -14,7 +14,7 @@ from utc_gb300.nbody import NBodyBatch, NBodySystem
 pytestmark = pytest.mark.gpu
 
 MODES = [("f32", "fast"), ("f32", "sym"), ("f32", "exact"), ("f64", "exact"), ("f64", "sym"),
-         ("f32comp", "fast"), ("f32comp", "sym")]
+         ("f64", "sym64"), ("f32comp", "fast"), ("f32comp", "sym")]
 
 
 def dtype_of(prec):

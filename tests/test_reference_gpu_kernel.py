@@ -152,7 +152,7 @@ def test_reference_kernel_f64_vs_exact_f64(ref_kernel, capsys):
     ms_ref = e0.elapsed_time(e1)
     p_ref = bufs[steps % 2].cpu().numpy()
     r_ref = n * n * steps / (ms_ref * 1e-3) / 1e9
-    for algo in ("exact", "sym"):
+    for algo in ("exact", "sym", "sym64"):
         with NBodySystem(n, "f64", algo, kick="reference", eps2=1e-4, damping=1.0, dt=1e-4) as sy:
             sy.set_state(p64, v64)
             sy.step(1)

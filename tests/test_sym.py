@@ -101,24 +101,86 @@ def test_sym_default_shape(cuda, n, shape):
     assert (info["block"], info["bpt"]) == shape
 
 
+F64_SYM = ["sym", "sym64"]  # float-float pair arithmetic; FP64 arithmetic throughout
+
+
+@pytest.mark.parametrize("algo", F64_SYM)
 @pytest.mark.parametrize("n", [1, 2, 33, 255, 256, 257, 1000, 2049, 5000])
-def test_sym_f64_accel_vs_oracle(cuda, n):
-    """FP64 symmetric kernel: accelerations within 1e-13 (|a| + mean|a|) of
-    the FP64 oracle (its 1/sqrt comes from the FP64 approximation refined by
-    two Newton steps; every other operation is FP64)."""
+def test_sym_f64_accel_vs_oracle(cuda, n, algo):
+    """Symmetric kernels for FP64 state: accelerations within 1e-13
+    (|a| + mean|a|) of the FP64 oracle -- the float-float kernel (exact
+    three-float position differences, error-free sums and products, a Halley
+    step on the FP32 rsqrt) and the FP64 one (FP64 rsqrt approximation and two
+    Newton steps)."""
     p, _ = ics.plummer(n, seed=n)
-    with NBodySystem(n, "f64", "sym", eps2=1e-3) as s:
+    with NBodySystem(n, "f64", algo, eps2=1e-3) as s:
         s.set_state(p, np.zeros_like(p))
         a = s.accel()
     assert close(a, oracle.accel(p, 1e-3), tol=1e-13)
 
 
+@pytest.mark.parametrize("algo", F64_SYM)
+def test_sym_f64_close_pairs_far_from_origin(cuda, algo):
+    """A dense core (radius 0.05) inside a halo, both 3.6e3 from the origin:
+    r = x_j - x_i of close pairs cancels all but the last 20 bits of the
+    coordinates, which a two-float position split would lose; the three-float
+    split keeps them."""
+    n = 4096
+    rng = np.random.default_rng(5)
+    p = np.empty((n, 4))
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    rad = np.where(np.arange(n) % 4 == 0, 0.05, 1.0) * rng.random(n) ** (1 / 3)
+    p[:, :3] = np.array([3.0e3, -2.0e3, 5.0e2]) + u * rad[:, None]
+    p[:, 3] = rng.uniform(0.5, 1.5, n) / n
+    with NBodySystem(n, "f64", algo, eps2=1e-4) as s:
+        s.set_state(p, np.zeros_like(p))
+        a = s.accel()
+    assert close(a, oracle.accel(p, 1e-4), tol=1e-13)
+
+
+@pytest.mark.parametrize("algo", F64_SYM)
+def test_sym_f64_si_units(cuda, algo):
+    """Planetary magnitudes in SI units (positions ~1e11 m, masses ~1e24 to
+    1e30 kg, eps2 = (1e7 m)^2): unscaled, the float-float kernel's inv^3
+    would underflow the float range; it scales positions and masses by powers
+    of two on the device each step and undoes that exactly."""
+    n = 1000
+    rng = np.random.default_rng(9)
+    p = np.empty((n, 4))
+    p[:, :3] = rng.normal(size=(n, 3)) * 1.5e11
+    p[:, 3] = 10.0 ** rng.uniform(24, 30, n)
+    with NBodySystem(n, "f64", algo, eps2=1e14, G=6.674e-11) as s:
+        s.set_state(p, np.zeros_like(p))
+        a = s.accel()
+    assert close(a, oracle.accel(p, 1e14), tol=1e-13)
+
+
+@pytest.mark.parametrize("algo", F64_SYM)
+def test_sym_f64_power_of_two_scale_invariance(cuda, algo):
+    """Positions x 2^10, masses x 2^5 and eps2 x 2^20 give the accelerations
+    x 2^-15 bit for bit: the float-float kernel works in units normalized by
+    powers of two, the FP64 kernel scales exactly."""
+    n = 777
+    p, _ = ics.plummer(n, seed=4)
+    q = p.copy()
+    q[:, :3] *= 2.0 ** 10
+    q[:, 3] *= 2.0 ** 5
+    out = []
+    for x, e in ((p, 1e-3), (q, 1e-3 * 2.0 ** 20)):
+        with NBodySystem(n, "f64", algo, eps2=e) as s:
+            s.set_state(x, np.zeros_like(x))
+            out.append(s.accel())
+    assert np.array_equal(out[1], out[0] * 2.0 ** -15)
+
+
+@pytest.mark.parametrize("algo", F64_SYM)
 @pytest.mark.parametrize("kick", ["reference", "physical"])
-def test_sym_f64_steps_vs_oracle(cuda, kick):
+def test_sym_f64_steps_vs_oracle(cuda, kick, algo):
     n, steps = 3000, 10
     p, v = ics.uniform_cube(n, seed=1)
     km = oracle.KICK_REFERENCE if kick == "reference" else oracle.KICK_PHYSICAL
-    with NBodySystem(n, "f64", "sym", kick=kick, eps2=1e-2, damping=0.999, dt=1e-3) as s:
+    with NBodySystem(n, "f64", algo, kick=kick, eps2=1e-2, damping=0.999, dt=1e-3) as s:
         s.set_state(p, v)
         s.step(steps)
         got, gv = s.get_state()
@@ -135,9 +197,9 @@ def test_gpu_scale_positions_after_100_steps_vs_fp64(cuda):
     """The GPU-scale workload as the bench runs it (N=65536 Plummer,
     eps2 = dt = 1e-4, 100 leapfrog steps): float positions from the symmetric
     and directed kernels within 1e-5 (|x| + 0.1) of an FP64 run of the same
-    float-rounded start.  The FP64 run is the FP64 symmetric kernel, itself
-    held to 1e-13 of the FP64 oracle (test_sym_f64_*); the CPU oracle would
-    need minutes for this size."""
+    float-rounded start.  The FP64 run is the float-float symmetric kernel
+    for FP64 state, itself held to 1e-13 of the FP64 oracle (test_sym_f64_*);
+    the CPU oracle would need minutes for this size."""
     n, steps = 65536, 100
     p, v = ics.plummer(n, seed=0)
     p32, v32 = ics.f32(p), ics.f32(v)

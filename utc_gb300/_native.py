@@ -17,7 +17,7 @@ HEADER = os.path.join(REPO, "include", "nbody_gb300.h")
 
 NB_OK, NB_ERR_INVALID, NB_ERR_CUDA, NB_ERR_OOM, NB_ERR_STATE, NB_ERR_UNSUPPORTED, NB_ERR_TIMEOUT = range(7)
 NB_F32, NB_F64, NB_F32_COMP = 0, 1, 2
-NB_ALGO_FAST, NB_ALGO_EXACT, NB_ALGO_SYM = 0, 1, 2
+NB_ALGO_FAST, NB_ALGO_EXACT, NB_ALGO_SYM, NB_ALGO_SYM_FP64 = 0, 1, 2, 3
 NB_KICK_REFERENCE, NB_KICK_PHYSICAL = 0, 1
 NB_HOST, NB_DEVICE = 0, 1
 NB_MEM_PAGEABLE, NB_MEM_PINNED, NB_MEM_UNIFIED = 0, 1, 2

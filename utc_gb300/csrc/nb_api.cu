@@ -81,6 +81,10 @@ struct nb_ctx {
     // symmetric algorithm: plan and its two partial arrays
     nb::SymPlan splan;
     float4 *sym_t = nullptr, *sym_s = nullptr;
+    // float-float path for FP64 state: scaled three-float positions (3 n
+    // float4) and the per-step scale record
+    float4 *ff_split = nullptr;
+    unsigned long long *ff_range = nullptr;
     // nb_step on a capturable stream replays a CUDA graph of kGraphSteps
     // steps (one per starting ping-pong buffer): small systems are otherwise
     // bound by the per-kernel launch cost
@@ -122,8 +126,11 @@ static int validate(const nb_params *p)
         return set_error(NB_ERR_INVALID, "n must be in [0, 2^30]");
     if (p->precision != NB_F32 && p->precision != NB_F64 && p->precision != NB_F32_COMP)
         return set_error(NB_ERR_INVALID, "unknown precision");
-    if (p->algo != NB_ALGO_FAST && p->algo != NB_ALGO_EXACT && p->algo != NB_ALGO_SYM)
+    if (p->algo != NB_ALGO_FAST && p->algo != NB_ALGO_EXACT && p->algo != NB_ALGO_SYM &&
+        p->algo != NB_ALGO_SYM_FP64)
         return set_error(NB_ERR_INVALID, "unknown algo");
+    if (p->algo == NB_ALGO_SYM_FP64 && p->precision != NB_F64)
+        return set_error(NB_ERR_UNSUPPORTED, "NB_ALGO_SYM_FP64 is for NB_F64 state");
     if (p->kick != NB_KICK_REFERENCE && p->kick != NB_KICK_PHYSICAL)
         return set_error(NB_ERR_INVALID, "unknown kick mode");
     if (p->memtype < NB_MEM_PAGEABLE || p->memtype > NB_MEM_UNIFIED)
@@ -182,6 +189,8 @@ static void free_ctx(nb_ctx *c)
     if (c->adj.ev_go) cudaEventDestroy(c->adj.ev_go);
     cudaFree(c->sym_t);
     cudaFree(c->sym_s);
+    cudaFree(c->ff_split);
+    cudaFree(c->ff_range);
     for (int k = 0; k < 2; ++k) {
         cudaFree(c->snap[k]);
         cudaFreeHost(c->stage[k]);
@@ -209,7 +218,12 @@ static bool uses_sym(const nb_ctx *c) { return c->p.precision == NB_F32 && c->p.
 // compensated context stepping with the compensated symmetric kernel
 static bool comp_sym(const nb_ctx *c) { return c->p.precision == NB_F32_COMP && c->p.algo == NB_ALGO_SYM; }
 // FP64 context stepping with the FP64 symmetric kernel
-static bool f64_sym(const nb_ctx *c) { return c->p.precision == NB_F64 && c->p.algo == NB_ALGO_SYM; }
+static bool f64_sym(const nb_ctx *c)
+{
+    return c->p.precision == NB_F64 && (c->p.algo == NB_ALGO_SYM || c->p.algo == NB_ALGO_SYM_FP64);
+}
+// FP64 state stepped by the float-float symmetric kernel (NB_ALGO_SYM)
+static bool ff_sym(const nb_ctx *c) { return c->p.precision == NB_F64 && c->p.algo == NB_ALGO_SYM; }
 // the directed stream-K plan (c->plan) also serves the symmetric context's
 // energy pass and adjoint
 static bool uses_fast(const nb_ctx *c)
@@ -287,7 +301,10 @@ int nb_create(const nb_params *p, nb_ctx **out)
         return st;
     }
     if (f64_sym(c) &&
-        ((st = nb::sym64_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan)) ||
+        ((st = ff_sym(c) ? nb::symff_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan)
+                         : nb::sym64_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan)) ||
+         (ff_sym(c) && (st = dev_alloc((void **)&c->ff_split, 3 * n * sizeof(float4), "split positions allocation"))) ||
+         (ff_sym(c) && (st = dev_alloc((void **)&c->ff_range, 2 * sizeof(unsigned long long), "scale record allocation"))) ||
          (st = dev_alloc((void **)&c->sym_t, (size_t)c->splan.slots * c->splan.rb * sizeof(double4),
                          "symmetric scratch allocation")) ||
          (st = dev_alloc((void **)&c->sym_s, (size_t)c->splan.spart_size * sizeof(double4),
@@ -433,12 +450,15 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
         return st;  // positions are updated in place: no ping-pong
     }
     if (f64_sym(c)) {
-        st = nb::sym64_force(c->splan, (const double4 *)po, p.eps2, (double4 *)c->sym_t, (double4 *)c->sym_s, s);
+        st = ff_sym(c) ? nb::symff_force(c->splan, (const double4 *)po, p.eps2, c->ff_split, c->ff_range,
+                                         (double4 *)c->sym_t, (double4 *)c->sym_s, s)
+                       : nb::sym64_force(c->splan, (const double4 *)po, p.eps2, (double4 *)c->sym_t,
+                                         (double4 *)c->sym_s, s);
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
         if (!st)
             st = nb::sym64_integrate(c->splan, (const double4 *)po, (double4 *)pn, (double4 *)c->vel,
                                      (const double4 *)c->sym_t, (const double4 *)c->sym_s, p.damping, p.dt,
-                                     p.kick, p.G, (double4 *)acc_out, s);
+                                     p.kick, p.G, (double4 *)acc_out, s, ff_sym(c) ? c->ff_range : nullptr);
     } else if (p.precision == NB_F64) {
         st = nb::exact_step_f64(p.n, (const double4 *)po, (double4 *)pn, (double4 *)c->vel, p.eps2,
                                 p.damping, p.dt, p.kick, p.G, (double4 *)acc_out, p.block, s);
@@ -876,6 +896,7 @@ int nb_launches_per_step(nb_ctx *c)
 {
     if (!c) return -1;
     if (c->p.n == 0) return 0;
+    if (ff_sym(c)) return 4;  // scale reduction, split, force, integrate
     return (uses_fast(c) || is_comp(c) || f64_sym(c)) ? 2 : 1;
 }
 

@@ -210,6 +210,7 @@ struct SymPlan {
     int grid = 0;
     int slots = 0;       // grid + nrb - 1 target-side slots of rb float4
     long long spart_size = 0;  // float4 entries of the source-side array
+    int sms = 0;         // SMs of the device planned for
 };
 // float4 entries of the source-side array for row blocks of rb bodies
 inline long long sym_spart_entries(int n, int rb)
@@ -228,13 +229,21 @@ int sym_integrate(const SymPlan &p, const float4 *pos_old, float4 *pos_new, floa
                   const float4 *tpart, const float4 *spart, float damping, float dt, int kick,
                   float G, float4 *acc_out, cudaStream_t s);
 
-// FP64 symmetric path (nb_sym64.cu): tpart / spart hold double4 entries
+// FP64 symmetric path (nb_sym64.cu): tpart / spart hold double4 entries.
+// sym64_integrate with ffrange (the float-float path's scale record) undoes
+// that path's power-of-two scaling of the sums.
 int sym64_plan(int n, int warps, int bpt, int device, SymPlan *pl);
 int sym64_force(const SymPlan &p, const double4 *pos, double eps2, double4 *tpart, double4 *spart,
                 cudaStream_t s);
 int sym64_integrate(const SymPlan &p, const double4 *pos_old, double4 *pos_new, double4 *vel,
                     const double4 *tpart, const double4 *spart, double damping, double dt, int kick,
-                    double G, double4 *acc_out, cudaStream_t s);
+                    double G, double4 *acc_out, cudaStream_t s, const unsigned long long *ffrange = nullptr);
+// Float-float symmetric path for FP64 state (nb_symff.cu): same layout and
+// double4 partials as the FP64 path; `split` holds 3 n float4 (the scaled
+// three-float positions), `range` 2 unsigned long long (the scale record).
+int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl);
+int symff_force(const SymPlan &p, const double4 *pos, double eps2, float4 *split, unsigned long long *range,
+                double4 *tpart, double4 *spart, cudaStream_t s);
 
 // Compensated kick / drift from compensated symmetric partials, or
 // (acc_out != nullptr) the bare FP64 accelerations (nb_precision.cu)

@@ -143,7 +143,8 @@ __global__ void sym64_integrate_kernel(const double4 *__restrict__ pos_old, doub
                                        double4 *__restrict__ vel, const double4 *__restrict__ tpart,
                                        const double4 *__restrict__ spart, int n, int rb, int nc, int nrb,
                                        long long total, int grid, double damping, double dt, int kick,
-                                       double G, double4 *__restrict__ acc_out)
+                                       double G, double4 *__restrict__ acc_out,
+                                       const unsigned long long *__restrict__ ffrange)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -166,6 +167,19 @@ __global__ void sym64_integrate_kernel(const double4 *__restrict__ pos_old, doub
         ax = __dadd_rn(ax, q.x);
         ay = __dadd_rn(ay, q.y);
         az = __dadd_rn(az, q.z);
+    }
+    if (ffrange) {
+        // float-float path: its sums are in units scaled by 2^kx (positions)
+        // and 2^km (masses), kx = -e(max |x|), km = -e(max m) with
+        // 2^(e-1) <= v < 2^e; a = a_scaled * 2^(2 kx - km), exact
+        auto ex = [](unsigned long long b) {
+            const int f = (int)((b >> 52) & 0x7ff);
+            return (f == 0 || f == 0x7ff) ? 0 : f - 1022;
+        };
+        const int k = ex(ffrange[1]) - 2 * ex(ffrange[0]);
+        ax = ldexp(ax, k);
+        ay = ldexp(ay, k);
+        az = ldexp(az, k);
     }
     if (acc_out) {
         acc_out[i] = make_double4(ax, ay, az, 0.0);
@@ -256,12 +270,12 @@ int sym64_force(const SymPlan &p, const double4 *pos, double eps2, double4 *tpar
 
 int sym64_integrate(const SymPlan &p, const double4 *pos_old, double4 *pos_new, double4 *vel,
                     const double4 *tpart, const double4 *spart, double damping, double dt, int kick,
-                    double G, double4 *acc_out, cudaStream_t s)
+                    double G, double4 *acc_out, cudaStream_t s, const unsigned long long *ffrange)
 {
     if (p.n == 0) return NB_OK;
     sym64_integrate_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(pos_old, pos_new, vel, tpart, spart, p.n, p.rb,
                                                              p.nc, p.nrb, p.total, p.grid, damping, dt, kick,
-                                                             G, acc_out);
+                                                             G, acc_out, ffrange);
     NB_LAUNCH_CHECK("sym64_integrate_kernel launch");
     return NB_OK;
 }

@@ -1,0 +1,421 @@
+// nb_symff.cu -- FP64-accurate symmetric step in float-float arithmetic
+// (NB_F64 with NB_ALGO_SYM).
+//
+// The app's default state type is double (benchapps/nbody/utc/nbody_main.cc
+// FTYPE), and the reference evaluates every ordered pair in FP64
+// (benchapps/nbody/cuda/bodysystem_kernel.cu:21-56).  On GB300 the FP64 pipe
+// runs at about 1/76 of the FP32 rate (measured: 1.06 TFLOP/s DFMA against
+// 78.5 TFLOP/s FFMA), so the FP64 symmetric kernel (nb_sym64.cu) is held to
+// some 45 G interactions/s however it is arranged.  This kernel gets FP64
+// accuracy from the FP32 pipe instead, with the standard float-float
+// (double-single) techniques:
+//  * error-free sums: Knuth's two-sum (s + e == a + b exactly) and Dekker's
+//    fast two-sum for |a| >= |b|;
+//  * error-free products from the FMA: p = a*b, e = fma(a, b, -p);
+//  * float-float numbers hi + lo with |lo| <= ulp(hi)/2, about 48 bits.
+// Per step, positions and masses are scaled by exact powers of two (the
+// largest coordinate and the largest mass into [1/2, 1), found by a
+// reduction on the device) and split into three floats, h + m + l == x
+// exactly.  Per unordered pair (the symmetric layout of nb_sym.cu: row
+// blocks of 32*BPT targets per warp x 32-body chunks, the chunk rotating
+// through the warp with its reaction):
+//  * r = x_j - x_i: two-sums of the high and of the middle parts, the low
+//    parts' rounded difference, normalized to a float-float -- as accurate
+//    as FP64's own difference, also for close pairs far from the origin
+//    (a two-float split would lose the position bits below 2^-49 |x|);
+//  * d2 = |r|^2 + eps2 in float-float;
+//  * 1/sqrt(d2): the FP32 approximation y0 refined by one Halley step,
+//    y = y0 (1 + t/2 + 3t^2/8) with t = 1 - d2 y0^2 formed from an
+//    error-free y0^2 (cubic convergence: the approximation's 2^-23 becomes
+//    the arithmetic's 2^-48);
+//  * inv^3, the weights m_j inv^3 and m_i inv^3, and the six products with
+//    r in float-float; target and reaction sums in float-float, renormalized
+//    after every term.
+// Each target's 32-source chunk sum is folded into FP64 accumulators; each
+// reaction (one chunk body, the warp's 32*BPT targets) is written as FP64.
+// The FP64 integrator of nb_sym64.cu then sums the partials in FP64, undoes
+// the scaling and integrates.  246 FP32 operations and one approximation
+// per pair (123 per interaction); results within a few 1e-15 of the FP64
+// oracle (FP64 arithmetic: a few 1e-16), not bit-identical (NB_ALGO_EXACT is).
+// Range: the scaled squared distances and eps2 must stay normal floats:
+// eps2 >= 2^-100 max|x|^2 and body masses >= 2^-100 of the largest.
+#include "nb_internal.cuh"
+
+namespace nb {
+
+namespace {
+
+// Knuth's two-sum: s + e == a + b exactly.
+__device__ __forceinline__ void ff_two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Dekker's fast two-sum, exact when |a| >= |b| (or a == 0).
+__device__ __forceinline__ void ff_fast_two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+// r = s - p from three-float parts, as a normalized float-float: the high
+// and middle differences error-free, the low one rounded (2^-72 |x|).
+__device__ __forceinline__ void ff_diff(float sh, float sm, float sl, float ph, float pm, float pl, float &rh,
+                                        float &rl)
+{
+    float A, a, B, b, s1, e1;
+    ff_two_sum(sh, -ph, A, a);
+    ff_two_sum(sm, -pm, B, b);
+    const float C = __fsub_rn(sl, pl);
+    ff_two_sum(A, B, s1, e1);
+    const float t = __fadd_rn(__fadd_rn(e1, a), __fadd_rn(b, C));
+    ff_two_sum(s1, t, rh, rl);
+}
+
+// A += r * w (float-float, renormalized)
+__device__ __forceinline__ void ff_acc(float &Ah, float &Al, float rh, float rl, float wh, float wl)
+{
+    const float p = __fmul_rn(rh, wh);
+    float e = __fmaf_rn(rh, wh, -p);
+    e = __fmaf_rn(rh, wl, e);
+    e = __fmaf_rn(rl, wh, e);
+    float s, t;
+    ff_two_sum(Ah, p, s, t);
+    ff_fast_two_sum(s, __fadd_rn(Al, __fadd_rn(t, e)), Ah, Al);
+}
+
+struct FFPair {
+    float rxh, rxl, ryh, ryl, rzh, rzl;  // r = x_j - x_i
+    float wjh, wjl;                      // m_j inv^3 (weight on the target)
+    float wih, wil;                      // m_i inv^3 with m_i as passed (reaction)
+};
+
+// Pair pieces for source (sH, sM, sL) and target (p*), eps2 = eh + el.
+template <bool REACT>
+__device__ __forceinline__ void ff_pair(float4 sH, float4 sM, float4 sL, float pxh, float pxm, float pxl, float pyh,
+                                        float pym, float pyl, float pzh, float pzm, float pzl, float mih, float mil,
+                                        float eh, float el, FFPair &o)
+{
+    ff_diff(sH.x, sM.x, sL.x, pxh, pxm, pxl, o.rxh, o.rxl);
+    ff_diff(sH.y, sM.y, sL.y, pyh, pym, pyl, o.ryh, o.ryl);
+    ff_diff(sH.z, sM.z, sL.z, pzh, pzm, pzl, o.rzh, o.rzl);
+    // squares as (p, e) with p + e = r^2 to float-float accuracy
+    const float qx = __fmul_rn(o.rxh, o.rxh), qy = __fmul_rn(o.ryh, o.ryh), qz = __fmul_rn(o.rzh, o.rzh);
+    float ex = __fmaf_rn(o.rxh, o.rxh, -qx), ey = __fmaf_rn(o.ryh, o.ryh, -qy), ez = __fmaf_rn(o.rzh, o.rzh, -qz);
+    ex = __fmaf_rn(__fadd_rn(o.rxh, o.rxh), o.rxl, ex);
+    ey = __fmaf_rn(__fadd_rn(o.ryh, o.ryh), o.ryl, ey);
+    ez = __fmaf_rn(__fadd_rn(o.rzh, o.rzh), o.rzl, ez);
+    float S, t1, t2, t3;
+    ff_two_sum(eh, qx, S, t1);
+    ff_two_sum(S, qy, S, t2);
+    ff_two_sum(S, qz, S, t3);
+    const float L = __fadd_rn(__fadd_rn(__fadd_rn(el, ex), __fadd_rn(ey, ez)), __fadd_rn(__fadd_rn(t1, t2), t3));
+    float Dh, Dl;
+    ff_fast_two_sum(S, L, Dh, Dl);  // all terms >= 0: |S| >= |L|
+    // 1/sqrt(D): one Halley step from the FP32 approximation
+    const float y0 = rsqrt_approx(Dh);
+    const float q = __fmul_rn(y0, y0);
+    const float qe = __fmaf_rn(y0, y0, -q);
+    const float t = __fmul_rn(Dh, q);
+    float c = __fmaf_rn(Dh, q, -t);
+    c = __fmaf_rn(Dh, qe, c);
+    c = __fmaf_rn(Dl, q, c);
+    const float u = __fsub_rn(__fsub_rn(1.0f, t), c);  // 1 - t is exact (t near 1)
+    const float corr = __fmul_rn(y0, __fmul_rn(u, __fmaf_rn(0.375f, u, 0.5f)));
+    float yh, yl;
+    ff_fast_two_sum(y0, corr, yh, yl);
+    // inv^3 = y^3
+    const float p2 = __fmul_rn(yh, yh);
+    float e2 = __fmaf_rn(yh, yh, -p2);
+    e2 = __fmaf_rn(__fadd_rn(yh, yh), yl, e2);
+    const float p3 = __fmul_rn(p2, yh);
+    float e3 = __fmaf_rn(p2, yh, -p3);
+    e3 = __fmaf_rn(p2, yl, e3);
+    e3 = __fmaf_rn(e2, yh, e3);
+    float y3h, y3l;
+    ff_fast_two_sum(p3, e3, y3h, y3l);
+    // weights (mass as the float-float h + m of its split)
+    o.wjh = __fmul_rn(sH.w, y3h);
+    float we = __fmaf_rn(sH.w, y3h, -o.wjh);
+    we = __fmaf_rn(sH.w, y3l, we);
+    o.wjl = __fmaf_rn(sM.w, y3h, we);
+    if (REACT) {
+        o.wih = __fmul_rn(mih, y3h);
+        float wr = __fmaf_rn(mih, y3h, -o.wih);
+        wr = __fmaf_rn(mih, y3l, wr);
+        o.wil = __fmaf_rn(mil, y3h, wr);
+    }
+}
+
+// binary exponent e of a non-negative double given by its bits, with
+// 2^(e-1) <= v < 2^e; 0 for zero, subnormal, infinite or NaN values
+__device__ __forceinline__ int ff_exponent(unsigned long long bits)
+{
+    const int field = (int)((bits >> 52) & 0x7ff);
+    return (field == 0 || field == 0x7ff) ? 0 : field - 1022;
+}
+
+}  // namespace
+
+// range[0] = bits of max |coordinate|, range[1] = bits of max |mass| (non-
+// negative doubles order like their bit patterns); range zeroed beforehand.
+__global__ void ff_range_kernel(const double4 *__restrict__ pos, int n, unsigned long long *__restrict__ range)
+{
+    unsigned long long mc = 0, mm = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double4 q = pos[i];
+        const double c = fmax(fabs(q.x), fmax(fabs(q.y), fabs(q.z)));
+        const unsigned long long bc = (unsigned long long)__double_as_longlong(c);
+        const unsigned long long bm = (unsigned long long)__double_as_longlong(fabs(q.w));
+        mc = bc > mc ? bc : mc;
+        mm = bm > mm ? bm : mm;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long a = __shfl_xor_sync(0xffffffffu, mc, o);
+        const unsigned long long b = __shfl_xor_sync(0xffffffffu, mm, o);
+        mc = a > mc ? a : mc;
+        mm = b > mm ? b : mm;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&range[0], mc);
+        atomicMax(&range[1], mm);
+    }
+}
+
+// Scaled three-float split: H + M + L == x * 2^kx (coordinates) and
+// m * 2^km (mass) exactly.
+__global__ void ff_split_kernel(const double4 *__restrict__ pos, int n, const unsigned long long *__restrict__ range,
+                                float4 *__restrict__ H, float4 *__restrict__ M, float4 *__restrict__ L)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int kx = -ff_exponent(range[0]), km = -ff_exponent(range[1]);
+    const double4 q = pos[i];
+    const double v[4] = {ldexp(q.x, kx), ldexp(q.y, kx), ldexp(q.z, kx), ldexp(q.w, km)};
+    float h[4], m[4], l[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        h[k] = __double2float_rn(v[k]);
+        const double r1 = v[k] - (double)h[k];  // exact
+        m[k] = __double2float_rn(r1);
+        l[k] = __double2float_rn(r1 - (double)m[k]);  // exact
+    }
+    H[i] = make_float4(h[0], h[1], h[2], h[3]);
+    M[i] = make_float4(m[0], m[1], m[2], m[3]);
+    L[i] = make_float4(l[0], l[1], l[2], l[3]);
+}
+
+template <int W, int BPT, int MINB>
+__global__ void __launch_bounds__(32 * W, MINB)
+    symff_force_kernel(const float4 *__restrict__ H, const float4 *__restrict__ Mi, const float4 *__restrict__ Lo,
+                       int n, double eps2, const unsigned long long *__restrict__ range,
+                       double4 *__restrict__ tpart, double4 *__restrict__ spart, long long total, int nc, int nrb)
+{
+    constexpr int WB = 32 * BPT;
+    constexpr int RB = W * WB;
+    constexpr int RC = RB / 32;
+    __shared__ __align__(16) float4 sH[32], sM[32], sL[32];
+    __shared__ double sF[3][W][32];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const int c = blockIdx.x;
+    // eps2 in the scaled units (x 2^(2 kx)), as a float-float
+    const double e2s = ldexp(eps2, -2 * ff_exponent(range[0]));
+    const float eh = __double2float_rn(e2s), el = __double2float_rn(e2s - (double)eh);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    long long it = sk_start(c, total, gridDim.x);
+    const long long end = sk_start(c + 1, total, gridDim.x);
+
+    while (it < end) {
+        const int I = sym_row_of(it, nc, RC, nrb);
+        const long long rfirst = sym_prefix(I, nc, RC);
+        const long long rend = sym_prefix(I + 1, nc, RC);
+        const long long seg_end = end < rend ? end : rend;
+        const int kc0 = I * RC + (int)(it - rfirst);
+        const int kc1 = I * RC + (int)(seg_end - rfirst);
+        const int tbase = I * RB + wid * WB;
+
+        // missing targets: zero mass, so their reactions are 0; masses
+        // negated: reactions point along -r
+        float pxh[BPT], pxm[BPT], pxl[BPT], pyh[BPT], pym[BPT], pyl[BPT], pzh[BPT], pzm[BPT], pzl[BPT];
+        float nmh[BPT], nml[BPT];
+        double ax[BPT], ay[BPT], az[BPT];
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const int i = tbase + lane + 32 * k;
+            const float4 a = i < n ? H[i] : zero;
+            const float4 m = i < n ? Mi[i] : zero;
+            const float4 b = i < n ? Lo[i] : zero;
+            pxh[k] = a.x; pxm[k] = m.x; pxl[k] = b.x;
+            pyh[k] = a.y; pym[k] = m.y; pyl[k] = b.y;
+            pzh[k] = a.z; pzm[k] = m.z; pzl[k] = b.z;
+            nmh[k] = -a.w; nml[k] = -m.w;
+            ax[k] = ay[k] = az[k] = 0.0;
+        }
+        for (int kc = kc0; kc < kc1; ++kc) {
+            const int jb = kc * 32;
+            const bool in = jb + lane < n;
+            __syncthreads();  // previous chunk: shared reads are done
+            if (wid == 0) {
+                // padding: far away (scaled coordinates are below 1), no mass
+                sH[lane] = in ? H[jb + lane] : make_float4(1.0e6f, 1.0e6f, 1.0e6f, 0.f);
+                sM[lane] = in ? Mi[jb + lane] : zero;
+                sL[lane] = in ? Lo[jb + lane] : zero;
+            }
+            __syncthreads();
+            float Axh[BPT], Axl[BPT], Ayh[BPT], Ayl[BPT], Azh[BPT], Azl[BPT];
+#pragma unroll
+            for (int k = 0; k < BPT; ++k) Axh[k] = Axl[k] = Ayh[k] = Ayl[k] = Azh[k] = Azl[k] = 0.f;
+            if (kc < (I + 1) * RC) {
+                // chunk inside the own row block: directed, target side only
+#pragma unroll 1
+                for (int j = 0; j < 32; ++j) {
+                    const float4 a = sH[j], am = sM[j], b = sL[j];
+#pragma unroll
+                    for (int k = 0; k < BPT; ++k) {
+                        FFPair w;
+                        ff_pair<false>(a, am, b, pxh[k], pxm[k], pxl[k], pyh[k], pym[k], pyl[k], pzh[k], pzm[k],
+                                       pzl[k], 0.f, 0.f, eh, el, w);
+                        ff_acc(Axh[k], Axl[k], w.rxh, w.rxl, w.wjh, w.wjl);
+                        ff_acc(Ayh[k], Ayl[k], w.ryh, w.ryl, w.wjh, w.wjl);
+                        ff_acc(Azh[k], Azl[k], w.rzh, w.rzl, w.wjh, w.wjl);
+                    }
+                }
+            } else {
+                float Fxh = 0.f, Fxl = 0.f, Fyh = 0.f, Fyl = 0.f, Fzh = 0.f, Fzl = 0.f;
+#pragma unroll 1
+                for (int r = 0; r < 32; ++r) {
+                    const int idx = (lane + r) & 31;
+                    const float4 a = sH[idx], am = sM[idx], b = sL[idx];
+#pragma unroll
+                    for (int k = 0; k < BPT; ++k) {
+                        FFPair w;
+                        ff_pair<true>(a, am, b, pxh[k], pxm[k], pxl[k], pyh[k], pym[k], pyl[k], pzh[k], pzm[k],
+                                      pzl[k], nmh[k], nml[k], eh, el, w);
+                        ff_acc(Axh[k], Axl[k], w.rxh, w.rxl, w.wjh, w.wjl);
+                        ff_acc(Ayh[k], Ayl[k], w.ryh, w.ryl, w.wjh, w.wjl);
+                        ff_acc(Azh[k], Azl[k], w.rzh, w.rzl, w.wjh, w.wjl);
+                        ff_acc(Fxh, Fxl, w.rxh, w.rxl, w.wih, w.wil);
+                        ff_acc(Fyh, Fyl, w.ryh, w.ryl, w.wih, w.wil);
+                        ff_acc(Fzh, Fzl, w.rzh, w.rzl, w.wih, w.wil);
+                    }
+                    const int from = (lane + 1) & 31;
+                    Fxh = __shfl_sync(0xffffffffu, Fxh, from);
+                    Fxl = __shfl_sync(0xffffffffu, Fxl, from);
+                    Fyh = __shfl_sync(0xffffffffu, Fyh, from);
+                    Fyl = __shfl_sync(0xffffffffu, Fyl, from);
+                    Fzh = __shfl_sync(0xffffffffu, Fzh, from);
+                    Fzl = __shfl_sync(0xffffffffu, Fzl, from);
+                }
+                // lane l now holds the reaction on chunk body l from this warp
+                const double fx = (double)Fxh + (double)Fxl, fy = (double)Fyh + (double)Fyl,
+                             fz = (double)Fzh + (double)Fzl;
+                const long long so = sym_soff(I, n, RB) + (jb + lane - (I + 1) * RB);
+                if (W == 1) {
+                    if (in) spart[so] = make_double4(fx, fy, fz, 0.0);
+                } else {
+                    sF[0][wid][lane] = fx;
+                    sF[1][wid][lane] = fy;
+                    sF[2][wid][lane] = fz;
+                    __syncthreads();
+                    if (wid == 0 && in) {
+                        double sx = 0.0, sy = 0.0, sz = 0.0;
+#pragma unroll
+                        for (int w = 0; w < W; ++w) {
+                            sx += sF[0][w][lane];
+                            sy += sF[1][w][lane];
+                            sz += sF[2][w][lane];
+                        }
+                        spart[so] = make_double4(sx, sy, sz, 0.0);
+                    }
+                }
+            }
+            // fold the chunk's sums into FP64
+#pragma unroll
+            for (int k = 0; k < BPT; ++k) {
+                ax[k] += (double)Axh[k] + (double)Axl[k];
+                ay[k] += (double)Ayh[k] + (double)Ayl[k];
+                az[k] += (double)Azh[k] + (double)Azl[k];
+            }
+        }
+        double4 *dst = tpart + (size_t)(c + I) * RB + wid * WB;
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) dst[lane + 32 * k] = make_double4(ax[k], ay[k], az[k], 0.0);
+        it = seg_end;
+    }
+}
+
+typedef void (*symff_kernel_t)(const float4 *, const float4 *, const float4 *, int, double,
+                               const unsigned long long *, double4 *, double4 *, long long, int, int);
+
+static symff_kernel_t symff_kernel_for(int w, int bpt)
+{
+    if (w == 1 && bpt == 2) return symff_force_kernel<1, 2, 16>;
+    if (w == 1 && bpt == 4) return symff_force_kernel<1, 4, 8>;
+    if (w == 4 && bpt == 4) return symff_force_kernel<4, 4, 2>;
+    if (w == 8 && bpt == 4) return symff_force_kernel<8, 4, 1>;
+    if (w == 8 && bpt == 8) return symff_force_kernel<8, 8, 1>;
+    return nullptr;
+}
+
+int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl)
+{
+    if (warps == 0 && bpt == 0) {
+        // one-warp CTAs x 2 targets (row block 64); then 1 x 4 (128), 4 x 4
+        // (512), 8 x 4 (1024), 8 x 8 (2048) while the source-side array
+        // (32 B entries) is over budget
+        static const int shapes[5][2] = {{1, 2}, {1, 4}, {4, 4}, {8, 4}, {8, 8}};
+        int s = 0;
+        while (s < 4 && sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) * (long long)sizeof(double4) >
+                            kSymSpartBudget)
+            ++s;
+        warps = shapes[s][0];
+        bpt = shapes[s][1];
+    }
+    symff_kernel_t k = symff_kernel_for(warps, bpt);
+    if (!k) return set_error(NB_ERR_UNSUPPORTED, "float-float symmetric kernel shape not compiled");
+    SymPlan p;
+    p.n = n;
+    p.warps = warps;
+    p.bpt = bpt;
+    p.rb = warps * 32 * bpt;
+    p.nc = (n + 31) / 32;
+    p.nrb = (n + p.rb - 1) / p.rb;
+    p.total = n > 0 ? sym_prefix(p.nrb, p.nc, p.rb / 32) : 0;
+    int sms = 0, occ = 0;
+    NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * warps, 0));
+    if (occ < 1) return set_error(NB_ERR_UNSUPPORTED, "float-float symmetric kernel does not fit on an SM");
+    long long grid = (long long)sms * occ;
+    if (p.total > 0 && grid > p.total) grid = p.total;
+    p.grid = p.total > 0 ? (int)grid : 0;
+    p.slots = p.total > 0 ? p.grid + p.nrb - 1 : 0;
+    p.spart_size = sym_spart_entries(n, p.rb);
+    p.sms = sms;
+    *pl = p;
+    return NB_OK;
+}
+
+int symff_force(const SymPlan &p, const double4 *pos, double eps2, float4 *split, unsigned long long *range,
+                double4 *tpart, double4 *spart, cudaStream_t s)
+{
+    if (p.n == 0) return NB_OK;
+    symff_kernel_t k = symff_kernel_for(p.warps, p.bpt);
+    if (!k) return set_error(NB_ERR_UNSUPPORTED, "float-float symmetric kernel shape not compiled");
+    float4 *H = split, *M = split + p.n, *L = split + 2 * (size_t)p.n;
+    NB_CUDA(cudaMemsetAsync(range, 0, 2 * sizeof(unsigned long long), s));
+    const long long want = (p.n + 255) / 256, cap = 4ll * (p.sms > 0 ? p.sms : 1);
+    const long long blocks = want < cap ? want : cap;
+    ff_range_kernel<<<(unsigned)blocks, 256, 0, s>>>(pos, p.n, range);
+    NB_LAUNCH_CHECK("ff_range_kernel launch");
+    ff_split_kernel<<<(unsigned)((p.n + 255) / 256), 256, 0, s>>>(pos, p.n, range, H, M, L);
+    NB_LAUNCH_CHECK("ff_split_kernel launch");
+    k<<<p.grid, 32 * p.warps, 0, s>>>(H, M, L, p.n, eps2, range, tpart, spart, p.total, p.nc, p.nrb);
+    NB_LAUNCH_CHECK("symff_force_kernel launch");
+    return NB_OK;
+}
+
+}  // namespace nb

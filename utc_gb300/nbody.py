@@ -15,7 +15,7 @@ import numpy as np
 from . import _native as N
 
 _PREC = {"f32": N.NB_F32, "f64": N.NB_F64, "f32comp": N.NB_F32_COMP}
-_ALGO = {"fast": N.NB_ALGO_FAST, "exact": N.NB_ALGO_EXACT, "sym": N.NB_ALGO_SYM}
+_ALGO = {"fast": N.NB_ALGO_FAST, "exact": N.NB_ALGO_EXACT, "sym": N.NB_ALGO_SYM, "sym64": N.NB_ALGO_SYM_FP64}
 _KICK = {"reference": N.NB_KICK_REFERENCE, "physical": N.NB_KICK_PHYSICAL}
 
 
