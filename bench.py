@@ -24,6 +24,13 @@ Extension workloads, one JSON line each (not the headline):
   --workload batched    512 Plummer systems, N log-uniform in [128, 16384],
                         eps2=1e-3, dt=1e-3, 50 steps: autotuned persistent
                         launch in a CUDA graph vs per-system launches
+  --workload double     the app's default state type: N=16384 Plummer in
+                        FP64, reference kick, eps2=dt=1e-4, 10 steps, through
+                        the float-float symmetric kernel (default), the FP64
+                        symmetric kernel and the reference-exact FP64 kernel:
+                        throughput, force error against the FP64 oracle
+                        (512-body subsample), final positions against the
+                        reference-exact run
 """
 from __future__ import annotations
 
@@ -493,6 +500,69 @@ def run_precision(args):
     return 0
 
 
+# FP32 pipe instructions per unordered pair of the float-float kernel (and
+# one rsqrt approximation): exact three-float differences 84, |r|^2 + eps2
+# 39, Halley step 14, inv^3 11, weights 8, six float-float accumulations 90
+FF_OPS_PER_PAIR = 246
+
+
+def run_double(args):
+    import oracle
+    from utc_gb300 import ics
+    from utc_gb300.nbody import NBodySystem, probe_fma_peak
+
+    n = args.n or 16384
+    steps = args.steps if args.steps_given else 10
+    eps2, dt = 1e-4, 1e-4
+    p64, v64 = ics.plummer(n, seed=3)
+    tidx = np.sort(np.random.default_rng(11).choice(n, min(512, n), replace=False)).astype(np.int32)
+    ref_a = oracle.accel_subset_f64(p64, tidx, eps2)
+    out = {"workload": "double", "n": n, "steps": steps, "eps2": eps2, "dt": dt, "kick": "reference",
+           "data": "synthetic (seeded Plummer sphere, float64)", "modes": {}}
+    final = {}
+    for algo in ("sym", "sym64", "exact"):
+        with NBodySystem(n, "f64", algo, kick="reference", eps2=eps2, damping=1.0, dt=dt) as s:
+            s.set_state(p64, v64)
+            a = s.accel()
+            s.step(2)  # warm-up
+            s.set_state(p64, v64)
+            f, g = s.step_timed(steps)
+            final[algo] = s.get_state()[0]
+            info = s.plan_info() if algo != "exact" else None
+        rate = float(n) ** 2 * steps / ((f + g) * 1e-3) / 1e9
+        fe = _body_rel(a[tidx], ref_a)
+        out["modes"][algo] = {"G_interactions_per_s": rate, "force_ms_per_step": f / steps,
+                              "integrate_ms_per_step": g / steps,
+                              "force_rel_max_vs_fp64_oracle": float(fe.max()),
+                              "force_rel_median_vs_fp64_oracle": float(np.median(fe)), "plan": info}
+    ex = final["exact"][:, :3]
+    scale = np.linalg.norm(ex, axis=1) + 0.1
+    for algo in ("sym", "sym64"):
+        out["modes"][algo]["pos_rel_max_vs_exact"] = float(
+            (np.linalg.norm(final[algo][:, :3] - ex, axis=1) / scale).max())
+    out["modes"]["sym"]["kernel"] = "symff_force_kernel (float-float on the FP32 pipe)"
+    out["modes"]["sym64"]["kernel"] = "sym64_force_kernel (FP64 pipe)"
+    out["modes"]["exact"]["kernel"] = "exact_step_kernel<double> (reference operation order)"
+    peak32, _ = probe_fma_peak(20000, True)
+    peak64, _ = probe_fma_peak(2000, packed=2)
+    ms = out["modes"]["sym"]["force_ms_per_step"]
+    # unordered pairs across row blocks, ordered pairs inside each row block
+    rb = out["modes"]["sym"]["plan"]["tbsize"]  # the row block
+    pairs = float(n) * n / 2 + float(n) * rb / 2
+    out["roofline"] = {"kernel": "symff_force_kernel", "bound": "fp32",
+                       "achieved": pairs * FF_OPS_PER_PAIR / (ms * 1e-3) / 1e12,
+                       "peak": peak32 / 2 / 1e12, "unit": "T FP32 instructions/s",
+                       "frac": pairs * FF_OPS_PER_PAIR / (ms * 1e-3) / (peak32 / 2),
+                       "ops_per_pair": FF_OPS_PER_PAIR,
+                       "note": "force ms per step includes the scale reduction and split kernels; peak = "
+                               "FP32 FMA probe rate in instructions (FLOP/2)"}
+    out["fp64_dfma_peak_tflops_probe"] = peak64 / 1e12
+    out["speedup_sym_vs_sym64"] = out["modes"]["sym"]["G_interactions_per_s"] / out["modes"]["sym64"][
+        "G_interactions_per_s"]
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_adjoint(args):
     import torch
 
@@ -726,7 +796,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "precision", "adjoint", "batched"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "precision", "adjoint", "batched", "double"])
     ap.add_argument("--algo", default="sym", choices=["fast", "sym"],
                     help="force algorithm (plain, adjoint and batched workloads)")
     ap.add_argument("--n", type=int, default=0, help="body count override for extension workloads")
@@ -742,6 +812,8 @@ def main():
         return run_adjoint(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "double":
+        return run_double(args)
     return run_ours(args)
 
 
