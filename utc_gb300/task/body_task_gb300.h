@@ -13,9 +13,11 @@
  *     copyin, copyout} seconds (body_task_sgpu.cu:40-137).
  * The work goes through the C ABI (include/nbody_gb300.h) on
  * UserTaskBase::__streamId.  Both state types run the symmetric kernel
- * (NB_ALGO_SYM) by default: in FP32 for T = float, in FP64 for T = double
- * (FP64-accurate, not bit-identical to the sequential reference;
- * setAlgo(NB_ALGO_EXACT) gives the reference-exact kernel).  `blocksize` is
+ * (NB_ALGO_SYM) by default: in FP32 for T = float; for T = double with
+ * FP64-accurate float-float pair terms on the FP32 pipe (not bit-identical
+ * to the sequential reference; setAlgo(NB_ALGO_SYM_FP64) keeps FP64
+ * arithmetic throughout, setAlgo(NB_ALGO_EXACT) gives the reference-exact
+ * kernel).  `blocksize` is
  * the CTA size of the exact kernel; the other kernels choose their own
  * launch shape.
  * Errors do not stop the process: the message goes to stderr (as the

@@ -8,8 +8,9 @@
  *   -b block size (exact kernel CTA size; N is rounded up to a multiple)
  * additions:
  *   -F  use float state (the reference fixes FTYPE=double at compile time)
- *   -a 0|1|2  force algorithm: 0 directed fast (float only), 1 reference-exact,
- *             2 symmetric (the default, float and double)
+ *   -a 0|1|2|3  force algorithm: 0 directed fast (float only), 1 reference-exact,
+ *             2 symmetric (the default; float-float pair terms for double),
+ *             3 symmetric in FP64 arithmetic throughout (double only)
  *
  * Bodies come from NbodyInit (SHELL), run through Task<BodySystemGB300<T>>,
  * frames go through Task<Output<T>>; timers are printed as the reference
