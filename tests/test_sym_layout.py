@@ -48,6 +48,7 @@ def spart_entries(n, rb):
 @pytest.mark.parametrize("n,rb,grid", [
     (1, 512, 1216), (31, 512, 1216), (512, 512, 8), (513, 512, 1216), (1000, 256, 7),
     (4097, 384, 300), (9000, 512, 1216), (20000, 2560, 304), (65536, 512, 1216), (70001, 640, 999),
+    (1000, 64, 2432), (4097, 128, 1216), (16384, 64, 2432), (3001, 1024, 152), (9000, 2048, 152),
 ])
 def test_symmetric_layout(n, rb, grid):
     rc = rb // 32
