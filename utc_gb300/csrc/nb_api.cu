@@ -619,7 +619,21 @@ int nb_energy(nb_ctx *c, double *out5, void *accphi_dev, void *stream)
     cudaStream_t s = (cudaStream_t)stream;
     const nb_params &p = c->p;
     int st;
-    if (p.precision == NB_F64) {
+    if (ff_sym(c)) {
+        // the float-float symmetric pass with the potential, summed and
+        // unscaled by the FP64 integrator into (acc, phi) per body
+        const double4 *pos = (const double4 *)c->pos[c->cur];
+        st = nb::symff_force(c->splan, pos, p.eps2, c->ff_split, c->ff_range, (double4 *)c->sym_t,
+                             (double4 *)c->sym_s, s, 1);
+        if (!st)
+            st = nb::sym64_integrate(c->splan, pos, nullptr, nullptr, (const double4 *)c->sym_t,
+                                     (const double4 *)c->sym_s, p.damping, p.dt, p.kick, p.G,
+                                     (double4 *)c->acc_tmp, s, c->ff_range);
+        if (!st)
+            st = nb::energy_reduce(p.n, nullptr, pos, nullptr, nullptr, nullptr,
+                                   (const double4 *)c->acc_tmp, p.G, c->e_blocks, c->e_out, s,
+                                   (const double4 *)c->vel);
+    } else if (p.precision == NB_F64) {
         const double4 *pos = (const double4 *)c->pos[c->cur];
         st = nb::energy_phi_f64(p.n, pos, p.eps2, (double4 *)c->acc_tmp, s);
         if (!st)

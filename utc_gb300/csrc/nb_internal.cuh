@@ -243,7 +243,7 @@ int sym64_integrate(const SymPlan &p, const double4 *pos_old, double4 *pos_new, 
 // three-float positions), `range` 2 unsigned long long (the scale record).
 int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl);
 int symff_force(const SymPlan &p, const double4 *pos, double eps2, float4 *split, unsigned long long *range,
-                double4 *tpart, double4 *spart, cudaStream_t s);
+                double4 *tpart, double4 *spart, cudaStream_t s, int phi = 0);
 
 // Compensated kick / drift from compensated symmetric partials, or
 // (acc_out != nullptr) the bare FP64 accelerations (nb_precision.cu)

@@ -153,12 +153,15 @@ __global__ void sym64_integrate_kernel(const double4 *__restrict__ pos_old, doub
     const int c0 = sk_owner(sym_prefix(I, nc, rc), total, grid);
     const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1, total, grid);
     const int li = i - I * rb;
-    double ax = 0.0, ay = 0.0, az = 0.0;
+    // w: the potential sum_j m_j / sqrt(d2), j != i, when the force pass
+    // recorded it (the float-float energy pass), else 0
+    double ax = 0.0, ay = 0.0, az = 0.0, aw = 0.0;
     for (int c = c0; c <= c1; ++c) {
         const double4 q = tpart[(size_t)(c + I) * rb + li];
         ax = __dadd_rn(ax, q.x);
         ay = __dadd_rn(ay, q.y);
         az = __dadd_rn(az, q.z);
+        aw = __dadd_rn(aw, q.w);
     }
     long long off = (long long)i - rb;  // row r at soff(r) + i - (r + 1) rb
     for (int r = 0; r < I; ++r) {
@@ -167,22 +170,26 @@ __global__ void sym64_integrate_kernel(const double4 *__restrict__ pos_old, doub
         ax = __dadd_rn(ax, q.x);
         ay = __dadd_rn(ay, q.y);
         az = __dadd_rn(az, q.z);
+        aw = __dadd_rn(aw, q.w);
     }
     if (ffrange) {
         // float-float path: its sums are in units scaled by 2^kx (positions)
         // and 2^km (masses), kx = -e(max |x|), km = -e(max m) with
-        // 2^(e-1) <= v < 2^e; a = a_scaled * 2^(2 kx - km), exact
+        // 2^(e-1) <= v < 2^e; a = a_scaled * 2^(2 kx - km) and
+        // phi = phi_scaled * 2^(kx - km), exact
         auto ex = [](unsigned long long b) {
             const int f = (int)((b >> 52) & 0x7ff);
             return (f == 0 || f == 0x7ff) ? 0 : f - 1022;
         };
-        const int k = ex(ffrange[1]) - 2 * ex(ffrange[0]);
+        const int em = ex(ffrange[1]), ex0 = ex(ffrange[0]);
+        const int k = em - 2 * ex0;
         ax = ldexp(ax, k);
         ay = ldexp(ay, k);
         az = ldexp(az, k);
+        aw = ldexp(aw, em - ex0);
     }
     if (acc_out) {
-        acc_out[i] = make_double4(ax, ay, az, 0.0);
+        acc_out[i] = make_double4(ax, ay, az, aw);
         return;
     }
     double4 p = pos_old[i];

@@ -90,7 +90,25 @@ struct FFPair {
     float rxh, rxl, ryh, ryl, rzh, rzl;  // r = x_j - x_i
     float wjh, wjl;                      // m_j inv^3 (weight on the target)
     float wih, wil;                      // m_i inv^3 with m_i as passed (reaction)
+    float yh, yl;                        // inv = 1/sqrt(|r|^2 + eps2)
 };
+
+// A += v (float-float, renormalized)
+__device__ __forceinline__ void ff_add(float &Ah, float &Al, float vh, float vl)
+{
+    float s, t;
+    ff_two_sum(Ah, vh, s, t);
+    ff_fast_two_sum(s, __fadd_rn(Al, __fadd_rn(t, vl)), Ah, Al);
+}
+
+// m * y for a float-float mass (mh, ml) and y (yh, yl), unnormalized
+__device__ __forceinline__ void ff_mul(float mh, float ml, float yh, float yl, float &ph, float &pl)
+{
+    ph = __fmul_rn(mh, yh);
+    float e = __fmaf_rn(mh, yh, -ph);
+    e = __fmaf_rn(mh, yl, e);
+    pl = __fmaf_rn(ml, yh, e);
+}
 
 // Pair pieces for source (sH, sM, sL) and target (p*), eps2 = eh + el.
 template <bool REACT>
@@ -126,6 +144,8 @@ __device__ __forceinline__ void ff_pair(float4 sH, float4 sM, float4 sL, float p
     const float corr = __fmul_rn(y0, __fmul_rn(u, __fmaf_rn(0.375f, u, 0.5f)));
     float yh, yl;
     ff_fast_two_sum(y0, corr, yh, yl);
+    o.yh = yh;
+    o.yl = yl;
     // inv^3 = y^3
     const float p2 = __fmul_rn(yh, yh);
     float e2 = __fmaf_rn(yh, yh, -p2);
@@ -208,7 +228,9 @@ __global__ void ff_split_kernel(const double4 *__restrict__ pos, int n, const un
     L[i] = make_float4(l[0], l[1], l[2], l[3]);
 }
 
-template <int W, int BPT, int MINB>
+// PHI: also the potential sum_j m_j inv (j != i) in the partials' w, the
+// reaction's included (energy pass).
+template <int W, int BPT, int MINB, bool PHI>
 __global__ void __launch_bounds__(32 * W, MINB)
     symff_force_kernel(const float4 *__restrict__ H, const float4 *__restrict__ Mi, const float4 *__restrict__ Lo,
                        int n, double eps2, const unsigned long long *__restrict__ range,
@@ -218,7 +240,7 @@ __global__ void __launch_bounds__(32 * W, MINB)
     constexpr int RB = W * WB;
     constexpr int RC = RB / 32;
     __shared__ __align__(16) float4 sH[32], sM[32], sL[32];
-    __shared__ double sF[3][W][32];
+    __shared__ double sF[4][W][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const int c = blockIdx.x;
@@ -242,7 +264,7 @@ __global__ void __launch_bounds__(32 * W, MINB)
         // negated: reactions point along -r
         float pxh[BPT], pxm[BPT], pxl[BPT], pyh[BPT], pym[BPT], pyl[BPT], pzh[BPT], pzm[BPT], pzl[BPT];
         float nmh[BPT], nml[BPT];
-        double ax[BPT], ay[BPT], az[BPT];
+        double ax[BPT], ay[BPT], az[BPT], aphi[BPT];
 #pragma unroll
         for (int k = 0; k < BPT; ++k) {
             const int i = tbase + lane + 32 * k;
@@ -253,7 +275,7 @@ __global__ void __launch_bounds__(32 * W, MINB)
             pyh[k] = a.y; pym[k] = m.y; pyl[k] = b.y;
             pzh[k] = a.z; pzm[k] = m.z; pzl[k] = b.z;
             nmh[k] = -a.w; nml[k] = -m.w;
-            ax[k] = ay[k] = az[k] = 0.0;
+            ax[k] = ay[k] = az[k] = aphi[k] = 0.0;
         }
         for (int kc = kc0; kc < kc1; ++kc) {
             const int jb = kc * 32;
@@ -266,9 +288,10 @@ __global__ void __launch_bounds__(32 * W, MINB)
                 sL[lane] = in ? Lo[jb + lane] : zero;
             }
             __syncthreads();
-            float Axh[BPT], Axl[BPT], Ayh[BPT], Ayl[BPT], Azh[BPT], Azl[BPT];
+            float Axh[BPT], Axl[BPT], Ayh[BPT], Ayl[BPT], Azh[BPT], Azl[BPT], Aph[BPT], Apl[BPT];
 #pragma unroll
-            for (int k = 0; k < BPT; ++k) Axh[k] = Axl[k] = Ayh[k] = Ayl[k] = Azh[k] = Azl[k] = 0.f;
+            for (int k = 0; k < BPT; ++k)
+                Axh[k] = Axl[k] = Ayh[k] = Ayl[k] = Azh[k] = Azl[k] = Aph[k] = Apl[k] = 0.f;
             if (kc < (I + 1) * RC) {
                 // chunk inside the own row block: directed, target side only
 #pragma unroll 1
@@ -282,10 +305,15 @@ __global__ void __launch_bounds__(32 * W, MINB)
                         ff_acc(Axh[k], Axl[k], w.rxh, w.rxl, w.wjh, w.wjl);
                         ff_acc(Ayh[k], Ayl[k], w.ryh, w.ryl, w.wjh, w.wjl);
                         ff_acc(Azh[k], Azl[k], w.rzh, w.rzl, w.wjh, w.wjl);
+                        if (PHI && jb + j != tbase + lane + 32 * k) {  // no self term
+                            float vh, vl;
+                            ff_mul(a.w, am.w, w.yh, w.yl, vh, vl);
+                            ff_add(Aph[k], Apl[k], vh, vl);
+                        }
                     }
                 }
             } else {
-                float Fxh = 0.f, Fxl = 0.f, Fyh = 0.f, Fyl = 0.f, Fzh = 0.f, Fzl = 0.f;
+                float Fxh = 0.f, Fxl = 0.f, Fyh = 0.f, Fyl = 0.f, Fzh = 0.f, Fzl = 0.f, Fph = 0.f, Fpl = 0.f;
 #pragma unroll 1
                 for (int r = 0; r < 32; ++r) {
                     const int idx = (lane + r) & 31;
@@ -301,6 +329,13 @@ __global__ void __launch_bounds__(32 * W, MINB)
                         ff_acc(Fxh, Fxl, w.rxh, w.rxl, w.wih, w.wil);
                         ff_acc(Fyh, Fyl, w.ryh, w.ryl, w.wih, w.wil);
                         ff_acc(Fzh, Fzl, w.rzh, w.rzl, w.wih, w.wil);
+                        if (PHI) {
+                            float vh, vl;
+                            ff_mul(a.w, am.w, w.yh, w.yl, vh, vl);
+                            ff_add(Aph[k], Apl[k], vh, vl);
+                            ff_mul(-nmh[k], -nml[k], w.yh, w.yl, vh, vl);
+                            ff_add(Fph, Fpl, vh, vl);
+                        }
                     }
                     const int from = (lane + 1) & 31;
                     Fxh = __shfl_sync(0xffffffffu, Fxh, from);
@@ -309,27 +344,33 @@ __global__ void __launch_bounds__(32 * W, MINB)
                     Fyl = __shfl_sync(0xffffffffu, Fyl, from);
                     Fzh = __shfl_sync(0xffffffffu, Fzh, from);
                     Fzl = __shfl_sync(0xffffffffu, Fzl, from);
+                    if (PHI) {
+                        Fph = __shfl_sync(0xffffffffu, Fph, from);
+                        Fpl = __shfl_sync(0xffffffffu, Fpl, from);
+                    }
                 }
                 // lane l now holds the reaction on chunk body l from this warp
                 const double fx = (double)Fxh + (double)Fxl, fy = (double)Fyh + (double)Fyl,
-                             fz = (double)Fzh + (double)Fzl;
+                             fz = (double)Fzh + (double)Fzl, fp = PHI ? (double)Fph + (double)Fpl : 0.0;
                 const long long so = sym_soff(I, n, RB) + (jb + lane - (I + 1) * RB);
                 if (W == 1) {
-                    if (in) spart[so] = make_double4(fx, fy, fz, 0.0);
+                    if (in) spart[so] = make_double4(fx, fy, fz, fp);
                 } else {
                     sF[0][wid][lane] = fx;
                     sF[1][wid][lane] = fy;
                     sF[2][wid][lane] = fz;
+                    sF[3][wid][lane] = fp;
                     __syncthreads();
                     if (wid == 0 && in) {
-                        double sx = 0.0, sy = 0.0, sz = 0.0;
+                        double sx = 0.0, sy = 0.0, sz = 0.0, sp = 0.0;
 #pragma unroll
                         for (int w = 0; w < W; ++w) {
                             sx += sF[0][w][lane];
                             sy += sF[1][w][lane];
                             sz += sF[2][w][lane];
+                            sp += sF[3][w][lane];
                         }
-                        spart[so] = make_double4(sx, sy, sz, 0.0);
+                        spart[so] = make_double4(sx, sy, sz, sp);
                     }
                 }
             }
@@ -339,11 +380,12 @@ __global__ void __launch_bounds__(32 * W, MINB)
                 ax[k] += (double)Axh[k] + (double)Axl[k];
                 ay[k] += (double)Ayh[k] + (double)Ayl[k];
                 az[k] += (double)Azh[k] + (double)Azl[k];
+                if (PHI) aphi[k] += (double)Aph[k] + (double)Apl[k];
             }
         }
         double4 *dst = tpart + (size_t)(c + I) * RB + wid * WB;
 #pragma unroll
-        for (int k = 0; k < BPT; ++k) dst[lane + 32 * k] = make_double4(ax[k], ay[k], az[k], 0.0);
+        for (int k = 0; k < BPT; ++k) dst[lane + 32 * k] = make_double4(ax[k], ay[k], az[k], aphi[k]);
         it = seg_end;
     }
 }
@@ -351,13 +393,13 @@ __global__ void __launch_bounds__(32 * W, MINB)
 typedef void (*symff_kernel_t)(const float4 *, const float4 *, const float4 *, int, double,
                                const unsigned long long *, double4 *, double4 *, long long, int, int);
 
-static symff_kernel_t symff_kernel_for(int w, int bpt)
+static symff_kernel_t symff_kernel_for(int w, int bpt, bool phi = false)
 {
-    if (w == 1 && bpt == 2) return symff_force_kernel<1, 2, 16>;
-    if (w == 1 && bpt == 4) return symff_force_kernel<1, 4, 8>;
-    if (w == 4 && bpt == 4) return symff_force_kernel<4, 4, 2>;
-    if (w == 8 && bpt == 4) return symff_force_kernel<8, 4, 1>;
-    if (w == 8 && bpt == 8) return symff_force_kernel<8, 8, 1>;
+    if (w == 1 && bpt == 2) return phi ? symff_force_kernel<1, 2, 16, true> : symff_force_kernel<1, 2, 16, false>;
+    if (w == 1 && bpt == 4) return phi ? symff_force_kernel<1, 4, 8, true> : symff_force_kernel<1, 4, 8, false>;
+    if (w == 4 && bpt == 4) return phi ? symff_force_kernel<4, 4, 2, true> : symff_force_kernel<4, 4, 2, false>;
+    if (w == 8 && bpt == 4) return phi ? symff_force_kernel<8, 4, 1, true> : symff_force_kernel<8, 4, 1, false>;
+    if (w == 8 && bpt == 8) return phi ? symff_force_kernel<8, 8, 1, true> : symff_force_kernel<8, 8, 1, false>;
     return nullptr;
 }
 
@@ -388,6 +430,9 @@ int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl)
     int sms = 0, occ = 0;
     NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * warps, 0));
+    int occ_phi = 0;  // the energy pass runs on the same plan
+    NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_phi, symff_kernel_for(warps, bpt, true), 32 * warps, 0));
+    if (occ_phi < occ) occ = occ_phi;
     if (occ < 1) return set_error(NB_ERR_UNSUPPORTED, "float-float symmetric kernel does not fit on an SM");
     long long grid = (long long)sms * occ;
     if (p.total > 0 && grid > p.total) grid = p.total;
@@ -400,10 +445,10 @@ int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl)
 }
 
 int symff_force(const SymPlan &p, const double4 *pos, double eps2, float4 *split, unsigned long long *range,
-                double4 *tpart, double4 *spart, cudaStream_t s)
+                double4 *tpart, double4 *spart, cudaStream_t s, int phi)
 {
     if (p.n == 0) return NB_OK;
-    symff_kernel_t k = symff_kernel_for(p.warps, p.bpt);
+    symff_kernel_t k = symff_kernel_for(p.warps, p.bpt, phi != 0);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "float-float symmetric kernel shape not compiled");
     float4 *H = split, *M = split + p.n, *L = split + 2 * (size_t)p.n;
     NB_CUDA(cudaMemsetAsync(range, 0, 2 * sizeof(unsigned long long), s));
