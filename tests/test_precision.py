@@ -85,7 +85,8 @@ def test_compensated_steps_vs_fp64_oracle(cuda, algo):
 
 
 @pytest.mark.parametrize("precision,algo", [("f32", "fast"), ("f32", "sym"), ("f32comp", "fast"),
-                                            ("f32comp", "sym"), ("f64", "sym"), ("f64", "exact")])
+                                            ("f32comp", "sym"), ("f64", "sym"), ("f64", "sym64"),
+                                            ("f64", "exact")])
 def test_energy_momentum_vs_fp64(cuda, precision, algo):
     n = 4096
     p, v = ics.plummer(n, seed=4)
@@ -147,3 +148,30 @@ def test_compensated_sym_default_shape(cuda, n, shape):
     with NBodySystem(n, "f32comp", "sym") as s:
         info = s.plan_info()
     assert (info["block"], info["bpt"]) == shape
+
+
+def test_f64_energy_paths_agree_and_timing(cuda, capsys):
+    """FP64 state: the float-float energy pass (symmetric kernel with the
+    potential, NB_ALGO_SYM) and the FP64 one (NB_ALGO_SYM_FP64) agree to
+    1e-13 per body in (acc, phi) and in the totals; both timed."""
+    import time
+
+    import torch
+
+    n = 16384
+    p, v = ics.plummer(n, seed=8)
+    out = {}
+    for algo in ("sym", "sym64"):
+        with NBodySystem(n, "f64", algo, kick="physical", eps2=1e-4) as s:
+            s.set_state(p, v)
+            s.energy()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e, bodies = s.energy(with_bodies=True)
+            out[algo] = (e, bodies, time.perf_counter() - t0)
+    (ea, ba, ta), (eb, bb, tb) = out["sym"], out["sym64"]
+    assert np.abs(ea - eb).max() <= 1e-13 * np.abs(eb).max()
+    scale = np.abs(bb).max(axis=0)
+    assert (np.abs(ba - bb) <= 1e-13 * scale).all()
+    with capsys.disabled():
+        print(f"\n[energy f64] N={n}: float-float pass {ta * 1e3:.2f} ms, FP64 pass {tb * 1e3:.2f} ms")
