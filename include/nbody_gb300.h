@@ -107,7 +107,10 @@ typedef struct nb_params {
     double damping;
     double dt;
     double G;         /* used in NB_KICK_PHYSICAL mode */
-    int block;        /* fast kernel threads per CTA (0 = tuned/auto) */
+    int block;        /* threads per CTA (0 = tuned/auto): fast kernel; symmetric
+                         kernels (warps x 32); exact kernel upper bound (it
+                         takes smaller CTAs when they spread over more SMs;
+                         its results do not depend on the CTA size) */
     int bpt;          /* fast kernel bodies per thread (0 = tuned/auto) */
     int ctas_per_sm;  /* fast kernel persistent CTAs per SM (0 = occupancy) */
     int memtype;      /* nb_memtype, for nb_run_host staging */

@@ -102,6 +102,20 @@ static int exact_launch(int n, const typename vec4_of<T>::type *pos_old,
     if (block <= 0) block = 256;
     if (block % 32 != 0 || block > 1024)
         return set_error(NB_ERR_INVALID, "exact kernel block size must be a multiple of 32, <= 1024");
+    // The results do not depend on the CTA size (every thread sums its
+    // sources in index order), so the requested size is only an upper bound:
+    // halve it while that lowers the most warps one SM has to run (a small N
+    // in large CTAs leaves SMs idle: N=16384 in CTAs of 256 covers 64 of
+    // 152 SMs).  Ties keep the larger CTA.
+    int dev = 0, sms = 0;
+    NB_CUDA(cudaGetDevice(&dev));
+    NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    auto load = [&](int b) {
+        const long long grid = ((long long)n + b - 1) / b;
+        return ((grid + sms - 1) / sms) * (b / 32);
+    };
+    for (int b = block / 2; b >= 32 && b % 32 == 0; b /= 2)
+        if (load(b) < load(block)) block = b;
     const size_t smem = sizeof(typename vec4_of<T>::type) * block;
     exact_step_kernel<T><<<(n + block - 1) / block, block, smem, s>>>(pos_old, pos_new, vel, n, eps2,
                                                                      damping, dt, kick, G, acc_out);
