@@ -328,14 +328,15 @@ __global__ void __launch_bounds__(kPhi64Block) phi64_kernel(const double4 *__res
                                                             double eps2, double4 *__restrict__ out)
 {
     __shared__ double4 sp[kPhi64Block];
-    const int i = blockIdx.x * kPhi64Block + threadIdx.x;
+    const int nt = blockDim.x;  // <= kPhi64Block
+    const int i = blockIdx.x * nt + threadIdx.x;
     const double4 pi = i < n ? pos[i] : make_double4(0.0, 0.0, 0.0, 0.0);
     double ax = 0.0, ay = 0.0, az = 0.0, phi = 0.0;
-    for (int jt = 0; jt < n; jt += kPhi64Block) {
+    for (int jt = 0; jt < n; jt += nt) {
         __syncthreads();
         if (jt + (int)threadIdx.x < n) sp[threadIdx.x] = pos[jt + threadIdx.x];
         __syncthreads();
-        const int cnt = min(kPhi64Block, n - jt);
+        const int cnt = min(nt, n - jt);
         for (int j = 0; j < cnt; ++j) {
             if (jt + j == i) continue;
             const double4 q = sp[j];
@@ -358,7 +359,19 @@ __global__ void __launch_bounds__(kPhi64Block) phi64_kernel(const double4 *__res
 int energy_phi_f64(int n, const double4 *pos, double eps2, double4 *out, cudaStream_t s)
 {
     if (n == 0) return NB_OK;
-    phi64_kernel<<<(n + kPhi64Block - 1) / kPhi64Block, kPhi64Block, 0, s>>>(pos, n, eps2, out);
+    // one thread per body: CTAs of 256 down to 32, whichever puts the fewest
+    // warps on the busiest SM (small N in large CTAs leaves SMs idle)
+    int dev = 0, sms = 0;
+    NB_CUDA(cudaGetDevice(&dev));
+    NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    auto load = [&](int b) {
+        const long long grid = ((long long)n + b - 1) / b;
+        return ((grid + sms - 1) / sms) * (b / 32);
+    };
+    int block = kPhi64Block;
+    for (int b = kPhi64Block / 2; b >= 32; b /= 2)
+        if (load(b) < load(block)) block = b;
+    phi64_kernel<<<(n + block - 1) / block, block, 0, s>>>(pos, n, eps2, out);
     NB_LAUNCH_CHECK("phi64_kernel launch");
     return NB_OK;
 }
