@@ -93,7 +93,7 @@ def test_batch_argument_checks(cuda):
     sizes = np.array([4, 9], np.int32)
     prm.algo = N.NB_ALGO_EXACT
     assert lib.nb_batch_create(C.byref(prm), 2, sizes.ctypes.data_as(C.c_void_p), C.byref(h)) == N.NB_ERR_UNSUPPORTED
-    prm.algo = N.NB_ALGO_SYM
+    prm.algo = N.NB_ALGO_FAST  # FP64 batches run the (float-float) symmetric algorithm only
     prm.precision = N.NB_F64
     assert lib.nb_batch_create(C.byref(prm), 2, sizes.ctypes.data_as(C.c_void_p), C.byref(h)) == N.NB_ERR_UNSUPPORTED
     with NBodyBatch([4, 9]) as b:

@@ -37,6 +37,7 @@
 #include <thread>
 #include <vector>
 
+#include "nb_ff.cuh"
 #include "nb_internal.cuh"
 
 namespace nb {
@@ -345,6 +346,211 @@ __global__ void bks_integrate_kernel(const float4 *__restrict__ pos_old, float4 
         az = __fadd_rn(az, q.z);
     }
     batch_kick_drift(i, ax, ay, az, pos_old, pos_new, vel, damping, dt, kick, G, acc_out);
+}
+
+// Float-float batched symmetric kernel for FP64 state: the layout and work
+// split of bks_force_kernel, the pair arithmetic of symff_force_kernel
+// (nb_ff.cuh; three-float positions scaled by the batch's powers of two),
+// each chunk's target sums folded into FP64, reactions written as FP64.
+template <int WPB, int BPT>
+__global__ void __launch_bounds__(32 * WPB)
+    bksff_force_kernel(const float4 *__restrict__ H, const float4 *__restrict__ Mi, const float4 *__restrict__ Lo,
+                       BatchSymDev bd, double eps2, const unsigned long long *__restrict__ range,
+                       double4 *__restrict__ tpart, double4 *__restrict__ spart, long long total, int workers)
+{
+    constexpr int RB = 32 * BPT;
+    constexpr int RC = BPT;
+    __shared__ __align__(16) float4 sH[WPB][32], sM[WPB][32], sL[WPB][32];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const int w = blockIdx.x * WPB + wid;
+    if (w >= workers) return;
+    long long it = sk_start(w, total, workers);
+    const long long end = sk_start(w + 1, total, workers);
+    if (it >= end) return;
+    // eps2 in the scaled units (x 2^(2 kx)), as a float-float
+    const double e2s = ldexp(eps2, -2 * ff_exponent(range[0]));
+    const float eh = __double2float_rn(e2s), el = __double2float_rn(e2s - (double)eh);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    int s = find_sys(bd.it_off, bd.nsys, it);
+    while (it < end) {
+        while (it >= bd.it_off[s + 1]) ++s;
+        const int o = bd.sys_off[s];
+        const int ns = bd.sys_off[s + 1] - o;
+        const int nc = (ns + 31) / 32, nrb = (ns + RB - 1) / RB;
+        const long long base = bd.it_off[s];
+        const int I = sym_row_of(it - base, nc, RC, nrb);
+        const long long rfirst = base + sym_prefix(I, nc, RC);
+        const long long rend = base + sym_prefix(I + 1, nc, RC);
+        const long long seg_end = end < rend ? end : rend;
+        const int kc0 = I * RC + (int)(it - rfirst);
+        const int kc1 = I * RC + (int)(seg_end - rfirst);
+        const int tbase = I * RB;
+        // missing targets: zero mass, so their reactions are 0; masses
+        // negated: reactions point along -r
+        float pxh[BPT], pxm[BPT], pxl[BPT], pyh[BPT], pym[BPT], pyl[BPT], pzh[BPT], pzm[BPT], pzl[BPT];
+        float nmh[BPT], nml[BPT];
+        double ax[BPT], ay[BPT], az[BPT];
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const int li = tbase + lane + 32 * k;
+            const float4 a = li < ns ? H[o + li] : zero;
+            const float4 m = li < ns ? Mi[o + li] : zero;
+            const float4 q = li < ns ? Lo[o + li] : zero;
+            pxh[k] = a.x; pxm[k] = m.x; pxl[k] = q.x;
+            pyh[k] = a.y; pym[k] = m.y; pyl[k] = q.y;
+            pzh[k] = a.z; pzm[k] = m.z; pzl[k] = q.z;
+            nmh[k] = -a.w; nml[k] = -m.w;
+            ax[k] = ay[k] = az[k] = 0.0;
+        }
+        for (int kc = kc0; kc < kc1; ++kc) {
+            const int jb = kc * 32;
+            const bool in = jb + lane < ns;
+            __syncwarp();  // previous chunk's reads are done
+            // padding: far away (scaled coordinates are below 1), no mass
+            sH[wid][lane] = in ? H[o + jb + lane] : make_float4(1.0e6f, 1.0e6f, 1.0e6f, 0.f);
+            sM[wid][lane] = in ? Mi[o + jb + lane] : zero;
+            sL[wid][lane] = in ? Lo[o + jb + lane] : zero;
+            __syncwarp();
+            float Axh[BPT], Axl[BPT], Ayh[BPT], Ayl[BPT], Azh[BPT], Azl[BPT];
+#pragma unroll
+            for (int k = 0; k < BPT; ++k) Axh[k] = Axl[k] = Ayh[k] = Ayl[k] = Azh[k] = Azl[k] = 0.f;
+            if (kc < (I + 1) * RC) {
+                // chunk inside the own row block: directed, target side only
+#pragma unroll 1
+                for (int j = 0; j < 32; ++j) {
+                    const float4 a = sH[wid][j], am = sM[wid][j], q = sL[wid][j];
+#pragma unroll
+                    for (int k = 0; k < BPT; ++k) {
+                        FFPair f;
+                        ff_pair<false>(a, am, q, pxh[k], pxm[k], pxl[k], pyh[k], pym[k], pyl[k], pzh[k], pzm[k],
+                                       pzl[k], 0.f, 0.f, eh, el, f);
+                        ff_acc(Axh[k], Axl[k], f.rxh, f.rxl, f.wjh, f.wjl);
+                        ff_acc(Ayh[k], Ayl[k], f.ryh, f.ryl, f.wjh, f.wjl);
+                        ff_acc(Azh[k], Azl[k], f.rzh, f.rzl, f.wjh, f.wjl);
+                    }
+                }
+            } else {
+                float Fxh = 0.f, Fxl = 0.f, Fyh = 0.f, Fyl = 0.f, Fzh = 0.f, Fzl = 0.f;
+#pragma unroll 1
+                for (int r = 0; r < 32; ++r) {
+                    const int idx = (lane + r) & 31;
+                    const float4 a = sH[wid][idx], am = sM[wid][idx], q = sL[wid][idx];
+#pragma unroll
+                    for (int k = 0; k < BPT; ++k) {
+                        FFPair f;
+                        ff_pair<true>(a, am, q, pxh[k], pxm[k], pxl[k], pyh[k], pym[k], pyl[k], pzh[k], pzm[k],
+                                      pzl[k], nmh[k], nml[k], eh, el, f);
+                        ff_acc(Axh[k], Axl[k], f.rxh, f.rxl, f.wjh, f.wjl);
+                        ff_acc(Ayh[k], Ayl[k], f.ryh, f.ryl, f.wjh, f.wjl);
+                        ff_acc(Azh[k], Azl[k], f.rzh, f.rzl, f.wjh, f.wjl);
+                        ff_acc(Fxh, Fxl, f.rxh, f.rxl, f.wih, f.wil);
+                        ff_acc(Fyh, Fyl, f.ryh, f.ryl, f.wih, f.wil);
+                        ff_acc(Fzh, Fzl, f.rzh, f.rzl, f.wih, f.wil);
+                    }
+                    const int from = (lane + 1) & 31;
+                    Fxh = __shfl_sync(0xffffffffu, Fxh, from);
+                    Fxl = __shfl_sync(0xffffffffu, Fxl, from);
+                    Fyh = __shfl_sync(0xffffffffu, Fyh, from);
+                    Fyl = __shfl_sync(0xffffffffu, Fyl, from);
+                    Fzh = __shfl_sync(0xffffffffu, Fzh, from);
+                    Fzl = __shfl_sync(0xffffffffu, Fzl, from);
+                }
+                // lane l holds the reaction on chunk body l
+                if (in)
+                    spart[bd.sp_off[s] + sym_soff(I, ns, RB) + (jb + lane - (I + 1) * RB)] =
+                        make_double4((double)Fxh + (double)Fxl, (double)Fyh + (double)Fyl,
+                                     (double)Fzh + (double)Fzl, 0.0);
+            }
+#pragma unroll
+            for (int k = 0; k < BPT; ++k) {
+                ax[k] += (double)Axh[k] + (double)Axl[k];
+                ay[k] += (double)Ayh[k] + (double)Ayl[k];
+                az[k] += (double)Azh[k] + (double)Azl[k];
+            }
+        }
+        double4 *dst = tpart + ((long long)w + bd.row_off[s] + I) * RB;
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) dst[lane + 32 * k] = make_double4(ax[k], ay[k], az[k], 0.0);
+        it = seg_end;
+    }
+}
+
+// Per body: FP64 sums of the target-side slots of its row (warp order) and
+// the source-side entries of rows 0..I-1 of its system (row order), the
+// batch's scaling undone (a = a_scaled * 2^(2 kx - km), exact), then the
+// reference's kick / damping / drift in its order with unfused IEEE
+// operations (bodysystem.cc:135-182), or the bare acceleration.
+__global__ void bksff_integrate_kernel(const double4 *__restrict__ pos_old, double4 *__restrict__ pos_new,
+                                       double4 *__restrict__ vel, const double4 *__restrict__ tpart,
+                                       const double4 *__restrict__ spart, BatchSymDev bd, int nbody, int rb,
+                                       long long total, int workers, double damping, double dt, int kick,
+                                       double G, const unsigned long long *__restrict__ range,
+                                       double4 *__restrict__ acc_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbody) return;
+    const int s = bd.body_sys[i];
+    const int o = bd.sys_off[s];
+    const int ns = bd.sys_off[s + 1] - o;
+    const int li = i - o;
+    const int rc = rb / 32;
+    const int nc = (ns + 31) / 32;
+    const int I = li / rb;
+    const long long base = bd.it_off[s];
+    const int c0 = sk_owner(base + sym_prefix(I, nc, rc), total, workers);
+    const int c1 = sk_owner(base + sym_prefix(I + 1, nc, rc) - 1, total, workers);
+    const long long grow = (long long)bd.row_off[s] + I;
+    const int lj = li - I * rb;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int c = c0; c <= c1; ++c) {
+        const double4 q = tpart[(c + grow) * rb + lj];
+        ax = __dadd_rn(ax, q.x);
+        ay = __dadd_rn(ay, q.y);
+        az = __dadd_rn(az, q.z);
+    }
+    long long off = bd.sp_off[s] + li - rb;  // row r at soff(r) + li - (r + 1) rb
+    for (int r = 0; r < I; ++r) {
+        const double4 q = spart[off];
+        off += (long long)ns - (long long)(r + 2) * rb;
+        ax = __dadd_rn(ax, q.x);
+        ay = __dadd_rn(ay, q.y);
+        az = __dadd_rn(az, q.z);
+    }
+    const int k2 = ff_exponent(range[1]) - 2 * ff_exponent(range[0]);
+    ax = ldexp(ax, k2);
+    ay = ldexp(ay, k2);
+    az = ldexp(az, k2);
+    if (acc_out) {
+        acc_out[i] = make_double4(ax, ay, az, 0.0);
+        return;
+    }
+    double4 p = pos_old[i];
+    double4 v = vel[i];
+    const double k = kick == NB_KICK_REFERENCE ? p.w : G;
+    v.x = __dadd_rn(v.x, __dmul_rn(__dmul_rn(ax, k), dt));
+    v.y = __dadd_rn(v.y, __dmul_rn(__dmul_rn(ay, k), dt));
+    v.z = __dadd_rn(v.z, __dmul_rn(__dmul_rn(az, k), dt));
+    v.x = __dmul_rn(v.x, damping);
+    v.y = __dmul_rn(v.y, damping);
+    v.z = __dmul_rn(v.z, damping);
+    p.x = __dadd_rn(p.x, __dmul_rn(v.x, dt));
+    p.y = __dadd_rn(p.y, __dmul_rn(v.y, dt));
+    p.z = __dadd_rn(p.z, __dmul_rn(v.z, dt));
+    pos_new[i] = p;
+    vel[i] = v;
+}
+
+typedef void (*bksff_kernel_t)(const float4 *, const float4 *, const float4 *, BatchSymDev, double,
+                               const unsigned long long *, double4 *, double4 *, long long, int);
+
+static bksff_kernel_t bksff_kernel_for(int wpb, int bpt)
+{
+#define NB_BKSFF(W, B) \
+    if (wpb == W && bpt == B) return bksff_force_kernel<W, B>;
+    NB_BKSFF(1, 2) NB_BKSFF(1, 4) NB_BKSFF(2, 2) NB_BKSFF(2, 4) NB_BKSFF(4, 2) NB_BKSFF(4, 4)
+#undef NB_BKSFF
+    return nullptr;
 }
 
 typedef void (*bks_kernel_t)(const float4 *, BatchSymDev, float, float4 *, float4 *, long long, int);
@@ -751,6 +957,13 @@ struct nb_batch {
     int graph_steps = 0, graph_cur = -1;
     // scratch of the per-system baseline (target-side and source-side)
     float4 *sys_partial = nullptr, *sys_spart = nullptr;
+    // NB_F64 state (NB_ALGO_SYM): pos / vel / partial / spart hold double4
+    // (twice the float4 entries), stepped by the float-float batched kernel
+    // from the scaled three-float split (3 nbody float4) and the batch's
+    // scale record
+    bool f64 = false;
+    float4 *ff_split = nullptr;
+    unsigned long long *ff_range = nullptr;
     // plan, scratch and device tables agree; false after a failed plan change
     // (launches then refuse to run rather than use a stale or NULL scratch)
     bool plan_ok = false;
@@ -779,7 +992,9 @@ using nb::set_error;
 static int batch_plan_for(nb_batch *b, int wpb, int bpt, BatchPlan *out, std::vector<long long> *it_off,
                           std::vector<int> *tb_off, std::vector<long long> *sp_off)
 {
-    const void *k = b->sym ? (const void *)nb::bks_kernel_for(wpb, bpt) : (const void *)nb::bk_kernel_for(wpb, bpt);
+    const void *k = b->f64 ? (const void *)nb::bksff_kernel_for(wpb, bpt)
+                    : b->sym ? (const void *)nb::bks_kernel_for(wpb, bpt)
+                             : (const void *)nb::bk_kernel_for(wpb, bpt);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "batched kernel shape not compiled");
     const int wtb = 32 * bpt;
     it_off->assign(b->nsys + 1, 0);
@@ -828,7 +1043,8 @@ static int batch_apply_plan(nb_batch *b, int wpb, int bpt, cudaStream_t s)
         b->graph = nullptr;
         b->graph_cur = -1;
     }
-    const size_t need = (size_t)p.slots * 32 * bpt;
+    const size_t wide = b->f64 ? 2 : 1;  // float4 entries per partial entry
+    const size_t need = (size_t)p.slots * 32 * bpt * wide;
     if (need > b->partial_cap) {
         cudaFree(b->partial);
         b->partial = nullptr;
@@ -837,13 +1053,13 @@ static int batch_apply_plan(nb_batch *b, int wpb, int bpt, cudaStream_t s)
         if (e != cudaSuccess) return nb::cuda_error(e, "batched scratch allocation");
         b->partial_cap = need;
     }
-    if ((size_t)p.spart > b->spart_cap) {
+    if ((size_t)p.spart * wide > b->spart_cap) {
         cudaFree(b->spart);
         b->spart = nullptr;
         b->spart_cap = 0;
-        cudaError_t e = cudaMalloc((void **)&b->spart, (size_t)p.spart * sizeof(float4));
+        cudaError_t e = cudaMalloc((void **)&b->spart, (size_t)p.spart * wide * sizeof(float4));
         if (e != cudaSuccess) return nb::cuda_error(e, "batched source-side allocation");
-        b->spart_cap = (size_t)p.spart;
+        b->spart_cap = (size_t)p.spart * wide;
     }
     if (b->sym)
         NB_CUDA(cudaMemcpyAsync(b->d_sp_off, sp_off.data(), sp_off.size() * sizeof(long long),
@@ -888,6 +1104,16 @@ static int batch_force(nb_batch *b, const float4 *po, cudaStream_t s)
     if (b->nbody == 0) return NB_OK;
     if (!b->plan_ok)
         return set_error(NB_ERR_STATE, "batch has no valid launch plan (a plan change or autotune failed)");
+    if (b->f64) {
+        float4 *H = b->ff_split, *M = H + b->nbody, *L = M + b->nbody;
+        int st = nb::ff_scale_split((const double4 *)po, b->nbody, b->sms, H, M, L, b->ff_range, s);
+        if (st) return st;
+        nb::bksff_kernel_t k = nb::bksff_kernel_for(p.wpb, p.bpt);
+        k<<<p.grid, 32 * p.wpb, 0, s>>>(H, M, L, batch_sym_dev(b), b->p.eps2, b->ff_range, (double4 *)b->partial,
+                                        (double4 *)b->spart, p.total, p.workers);
+        NB_LAUNCH_CHECK("bksff_force_kernel launch");
+        return NB_OK;
+    }
     if (b->sym) {
         nb::bks_kernel_t k = nb::bks_kernel_for(p.wpb, p.bpt);
         k<<<p.grid, 32 * p.wpb, 0, s>>>(po, batch_sym_dev(b), (float)b->p.eps2, b->partial, b->spart,
@@ -910,6 +1136,14 @@ static int batch_integrate(nb_batch *b, const float4 *po, float4 *pn, float4 *ve
     if (b->nbody == 0) return NB_OK;
     if (!b->plan_ok)
         return set_error(NB_ERR_STATE, "batch has no valid launch plan (a plan change or autotune failed)");
+    if (b->f64) {
+        nb::bksff_integrate_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
+            (const double4 *)po, (double4 *)pn, (double4 *)vel, (const double4 *)b->partial,
+            (const double4 *)b->spart, batch_sym_dev(b), b->nbody, 32 * p.bpt, p.total, p.workers, b->p.damping,
+            b->p.dt, b->p.kick, b->p.G, b->ff_range, (double4 *)acc_out);
+        NB_LAUNCH_CHECK("bksff_integrate_kernel launch");
+        return NB_OK;
+    }
     if (b->sym) {
         nb::bks_integrate_kernel<<<(b->nbody + 255) / 256, 256, 0, s>>>(
             po, pn, vel, b->partial, b->spart, batch_sym_dev(b), b->nbody, 32 * p.bpt, p.total,
@@ -1023,6 +1257,8 @@ static void free_batch(nb_batch *b)
     cudaFree(b->d_sp_off);
     cudaFree(b->sys_partial);
     cudaFree(b->sys_spart);
+    cudaFree(b->ff_split);
+    cudaFree(b->ff_range);
     cudaFree(b->d_it_off_v);
     cudaFree(b->d_tb_off_v);
     cudaFree(b->vpartial);
@@ -1054,8 +1290,10 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
     if (!out) return set_error(NB_ERR_INVALID, "out is NULL");
     *out = nullptr;
     if (!p || nsys < 0 || (nsys > 0 && !sizes)) return set_error(NB_ERR_INVALID, "bad batch arguments");
-    if (p->precision != NB_F32 || (p->algo != NB_ALGO_FAST && p->algo != NB_ALGO_SYM))
-        return set_error(NB_ERR_UNSUPPORTED, "batches run NB_F32 with the fast or symmetric algorithm");
+    if (!((p->precision == NB_F32 && (p->algo == NB_ALGO_FAST || p->algo == NB_ALGO_SYM)) ||
+          (p->precision == NB_F64 && p->algo == NB_ALGO_SYM)))
+        return set_error(NB_ERR_UNSUPPORTED,
+                         "batches run NB_F32 with the fast or symmetric algorithm, or NB_F64 with the symmetric one");
     if (p->kick != NB_KICK_REFERENCE && p->kick != NB_KICK_PHYSICAL)
         return set_error(NB_ERR_INVALID, "unknown kick mode");
     if (!std::isfinite(p->eps2) || !std::isfinite(p->damping) || !std::isfinite(p->dt) || !std::isfinite(p->G))
@@ -1072,6 +1310,7 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
     b->nbody = (int)nbody;
     b->sizes.assign(sizes, sizes + nsys);
     b->sym = p->algo == NB_ALGO_SYM;
+    b->f64 = p->precision == NB_F64;
     cudaError_t e = cudaGetDevice(&b->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
     if (e != cudaSuccess) {
@@ -1083,7 +1322,7 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
         sys_off[s + 1] = sys_off[s] + sizes[s];
         for (int i = sys_off[s]; i < sys_off[s + 1]; ++i) body_sys[i] = s;
     }
-    const size_t sb = (size_t)nbody * sizeof(float4);
+    const size_t sb = (size_t)nbody * (b->f64 ? sizeof(double4) : sizeof(float4));
 #define NB_BALLOC(ptr, bytes)                                                  \
     do {                                                                       \
         cudaError_t _e = cudaMalloc((void **)&(ptr), (bytes) ? (bytes) : 16);  \
@@ -1100,6 +1339,10 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
     NB_BALLOC(b->pos[0], sb);
     NB_BALLOC(b->pos[1], sb);
     NB_BALLOC(b->vel, sb);
+    if (b->f64) {
+        NB_BALLOC(b->ff_split, 3 * (size_t)nbody * sizeof(float4));
+        NB_BALLOC(b->ff_range, 2 * sizeof(unsigned long long));
+    }
 #undef NB_BALLOC
     e = cudaMemcpy(b->d_sys_off, sys_off.data(), sizeof(int) * (nsys + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && nbody)
@@ -1108,9 +1351,10 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
         free_batch(b);
         return nb::cuda_error(e, "batch tables");
     }
-    // defaults: symmetric one-warp workers x 16 targets; directed 4 x 4
+    // defaults: float symmetric one-warp workers x 16 targets, directed
+    // 4 x 4, float-float (FP64 state) one-warp workers x 2
     const int wpb = p->block ? p->block / 32 : (b->sym ? 1 : 4);
-    const int bpt = p->bpt ? p->bpt : (b->sym ? 16 : 4);
+    const int bpt = p->bpt ? p->bpt : (b->f64 ? 2 : (b->sym ? 16 : 4));
     int st = batch_apply_plan(b, wpb, bpt, nullptr);
     if (st) {
         free_batch(b);
@@ -1131,7 +1375,7 @@ int nb_batch_destroy(nb_batch *b)
 int nb_batch_set_state(nb_batch *b, const void *pos, const void *vel, int where, void *stream)
 {
     if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
-    const size_t sb = (size_t)b->nbody * sizeof(float4);
+    const size_t sb = (size_t)b->nbody * (b->f64 ? sizeof(double4) : sizeof(float4));
     if (sb && (!pos || !vel)) return set_error(NB_ERR_INVALID, "pos/vel is NULL");
     cudaStream_t s = (cudaStream_t)stream;
     b->cur = 0;
@@ -1148,7 +1392,7 @@ int nb_batch_get_state(nb_batch *b, void *pos, void *vel, int where, void *strea
 {
     if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
     if (!b->has_state) return set_error(NB_ERR_STATE, "no state loaded");
-    const size_t sb = (size_t)b->nbody * sizeof(float4);
+    const size_t sb = (size_t)b->nbody * (b->f64 ? sizeof(double4) : sizeof(float4));
     cudaStream_t s = (cudaStream_t)stream;
     if (sb) {
         if (pos) NB_CUDA(cudaMemcpyAsync(pos, b->pos[b->cur], sb, cudaMemcpyDefault, s));
@@ -1271,7 +1515,7 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
     NB_CUDA(cudaGetDeviceProperties(&prop, b->device));
     std::ostringstream key;
     key << prop.name << "|sms" << prop.multiProcessorCount << "|kick" << b->p.kick
-        << (b->sym ? "|sym" : "|dir") << "|";
+        << (b->f64 ? "|symff" : (b->sym ? "|sym" : "|dir")) << "|";
     {
         std::map<int, int> hist;
         for (int n : b->sizes) {
@@ -1302,7 +1546,7 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
             }
         }
     }
-    const size_t sb = (size_t)b->nbody * sizeof(float4);
+    const size_t sb = (size_t)b->nbody * (b->f64 ? sizeof(double4) : sizeof(float4));
     float4 *save_p = nullptr, *save_v = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     auto release = [&] {
@@ -1327,8 +1571,11 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
     }
     static const int cand_dir[][2] = {{2, 4}, {2, 8}, {4, 2}, {4, 4}, {4, 8}, {8, 2}, {8, 4}, {8, 8}};
     static const int cand_sym[][2] = {{1, 8}, {1, 12}, {1, 16}, {2, 8}, {2, 16}, {4, 8}, {4, 16}};
+    static const int cand_ff[][2] = {{1, 2}, {1, 4}, {2, 2}, {2, 4}, {4, 2}, {4, 4}};
     std::vector<std::array<int, 2>> cands;
-    if (b->sym)
+    if (b->f64)
+        for (auto &c : cand_ff) cands.push_back({c[0], c[1]});
+    else if (b->sym)
         for (auto &c : cand_sym) cands.push_back({c[0], c[1]});
     else
         for (auto &c : cand_dir) cands.push_back({c[0], c[1]});
@@ -1384,20 +1631,26 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
 // scratch each kind needs.
 struct SysPlans {
     std::vector<nb::SkPlan> dir;
-    std::vector<nb::SymPlan> sym;
-    size_t tpart = 1, spart = 1;  // float4 entries
+    std::vector<nb::SymPlan> sym;  // float symmetric or float-float (FP64 state)
+    std::vector<int> off;          // body offsets of the systems
+    size_t tpart = 1, spart = 1;   // float4 entries (double4 state: twice the partial entries)
 };
 
 static int sys_plans_for(nb_batch *b, SysPlans *out)
 {
     SysPlans sp;
+    const size_t wide = b->f64 ? 2 : 1;
+    sp.off.assign(b->nsys + 1, 0);
     for (int i = 0; i < b->nsys; ++i) {
+        sp.off[i + 1] = sp.off[i] + b->sizes[i];
         int st;
         if (b->sym) {
             nb::SymPlan q;
-            if ((st = nb::sym_plan(b->sizes[i], 0, 0, b->device, &q))) return st;
-            sp.tpart = std::max(sp.tpart, (size_t)q.slots * q.rb);
-            sp.spart = std::max(sp.spart, (size_t)q.spart_size);
+            if ((st = b->f64 ? nb::symff_plan(b->sizes[i], 0, 0, b->device, &q)
+                             : nb::sym_plan(b->sizes[i], 0, 0, b->device, &q)))
+                return st;
+            sp.tpart = std::max(sp.tpart, (size_t)q.slots * q.rb * wide);
+            sp.spart = std::max(sp.spart, (size_t)q.spart_size * wide);
             sp.sym.push_back(q);
         } else {
             nb::SkPlan q;
@@ -1410,12 +1663,26 @@ static int sys_plans_for(nb_batch *b, SysPlans *out)
     return NB_OK;
 }
 
-// System i stepped on its own: force + integrate launches.
-static int sys_step(const nb_batch *b, const SysPlans &sp, int i, const float4 *po, float4 *pn,
-                    float4 *vel, float4 *tpart, float4 *spart, cudaStream_t s)
+// System i stepped on its own from pos[c] into pos[c ^ 1]: force + integrate
+// launches (float-float for FP64 state: its own scale record `range` and
+// its slice of the split buffer).
+static int sys_step(const nb_batch *b, const SysPlans &sp, int i, int c, float4 *tpart, float4 *spart,
+                    unsigned long long *range, cudaStream_t s)
 {
     const nb_params &p = b->p;
+    const int o = sp.off[i];
     int st;
+    if (b->f64) {
+        const double4 *po = (const double4 *)b->pos[c] + o;
+        double4 *pn = (double4 *)b->pos[c ^ 1] + o, *vel = (double4 *)b->vel + o;
+        if ((st = nb::symff_force(sp.sym[i], po, p.eps2, b->ff_split + 3 * (size_t)o, range, (double4 *)tpart,
+                                  (double4 *)spart, s)))
+            return st;
+        return nb::sym64_integrate(sp.sym[i], po, pn, vel, (const double4 *)tpart, (const double4 *)spart,
+                                   p.damping, p.dt, p.kick, p.G, nullptr, s, range);
+    }
+    const float4 *po = b->pos[c] + o;
+    float4 *pn = b->pos[c ^ 1] + o, *vel = b->vel + o;
     if (b->sym) {
         if ((st = nb::sym_force(sp.sym[i], po, (float)p.eps2, tpart, spart, s))) return st;
         return nb::sym_integrate(sp.sym[i], po, pn, vel, tpart, spart, (float)p.damping, (float)p.dt,
@@ -1451,13 +1718,9 @@ int nb_batch_step_per_system(nb_batch *b, int steps, void *stream)
         b->sys_partial = t;
         b->sys_spart = u;
     }
-    std::vector<int> off(b->nsys + 1, 0);
-    for (int i = 0; i < b->nsys; ++i) off[i + 1] = off[i] + b->sizes[i];
     for (int t = 0; t < steps; ++t) {
         for (int i = 0; i < b->nsys; ++i) {
-            if ((st = sys_step(b, sp, i, b->pos[b->cur] + off[i], b->pos[b->cur ^ 1] + off[i],
-                               b->vel + off[i], b->sys_partial, b->sys_spart, s)))
-                return st;
+            if ((st = sys_step(b, sp, i, b->cur, b->sys_partial, b->sys_spart, b->ff_range, s))) return st;
         }
         b->cur ^= 1;
     }
@@ -1476,23 +1739,24 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
     if (ntasks < 1 || steps < 0) return set_error(NB_ERR_INVALID, "ntasks >= 1 and steps >= 0");
     NB_CUDA(cudaDeviceSynchronize());
     if (ntasks > b->nsys) ntasks = b->nsys > 0 ? b->nsys : 1;
-    std::vector<int> off(b->nsys + 1, 0);
-    for (int i = 0; i < b->nsys; ++i) off[i + 1] = off[i] + b->sizes[i];
     SysPlans sp;
     int st0 = sys_plans_for(b, &sp);
     if (st0) return st0;
     std::vector<float4 *> tscratch(ntasks, nullptr), sscratch(ntasks, nullptr);
+    std::vector<unsigned long long *> ranges(ntasks, nullptr);  // float-float scale records
     std::vector<cudaStream_t> streams(ntasks, nullptr);
     auto release = [&] {
         for (int t = 0; t < ntasks; ++t) {
             cudaFree(tscratch[t]);
             cudaFree(sscratch[t]);
+            cudaFree(ranges[t]);
             if (streams[t]) cudaStreamDestroy(streams[t]);
         }
     };
     for (int t = 0; t < ntasks; ++t) {
         cudaError_t e = cudaMalloc((void **)&tscratch[t], sp.tpart * sizeof(float4));
         if (e == cudaSuccess) e = cudaMalloc((void **)&sscratch[t], sp.spart * sizeof(float4));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&ranges[t], 2 * sizeof(unsigned long long));
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&streams[t], cudaStreamNonBlocking);
         if (e != cudaSuccess) {
             release();
@@ -1508,8 +1772,7 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
             for (int i = t; i < b->nsys && status[t] == NB_OK; i += ntasks) {
                 int c = cur;
                 for (int k = 0; k < steps && status[t] == NB_OK; ++k) {
-                    int st = sys_step(b, sp, i, b->pos[c] + off[i], b->pos[c ^ 1] + off[i], b->vel + off[i],
-                                      tscratch[t], sscratch[t], streams[t]);
+                    int st = sys_step(b, sp, i, c, tscratch[t], sscratch[t], ranges[t], streams[t]);
                     if (!st && cudaStreamSynchronize(streams[t]) != cudaSuccess) st = NB_ERR_CUDA;
                     status[t] = st;
                     c ^= 1;
@@ -1525,7 +1788,12 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
     return NB_OK;
 }
 
-int nb_batch_launches_per_step(nb_batch *b) { return b ? (b->nbody ? 2 : 0) : -1; }
+int nb_batch_launches_per_step(nb_batch *b)
+{
+    if (!b) return -1;
+    if (!b->nbody) return 0;
+    return b->f64 ? 4 : 2;  // float-float: scale reduction, split, force, integrate
+}
 
 // Batched adjoint: every system's state advanced `steps` steps with a
 // checkpoint every ckpt_every steps, then the reverse pass for all systems
@@ -1534,6 +1802,7 @@ int nb_batch_launches_per_step(nb_batch *b) { return b ? (b->nbody ? 2 : 0) : -1
 int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream)
 {
     if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
+    if (b->f64) return set_error(NB_ERR_UNSUPPORTED, "the batched adjoint runs NB_F32 batches");
     if (!b->has_state) return set_error(NB_ERR_STATE, "no state loaded");
     if (steps < 1 || ckpt_every < 1) return set_error(NB_ERR_INVALID, "steps and ckpt_every must be >= 1");
     if (ckpt_every > steps) ckpt_every = steps;
@@ -1603,6 +1872,7 @@ int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void 
                           void *gm, void *stream)
 {
     if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
+    if (b->f64) return set_error(NB_ERR_UNSUPPORTED, "the batched adjoint runs NB_F32 batches");
     if (!b->adj_ready) return set_error(NB_ERR_STATE, "nb_batch_adj_backward needs a preceding nb_batch_adj_forward");
     if (b->nbody == 0) return NB_OK;
     if (!gx_T || !gx0 || !gv0 || !gm) return set_error(NB_ERR_INVALID, "NULL gradient buffer");

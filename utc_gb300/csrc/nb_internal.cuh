@@ -244,6 +244,11 @@ int sym64_integrate(const SymPlan &p, const double4 *pos_old, double4 *pos_new, 
 int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl);
 int symff_force(const SymPlan &p, const double4 *pos, double eps2, float4 *split, unsigned long long *range,
                 double4 *tpart, double4 *spart, cudaStream_t s, int phi = 0);
+// The float-float paths' per-step preparation: range (2 unsigned long long)
+// <- bits of the largest |coordinate| and |mass|; H + M + L <- the positions
+// and masses scaled by those powers of two, split into three floats.
+int ff_scale_split(const double4 *pos, int n, int sms, float4 *H, float4 *M, float4 *L, unsigned long long *range,
+                   cudaStream_t s);
 
 // Compensated kick / drift from compensated symmetric partials, or
 // (acc_out != nullptr) the bare FP64 accelerations (nb_precision.cu)

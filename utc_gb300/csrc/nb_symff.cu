@@ -39,145 +39,10 @@
 // oracle (FP64 arithmetic: a few 1e-16), not bit-identical (NB_ALGO_EXACT is).
 // Range: the scaled squared distances and eps2 must stay normal floats:
 // eps2 >= 2^-100 max|x|^2 and body masses >= 2^-100 of the largest.
-#include "nb_internal.cuh"
+#include "nb_ff.cuh"
 
 namespace nb {
 
-namespace {
-
-// Knuth's two-sum: s + e == a + b exactly.
-__device__ __forceinline__ void ff_two_sum(float a, float b, float &s, float &e)
-{
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-// Dekker's fast two-sum, exact when |a| >= |b| (or a == 0).
-__device__ __forceinline__ void ff_fast_two_sum(float a, float b, float &s, float &e)
-{
-    s = __fadd_rn(a, b);
-    e = __fsub_rn(b, __fsub_rn(s, a));
-}
-
-// r = s - p from three-float parts, as a normalized float-float: the high
-// and middle differences error-free, the low one rounded (2^-72 |x|).
-__device__ __forceinline__ void ff_diff(float sh, float sm, float sl, float ph, float pm, float pl, float &rh,
-                                        float &rl)
-{
-    float A, a, B, b, s1, e1;
-    ff_two_sum(sh, -ph, A, a);
-    ff_two_sum(sm, -pm, B, b);
-    const float C = __fsub_rn(sl, pl);
-    ff_two_sum(A, B, s1, e1);
-    const float t = __fadd_rn(__fadd_rn(e1, a), __fadd_rn(b, C));
-    ff_two_sum(s1, t, rh, rl);
-}
-
-// A += r * w (float-float, renormalized)
-__device__ __forceinline__ void ff_acc(float &Ah, float &Al, float rh, float rl, float wh, float wl)
-{
-    const float p = __fmul_rn(rh, wh);
-    float e = __fmaf_rn(rh, wh, -p);
-    e = __fmaf_rn(rh, wl, e);
-    e = __fmaf_rn(rl, wh, e);
-    float s, t;
-    ff_two_sum(Ah, p, s, t);
-    ff_fast_two_sum(s, __fadd_rn(Al, __fadd_rn(t, e)), Ah, Al);
-}
-
-struct FFPair {
-    float rxh, rxl, ryh, ryl, rzh, rzl;  // r = x_j - x_i
-    float wjh, wjl;                      // m_j inv^3 (weight on the target)
-    float wih, wil;                      // m_i inv^3 with m_i as passed (reaction)
-    float yh, yl;                        // inv = 1/sqrt(|r|^2 + eps2)
-};
-
-// A += v (float-float, renormalized)
-__device__ __forceinline__ void ff_add(float &Ah, float &Al, float vh, float vl)
-{
-    float s, t;
-    ff_two_sum(Ah, vh, s, t);
-    ff_fast_two_sum(s, __fadd_rn(Al, __fadd_rn(t, vl)), Ah, Al);
-}
-
-// m * y for a float-float mass (mh, ml) and y (yh, yl), unnormalized
-__device__ __forceinline__ void ff_mul(float mh, float ml, float yh, float yl, float &ph, float &pl)
-{
-    ph = __fmul_rn(mh, yh);
-    float e = __fmaf_rn(mh, yh, -ph);
-    e = __fmaf_rn(mh, yl, e);
-    pl = __fmaf_rn(ml, yh, e);
-}
-
-// Pair pieces for source (sH, sM, sL) and target (p*), eps2 = eh + el.
-template <bool REACT>
-__device__ __forceinline__ void ff_pair(float4 sH, float4 sM, float4 sL, float pxh, float pxm, float pxl, float pyh,
-                                        float pym, float pyl, float pzh, float pzm, float pzl, float mih, float mil,
-                                        float eh, float el, FFPair &o)
-{
-    ff_diff(sH.x, sM.x, sL.x, pxh, pxm, pxl, o.rxh, o.rxl);
-    ff_diff(sH.y, sM.y, sL.y, pyh, pym, pyl, o.ryh, o.ryl);
-    ff_diff(sH.z, sM.z, sL.z, pzh, pzm, pzl, o.rzh, o.rzl);
-    // squares as (p, e) with p + e = r^2 to float-float accuracy
-    const float qx = __fmul_rn(o.rxh, o.rxh), qy = __fmul_rn(o.ryh, o.ryh), qz = __fmul_rn(o.rzh, o.rzh);
-    float ex = __fmaf_rn(o.rxh, o.rxh, -qx), ey = __fmaf_rn(o.ryh, o.ryh, -qy), ez = __fmaf_rn(o.rzh, o.rzh, -qz);
-    ex = __fmaf_rn(__fadd_rn(o.rxh, o.rxh), o.rxl, ex);
-    ey = __fmaf_rn(__fadd_rn(o.ryh, o.ryh), o.ryl, ey);
-    ez = __fmaf_rn(__fadd_rn(o.rzh, o.rzh), o.rzl, ez);
-    float S, t1, t2, t3;
-    ff_two_sum(eh, qx, S, t1);
-    ff_two_sum(S, qy, S, t2);
-    ff_two_sum(S, qz, S, t3);
-    const float L = __fadd_rn(__fadd_rn(__fadd_rn(el, ex), __fadd_rn(ey, ez)), __fadd_rn(__fadd_rn(t1, t2), t3));
-    float Dh, Dl;
-    ff_fast_two_sum(S, L, Dh, Dl);  // all terms >= 0: |S| >= |L|
-    // 1/sqrt(D): one Halley step from the FP32 approximation
-    const float y0 = rsqrt_approx(Dh);
-    const float q = __fmul_rn(y0, y0);
-    const float qe = __fmaf_rn(y0, y0, -q);
-    const float t = __fmul_rn(Dh, q);
-    float c = __fmaf_rn(Dh, q, -t);
-    c = __fmaf_rn(Dh, qe, c);
-    c = __fmaf_rn(Dl, q, c);
-    const float u = __fsub_rn(__fsub_rn(1.0f, t), c);  // 1 - t is exact (t near 1)
-    const float corr = __fmul_rn(y0, __fmul_rn(u, __fmaf_rn(0.375f, u, 0.5f)));
-    float yh, yl;
-    ff_fast_two_sum(y0, corr, yh, yl);
-    o.yh = yh;
-    o.yl = yl;
-    // inv^3 = y^3
-    const float p2 = __fmul_rn(yh, yh);
-    float e2 = __fmaf_rn(yh, yh, -p2);
-    e2 = __fmaf_rn(__fadd_rn(yh, yh), yl, e2);
-    const float p3 = __fmul_rn(p2, yh);
-    float e3 = __fmaf_rn(p2, yh, -p3);
-    e3 = __fmaf_rn(p2, yl, e3);
-    e3 = __fmaf_rn(e2, yh, e3);
-    float y3h, y3l;
-    ff_fast_two_sum(p3, e3, y3h, y3l);
-    // weights (mass as the float-float h + m of its split)
-    o.wjh = __fmul_rn(sH.w, y3h);
-    float we = __fmaf_rn(sH.w, y3h, -o.wjh);
-    we = __fmaf_rn(sH.w, y3l, we);
-    o.wjl = __fmaf_rn(sM.w, y3h, we);
-    if (REACT) {
-        o.wih = __fmul_rn(mih, y3h);
-        float wr = __fmaf_rn(mih, y3h, -o.wih);
-        wr = __fmaf_rn(mih, y3l, wr);
-        o.wil = __fmaf_rn(mil, y3h, wr);
-    }
-}
-
-// binary exponent e of a non-negative double given by its bits, with
-// 2^(e-1) <= v < 2^e; 0 for zero, subnormal, infinite or NaN values
-__device__ __forceinline__ int ff_exponent(unsigned long long bits)
-{
-    const int field = (int)((bits >> 52) & 0x7ff);
-    return (field == 0 || field == 0x7ff) ? 0 : field - 1022;
-}
-
-}  // namespace
 
 // range[0] = bits of max |coordinate|, range[1] = bits of max |mass| (non-
 // negative doubles order like their bit patterns); range zeroed beforehand.
@@ -444,6 +309,20 @@ int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl)
     return NB_OK;
 }
 
+int ff_scale_split(const double4 *pos, int n, int sms, float4 *H, float4 *M, float4 *L, unsigned long long *range,
+                   cudaStream_t s)
+{
+    if (n == 0) return NB_OK;
+    NB_CUDA(cudaMemsetAsync(range, 0, 2 * sizeof(unsigned long long), s));
+    const long long want = (n + 255) / 256, cap = 4ll * (sms > 0 ? sms : 1);
+    const long long blocks = want < cap ? want : cap;
+    ff_range_kernel<<<(unsigned)blocks, 256, 0, s>>>(pos, n, range);
+    NB_LAUNCH_CHECK("ff_range_kernel launch");
+    ff_split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(pos, n, range, H, M, L);
+    NB_LAUNCH_CHECK("ff_split_kernel launch");
+    return NB_OK;
+}
+
 int symff_force(const SymPlan &p, const double4 *pos, double eps2, float4 *split, unsigned long long *range,
                 double4 *tpart, double4 *spart, cudaStream_t s, int phi)
 {
@@ -451,13 +330,8 @@ int symff_force(const SymPlan &p, const double4 *pos, double eps2, float4 *split
     symff_kernel_t k = symff_kernel_for(p.warps, p.bpt, phi != 0);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "float-float symmetric kernel shape not compiled");
     float4 *H = split, *M = split + p.n, *L = split + 2 * (size_t)p.n;
-    NB_CUDA(cudaMemsetAsync(range, 0, 2 * sizeof(unsigned long long), s));
-    const long long want = (p.n + 255) / 256, cap = 4ll * (p.sms > 0 ? p.sms : 1);
-    const long long blocks = want < cap ? want : cap;
-    ff_range_kernel<<<(unsigned)blocks, 256, 0, s>>>(pos, p.n, range);
-    NB_LAUNCH_CHECK("ff_range_kernel launch");
-    ff_split_kernel<<<(unsigned)((p.n + 255) / 256), 256, 0, s>>>(pos, p.n, range, H, M, L);
-    NB_LAUNCH_CHECK("ff_split_kernel launch");
+    int st = ff_scale_split(pos, p.n, p.sms, H, M, L, range, s);
+    if (st) return st;
     k<<<p.grid, 32 * p.warps, 0, s>>>(H, M, L, p.n, eps2, range, tpart, spart, p.total, p.nc, p.nrb);
     NB_LAUNCH_CHECK("symff_force_kernel launch");
     return NB_OK;

@@ -245,15 +245,20 @@ def probe_fma_peak(iters=20000, packed=True, stream=None):
 
 class NBodyBatch:
     """Many independent systems (sizes[s] bodies each) in one context; state
-    arrays are the systems' (n, 4) float32 arrays concatenated.  algo "sym"
-    (each unordered pair once) or "fast" (directed)."""
+    arrays are the systems' (n, 4) arrays concatenated: float32 for precision
+    "f32" (algo "sym", each unordered pair once, or "fast", directed), float64
+    for "f64" (algo "sym": float-float pair terms on the FP32 pipe, the
+    reference multi-task app's default state type)."""
 
     def __init__(self, sizes, kick="physical", eps2=1e-3, damping=1.0, dt=1e-3, G=1.0,
-                 warps_per_cta=0, bodies_per_lane=0, algo="sym"):
+                 warps_per_cta=0, bodies_per_lane=0, algo="sym", precision="f32"):
         self.lib = N.lib()
         p = N.NbParams()
         self.lib.nb_params_default(C.byref(p))
+        p.precision = _PREC[precision]
         p.algo = _ALGO[algo]
+        self.precision = precision
+        self.dtype = np.float64 if precision == "f64" else np.float32
         p.kick = _KICK[kick]
         p.eps2, p.damping, p.dt, p.G = float(eps2), float(damping), float(dt), float(G)
         p.block = int(warps_per_cta) * 32
@@ -288,23 +293,24 @@ class NBodyBatch:
         s = current_stream_handle() if stream is None else stream
         if _is_torch(pos) or _is_torch(vel):
             torch = _torch()
-            p = _device_buffer(pos, (self.nbody, 4), torch.float32, "pos")
-            v = _device_buffer(vel, (self.nbody, 4), torch.float32, "vel")
+            tdt = torch.float64 if self.dtype == np.float64 else torch.float32
+            p = _device_buffer(pos, (self.nbody, 4), tdt, "pos")
+            v = _device_buffer(vel, (self.nbody, 4), tdt, "vel")
             N.check(self.lib.nb_batch_set_state(self.handle, C.c_void_p(p.data_ptr()),
                                                 C.c_void_p(v.data_ptr()), N.NB_DEVICE, C.c_void_p(s)),
                     "nb_batch_set_state")
             if p is not pos or v is not vel:
                 torch.cuda.synchronize()  # the copies read converted temporaries
             return
-        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(self.nbody, 4)
-        vel = np.ascontiguousarray(vel, dtype=np.float32).reshape(self.nbody, 4)
+        pos = np.ascontiguousarray(pos, dtype=self.dtype).reshape(self.nbody, 4)
+        vel = np.ascontiguousarray(vel, dtype=self.dtype).reshape(self.nbody, 4)
         N.check(self.lib.nb_batch_set_state(self.handle, pos.ctypes.data_as(C.c_void_p),
                                             vel.ctypes.data_as(C.c_void_p), N.NB_HOST, C.c_void_p(s)),
                 "nb_batch_set_state")
 
     def get_state(self, stream=None):
-        pos = np.empty((self.nbody, 4), np.float32)
-        vel = np.empty((self.nbody, 4), np.float32)
+        pos = np.empty((self.nbody, 4), self.dtype)
+        vel = np.empty((self.nbody, 4), self.dtype)
         s = current_stream_handle() if stream is None else stream
         N.check(self.lib.nb_batch_get_state(self.handle, pos.ctypes.data_as(C.c_void_p),
                                             vel.ctypes.data_as(C.c_void_p), N.NB_HOST, C.c_void_p(s)),
