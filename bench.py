@@ -680,9 +680,10 @@ def run_batched(args):
     ps, vs = [], []
     for k, nn in enumerate(sizes):
         p, v = ics.plummer(int(nn), seed=1000 + k)
-        ps.append(ics.f32(p))
-        vs.append(ics.f32(v))
-    pos, vel = np.concatenate(ps), np.concatenate(vs)
+        ps.append(p)
+        vs.append(v)
+    pos64, vel64 = np.concatenate(ps), np.concatenate(vs)
+    pos, vel = ics.f32(pos64), ics.f32(vel64)
     pairs = float(np.sum(sizes.astype(np.float64) ** 2))
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
@@ -784,6 +785,39 @@ def run_batched(args):
                             "launched step by step"},
     })
     out["other_algo"] = graph_and_per_system(other)
+
+    # FP64 state (the reference multi-task app's FTYPE double): the
+    # float-float batched kernel against per-system float-float launches and
+    # the reference's task pattern, same systems, 10 steps
+    f64_steps = 10
+    with torch.cuda.stream(stream), NBodyBatch(sizes, kick="physical", eps2=1e-3, dt=1e-3,
+                                               precision="f64") as b:
+        b.set_state(pos64, vel64, stream=sh)
+        tune64 = b.autotune(reps=1, cache_path=cache, stream=sh)
+        res = {}
+        for name, fn in (("graph", lambda: b.run(f64_steps, sh)),
+                         ("per_system", lambda: b.step_per_system(f64_steps, sh))):
+            b.set_state(pos64, vel64, stream=sh)
+            fn()  # warm-up
+            b.set_state(pos64, vel64, stream=sh)
+            stream.synchronize()
+            a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            c.record(stream)
+            c.synchronize()
+            res[name] = a.elapsed_time(c)
+        b.set_state(pos64, vel64, stream=sh)
+        stream.synchronize()
+        t0 = time.perf_counter()
+        b.step_tasks(f64_steps, ntasks)
+        res["tasks"] = (time.perf_counter() - t0) * 1e3
+    out["f64"] = {"steps": f64_steps, "kernel": "bksff_force_kernel (float-float, FP64 state)",
+                  "autotune": tune64, "ms_batched_graph": res["graph"],
+                  "ms_per_system_launches": res["per_system"], "ms_per_system_tasks": res["tasks"],
+                  "speedup_vs_per_system": res["per_system"] / res["graph"],
+                  "speedup_vs_per_system_tasks": res["tasks"] / res["graph"],
+                  "G_interactions_per_s_batched": pairs * f64_steps / (res["graph"] * 1e-3) / 1e9}
     out["speedup_vs_other_algo_per_system"] = out["other_algo"]["ms_per_system_launches"] / t_graph
     print(json.dumps(out), flush=True)
     return 0
