@@ -217,10 +217,13 @@ int nb_step_f32_noalloc(const float *pos_old, float *pos_new, float *vel, int n,
  * Batches: many independent systems of uneven size advanced together, one
  * persistent launch per step for all of them.  Replaces running one
  * Task<BodySystemSGPU<T>> per system (benchapps/nbody/utc/nbody_mtask.cc:
- * 199-231).  Bodies of all systems are concatenated float4 (system s after
- * systems 0..s-1); all systems share eps2, damping, dt, G and kick mode from
- * *p (p->n is ignored; p->block / p->bpt, when set, give the initial warps per
- * CTA * 32 and bodies per lane).
+ * 199-231).  Bodies of all systems are concatenated (system s after
+ * systems 0..s-1): float4 for NB_F32 batches (NB_ALGO_SYM or NB_ALGO_FAST),
+ * double4 for NB_F64 batches (NB_ALGO_SYM: float-float pair terms, the
+ * multi-task app's FTYPE double; no batched adjoint).  All systems share
+ * eps2, damping, dt, G and kick mode from *p (p->n is ignored; p->block /
+ * p->bpt, when set, give the initial warps per CTA * 32 and bodies per
+ * lane).
  * ---------------------------------------------------------------------- */
 typedef struct nb_batch nb_batch;
 int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **out);
