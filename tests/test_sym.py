@@ -140,6 +140,29 @@ def test_sym_f64_close_pairs_far_from_origin(cuda, algo):
 
 
 @pytest.mark.parametrize("algo", F64_SYM)
+def test_sym_f64_tight_binaries(cuda, algo):
+    """Tight binaries (separation 1e-4, softening 1e-5 of it): each body's
+    acceleration is dominated by its partner's single pair term, so the pair
+    term's own accuracy is the result's -- checked per body, without the
+    mean-magnitude cushion, to 5e-14."""
+    nb = 600
+    rng = np.random.default_rng(12)
+    c = rng.normal(size=(nb, 3))
+    d = rng.normal(size=(nb, 3))
+    d *= 1e-4 / np.linalg.norm(d, axis=1, keepdims=True)
+    p = np.empty((2 * nb, 4))
+    p[0::2, :3] = c - d / 2
+    p[1::2, :3] = c + d / 2
+    p[:, 3] = rng.uniform(0.5, 1.5, 2 * nb)
+    with NBodySystem(2 * nb, "f64", algo, eps2=1e-18) as s:
+        s.set_state(p, np.zeros_like(p))
+        a = s.accel()
+    want = oracle.accel(p, 1e-18)
+    rel = np.linalg.norm(a - want, axis=1) / np.linalg.norm(want, axis=1)
+    assert rel.max() <= 5e-14, rel.max()
+
+
+@pytest.mark.parametrize("algo", F64_SYM)
 def test_sym_f64_si_units(cuda, algo):
     """Planetary magnitudes in SI units (positions ~1e11 m, masses ~1e24 to
     1e30 kg, eps2 = (1e7 m)^2): unscaled, the float-float kernel's inv^3

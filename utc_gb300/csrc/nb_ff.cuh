@@ -96,8 +96,11 @@ __device__ __forceinline__ void ff_pair(float4 sH, float4 sM, float4 sL, float p
     const float L = __fadd_rn(__fadd_rn(__fadd_rn(el, ex), __fadd_rn(ey, ez)), __fadd_rn(__fadd_rn(t1, t2), t3));
     float Dh, Dl;
     ff_fast_two_sum(S, L, Dh, Dl);  // all terms >= 0: |S| >= |L|
-    // 1/sqrt(D): one Halley step from the FP32 approximation
-    const float y0 = rsqrt_approx(Dh);
+    // 1/sqrt(D): the FP32 approximation, one Newton step in FP32 (error
+    // near 2^-24, so that u below is near 2^-23 and the roundings that scale
+    // with it stay near 2^-47), then one Halley step in float-float
+    const float ya = rsqrt_approx(Dh);
+    const float y0 = __fmaf_rn(__fmul_rn(ya, 0.5f), __fmaf_rn(-Dh, __fmul_rn(ya, ya), 1.0f), ya);
     const float q = __fmul_rn(y0, y0);
     const float qe = __fmaf_rn(y0, y0, -q);
     const float t = __fmul_rn(Dh, q);

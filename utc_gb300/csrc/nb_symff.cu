@@ -24,18 +24,18 @@
 //    as FP64's own difference, also for close pairs far from the origin
 //    (a two-float split would lose the position bits below 2^-49 |x|);
 //  * d2 = |r|^2 + eps2 in float-float;
-//  * 1/sqrt(d2): the FP32 approximation y0 refined by one Halley step,
-//    y = y0 (1 + t/2 + 3t^2/8) with t = 1 - d2 y0^2 formed from an
-//    error-free y0^2 (cubic convergence: the approximation's 2^-23 becomes
-//    the arithmetic's 2^-48);
+//  * 1/sqrt(d2): the FP32 approximation refined by one FP32 Newton step
+//    (to ~2^-24) and one Halley step in float-float, y = y0 (1 + t/2 +
+//    3t^2/8) with t = 1 - d2 y0^2 formed from an error-free y0^2 (cubic
+//    convergence; the small t keeps the correction's roundings near 2^-47);
 //  * inv^3, the weights m_j inv^3 and m_i inv^3, and the six products with
 //    r in float-float; target and reaction sums in float-float, renormalized
 //    after every term.
 // Each target's 32-source chunk sum is folded into FP64 accumulators; each
 // reaction (one chunk body, the warp's 32*BPT targets) is written as FP64.
 // The FP64 integrator of nb_sym64.cu then sums the partials in FP64, undoes
-// the scaling and integrates.  246 FP32 operations and one approximation
-// per pair (123 per interaction); results within a few 1e-15 of the FP64
+// the scaling and integrates.  250 FP32 operations and one approximation
+// per pair (125 per interaction); results within a few 1e-15 of the FP64
 // oracle (FP64 arithmetic: a few 1e-16), not bit-identical (NB_ALGO_EXACT is).
 // Range: the scaled squared distances and eps2 must stay normal floats:
 // eps2 >= 2^-100 max|x|^2 and body masses >= 2^-100 of the largest.
