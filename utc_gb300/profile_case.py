@@ -10,7 +10,8 @@ case adjoint: a checkpointed forward of `steps` steps (one segment) and the
               reverse pass (`steps` VJP launches) on a uniform cube
               (eps2=1e-2, dt=1e-3);
 case batch:   `steps` batched steps of `systems` Plummer systems with sizes
-              log-uniform in [128, n].
+              log-uniform in [128, n] (float state, or double with
+              --precision f64).
 Prints the launch plan; used as the command under ncu.
 """
 import argparse
@@ -37,12 +38,14 @@ def main():
 
     if a.case == "batch":
         sizes = ics.batch_sizes(a.systems, lo=128, hi=a.n, seed=0)
+        f64 = a.precision == "f64"
         ps, vs = [], []
         for k, nn in enumerate(sizes):
             p, v = ics.plummer(int(nn), seed=1000 + k)
-            ps.append(ics.f32(p))
-            vs.append(ics.f32(v))
-        with NBodyBatch(sizes, kick=a.kick, eps2=np.float32(1e-3), dt=np.float32(1e-3), algo=a.algo,
+            ps.append(p if f64 else ics.f32(p))
+            vs.append(v if f64 else ics.f32(v))
+        with NBodyBatch(sizes, kick=a.kick, eps2=1e-3 if f64 else np.float32(1e-3),
+                        dt=1e-3 if f64 else np.float32(1e-3), algo=a.algo, precision="f64" if f64 else "f32",
                         warps_per_cta=a.block // 32, bodies_per_lane=a.bpt) as b:
             b.set_state(np.concatenate(ps), np.concatenate(vs))
             b.step(a.steps)
