@@ -119,6 +119,25 @@ def test_sym_f64_accel_vs_oracle(cuda, n, algo):
     assert close(a, oracle.accel(p, 1e-3), tol=1e-13)
 
 
+@pytest.mark.parametrize("algo,shape", [("sym", s) for s in [(32, 2), (32, 4), (128, 4), (256, 4), (256, 8)]] +
+                         [("sym64", s) for s in [(32, 8), (32, 4), (128, 8), (256, 8)]])
+@pytest.mark.parametrize("n", [1000, 4097])
+def test_sym_f64_every_shape_vs_oracle(cuda, algo, shape, n):
+    """Every compiled shape of both FP64-state symmetric kernels, including
+    the multi-warp ones the default plan only picks for large N (their
+    reactions are summed across the CTA's warps through shared memory)."""
+    p, _ = ics.plummer(n, seed=n + 1)
+    with NBodySystem(n, "f64", algo, eps2=1e-3, block=shape[0], bpt=shape[1]) as s:
+        info = s.plan_info()
+        assert (info["block"], info["bpt"]) == shape
+        s.set_state(p, np.zeros_like(p))
+        a = s.accel()
+        e, bodies = s.energy(with_bodies=True)
+    want = oracle.accel(p, 1e-3)
+    assert close(a, want, tol=1e-13)
+    assert close(bodies[:, :3], want, tol=1e-13)
+
+
 @pytest.mark.parametrize("algo", F64_SYM)
 def test_sym_f64_close_pairs_far_from_origin(cuda, algo):
     """A dense core (radius 0.05) inside a halo, both 3.6e3 from the origin:
