@@ -268,9 +268,11 @@ def test_drop_in_task_f64_exact_matches_oracle(cuda):
         assert out[k].tobytes() == p.tobytes()
 
 
-def test_drop_in_task_f64_default_symmetric(cuda):
-    """The double task's default algorithm (FP64 symmetric) against the
-    FP64 oracle: positions within 1e-12 relative after the run."""
+@pytest.mark.parametrize("memtype", [0, 1, 2])
+def test_drop_in_task_f64_default_symmetric(cuda, memtype):
+    """The double task's default algorithm (the float-float symmetric kernel)
+    against the FP64 oracle, frames every 4 steps, pageable / pinned / unified
+    staging: positions within 1e-12 relative in every frame."""
     import ctypes as C
 
     from utc_gb300 import _native as N
@@ -283,7 +285,7 @@ def test_drop_in_task_f64_default_symmetric(cuda):
     rt = (C.c_double * 4)()
     rc = N.task_lib().nbt_run_f64(n, eps2, float(np.float32(damp)), pos.ctypes.data_as(C.c_void_p),
                                   vel.ctypes.data_as(C.c_void_p), rt, loops, oi, 128,
-                                  float(np.float32(dt)), out.ctypes.data_as(C.c_void_p), 0, -1, 0)
+                                  float(np.float32(dt)), out.ctypes.data_as(C.c_void_p), memtype, -1, 0)
     assert rc == 0
     p, v = pos, vel
     for k in range(loops // oi):
