@@ -1,0 +1,91 @@
+"""The drop-in task (BodySystemGB300<T> on the UTC task stand-in) run on the
+CPU against a host-only mock of the C ABI (tests/mock_abi.cc: nb_run_host
+steps with the oracle; the stand-in's four CUDA runtime calls hand out a
+recognisable fake stream).  Checks the task's plumbing without a GPU:
+initImpl keeps the caller's pointers and runImpl reads them at run time,
+frames land at outbuffer + f * 4N, runtime[4] is filled, the parameters and
+the worker's own stream reach the C ABI, the input arrays are not updated,
+and a failing C-ABI call comes back as the task's status.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def mock_task(tmp_path_factory):
+    oracle.build(ref=False)
+    out = str(tmp_path_factory.mktemp("taskmock") / "libtaskmock.so")
+    cuda_home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    odir = os.path.join(REPO, "oracle")
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-shared", "-o", out,
+           os.path.join(REPO, "utc_gb300", "task", "body_task_gb300.cc"), os.path.join(REPO, "tests", "mock_abi.cc"),
+           "-I", os.path.join(REPO, "include"), "-I", os.path.join(REPO, "utc_gb300", "task"), "-I", odir,
+           "-I", os.path.join(cuda_home, "include"), "-L", odir, "-loracle", "-Wl,-rpath," + odir, "-lpthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    lib = C.CDLL(out)
+    vp, I, D = C.c_void_p, C.c_int, C.c_double
+    lib.nbt_run_f64.argtypes = [C.c_uint, D, D, vp, vp, vp, I, I, I, D, vp, I, I, I]
+    lib.nbt_run_f32.argtypes = [C.c_uint, C.c_float, C.c_float, vp, vp, vp, I, I, I, C.c_float, vp, I, I, I]
+    lib.mock_fake_stream.restype = vp
+    lib.mock_record.argtypes = [C.POINTER(vp), vp, vp]
+    return lib
+
+
+def record(lib):
+    s = C.c_void_p()
+    ints = np.zeros(9, np.int32)
+    dbl = np.zeros(3, np.float64)
+    lib.mock_record(C.byref(s), ints.ctypes.data_as(C.c_void_p), dbl.ctypes.data_as(C.c_void_p))
+    return s.value, ints, dbl
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_task_plumbing_on_the_mock(mock_task, dtype):
+    n, loops, oi = 96, 12, 4
+    pos, vel = oracle.randomize(1, n, dtype)
+    pos0, vel0 = pos.copy(), vel.copy()
+    eps2, damp, dt = 0.01, 0.999, 0.005
+    frames = np.full((loops // oi + 1, n, 4), -7.0, dtype)  # one spare frame stays untouched
+    rt = np.zeros(4, np.float64)
+    run = mock_task.nbt_run_f64 if dtype == np.float64 else mock_task.nbt_run_f32
+    rc = run(n, eps2, damp, pos.ctypes.data, vel.ctypes.data, rt.ctypes.data, loops, oi, 128, dt,
+             frames.ctypes.data, 1, -1, 0)
+    assert rc == 0
+    # the caller's arrays are read, not updated (body_task_sgpu.cu:20-26)
+    assert np.array_equal(pos, pos0) and np.array_equal(vel, vel0)
+    # frames f = 0.. at outbuffer + f * 4N, each after (f + 1) * oi steps
+    p, v = pos0, vel0
+    for f in range(loops // oi):
+        p, v = oracle.step(p, v, dtype(eps2), dtype(damp), dtype(dt), oi)
+        assert np.array_equal(frames[f], p)
+    assert (frames[-1] == -7.0).all()
+    assert list(rt) == [1.0, 2.0, 3.0, 4.0]
+    stream, ints, dbl = record(mock_task)
+    calls, rn, rloops, roi, prec, algo, memtype, made, destroyed = ints
+    assert stream == mock_task.mock_fake_stream()  # launched on the worker's own stream
+    assert (rn, rloops, roi) == (n, loops, oi)
+    assert prec == (1 if dtype == np.float64 else 0)  # NB_F64 / NB_F32
+    assert algo == 2  # NB_ALGO_SYM, the task's default for both state types
+    assert memtype == 1  # NB_MEM_PINNED passed through
+    np.testing.assert_allclose(dbl, [float(dtype(eps2)), float(dtype(damp)), float(dtype(dt))])
+    assert made >= 1 and destroyed >= 1  # the worker made and released its stream
+
+
+def test_task_reports_a_failing_call(mock_task):
+    n = 3  # the mock refuses this size
+    pos, vel = oracle.randomize(1, 4, np.float64)
+    frames = np.full((2, 4, 4), -7.0)
+    rt = np.zeros(4, np.float64)
+    rc = mock_task.nbt_run_f64(n, 0.01, 1.0, pos.ctypes.data, vel.ctypes.data, rt.ctypes.data, 2, 1, 128, 0.01,
+                               frames.ctypes.data, 0, -1, 0)
+    assert rc == 1  # NB_ERR_INVALID from nb_create, kept as the task's status
+    assert (frames == -7.0).all() and (rt == 0).all()
