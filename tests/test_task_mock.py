@@ -28,7 +28,10 @@ def mock_task(tmp_path_factory):
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-shared", "-o", out,
            os.path.join(REPO, "utc_gb300", "task", "body_task_gb300.cc"), os.path.join(REPO, "tests", "mock_abi.cc"),
            "-I", os.path.join(REPO, "include"), "-I", os.path.join(REPO, "utc_gb300", "task"), "-I", odir,
-           "-I", os.path.join(cuda_home, "include"), "-L", odir, "-loracle", "-Wl,-rpath," + odir, "-lpthread"]
+           "-I", os.path.join(cuda_home, "include"), "-L", odir, "-loracle", "-Wl,-rpath," + odir, "-lpthread",
+           # bind the library's calls to its own mock definitions even when a real CUDA runtime (torch's)
+           # is already in the process's global symbol scope
+           "-Wl,-Bsymbolic"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     lib = C.CDLL(out)
