@@ -362,3 +362,35 @@ def test_zero_softening_is_nan_like_the_reference(cuda, prec, algo):
     with NBodySystem(64, prec, algo, kick="physical", eps2=0.0, damping=1.0) as s:
         s.set_state(host, np.zeros_like(host))
         assert np.isnan(s.accel()).all()
+
+
+TOL = {("f32", "fast"): 2e-5, ("f32", "sym"): 2e-5, ("f32", "exact"): 2e-5, ("f64", "exact"): 1e-14,
+       ("f64", "sym"): 1e-13, ("f64", "sym64"): 1e-13, ("f32comp", "fast"): 2e-6, ("f32comp", "sym"): 2e-6}
+
+
+@pytest.mark.parametrize("prec,algo", MODES)
+@pytest.mark.parametrize("n", [1, 3, 4, 5, 127, 128, 129])
+def test_small_sizes_every_mode(cuda, prec, algo, n):
+    """The small sizes of the test plan (tails of every tile and warp): the
+    accelerations against the oracle at each mode's tolerance, and one step's
+    positions against the oracle's step."""
+    p, v = ics.plummer(n, seed=50 + n)
+    dt = dtype_of(prec)
+    pos = p.astype(np.float32).astype(dt) if prec == "f32" else p.astype(dt)
+    vel = v.astype(np.float32).astype(dt) if prec == "f32" else v.astype(dt)
+    eps2 = 1e-2 if dt == np.float64 else np.float32(1e-2)
+    with NBodySystem(n, prec, algo, kick="physical", eps2=eps2, damping=1.0, dt=1e-3 if dt == np.float64
+                     else np.float32(1e-3)) as s:
+        s.set_state(pos, vel)
+        a = np.asarray(s.accel(), np.float64)
+        s.step(1)
+        p1, _ = s.get_state()
+    want = oracle.accel(np.asarray(pos, np.float64), float(eps2))
+    d = np.linalg.norm(a - want, axis=1)
+    w = np.linalg.norm(want, axis=1)
+    assert (d <= TOL[(prec, algo)] * (w + w.mean())).all()
+    wp, _ = oracle.step(np.asarray(pos, np.float64), np.asarray(vel, np.float64), float(eps2), 1.0,
+                        float(np.float32(1e-3)) if dt != np.float64 else 1e-3, 1, kick_mode=oracle.KICK_PHYSICAL)
+    rel = np.linalg.norm(np.asarray(p1, np.float64)[:, :3] - wp[:, :3], axis=1) / (
+        np.linalg.norm(wp[:, :3], axis=1) + 0.1)
+    assert rel.max() <= 1e-6
