@@ -282,8 +282,9 @@ size_t nb_ics_scratch_bytes(int n);
 /* Device pointers of the current state (valid until the next nb_step). */
 int nb_state_ptrs(nb_ctx *ctx, void **pos_dev, void **vel_dev);
 
-/* Resolved launch shape of the fast kernel: {block, bpt, grid, target
- * block size, slots}. */
+/* Resolved launch shape of the context's force kernel: {block, bpt, grid,
+ * target block size, slots}; for the symmetric kernels block = warps per
+ * CTA * 32, bpt = targets per lane and the target block is the row block. */
 int nb_plan_info(nb_ctx *ctx, int *info5);
 
 /* Number of kernels nb_step launches per step for this context. */
