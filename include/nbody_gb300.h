@@ -77,14 +77,15 @@ typedef enum {
      * order; deterministic.  NB_F32, NB_F32_COMP (compensated partial sums)
      * and NB_F64: pair terms in float-float arithmetic on the FP32 pipe
      * (positions scaled by powers of two and split exactly into three
-     * floats, error-free sums and products, one Halley step on the FP32
-     * rsqrt; chunk sums folded into FP64), within a few 1e-15 of the FP64
+     * floats, error-free sums and products, an FP32 Newton and a
+     * float-float Halley step on the FP32 rsqrt; chunk sums folded into
+     * FP64), within a few 1e-15 of the FP64
      * reference, not bit for bit.  Range for NB_F64: eps2 >= 2^-100 max|x|^2
      * and masses >= 2^-100 of the largest. */
     NB_ALGO_SYM = 2,
     /* NB_F64 only: the symmetric algorithm in FP64 arithmetic throughout
      * (1/sqrt from the FP64 approximation and two Newton steps), within a
-     * few 1e-16 of the FP64 reference, any range; about 1/5.7 the speed of
+     * few 1e-16 of the FP64 reference, any range; about 1/5 the speed of
      * NB_ALGO_SYM on GB300's narrow FP64 pipe. */
     NB_ALGO_SYM_FP64 = 3
 } nb_algo;
@@ -161,7 +162,8 @@ int nb_accel(nb_ctx *ctx, void *acc_dev, void *stream);
 /* Total energy and momentum of the current state, reduced in FP64 on the
  * GPU: out5 = {kinetic sum 0.5 m |v|^2, potential -0.5 G sum_i sum_{j!=i}
  * m_i m_j / sqrt(r^2 + eps2), momentum x, y, z}.  The pair terms are FP32
- * (compensated in NB_F32_COMP) or FP64 (NB_F64, any algorithm).  accphi_dev
+ * (compensated in NB_F32_COMP) or FP64-accurate (NB_F64: float-float with
+ * NB_ALGO_SYM, FP64 arithmetic with the other algorithms).  accphi_dev
  * (may be NULL) receives per body the bare acceleration and, in w, the
  * potential sum over j != i, as n float4 (NB_F32) or double4 (NB_F32_COMP,
  * NB_F64).  NB_F32 needs the fast or symmetric algorithm.  Needs eps2 > 0.
