@@ -166,7 +166,8 @@ int nb_accel(nb_ctx *ctx, void *acc_dev, void *stream);
  * NB_ALGO_SYM, FP64 arithmetic with the other algorithms).  accphi_dev
  * (may be NULL) receives per body the bare acceleration and, in w, the
  * potential sum over j != i, as n float4 (NB_F32) or double4 (NB_F32_COMP,
- * NB_F64).  NB_F32 needs the fast or symmetric algorithm.  Needs eps2 > 0.
+ * NB_F64).  NB_F32 reference-exact contexts take FP64 pair terms on their
+ * float positions (scratch allocated on the first call).  Needs eps2 > 0.
  * Synchronises `stream`.  No counterpart in the reference (used by the
  * precision study). */
 int nb_energy(nb_ctx *ctx, double *out5, void *accphi_dev, void *stream);

@@ -394,3 +394,25 @@ def test_small_sizes_every_mode(cuda, prec, algo, n):
     rel = np.linalg.norm(np.asarray(p1, np.float64)[:, :3] - wp[:, :3], axis=1) / (
         np.linalg.norm(wp[:, :3], axis=1) + 0.1)
     assert rel.max() <= 1e-6
+
+
+@pytest.mark.parametrize("prec,algo", MODES)
+@pytest.mark.parametrize("n", [0, 1, 2])
+def test_energy_tiny_systems_every_mode(cuda, prec, algo, n):
+    """nb_energy in every mode on 0, 1 and 2 bodies: zeros for none, no
+    potential for one (the sum runs over j != i), the oracle's values for
+    two."""
+    dt = dtype_of(prec)
+    p, v = ics.plummer(max(n, 1), seed=7)
+    pos, vel = p[:n].astype(dt), v[:n].astype(dt)
+    eps2 = 1e-2 if dt == np.float64 else np.float32(1e-2)
+    with NBodySystem(n, prec, algo, kick="physical", eps2=eps2) as s:
+        s.set_state(pos, vel)
+        e = s.energy()
+    if n == 0:
+        assert np.array_equal(e, np.zeros(5))
+        return
+    ref = np.array(oracle.energy(np.asarray(pos, np.float64), np.asarray(vel, np.float64), float(eps2)))
+    assert np.allclose(e, ref, rtol=1e-5, atol=1e-12)
+    if n == 1:
+        assert e[1] == 0.0

@@ -84,7 +84,7 @@ def test_compensated_steps_vs_fp64_oracle(cuda, algo):
     assert dv.max() <= 1e-6, dv.max()
 
 
-@pytest.mark.parametrize("precision,algo", [("f32", "fast"), ("f32", "sym"), ("f32comp", "fast"),
+@pytest.mark.parametrize("precision,algo", [("f32", "fast"), ("f32", "sym"), ("f32", "exact"), ("f32comp", "fast"),
                                             ("f32comp", "sym"), ("f64", "sym"), ("f64", "sym64"),
                                             ("f64", "exact")])
 def test_energy_momentum_vs_fp64(cuda, precision, algo):

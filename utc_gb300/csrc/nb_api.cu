@@ -78,6 +78,7 @@ struct nb_ctx {
     void *acc_tmp = nullptr;
     double *e_blocks = nullptr;
     double *e_out = nullptr;
+    double4 *e_pos64 = nullptr;  // NB_F32 exact contexts: positions widened for the energy pass
     // symmetric algorithm: plan and its two partial arrays
     nb::SymPlan splan;
     float4 *sym_t = nullptr, *sym_s = nullptr;
@@ -168,6 +169,7 @@ static void free_ctx(nb_ctx *c)
     cudaFree(c->acc_tmp);
     cudaFree(c->e_blocks);
     cudaFree(c->e_out);
+    cudaFree(c->e_pos64);
     cudaFree(c->adj.ckpt_pos);
     cudaFree(c->adj.ckpt_vel);
     cudaFree(c->adj.seg_pos);
@@ -612,13 +614,45 @@ int nb_energy(nb_ctx *c, double *out5, void *accphi_dev, void *stream)
 {
     if (!c || !out5) return set_error(NB_ERR_INVALID, "ctx/out is NULL");
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
-    if (!(uses_fast(c) || is_comp(c) || c->p.precision == NB_F64))
-        return set_error(NB_ERR_UNSUPPORTED,
-                         "nb_energy needs an NB_F32 fast or symmetric, NB_F32_COMP or NB_F64 context");
     if (!(c->p.eps2 > 0.0)) return set_error(NB_ERR_INVALID, "nb_energy needs eps2 > 0");
     cudaStream_t s = (cudaStream_t)stream;
     const nb_params &p = c->p;
     int st;
+    const bool exact32 = p.precision == NB_F32 && p.algo == NB_ALGO_EXACT;
+    if (exact32 && p.n == 0) {
+        for (int k = 0; k < 5; ++k) out5[k] = 0.0;
+        return NB_OK;
+    }
+    if (exact32 && !c->e_pos64) {
+        // first energy call of a reference-exact float context: its scratch,
+        // all or nothing
+        void *m[4] = {};
+        const size_t bytes[4] = {(size_t)p.n * sizeof(double4), (size_t)p.n * sizeof(double4),
+                                 (size_t)(nb::energy_blocks(p.n) + 1) * 5 * sizeof(double), 8 * sizeof(double)};
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaMalloc(&m[k], bytes[k]);
+        if (e != cudaSuccess) {
+            for (void *q : m) cudaFree(q);
+            return nb::cuda_error(e, "energy scratch allocation");
+        }
+        c->acc_tmp = m[1];
+        c->e_blocks = (double *)m[2];
+        c->e_out = (double *)m[3];
+        c->e_pos64 = (double4 *)m[0];
+    }
+    if (exact32) {
+        // FP64 potential pass on the float positions widened to double
+        st = nb::widen_f32(p.n, (const float4 *)c->pos[c->cur], c->e_pos64, s);
+        if (!st) st = nb::energy_phi_f64(p.n, c->e_pos64, p.eps2, (double4 *)c->acc_tmp, s);
+        if (!st)
+            st = nb::energy_reduce(p.n, nullptr, c->e_pos64, (const float4 *)c->vel, nullptr, nullptr,
+                                   (const double4 *)c->acc_tmp, p.G, c->e_blocks, c->e_out, s);
+        if (!st && accphi_dev) st = nb::narrow_f64(p.n, (const double4 *)c->acc_tmp, (float4 *)accphi_dev, s);
+        if (st) return st;
+        NB_CUDA(cudaMemcpyAsync(out5, c->e_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        NB_CUDA(cudaStreamSynchronize(s));
+        return NB_OK;
+    }
     if (ff_sym(c)) {
         // the float-float symmetric pass with the potential, summed and
         // unscaled by the FP64 integrator into (acc, phi) per body

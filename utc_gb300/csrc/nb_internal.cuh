@@ -164,6 +164,9 @@ int comp_integrate(const SkPlan &p, const float4 *partial, double4 *pos64, float
 int energy_blocks(int n);
 // FP64 accelerations and potentials over j != i of an NB_F64 state, into
 // out (ax, ay, az, phi) (nb_precision.cu)
+// float4 <-> double4 copies (each value converted; narrowing rounds to nearest)
+int widen_f32(int n, const float4 *in, double4 *out, cudaStream_t s);
+int narrow_f64(int n, const double4 *in, float4 *out, cudaStream_t s);
 int energy_phi_f64(int n, const double4 *pos, double eps2, double4 *out, cudaStream_t s);
 // Energy and momentum in FP64 from the state (masses from pos64 if given,
 // else pos32; velocities from vel64 if given, else vel32 + vlo) and the

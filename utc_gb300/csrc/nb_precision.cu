@@ -356,6 +356,40 @@ __global__ void __launch_bounds__(kPhi64Block) phi64_kernel(const double4 *__res
     if (i < n) out[i] = make_double4(ax, ay, az, phi);
 }
 
+__global__ void widen_kernel(const float4 *__restrict__ in, double4 *__restrict__ out, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float4 q = in[i];
+        out[i] = make_double4(q.x, q.y, q.z, q.w);
+    }
+}
+
+__global__ void narrow_kernel(const double4 *__restrict__ in, float4 *__restrict__ out, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const double4 q = in[i];
+        out[i] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+    }
+}
+
+int widen_f32(int n, const float4 *in, double4 *out, cudaStream_t s)
+{
+    if (n == 0) return NB_OK;
+    widen_kernel<<<(n + 255) / 256, 256, 0, s>>>(in, out, n);
+    NB_LAUNCH_CHECK("widen_kernel launch");
+    return NB_OK;
+}
+
+int narrow_f64(int n, const double4 *in, float4 *out, cudaStream_t s)
+{
+    if (n == 0) return NB_OK;
+    narrow_kernel<<<(n + 255) / 256, 256, 0, s>>>(in, out, n);
+    NB_LAUNCH_CHECK("narrow_kernel launch");
+    return NB_OK;
+}
+
 int energy_phi_f64(int n, const double4 *pos, double eps2, double4 *out, cudaStream_t s)
 {
     if (n == 0) return NB_OK;
