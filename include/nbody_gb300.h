@@ -290,6 +290,17 @@ int nb_state_ptrs(nb_ctx *ctx, void **pos_dev, void **vel_dev);
  * CTA * 32, bpt = targets per lane and the target block is the row block. */
 int nb_plan_info(nb_ctx *ctx, int *info5);
 
+/* Time every compiled launch shape of the context's force kernel on its
+ * current state (`reps` steps each; the state is restored) and keep the
+ * fastest; shapes whose symmetric source-side array would pass 8 GiB are
+ * skipped.  cache_path (may be NULL) is a text file of earlier choices keyed
+ * by device, precision, algorithm and n: a hit applies the cached shape
+ * without timing.  chosen2 = {threads per CTA, bodies per lane}.  Drops
+ * captured step graphs and a recorded adjoint forward pass; the reference-
+ * exact kernel has nothing to tune.  Synchronises `stream`.  No counterpart in
+ * the reference (its block size is a command-line flag). */
+int nb_autotune(nb_ctx *ctx, int reps, const char *cache_path, void *stream, int *chosen2);
+
 /* Number of kernels nb_step launches per step for this context. */
 int nb_launches_per_step(nb_ctx *ctx);
 

@@ -88,6 +88,7 @@ def test_null_handles_are_rejected(built):
     assert lib.nb_create(None, None) == N.NB_ERR_INVALID
     assert lib.nb_destroy(None) == N.NB_OK
     assert lib.nb_launches_per_step(None) == -1
+    assert lib.nb_autotune(None, 1, None, None, None) == N.NB_ERR_INVALID
 
 
 # ---------------------------------------------------------------------------

@@ -58,6 +58,7 @@ def _declare(lib):
         "nb_energy": (I, [vp, P(D), vp, vp]),
         "nb_adj_forward": (I, [vp, I, I, vp]),
         "nb_adj_backward": (I, [vp, vp, vp, vp, vp, vp, vp]),
+        "nb_autotune": (I, [vp, I, C.c_char_p, vp, P(I)]),
         "nb_step_f32_noalloc": (I, [vp, vp, vp, I, C.c_float, C.c_float, C.c_float, I, C.c_float, vp]),
         "nb_run_host": (I, [vp, vp, vp, I, I, vp, P(D), vp]),
         "nb_state_ptrs": (I, [vp, P(vp), P(vp)]),

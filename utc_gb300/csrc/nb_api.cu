@@ -1,8 +1,12 @@
 // nb_api.cu -- the C ABI (include/nbody_gb300.h): contexts, state transfer,
 // stepping and the task-style host run.
+#include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <fstream>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -946,6 +950,216 @@ int nb_launches_per_step(nb_ctx *c)
     if (c->p.n == 0) return 0;
     if (ff_sym(c)) return 4;  // scale reduction, split, force, integrate
     return (uses_fast(c) || is_comp(c) || f64_sym(c)) ? 2 : 1;
+}
+
+// Single-system autotuner: every compiled shape of the context's force
+// kernel is timed on the current state (saved and restored), the fastest
+// is kept.  Candidates whose symmetric source-side array would pass the
+// budget are skipped; the scratch is sized for the largest candidate tried
+// and kept, so no step reallocates afterwards.
+int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *chosen2)
+{
+    if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
+    if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
+    if (reps < 1) reps = 3;
+    cudaStream_t s = (cudaStream_t)stream;
+    const nb_params &p = c->p;
+    const bool symm = uses_sym(c) || comp_sym(c) || f64_sym(c);
+    const bool fast = !symm && (uses_fast(c) || is_comp(c));
+    auto report = [&](int a, int b) {
+        if (chosen2) {
+            chosen2[0] = a;
+            chosen2[1] = b;
+        }
+    };
+    if ((!symm && !fast) || p.n == 0) {  // the exact kernel: nothing to tune
+        report(p.block, 0);
+        return NB_OK;
+    }
+    // candidates: (warps per CTA, targets per lane) or (block, bodies per thread)
+    std::vector<std::array<int, 2>> cands;
+    if (ff_sym(c))
+        cands = {{1, 2}, {1, 4}, {4, 4}, {8, 4}, {8, 8}};
+    else if (f64_sym(c))
+        cands = {{1, 8}, {1, 4}, {4, 8}, {8, 8}};
+    else if (comp_sym(c))
+        cands = {{1, 12}, {4, 12}, {8, 12}, {1, 8}, {8, 8}};
+    else if (uses_sym(c))
+        cands = {{1, 16}, {1, 8}, {1, 4}, {1, 20}, {2, 16}, {4, 20}, {8, 24}, {4, 8}, {8, 4}, {8, 8}};
+    else if (is_comp(c))
+        cands = {{256, 4}, {256, 8}};
+    else
+        cands = {{128, 2}, {128, 4}, {128, 8}, {256, 2}, {256, 4}, {256, 8}};
+    const size_t ent = (p.precision == NB_F64) ? sizeof(double4) : sizeof(float4);  // symmetric entries
+    const size_t halves = comp_sym(c) ? 2 : 1;
+    const size_t mult = is_comp(c) ? 2 : 1;  // directed compensated partials: hi and lo
+    const int cur_a = symm ? c->splan.warps : c->plan.block, cur_b = symm ? c->splan.bpt : c->plan.bpt;
+    auto make = [&](int a, int b, nb::SymPlan *sp, nb::SkPlan *fp) -> int {
+        if (symm) {
+            if (ff_sym(c)) return nb::symff_plan(p.n, a, b, c->device, sp);
+            if (f64_sym(c)) return nb::sym64_plan(p.n, a, b, c->device, sp);
+            return nb::sym_plan(p.n, a, b, c->device, sp, comp_sym(c) ? 1 : 0);
+        }
+        return nb::fast_plan(p.n, a, b, p.ctas_per_sm, c->device, fp, is_comp(c) ? nb::SK_COMP : 0);
+    };
+    auto t_bytes = [&](const nb::SymPlan &sp, const nb::SkPlan &fp) -> size_t {
+        return symm ? halves * (size_t)sp.slots * sp.rb * ent : mult * (size_t)fp.slots * fp.tbsize * sizeof(float4);
+    };
+    auto s_bytes = [&](const nb::SymPlan &sp) -> size_t { return symm ? halves * (size_t)sp.spart_size * ent : 0; };
+
+    // cache: device | mode | n -> shape
+    cudaDeviceProp prop;
+    NB_CUDA(cudaGetDeviceProperties(&prop, c->device));
+    std::ostringstream key;
+    key << "single|" << prop.name << "|sms" << prop.multiProcessorCount << "|prec" << p.precision << "|algo"
+        << p.algo << "|n" << p.n;
+    std::string k = key.str();
+    for (char &ch : k)
+        if (ch == ' ') ch = '_';
+    int best_a = cur_a, best_b = cur_b;
+    bool cached = false;
+    if (cache_path) {
+        std::ifstream in(cache_path);
+        std::string line;
+        while (std::getline(in, line)) {
+            std::istringstream ls(line);
+            std::string kk;
+            int a = 0, b = 0;
+            if ((ls >> kk >> a >> b) && kk == k) {
+                best_a = a;
+                best_b = b;
+                cached = true;
+            }
+        }
+    }
+    // viable candidates and the scratch they need
+    struct Cand {
+        int a, b;
+        nb::SymPlan sp;
+        nb::SkPlan fp;
+    };
+    std::vector<Cand> viable;
+    size_t need_t = 0, need_s = 0;
+    for (auto &cd : cands) {
+        if (cached && !(cd[0] == best_a && cd[1] == best_b)) continue;
+        Cand v{cd[0], cd[1], {}, {}};
+        if (make(v.a, v.b, &v.sp, &v.fp)) continue;  // not plannable (e.g. no occupancy)
+        const bool current = v.a == cur_a && v.b == cur_b;
+        if (symm && !current && (long long)s_bytes(v.sp) > nb::kSymSpartBudget) continue;
+        need_t = std::max(need_t, t_bytes(v.sp, v.fp));
+        need_s = std::max(need_s, s_bytes(v.sp));
+        viable.push_back(v);
+    }
+    if (viable.empty()) {
+        report(symm ? cur_a * 32 : cur_a, cur_b);
+        return NB_OK;
+    }
+    if (!symm) {  // the directed scratch also serves the energy pass
+        need_t = std::max(need_t, mult * (size_t)c->eplan.slots * c->eplan.tbsize * sizeof(float4));
+    }
+    // the plan from before stays usable on the new scratch (the fallback)
+    need_t = std::max(need_t, t_bytes(c->splan, c->plan));
+    need_s = std::max(need_s, s_bytes(c->splan));
+    // scratch for every candidate and a copy of the state, all or nothing
+    const size_t sb = state_bytes(c);
+    const size_t n = (size_t)p.n;
+    void *m[6] = {};
+    const size_t bytes[6] = {need_t, need_s, sb, sb, is_comp(c) ? n * sizeof(float4) : 0,
+                             is_comp(c) ? n * sizeof(float4) : 0};
+    cudaError_t e = cudaSuccess;
+    for (int q = 0; q < 6 && e == cudaSuccess; ++q)
+        if (bytes[q]) e = cudaMalloc(&m[q], bytes[q]);
+    if (e != cudaSuccess) {
+        for (void *q : m) cudaFree(q);
+        return nb::cuda_error(e, "autotune scratch allocation");
+    }
+    void *pos_now = is_comp(c) ? c->pos[0] : c->pos[c->cur];
+    const int cur0 = c->cur;
+    e = cudaMemcpyAsync(m[2], pos_now, sb, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m[3], c->vel, is_comp(c) ? n * sizeof(float4) : sb,
+                                              cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && is_comp(c)) e = cudaMemcpyAsync(m[4], c->pos32, n * sizeof(float4), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && is_comp(c)) e = cudaMemcpyAsync(m[5], c->vel_lo, n * sizeof(float4), cudaMemcpyDeviceToDevice, s);
+    auto restore = [&]() -> cudaError_t {
+        c->cur = cur0;
+        void *dst = is_comp(c) ? c->pos[0] : c->pos[cur0];
+        cudaError_t r = cudaMemcpyAsync(dst, m[2], sb, cudaMemcpyDeviceToDevice, s);
+        if (r == cudaSuccess) r = cudaMemcpyAsync(c->vel, m[3], is_comp(c) ? n * sizeof(float4) : sb,
+                                                  cudaMemcpyDeviceToDevice, s);
+        if (r == cudaSuccess && is_comp(c)) r = cudaMemcpyAsync(c->pos32, m[4], n * sizeof(float4), cudaMemcpyDeviceToDevice, s);
+        if (r == cudaSuccess && is_comp(c)) r = cudaMemcpyAsync(c->vel_lo, m[5], n * sizeof(float4), cudaMemcpyDeviceToDevice, s);
+        return r;
+    };
+    // the context runs on the new scratch from here on; the captured graphs
+    // and a recorded adjoint forward pass belong to the old plan
+    for (auto &g : c->step_graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    c->adj.ready = false;
+    c->adj.live_last = false;
+    cudaStreamSynchronize(s);  // the old scratch may still be in use
+    if (symm) {
+        cudaFree(c->sym_t);
+        cudaFree(c->sym_s);
+        c->sym_t = (float4 *)m[0];
+        c->sym_s = (float4 *)m[1];
+    } else {
+        cudaFree(c->partial);
+        c->partial = (float4 *)m[0];
+    }
+    int st = e == cudaSuccess ? NB_OK : nb::cuda_error(e, "autotune state copy");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (!st && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+        st = set_error(NB_ERR_CUDA, "autotune events");
+    float best = 1e30f;
+    const nb::SymPlan sp0 = c->splan;
+    const nb::SkPlan fp0 = c->plan;
+    const Cand *pick = nullptr;
+    for (const Cand &v : viable) {
+        if (st) break;
+        if (symm) c->splan = v.sp;
+        else c->plan = v.fp;
+        if (viable.size() == 1) {  // a cached choice: nothing to time
+            pick = &v;
+            break;
+        }
+        st = step_once(c, s, nullptr);  // warm-up
+        cudaError_t r = cudaEventRecord(e0, s);
+        for (int q = 0; q < reps && !st && r == cudaSuccess; ++q) st = step_once(c, s, nullptr);
+        if (r == cudaSuccess) r = cudaEventRecord(e1, s);
+        if (r == cudaSuccess) r = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (r == cudaSuccess) r = cudaEventElapsedTime(&ms, e0, e1);
+        if (r == cudaSuccess) r = restore();
+        if (!st && r != cudaSuccess) st = nb::cuda_error(r, "autotune timing");
+        if (!st && ms < best) {
+            best = ms;
+            pick = &v;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (!pick) {  // keep the plan from before (its scratch fits: the current shape was a candidate or smaller)
+        c->splan = sp0;
+        c->plan = fp0;
+    } else if (symm) {
+        c->splan = pick->sp;
+    } else {
+        c->plan = pick->fp;
+    }
+    restore();
+    cudaStreamSynchronize(s);
+    for (int q = 2; q < 6; ++q) cudaFree(m[q]);
+    if (st) return st;
+    const int ra = symm ? c->splan.warps * 32 : c->plan.block, rb = symm ? c->splan.bpt : c->plan.bpt;
+    if (cache_path && !cached && pick) {
+        std::ofstream outf(cache_path, std::ios::app);
+        if (outf) outf << k << " " << (symm ? c->splan.warps : c->plan.block) << " " << rb << "\n";
+    }
+    report(ra, rb);
+    return NB_OK;
 }
 
 int nb_plan_info(nb_ctx *c, int *info5)

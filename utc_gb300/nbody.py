@@ -232,6 +232,16 @@ class NBodySystem:
     def launches_per_step(self):
         return self.lib.nb_launches_per_step(self.handle)
 
+    def autotune(self, reps=3, cache_path=None, stream=None):
+        """Time every compiled shape of this context's force kernel on the
+        current state (restored afterwards) and keep the fastest; returns
+        (threads per CTA, bodies per lane)."""
+        s = current_stream_handle() if stream is None else stream
+        out = (C.c_int * 2)()
+        N.check(self.lib.nb_autotune(self.handle, int(reps), cache_path.encode() if cache_path else None,
+                                     C.c_void_p(s), out), "nb_autotune")
+        return int(out[0]), int(out[1])
+
 
 def probe_fma_peak(iters=20000, packed=True, stream=None):
     """Measured FMA peak in FLOP/s on the current device: FP32 (packed True or
