@@ -501,10 +501,10 @@ def run_precision(args):
 
 
 # FP32 pipe instructions per unordered pair of the float-float kernel (and
-# one rsqrt approximation): exact three-float differences 84, |r|^2 + eps2
-# 39, Newton and Halley steps 18, inv^3 11, weights 8, six float-float
+# one rsqrt approximation): exact grid differences 30, |r|^2 + eps2 39,
+# Newton and Halley steps 18, inv^3 11, weights 8, six float-float
 # accumulations 90
-FF_OPS_PER_PAIR = 250
+FF_OPS_PER_PAIR = 196
 
 
 def run_double(args):

@@ -76,16 +76,17 @@ typedef enum {
      * interactions.  Same per-pair terms as NB_ALGO_FAST, different summation
      * order; deterministic.  NB_F32, NB_F32_COMP (compensated partial sums)
      * and NB_F64: pair terms in float-float arithmetic on the FP32 pipe
-     * (positions scaled by powers of two and split exactly into three
-     * floats, error-free sums and products, an FP32 Newton and a
+     * (positions scaled by powers of two and split on fixed grids into
+     * three floats, error-free sums and products, an FP32 Newton and a
      * float-float Halley step on the FP32 rsqrt; chunk sums folded into
-     * FP64), within a few 1e-15 of the FP64
-     * reference, not bit for bit.  Range for NB_F64: eps2 >= 2^-100 max|x|^2
-     * and masses >= 2^-100 of the largest. */
+     * FP64), within a few 1e-15 of the FP64 reference, not bit for bit.
+     * Range for NB_F64: eps2 >= 2^-100 max|x|^2 and masses >= 2^-100 of the
+     * largest; coordinates within 2^-16 max|x| of zero are held to
+     * 2^-69 max|x|. */
     NB_ALGO_SYM = 2,
     /* NB_F64 only: the symmetric algorithm in FP64 arithmetic throughout
      * (1/sqrt from the FP64 approximation and two Newton steps), within a
-     * few 1e-16 of the FP64 reference, any range; about 1/5 the speed of
+     * few 1e-16 of the FP64 reference, any range; about 1/6 the speed of
      * NB_ALGO_SYM on GB300's narrow FP64 pipe. */
     NB_ALGO_SYM_FP64 = 3
 } nb_algo;

@@ -1,9 +1,9 @@
 """The float-float pair arithmetic of the FP64-state kernels
 (utc_gb300/csrc/nb_ff.cuh), restated step by step in numpy float32 and
 checked on the CPU against 80-bit long double over many random pairs:
-three-float splits are exact, the pair vector r is accurate to ~2^-48 even
-for close pairs far from the origin, 1/sqrt to 2^-45.5 and the weights
-m inv^3 to 2^-44.  Each float32 operation rounds to
+grid splits are exact (coordinates at least 2^-16 of the scale), the pair
+vector r is accurate to 2^-47 (exact for close pairs, also far from the
+origin), 1/sqrt to 2^-45.5 and the weights m inv^3 to 2^-44.  Each float32 operation rounds to
 nearest; an FMA is emulated by one FP64 evaluation rounded once to float32
 (the product of two floats is exact in FP64).  The FP32 rsqrt seed is
 emulated by a correctly rounded 1/sqrt perturbed by up to 2^-22; the
@@ -38,20 +38,27 @@ def fast_two_sum(a, b):
 
 
 def split3(x):
+    """Grid split of scaled coordinates (|x| < 1): h, m, l on 2^-20, 2^-44,
+    2^-68."""
+    gh = np.ldexp(np.rint(np.ldexp(x, 20)), -20)
+    r1 = x - gh
+    gm = np.ldexp(np.rint(np.ldexp(r1, 44)), -44)
+    r2 = r1 - gm
+    gl = np.ldexp(np.rint(np.ldexp(r2, 68)), -68)
+    return gh.astype(F), gm.astype(F), gl.astype(F)
+
+
+def split_mass(x):
     h = x.astype(F)
-    r1 = x - h.astype(np.float64)
-    m = r1.astype(F)
-    l = (r1 - m.astype(np.float64)).astype(F)
-    return h, m, l
+    return h, (x - h.astype(np.float64)).astype(F)
 
 
 def ff_diff(s, p):
-    A, a = two_sum(s[0], -p[0])
-    B, b = two_sum(s[1], -p[1])
+    A = (s[0] - p[0]).astype(F)
+    B = (s[1] - p[1]).astype(F)
     C = (s[2] - p[2]).astype(F)
-    s1, e1 = two_sum(A, B)
-    t = ((e1 + a).astype(F) + (b + C).astype(F)).astype(F)
-    return two_sum(s1, t)
+    s1, e1 = fast_two_sum(A, B)
+    return fast_two_sum(s1, (e1 + C).astype(F))
 
 
 def pair(xs, xi, ms, eps2, rng):
@@ -88,7 +95,7 @@ def pair(xs, xi, ms, eps2, rng):
     e3 = fma(p2, yl, e3)
     e3 = fma(e2, yh, e3)
     y3h, y3l = fast_two_sum(p3, e3)
-    mh, mm, _ = split3(ms)
+    mh, mm = split_mass(ms)
     wjh = (mh * y3h).astype(F)
     we = fma(mh, y3h, -wjh)
     we = fma(mh, y3l, we)
@@ -125,9 +132,17 @@ def test_ff_pair_terms_accuracy(center, spread):
     assert float((np.abs(value(wj) - w) / w).max()) <= 2.0 ** -44
 
 
-def test_three_float_split_is_exact():
+def test_grid_split():
+    """Exact for |x| >= 2^-16 (scaled units), within 2^-69 below; each part
+    exactly representable as float32."""
     rng = np.random.default_rng(2)
-    x = np.concatenate([rng.normal(size=100000) * 10.0 ** rng.integers(-10, 10, 100000),
-                        np.array([0.0, 1.0, -1.0, 2.0 ** -60, 1e300 / 1e290])])
+    x = np.concatenate([rng.uniform(-1, 1, 100000) * 2.0 ** -rng.integers(0, 40, 100000),
+                        np.array([0.0, 0.5, -0.999999999, 2.0 ** -16, -2.0 ** -30])])
+    x = x[np.abs(x) < 1]
     h, m, l = split3(x)
-    assert np.array_equal(h.astype(np.float64) + m.astype(np.float64) + l.astype(np.float64), x)
+    back = h.astype(np.float64) + m.astype(np.float64) + l.astype(np.float64)
+    big = np.abs(x) >= 2.0 ** -16
+    assert np.array_equal(back[big], x[big])
+    assert np.abs(back - x).max() <= 2.0 ** -69
+    gh = np.ldexp(np.rint(np.ldexp(x, 20)), -20)
+    assert np.array_equal(h.astype(np.float64), gh)

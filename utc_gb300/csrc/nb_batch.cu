@@ -350,7 +350,7 @@ __global__ void bks_integrate_kernel(const float4 *__restrict__ pos_old, float4 
 
 // Float-float batched symmetric kernel for FP64 state: the layout and work
 // split of bks_force_kernel, the pair arithmetic of symff_force_kernel
-// (nb_ff.cuh; three-float positions scaled by the batch's powers of two),
+// (nb_ff.cuh; grid-split positions scaled by the batch's powers of two),
 // each chunk's target sums folded into FP64, reactions written as FP64.
 template <int WPB, int BPT>
 __global__ void __launch_bounds__(32 * WPB)
@@ -959,7 +959,7 @@ struct nb_batch {
     float4 *sys_partial = nullptr, *sys_spart = nullptr;
     // NB_F64 state (NB_ALGO_SYM): pos / vel / partial / spart hold double4
     // (twice the float4 entries), stepped by the float-float batched kernel
-    // from the scaled three-float split (3 nbody float4) and the batch's
+    // from the scaled grid split (3 nbody float4) and the batch's
     // scale record
     bool f64 = false;
     float4 *ff_split = nullptr;

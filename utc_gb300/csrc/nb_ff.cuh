@@ -24,18 +24,19 @@ __device__ __forceinline__ void ff_fast_two_sum(float a, float b, float &s, floa
     e = __fsub_rn(b, __fsub_rn(s, a));
 }
 
-// r = s - p from three-float parts, as a normalized float-float: the high
-// and middle differences error-free, the low one rounded (2^-72 |x|).
+// r = s - p from grid-split coordinates (x = h + m + l with h, m and l on
+// the grids 2^-20, 2^-44 and 2^-68 of the scaled units, |x| < 1), as a
+// normalized float-float.  The three differences are exact (each fits 24
+// bits); A + B is split by Dekker's fast two-sum (|A| >= 2^-20 >= |B|, or
+// A == 0) and the low part added once: r to 2^-47 relative, exactly when the
+// high parts cancel (close pairs).
 __device__ __forceinline__ void ff_diff(float sh, float sm, float sl, float ph, float pm, float pl, float &rh,
                                         float &rl)
 {
-    float A, a, B, b, s1, e1;
-    ff_two_sum(sh, -ph, A, a);
-    ff_two_sum(sm, -pm, B, b);
-    const float C = __fsub_rn(sl, pl);
-    ff_two_sum(A, B, s1, e1);
-    const float t = __fadd_rn(__fadd_rn(e1, a), __fadd_rn(b, C));
-    ff_two_sum(s1, t, rh, rl);
+    const float A = __fsub_rn(sh, ph), B = __fsub_rn(sm, pm), C = __fsub_rn(sl, pl);
+    float s1, e1;
+    ff_fast_two_sum(A, B, s1, e1);
+    ff_fast_two_sum(s1, __fadd_rn(e1, C), rh, rl);
 }
 
 // A += r * w (float-float, renormalized)

@@ -15,14 +15,16 @@
 //  * float-float numbers hi + lo with |lo| <= ulp(hi)/2, about 48 bits.
 // Per step, positions and masses are scaled by exact powers of two (the
 // largest coordinate and the largest mass into [1/2, 1), found by a
-// reduction on the device) and split into three floats, h + m + l == x
-// exactly.  Per unordered pair (the symmetric layout of nb_sym.cu: row
+// reduction on the device); each scaled coordinate is split on fixed grids
+// into three floats, h (2^-20), m (2^-44) and l (2^-68), h + m + l == x
+// exactly for |x| >= 2^-16 and to 2^-69 below that (the mass into a
+// float-float).  Per unordered pair (the symmetric layout of nb_sym.cu: row
 // blocks of 32*BPT targets per warp x 32-body chunks, the chunk rotating
 // through the warp with its reaction):
-//  * r = x_j - x_i: two-sums of the high and of the middle parts, the low
-//    parts' rounded difference, normalized to a float-float -- as accurate
-//    as FP64's own difference, also for close pairs far from the origin
-//    (a two-float split would lose the position bits below 2^-49 |x|);
+//  * r = x_j - x_i: the three grid differences are exact; two fast
+//    two-sums normalize them to a float-float, to 2^-47 relative and
+//    exactly for close pairs -- also far from the origin, where a two-float
+//    split of the positions would lose the bits below 2^-49 |x|;
 //  * d2 = |r|^2 + eps2 in float-float;
 //  * 1/sqrt(d2): the FP32 approximation refined by one FP32 Newton step
 //    (to ~2^-24) and one Halley step in float-float, y = y0 (1 + t/2 +
@@ -34,8 +36,8 @@
 // Each target's 32-source chunk sum is folded into FP64 accumulators; each
 // reaction (one chunk body, the warp's 32*BPT targets) is written as FP64.
 // The FP64 integrator of nb_sym64.cu then sums the partials in FP64, undoes
-// the scaling and integrates.  250 FP32 operations and one approximation
-// per pair (125 per interaction); results within a few 1e-15 of the FP64
+// the scaling and integrates.  196 FP32 operations and one approximation
+// per pair (98 per interaction); results within a few 1e-15 of the FP64
 // oracle (FP64 arithmetic: a few 1e-16), not bit-identical (NB_ALGO_EXACT is).
 // Range: the scaled squared distances and eps2 must stay normal floats:
 // eps2 >= 2^-100 max|x|^2 and body masses >= 2^-100 of the largest.
@@ -70,8 +72,10 @@ __global__ void ff_range_kernel(const double4 *__restrict__ pos, int n, unsigned
     }
 }
 
-// Scaled three-float split: H + M + L == x * 2^kx (coordinates) and
-// m * 2^km (mass) exactly.
+// Scaled split: coordinates x * 2^kx (below 1 in magnitude) on the grids
+// H: 2^-20, M: 2^-44, L: 2^-68 (H + M + L == x * 2^kx exactly when
+// |x * 2^kx| >= 2^-16, otherwise to 2^-69); the mass m * 2^km as the
+// float-float H + M (L unused).
 __global__ void ff_split_kernel(const double4 *__restrict__ pos, int n, const unsigned long long *__restrict__ range,
                                 float4 *__restrict__ H, float4 *__restrict__ M, float4 *__restrict__ L)
 {
@@ -82,12 +86,18 @@ __global__ void ff_split_kernel(const double4 *__restrict__ pos, int n, const un
     const double v[4] = {ldexp(q.x, kx), ldexp(q.y, kx), ldexp(q.z, kx), ldexp(q.w, km)};
     float h[4], m[4], l[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        h[k] = __double2float_rn(v[k]);
-        const double r1 = v[k] - (double)h[k];  // exact
-        m[k] = __double2float_rn(r1);
-        l[k] = __double2float_rn(r1 - (double)m[k]);  // exact
+    for (int k = 0; k < 3; ++k) {
+        const double gh = ldexp(rint(ldexp(v[k], 20)), -20);  // |gh| <= 1: 21 bits
+        const double r1 = v[k] - gh;                              // exact, |r1| <= 2^-21
+        const double gm = ldexp(rint(ldexp(r1, 44)), -44);       // 24 bits
+        const double r2 = r1 - gm;                                // exact, |r2| <= 2^-45
+        h[k] = (float)gh;
+        m[k] = (float)gm;
+        l[k] = (float)ldexp(rint(ldexp(r2, 68)), -68);            // 24 bits
     }
+    h[3] = __double2float_rn(v[3]);
+    m[3] = __double2float_rn(v[3] - (double)h[3]);
+    l[3] = 0.f;
     H[i] = make_float4(h[0], h[1], h[2], h[3]);
     M[i] = make_float4(m[0], m[1], m[2], m[3]);
     L[i] = make_float4(l[0], l[1], l[2], l[3]);
