@@ -1,0 +1,45 @@
+"""The multi-task app driver (utc_gb300/nbody_mtask, the reference's
+benchapps/nbody/utc/nbody_mtask.cc flags): T systems through one batched
+launch per step (default) or one GPU task per system (-B 0, the reference's
+pattern); both write every system's frames with -O, and they agree to the
+printed precision in double (the app's FTYPE) and float state."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+APP = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "utc_gb300", "nbody_mtask")
+
+
+def frames_of(path, ntasks, n, nframes):
+    lines = open(path).read().splitlines()
+    assert len(lines) == ntasks * nframes * (n + 1)
+    vals = []
+    for k in range(ntasks * nframes):
+        block = lines[k * (n + 1):(k + 1) * (n + 1)]
+        float(block[0])  # the frame's time line
+        vals.append(np.array([[float(x) for x in ln.split()] for ln in block[1:]]))
+    return np.array(vals).reshape(ntasks, nframes, n, 4)
+
+
+@pytest.mark.parametrize("state", ["double", "float"])
+def test_mtask_batched_equals_per_task(cuda, tmp_path, state):
+    n, ntasks, loops, oi = 256, 4, 10, 5
+    extra = ["-F"] if state == "float" else []
+    out = {}
+    for mode in ("1", "0"):
+        path = str(tmp_path / f"out{mode}.txt")
+        r = subprocess.run([APP, "-v", "-n", str(n), "-T", str(ntasks), "-l", str(loops), "-o", str(oi),
+                            "-O", path, "-B", mode] + extra, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "Test complete !!!" in r.stdout and f"Number of tasks: {ntasks}" in r.stdout
+        out[mode] = frames_of(path, ntasks, n, loops // oi + 1)
+    batched, tasks = out["1"], out["0"]
+    # frame 0 is every system's start; the systems differ (one rand() stream)
+    assert np.array_equal(batched[:, 0], tasks[:, 0])
+    assert not np.array_equal(tasks[0, 0], tasks[1, 0])
+    tol = 2e-5 if state == "double" else 1e-4 * (np.abs(tasks).max() + 1)
+    assert np.abs(batched - tasks).max() <= tol

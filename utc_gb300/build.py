@@ -4,6 +4,7 @@ Produces, next to this file:
   libnbody_gb300.so  -- the CUDA kernels behind the C ABI (include/nbody_gb300.h)
   libnbody_task.so   -- BodySystemGB300<T> (the UTC-task drop-in) + Task stand-in
   nbody_main         -- the app driver with the reference's flags
+  nbody_mtask        -- the multi-task app driver (many systems, batched)
 
 Every .cu file is compiled for sm_103a only, in parallel, then linked.
 """
@@ -30,6 +31,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas"
 LIB = os.path.join(PKG, "libnbody_gb300.so")
 TASK_LIB = os.path.join(PKG, "libnbody_task.so")
 MAIN_BIN = os.path.join(PKG, "nbody_main")
+MTASK_BIN = os.path.join(PKG, "nbody_mtask")
 
 
 def cuda_home() -> str:
@@ -99,6 +101,10 @@ def build(force: bool = False, verbose: bool = False) -> None:
     if force or not _newer(MAIN_BIN, [main_src] + task_hdrs + [TASK_LIB]):
         _run([cxx] + common + ["-o", MAIN_BIN, main_src, "-L", PKG, "-lnbody_task"] + libs,
              os.path.join(BUILD_DIR, "main.log"))
+    mtask_src = os.path.join(TASK, "nbody_mtask_main.cc")
+    if force or not _newer(MTASK_BIN, [mtask_src] + task_hdrs + [TASK_LIB]):
+        _run([cxx] + common + ["-o", MTASK_BIN, mtask_src, "-L", PKG, "-lnbody_task"] + libs,
+             os.path.join(BUILD_DIR, "mtask.log"))
 
 
 def ptxas_report() -> str:
