@@ -129,6 +129,13 @@ void nb_params_default(nb_params *p);
  * scratch buffers.  Replaces the GpuData allocations of
  * body_task_sgpu.cu:55-58. */
 int nb_create(const nb_params *p, nb_ctx **out);
+/* Synchronise the device, then free the context.  Distinct contexts may be
+ * created, stepped and destroyed from several host threads at once (one UTC
+ * task per system): the library keeps its own graph captures apart from its
+ * allocations, frees and device synchronisations.  When a thread outside the
+ * library is capturing a graph the device cannot be synchronised: the call
+ * then returns NB_ERR_CUDA and keeps the context, to be destroyed again after
+ * that capture. */
 int nb_destroy(nb_ctx *ctx);
 
 /* Load / read back the state.  pos and vel hold 4*n values of the state type
@@ -140,7 +147,8 @@ int nb_get_state(nb_ctx *ctx, void *pos, void *vel, int where, void *stream);
 /* Advance `steps` steps on `stream` (asynchronous).  Replaces the launch
  * loop of BodySystemSGPU::runImpl, body_task_sgpu.cu:85-127.  On a stream
  * other than the legacy default stream, bulk steps replay a captured CUDA
- * graph. */
+ * graph; a capture that another thread's device-wide call invalidates is
+ * dropped and those steps are launched one by one (same results). */
 int nb_step(nb_ctx *ctx, int steps, void *stream);
 
 /* Change eps2 (the softening squared), damping, dt and G of a context (or of
@@ -237,8 +245,9 @@ int nb_batch_get_state(nb_batch *b, void *pos, void *vel, int where, void *strea
 /* `steps` steps, launched one by one. */
 int nb_batch_step(nb_batch *b, int steps, void *stream);
 /* `steps` steps as one CUDA graph (captured on first use for this step count
- * and parity, replayed afterwards); `stream` must not be the legacy default
- * stream. */
+ * and parity, replayed afterwards; launched one by one when the capture does
+ * not take, as nb_step); `stream` must not be the legacy default stream.
+ * nb_batch_destroy behaves as nb_destroy. */
 int nb_batch_run(nb_batch *b, int steps, void *stream);
 /* Time every compiled launch shape on this batch and keep the fastest
  * (state preserved); cache_path (may be NULL) is a text file of earlier

@@ -43,3 +43,16 @@ def test_mtask_batched_equals_per_task(cuda, tmp_path, state):
     assert not np.array_equal(tasks[0, 0], tasks[1, 0])
     tol = 2e-5 if state == "double" else 1e-4 * (np.abs(tasks).max() + 1)
     assert np.abs(batched - tasks).max() <= tol
+
+
+@pytest.mark.parametrize("state", ["double", "float"])
+def test_mtask_many_tasks_at_once(cuda, state):
+    # sixteen tasks, each on its own thread, create, capture their step graphs
+    # (50 steps per frame), copy and destroy at the same time; every run ends
+    # cleanly and every task reports success
+    extra = ["-F"] if state == "float" else []
+    for _ in range(3):
+        r = subprocess.run([APP, "-v", "-n", "1024", "-T", "16", "-l", "100", "-o", "50", "-B", "0"] + extra,
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+        assert "status" not in r.stderr and "Test complete !!!" in r.stdout

@@ -16,6 +16,12 @@ namespace nb {
 
 static thread_local std::string g_last_error;
 
+std::shared_mutex &capture_gate()
+{
+    static std::shared_mutex gate;
+    return gate;
+}
+
 int set_error(int status, const std::string &msg)
 {
     g_last_error = msg;
@@ -157,49 +163,49 @@ static void free_ctx(nb_ctx *c)
 {
     if (!c) return;
     for (auto &g : c->step_graph)
-        if (g) cudaGraphExecDestroy(g);
-    cudaFree(c->pos[0]);
-    cudaFree(c->pos[1]);
-    cudaFree(c->vel);
-    cudaFree(c->partial);
-    cudaFreeHost(c->stage_pos);
-    cudaFreeHost(c->stage_vel);
-    cudaFreeHost(c->stage_out);
+        if (g) nb::graph_exec_destroy(g);
+    nb::dfree(c->pos[0]);
+    nb::dfree(c->pos[1]);
+    nb::dfree(c->vel);
+    nb::dfree(c->partial);
+    nb::hfree(c->stage_pos);
+    nb::hfree(c->stage_vel);
+    nb::hfree(c->stage_out);
     for (cudaEvent_t e : c->events) cudaEventDestroy(e);
-    cudaFree(c->pos32);
-    cudaFree(c->vel_lo);
-    cudaFree(c->tmpA);
-    cudaFree(c->tmpB);
-    cudaFree(c->acc_tmp);
-    cudaFree(c->e_blocks);
-    cudaFree(c->e_out);
-    cudaFree(c->e_pos64);
-    cudaFree(c->adj.ckpt_pos);
-    cudaFree(c->adj.ckpt_vel);
-    cudaFree(c->adj.seg_pos);
-    cudaFree(c->adj.seg_acc);
-    cudaFree(c->adj.vel_tmp);
-    cudaFree(c->adj.lx);
-    cudaFree(c->adj.lv);
-    cudaFree(c->adj.gbuf);
-    cudaFree(c->adj.gm);
-    cudaFree(c->adj.partial);
-    cudaFree(c->adj.sym_t);
-    cudaFree(c->adj.sym_s);
-    cudaFree(c->adj.seg_pos2);
-    cudaFree(c->adj.seg_acc2);
-    cudaFree(c->adj.vel_tmp2);
+    nb::dfree(c->pos32);
+    nb::dfree(c->vel_lo);
+    nb::dfree(c->tmpA);
+    nb::dfree(c->tmpB);
+    nb::dfree(c->acc_tmp);
+    nb::dfree(c->e_blocks);
+    nb::dfree(c->e_out);
+    nb::dfree(c->e_pos64);
+    nb::dfree(c->adj.ckpt_pos);
+    nb::dfree(c->adj.ckpt_vel);
+    nb::dfree(c->adj.seg_pos);
+    nb::dfree(c->adj.seg_acc);
+    nb::dfree(c->adj.vel_tmp);
+    nb::dfree(c->adj.lx);
+    nb::dfree(c->adj.lv);
+    nb::dfree(c->adj.gbuf);
+    nb::dfree(c->adj.gm);
+    nb::dfree(c->adj.partial);
+    nb::dfree(c->adj.sym_t);
+    nb::dfree(c->adj.sym_s);
+    nb::dfree(c->adj.seg_pos2);
+    nb::dfree(c->adj.seg_acc2);
+    nb::dfree(c->adj.vel_tmp2);
     if (c->adj.rstream) cudaStreamDestroy(c->adj.rstream);
     for (auto &e : c->adj.ev_rec)
         if (e) cudaEventDestroy(e);
     if (c->adj.ev_go) cudaEventDestroy(c->adj.ev_go);
-    cudaFree(c->sym_t);
-    cudaFree(c->sym_s);
-    cudaFree(c->ff_split);
-    cudaFree(c->ff_range);
+    nb::dfree(c->sym_t);
+    nb::dfree(c->sym_s);
+    nb::dfree(c->ff_split);
+    nb::dfree(c->ff_range);
     for (int k = 0; k < 2; ++k) {
-        cudaFree(c->snap[k]);
-        cudaFreeHost(c->stage[k]);
+        nb::dfree(c->snap[k]);
+        nb::hfree(c->stage[k]);
         if (c->ev_snap[k]) cudaEventDestroy(c->ev_snap[k]);
         if (c->ev_c0[k]) cudaEventDestroy(c->ev_c0[k]);
         if (c->ev_c1[k]) cudaEventDestroy(c->ev_c1[k]);
@@ -214,8 +220,8 @@ static int dalloc(nb_ctx *c, void **p, size_t bytes)
         *p = nullptr;
         return NB_OK;
     }
-    cudaError_t e = c->p.memtype == NB_MEM_UNIFIED ? cudaMallocManaged(p, bytes)
-                                                   : cudaMalloc(p, bytes);
+    cudaError_t e = c->p.memtype == NB_MEM_UNIFIED ? nb::dmalloc_managed(p, bytes)
+                                                   : nb::dmalloc(p, bytes);
     if (e != cudaSuccess) return nb::cuda_error(e, "state allocation");
     return NB_OK;
 }
@@ -242,7 +248,7 @@ static int dev_alloc(void **p, size_t bytes, const char *what)
 {
     *p = nullptr;
     if (!bytes) return NB_OK;
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = nb::dmalloc(p, bytes);
     if (e != cudaSuccess) return nb::cuda_error(e, what);
     return NB_OK;
 }
@@ -365,7 +371,16 @@ int nb_create(const nb_params *p, nb_ctx **out)
 int nb_destroy(nb_ctx *c)
 {
     if (!c) return NB_OK;
-    cudaDeviceSynchronize();
+    // work queued on the caller's streams may still use the buffers.  A
+    // device that cannot be synchronised because a thread outside the
+    // library is capturing a graph keeps the context: freeing it could pull
+    // memory from under that work
+    const cudaError_t e = nb::device_sync();
+    if (nb::is_capture_error(e)) {
+        (void)cudaGetLastError();
+        return nb::cuda_error(e, "nb_destroy: the device cannot be synchronised while another thread captures "
+                                 "a graph; the context is kept, call again after the capture");
+    }
     free_ctx(c);
     return NB_OK;
 }
@@ -503,25 +518,34 @@ constexpr int kGraphSteps = 16;
 
 // Capture kGraphSteps steps from the current buffer into a graph.  The
 // kernels' arguments (buffers, plans, parameters) stay fixed until
-// nb_set_params, which destroys the captured graphs.
-static int capture_step_graph(nb_ctx *c, cudaStream_t s, cudaGraphExec_t *out)
+// nb_set_params, which destroys the captured graphs.  *out stays null when
+// the capture does not take: a device-wide call made by code outside the
+// library in another thread invalidates a capture without any fault of the
+// steps.  Nothing captured has run and c->cur is as before, so the caller
+// launches the steps one by one instead, where an error of the steps
+// themselves then shows.
+static void capture_step_graph(nb_ctx *c, cudaStream_t s, cudaGraphExec_t *out)
 {
+    *out = nullptr;
     const int cur0 = c->cur;
     cudaGraph_t g = nullptr;
-    NB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    int st = NB_OK;
-    for (int i = 0; i < kGraphSteps && !st; ++i) st = step_once(c, s, nullptr);
-    cudaError_t e = cudaStreamEndCapture(s, &g);
-    c->cur = cur0;
-    if (st) {
-        if (g) cudaGraphDestroy(g);
-        return st;
+    {
+        std::shared_lock<std::shared_mutex> gate(nb::capture_gate());
+        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            int st = NB_OK;
+            for (int i = 0; i < kGraphSteps && !st; ++i) st = step_once(c, s, nullptr);
+            if (cudaStreamEndCapture(s, &g) != cudaSuccess || st) {
+                if (g) cudaGraphDestroy(g);
+                g = nullptr;
+            }
+        }
     }
-    if (e != cudaSuccess) return nb::cuda_error(e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(out, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return nb::cuda_error(e, "cudaGraphInstantiate");
-    return NB_OK;
+    c->cur = cur0;
+    if (g) {
+        if (nb::graph_instantiate(out, g) != cudaSuccess) *out = nullptr;
+        cudaGraphDestroy(g);
+    }
+    (void)cudaGetLastError();  // a capture that did not take leaves its error behind
 }
 
 extern "C" {
@@ -545,7 +569,8 @@ int nb_step(nb_ctx *c, int steps, void *stream)
     if (graphs && steps >= 2 * kGraphSteps) {
         for (; steps >= kGraphSteps; steps -= kGraphSteps) {
             cudaGraphExec_t &g = c->step_graph[c->cur];
-            if (!g && (st = capture_step_graph(c, s, &g))) return st;
+            if (!g) capture_step_graph(c, s, &g);
+            if (!g) break;  // the capture did not take: the steps left go one by one
             NB_CUDA(cudaGraphLaunch(g, s));
         }
     }
@@ -562,7 +587,7 @@ int nb_set_params(nb_ctx *c, double eps2, double damping, double dt, double G)
     // captured graphs hold the old values as kernel arguments
     for (auto &g : c->step_graph)
         if (g) {
-            cudaGraphExecDestroy(g);
+            nb::graph_exec_destroy(g);
             g = nullptr;
         }
     c->p.eps2 = eps2;
@@ -634,9 +659,9 @@ int nb_energy(nb_ctx *c, double *out5, void *accphi_dev, void *stream)
         const size_t bytes[4] = {(size_t)p.n * sizeof(double4), (size_t)p.n * sizeof(double4),
                                  (size_t)(nb::energy_blocks(p.n) + 1) * 5 * sizeof(double), 8 * sizeof(double)};
         cudaError_t e = cudaSuccess;
-        for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaMalloc(&m[k], bytes[k]);
+        for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = nb::dmalloc(&m[k], bytes[k]);
         if (e != cudaSuccess) {
-            for (void *q : m) cudaFree(q);
+            for (void *q : m) nb::dfree(q);
             return nb::cuda_error(e, "energy scratch allocation");
         }
         c->acc_tmp = m[1];
@@ -719,14 +744,14 @@ static int adj_reserve(nb_ctx *c, int nckpt, int every)
     if (!A.gm) {
         // gm is allocated last: without it, a retry after a failed
         // allocation starts from nothing
-        cudaFree(A.sym_t);
-        cudaFree(A.sym_s);
-        cudaFree(A.partial);
-        cudaFree(A.vel_tmp);
-        cudaFree(A.vel_tmp2);
-        cudaFree(A.lx);
-        cudaFree(A.lv);
-        cudaFree(A.gbuf);
+        nb::dfree(A.sym_t);
+        nb::dfree(A.sym_s);
+        nb::dfree(A.partial);
+        nb::dfree(A.vel_tmp);
+        nb::dfree(A.vel_tmp2);
+        nb::dfree(A.lx);
+        nb::dfree(A.lv);
+        nb::dfree(A.gbuf);
         A.sym_t = A.sym_s = A.partial = A.vel_tmp = A.vel_tmp2 = A.lx = A.lv = A.gbuf = nullptr;
         A.sym = uses_sym(c);
         if (A.sym) {
@@ -752,8 +777,8 @@ static int adj_reserve(nb_ctx *c, int nckpt, int every)
             return st;
     }
     if (nckpt > A.cap_ckpt) {
-        cudaFree(A.ckpt_pos);
-        cudaFree(A.ckpt_vel);
+        nb::dfree(A.ckpt_pos);
+        nb::dfree(A.ckpt_vel);
         A.ckpt_pos = A.ckpt_vel = nullptr;
         A.cap_ckpt = 0;
         if ((st = dev_alloc((void **)&A.ckpt_pos, n * nckpt * sizeof(float4), "checkpoint allocation")) ||
@@ -762,10 +787,10 @@ static int adj_reserve(nb_ctx *c, int nckpt, int every)
         A.cap_ckpt = nckpt;
     }
     if (every > A.cap_seg) {
-        cudaFree(A.seg_pos);
-        cudaFree(A.seg_acc);
-        cudaFree(A.seg_pos2);
-        cudaFree(A.seg_acc2);
+        nb::dfree(A.seg_pos);
+        nb::dfree(A.seg_acc);
+        nb::dfree(A.seg_pos2);
+        nb::dfree(A.seg_acc2);
         A.seg_pos = A.seg_acc = A.seg_pos2 = A.seg_acc2 = nullptr;
         A.cap_seg = 0;
         if ((st = dev_alloc((void **)&A.seg_pos, n * (every + 1) * sizeof(float4), "segment allocation")) ||
@@ -1068,9 +1093,9 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
                              is_comp(c) ? n * sizeof(float4) : 0};
     cudaError_t e = cudaSuccess;
     for (int q = 0; q < 6 && e == cudaSuccess; ++q)
-        if (bytes[q]) e = cudaMalloc(&m[q], bytes[q]);
+        if (bytes[q]) e = nb::dmalloc(&m[q], bytes[q]);
     if (e != cudaSuccess) {
-        for (void *q : m) cudaFree(q);
+        for (void *q : m) nb::dfree(q);
         return nb::cuda_error(e, "autotune scratch allocation");
     }
     void *pos_now = is_comp(c) ? c->pos[0] : c->pos[c->cur];
@@ -1094,19 +1119,19 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
     // and a recorded adjoint forward pass belong to the old plan
     for (auto &g : c->step_graph)
         if (g) {
-            cudaGraphExecDestroy(g);
+            nb::graph_exec_destroy(g);
             g = nullptr;
         }
     c->adj.ready = false;
     c->adj.live_last = false;
     cudaStreamSynchronize(s);  // the old scratch may still be in use
     if (symm) {
-        cudaFree(c->sym_t);
-        cudaFree(c->sym_s);
+        nb::dfree(c->sym_t);
+        nb::dfree(c->sym_s);
         c->sym_t = (float4 *)m[0];
         c->sym_s = (float4 *)m[1];
     } else {
-        cudaFree(c->partial);
+        nb::dfree(c->partial);
         c->partial = (float4 *)m[0];
     }
     int st = e == cudaSuccess ? NB_OK : nb::cuda_error(e, "autotune state copy");
@@ -1151,7 +1176,7 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
     }
     restore();
     cudaStreamSynchronize(s);
-    for (int q = 2; q < 6; ++q) cudaFree(m[q]);
+    for (int q = 2; q < 6; ++q) nb::dfree(m[q]);
     if (st) return st;
     const int ra = symm ? c->splan.warps * 32 : c->plan.block, rb = symm ? c->splan.bpt : c->plan.bpt;
     if (cache_path && !cached && pick) {
@@ -1198,9 +1223,9 @@ int nb_run_host(nb_ctx *c, const void *pos, const void *vel, int loops, int out_
         // all three or none: a failed call leaves nothing half set up
         void *b3[3] = {nullptr, nullptr, nullptr};
         cudaError_t e = cudaSuccess;
-        for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMallocHost(&b3[k], sb);
+        for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = nb::hmalloc(&b3[k], sb);
         if (e != cudaSuccess) {
-            for (void *q : b3) cudaFreeHost(q);
+            for (void *q : b3) nb::hfree(q);
             return nb::cuda_error(e, "pinned staging allocation");
         }
         c->stage_pos = b3[0];
@@ -1242,16 +1267,16 @@ int nb_run_host(nb_ctx *c, const void *pos, const void *vel, int loops, int out_
         cudaEvent_t es[2] = {nullptr, nullptr}, e0[2] = {nullptr, nullptr}, e1[2] = {nullptr, nullptr};
         cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
         for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
-            e = cudaMalloc(&snap[k], sb);
-            if (e == cudaSuccess) e = cudaMallocHost(&stage[k], sb);
+            e = nb::dmalloc(&snap[k], sb);
+            if (e == cudaSuccess) e = nb::hmalloc(&stage[k], sb);
             if (e == cudaSuccess) e = cudaEventCreate(&es[k]);
             if (e == cudaSuccess) e = cudaEventCreate(&e0[k]);
             if (e == cudaSuccess) e = cudaEventCreate(&e1[k]);
         }
         if (e != cudaSuccess) {
             for (int k = 0; k < 2; ++k) {
-                cudaFree(snap[k]);
-                cudaFreeHost(stage[k]);
+                nb::dfree(snap[k]);
+                nb::hfree(stage[k]);
                 if (es[k]) cudaEventDestroy(es[k]);
                 if (e0[k]) cudaEventDestroy(e0[k]);
                 if (e1[k]) cudaEventDestroy(e1[k]);

@@ -1039,25 +1039,25 @@ static int batch_apply_plan(nb_batch *b, int wpb, int bpt, cudaStream_t s)
     // (its arguments) and the old plan are void until this call succeeds
     b->plan_ok = false;
     if (b->graph) {
-        cudaGraphExecDestroy(b->graph);
+        nb::graph_exec_destroy(b->graph);
         b->graph = nullptr;
         b->graph_cur = -1;
     }
     const size_t wide = b->f64 ? 2 : 1;  // float4 entries per partial entry
     const size_t need = (size_t)p.slots * 32 * bpt * wide;
     if (need > b->partial_cap) {
-        cudaFree(b->partial);
+        nb::dfree(b->partial);
         b->partial = nullptr;
         b->partial_cap = 0;
-        cudaError_t e = cudaMalloc((void **)&b->partial, need * sizeof(float4));
+        cudaError_t e = nb::dmalloc((void **)&b->partial, need * sizeof(float4));
         if (e != cudaSuccess) return nb::cuda_error(e, "batched scratch allocation");
         b->partial_cap = need;
     }
     if ((size_t)p.spart * wide > b->spart_cap) {
-        cudaFree(b->spart);
+        nb::dfree(b->spart);
         b->spart = nullptr;
         b->spart_cap = 0;
-        cudaError_t e = cudaMalloc((void **)&b->spart, (size_t)p.spart * wide * sizeof(float4));
+        cudaError_t e = nb::dmalloc((void **)&b->spart, (size_t)p.spart * wide * sizeof(float4));
         if (e != cudaSuccess) return nb::cuda_error(e, "batched source-side allocation");
         b->spart_cap = (size_t)p.spart * wide;
     }
@@ -1218,12 +1218,12 @@ static int batch_vplan_setup(nb_batch *b)
                               nb4, nb4, nb4, nb4, nb4,
                               std::max<size_t>((size_t)b->nbody, 1) * sizeof(float)};
     cudaError_t e = cudaSuccess;
-    for (int q = 0; q < 11 && e == cudaSuccess; ++q) e = cudaMalloc(&m[q], bytes[q]);
-    if (e == cudaSuccess) e = cudaMemcpy(m[0], it_off.data(), bytes[0], cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(m[1], tb_off.data(), bytes[1], cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(m[2], sp_off.data(), bytes[2], cudaMemcpyHostToDevice);
+    for (int q = 0; q < 11 && e == cudaSuccess; ++q) e = nb::dmalloc(&m[q], bytes[q]);
+    if (e == cudaSuccess) e = nb::dmemcpy(m[0], it_off.data(), bytes[0], cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = nb::dmemcpy(m[1], tb_off.data(), bytes[1], cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = nb::dmemcpy(m[2], sp_off.data(), bytes[2], cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
-        for (void *q : m) cudaFree(q);
+        for (void *q : m) nb::dfree(q);
         return nb::cuda_error(e, "batched adjoint allocation");
     }
     b->d_tb_off_v = (int *)m[1];
@@ -1244,42 +1244,42 @@ static int batch_vplan_setup(nb_batch *b)
 static void free_batch(nb_batch *b)
 {
     if (!b) return;
-    if (b->graph) cudaGraphExecDestroy(b->graph);
-    cudaFree(b->d_sys_off);
-    cudaFree(b->d_tb_off);
-    cudaFree(b->d_body_sys);
-    cudaFree(b->d_it_off);
-    cudaFree(b->pos[0]);
-    cudaFree(b->pos[1]);
-    cudaFree(b->vel);
-    cudaFree(b->partial);
-    cudaFree(b->spart);
-    cudaFree(b->d_sp_off);
-    cudaFree(b->sys_partial);
-    cudaFree(b->sys_spart);
-    cudaFree(b->ff_split);
-    cudaFree(b->ff_range);
-    cudaFree(b->d_it_off_v);
-    cudaFree(b->d_tb_off_v);
-    cudaFree(b->vpartial);
-    cudaFree(b->d_sp_off_v);
-    cudaFree(b->vspart);
-    cudaFree(b->ckpt_pos);
-    cudaFree(b->ckpt_vel);
-    cudaFree(b->seg_pos);
-    cudaFree(b->seg_acc);
-    cudaFree(b->vel_tmp);
-    cudaFree(b->seg_pos2);
-    cudaFree(b->seg_acc2);
-    cudaFree(b->vel_tmp2);
+    if (b->graph) nb::graph_exec_destroy(b->graph);
+    nb::dfree(b->d_sys_off);
+    nb::dfree(b->d_tb_off);
+    nb::dfree(b->d_body_sys);
+    nb::dfree(b->d_it_off);
+    nb::dfree(b->pos[0]);
+    nb::dfree(b->pos[1]);
+    nb::dfree(b->vel);
+    nb::dfree(b->partial);
+    nb::dfree(b->spart);
+    nb::dfree(b->d_sp_off);
+    nb::dfree(b->sys_partial);
+    nb::dfree(b->sys_spart);
+    nb::dfree(b->ff_split);
+    nb::dfree(b->ff_range);
+    nb::dfree(b->d_it_off_v);
+    nb::dfree(b->d_tb_off_v);
+    nb::dfree(b->vpartial);
+    nb::dfree(b->d_sp_off_v);
+    nb::dfree(b->vspart);
+    nb::dfree(b->ckpt_pos);
+    nb::dfree(b->ckpt_vel);
+    nb::dfree(b->seg_pos);
+    nb::dfree(b->seg_acc);
+    nb::dfree(b->vel_tmp);
+    nb::dfree(b->seg_pos2);
+    nb::dfree(b->seg_acc2);
+    nb::dfree(b->vel_tmp2);
     if (b->rstream) cudaStreamDestroy(b->rstream);
     for (auto &e : b->ev_rec)
         if (e) cudaEventDestroy(e);
     if (b->ev_go) cudaEventDestroy(b->ev_go);
-    cudaFree(b->lx);
-    cudaFree(b->lv);
-    cudaFree(b->gbuf);
-    cudaFree(b->gm);
+    nb::dfree(b->lx);
+    nb::dfree(b->lv);
+    nb::dfree(b->gbuf);
+    nb::dfree(b->gm);
     delete b;
 }
 
@@ -1325,7 +1325,7 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
     const size_t sb = (size_t)nbody * (b->f64 ? sizeof(double4) : sizeof(float4));
 #define NB_BALLOC(ptr, bytes)                                                  \
     do {                                                                       \
-        cudaError_t _e = cudaMalloc((void **)&(ptr), (bytes) ? (bytes) : 16);  \
+        cudaError_t _e = nb::dmalloc((void **)&(ptr), (bytes) ? (bytes) : 16);  \
         if (_e != cudaSuccess) {                                               \
             free_batch(b);                                                     \
             return nb::cuda_error(_e, "batch allocation");                     \
@@ -1344,9 +1344,9 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
         NB_BALLOC(b->ff_range, 2 * sizeof(unsigned long long));
     }
 #undef NB_BALLOC
-    e = cudaMemcpy(b->d_sys_off, sys_off.data(), sizeof(int) * (nsys + 1), cudaMemcpyHostToDevice);
+    e = nb::dmemcpy(b->d_sys_off, sys_off.data(), sizeof(int) * (nsys + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && nbody)
-        e = cudaMemcpy(b->d_body_sys, body_sys.data(), sizeof(int) * (size_t)nbody, cudaMemcpyHostToDevice);
+        e = nb::dmemcpy(b->d_body_sys, body_sys.data(), sizeof(int) * (size_t)nbody, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         free_batch(b);
         return nb::cuda_error(e, "batch tables");
@@ -1367,7 +1367,12 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
 int nb_batch_destroy(nb_batch *b)
 {
     if (!b) return NB_OK;
-    cudaDeviceSynchronize();
+    const cudaError_t e = nb::device_sync();
+    if (nb::is_capture_error(e)) {  // as nb_destroy: keep what may still be in use
+        (void)cudaGetLastError();
+        return nb::cuda_error(e, "nb_batch_destroy: the device cannot be synchronised while another thread "
+                                 "captures a graph; the batch is kept, call again after the capture");
+    }
     free_batch(b);
     return NB_OK;
 }
@@ -1437,24 +1442,39 @@ int nb_batch_run(nb_batch *b, int steps, void *stream)
     }
     if (!b->graph || b->graph_steps != steps || b->graph_cur != b->cur) {
         if (b->graph) {
-            cudaGraphExecDestroy(b->graph);
+            nb::graph_exec_destroy(b->graph);
             b->graph = nullptr;
         }
+        // a capture that does not take (a device-wide call made by code
+        // outside the library in another thread invalidates it) ran nothing
+        // and leaves b->cur as it was: the steps then go one by one, where an
+        // error of the steps themselves shows
         const int cur0 = b->cur;
         cudaGraph_t g = nullptr;
-        NB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        int st = NB_OK;
-        for (int i = 0; i < steps && !st; ++i) st = batch_step_once(b, s);
-        cudaError_t e = cudaStreamEndCapture(s, &g);
-        b->cur = cur0;
-        if (st) {
-            if (g) cudaGraphDestroy(g);
-            return st;
+        {
+            std::shared_lock<std::shared_mutex> gate(nb::capture_gate());
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                int st = NB_OK;
+                for (int i = 0; i < steps && !st; ++i) st = batch_step_once(b, s);
+                if (cudaStreamEndCapture(s, &g) != cudaSuccess || st) {
+                    if (g) cudaGraphDestroy(g);
+                    g = nullptr;
+                }
+            }
         }
-        if (e != cudaSuccess) return nb::cuda_error(e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&b->graph, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return nb::cuda_error(e, "cudaGraphInstantiate");
+        b->cur = cur0;
+        if (g) {
+            if (nb::graph_instantiate(&b->graph, g) != cudaSuccess) b->graph = nullptr;
+            cudaGraphDestroy(g);
+        }
+        (void)cudaGetLastError();
+        if (!b->graph) {
+            for (int i = 0; i < steps; ++i) {
+                int st = batch_step_once(b, s);
+                if (st) return st;
+            }
+            return NB_OK;
+        }
         b->graph_steps = steps;
         b->graph_cur = cur0;
     }
@@ -1469,7 +1489,7 @@ int nb_batch_set_params(nb_batch *b, double eps2, double damping, double dt, dou
     if (!std::isfinite(eps2) || !std::isfinite(damping) || !std::isfinite(dt) || !std::isfinite(G))
         return set_error(NB_ERR_INVALID, "eps2, damping, dt and G must be finite");
     if (b->graph) {  // it holds the old values as kernel arguments
-        cudaGraphExecDestroy(b->graph);
+        nb::graph_exec_destroy(b->graph);
         b->graph = nullptr;
         b->graph_cur = -1;
     }
@@ -1550,15 +1570,15 @@ int nb_batch_autotune(nb_batch *b, int reps, const char *cache_path, void *strea
     float4 *save_p = nullptr, *save_v = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     auto release = [&] {
-        cudaFree(save_p);
-        cudaFree(save_v);
+        nb::dfree(save_p);
+        nb::dfree(save_v);
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
     };
     cudaError_t ce = cudaSuccess;
     if (sb) {
-        ce = cudaMalloc((void **)&save_p, sb);
-        if (ce == cudaSuccess) ce = cudaMalloc((void **)&save_v, sb);
+        ce = nb::dmalloc((void **)&save_p, sb);
+        if (ce == cudaSuccess) ce = nb::dmalloc((void **)&save_v, sb);
         if (ce == cudaSuccess) ce = cudaMemcpyAsync(save_p, b->pos[b->cur], sb, cudaMemcpyDeviceToDevice, s);
         if (ce == cudaSuccess) ce = cudaMemcpyAsync(save_v, b->vel, sb, cudaMemcpyDeviceToDevice, s);
     }
@@ -1709,10 +1729,10 @@ int nb_batch_step_per_system(nb_batch *b, int steps, void *stream)
     if (!b->sys_partial) {
         // both or neither: a failure leaves no half-allocated pair behind
         float4 *t = nullptr, *u = nullptr;
-        cudaError_t e = cudaMalloc((void **)&t, sp.tpart * sizeof(float4));
-        if (e == cudaSuccess) e = cudaMalloc((void **)&u, sp.spart * sizeof(float4));
+        cudaError_t e = nb::dmalloc((void **)&t, sp.tpart * sizeof(float4));
+        if (e == cudaSuccess) e = nb::dmalloc((void **)&u, sp.spart * sizeof(float4));
         if (e != cudaSuccess) {
-            cudaFree(t);
+            nb::dfree(t);
             return nb::cuda_error(e, "per-system baseline scratch allocation");
         }
         b->sys_partial = t;
@@ -1737,7 +1757,7 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
     if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
     if (!b->has_state) return set_error(NB_ERR_STATE, "no state loaded");
     if (ntasks < 1 || steps < 0) return set_error(NB_ERR_INVALID, "ntasks >= 1 and steps >= 0");
-    NB_CUDA(cudaDeviceSynchronize());
+    NB_CUDA(nb::device_sync());
     if (ntasks > b->nsys) ntasks = b->nsys > 0 ? b->nsys : 1;
     SysPlans sp;
     int st0 = sys_plans_for(b, &sp);
@@ -1747,16 +1767,16 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
     std::vector<cudaStream_t> streams(ntasks, nullptr);
     auto release = [&] {
         for (int t = 0; t < ntasks; ++t) {
-            cudaFree(tscratch[t]);
-            cudaFree(sscratch[t]);
-            cudaFree(ranges[t]);
+            nb::dfree(tscratch[t]);
+            nb::dfree(sscratch[t]);
+            nb::dfree(ranges[t]);
             if (streams[t]) cudaStreamDestroy(streams[t]);
         }
     };
     for (int t = 0; t < ntasks; ++t) {
-        cudaError_t e = cudaMalloc((void **)&tscratch[t], sp.tpart * sizeof(float4));
-        if (e == cudaSuccess) e = cudaMalloc((void **)&sscratch[t], sp.spart * sizeof(float4));
-        if (e == cudaSuccess) e = cudaMalloc((void **)&ranges[t], 2 * sizeof(unsigned long long));
+        cudaError_t e = nb::dmalloc((void **)&tscratch[t], sp.tpart * sizeof(float4));
+        if (e == cudaSuccess) e = nb::dmalloc((void **)&sscratch[t], sp.spart * sizeof(float4));
+        if (e == cudaSuccess) e = nb::dmalloc((void **)&ranges[t], 2 * sizeof(unsigned long long));
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&streams[t], cudaStreamNonBlocking);
         if (e != cudaSuccess) {
             release();
@@ -1811,25 +1831,25 @@ int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream)
     const int nckpt = (steps + ckpt_every - 1) / ckpt_every;
     const size_t n = (size_t)b->nbody;
     if (nckpt > b->cap_ckpt) {
-        cudaFree(b->ckpt_pos);
-        cudaFree(b->ckpt_vel);
+        nb::dfree(b->ckpt_pos);
+        nb::dfree(b->ckpt_vel);
         b->ckpt_pos = b->ckpt_vel = nullptr;
         b->cap_ckpt = 0;
-        NB_CUDA(cudaMalloc((void **)&b->ckpt_pos, std::max<size_t>(n * nckpt, 1) * sizeof(float4)));
-        NB_CUDA(cudaMalloc((void **)&b->ckpt_vel, std::max<size_t>(n * nckpt, 1) * sizeof(float4)));
+        NB_CUDA(nb::dmalloc((void **)&b->ckpt_pos, std::max<size_t>(n * nckpt, 1) * sizeof(float4)));
+        NB_CUDA(nb::dmalloc((void **)&b->ckpt_vel, std::max<size_t>(n * nckpt, 1) * sizeof(float4)));
         b->cap_ckpt = nckpt;
     }
     if (ckpt_every > b->cap_seg) {
-        cudaFree(b->seg_pos);
-        cudaFree(b->seg_acc);
-        cudaFree(b->seg_pos2);
-        cudaFree(b->seg_acc2);
+        nb::dfree(b->seg_pos);
+        nb::dfree(b->seg_acc);
+        nb::dfree(b->seg_pos2);
+        nb::dfree(b->seg_acc2);
         b->seg_pos = b->seg_acc = b->seg_pos2 = b->seg_acc2 = nullptr;
         b->cap_seg = 0;
-        NB_CUDA(cudaMalloc((void **)&b->seg_pos, std::max<size_t>(n * (ckpt_every + 1), 1) * sizeof(float4)));
-        NB_CUDA(cudaMalloc((void **)&b->seg_acc, std::max<size_t>(n * ckpt_every, 1) * sizeof(float4)));
-        NB_CUDA(cudaMalloc((void **)&b->seg_pos2, std::max<size_t>(n * (ckpt_every + 1), 1) * sizeof(float4)));
-        NB_CUDA(cudaMalloc((void **)&b->seg_acc2, std::max<size_t>(n * ckpt_every, 1) * sizeof(float4)));
+        NB_CUDA(nb::dmalloc((void **)&b->seg_pos, std::max<size_t>(n * (ckpt_every + 1), 1) * sizeof(float4)));
+        NB_CUDA(nb::dmalloc((void **)&b->seg_acc, std::max<size_t>(n * ckpt_every, 1) * sizeof(float4)));
+        NB_CUDA(nb::dmalloc((void **)&b->seg_pos2, std::max<size_t>(n * (ckpt_every + 1), 1) * sizeof(float4)));
+        NB_CUDA(nb::dmalloc((void **)&b->seg_acc2, std::max<size_t>(n * ckpt_every, 1) * sizeof(float4)));
         b->cap_seg = ckpt_every;
     }
     cudaStream_t s = (cudaStream_t)stream;

@@ -371,7 +371,7 @@ int probe_fma(int iters, int packed, double *flops, float *ms, cudaStream_t s)
     const int grid = sms * std::max(occ, 1);
     float *out = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    cudaError_t e = cudaMalloc((void **)&out, sizeof(float) * grid * 256);
+    cudaError_t e = nb::dmalloc((void **)&out, sizeof(float) * grid * 256);
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (e == cudaSuccess) {
@@ -389,7 +389,7 @@ int probe_fma(int iters, int packed, double *flops, float *ms, cudaStream_t s)
     cudaStreamSynchronize(s);  // nothing of the probe is in flight below
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
-    cudaFree(out);
+    nb::dfree(out);
     if (e != cudaSuccess) return cuda_error(e, "probe_fma");
     // 16 lane-FMAs per thread per iteration either way, 2 FLOP each
     *flops = 2.0 * 16.0 * (double)iters * (double)grid * 256.0;

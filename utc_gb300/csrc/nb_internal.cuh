@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+#include <shared_mutex>
 #include <string>
 
 #include "nbody_gb300.h"
@@ -27,6 +29,79 @@ int cuda_error(cudaError_t e, const char *what);
         cudaError_t _e = cudaGetLastError();                      \
         if (_e != cudaSuccess) return ::nb::cuda_error(_e, what); \
     } while (0)
+
+// ---------------------------------------------------------------------------
+// the capture gate
+// ---------------------------------------------------------------------------
+// A call that synchronises the whole device (cudaMalloc, cudaFree and their
+// pinned-host and managed forms, cudaDeviceSynchronize, a synchronous
+// cudaMemcpy) made in one host thread while another thread captures a stream
+// into a graph invalidates that capture, and the synchronising call itself
+// may return without having synchronised.  Several host threads that each
+// step their own context (one UTC task per system) meet exactly so.  The
+// library's captures hold this gate shared and its device-wide calls hold it
+// exclusively, so the two never overlap within the library; a capture that
+// something outside the library invalidates falls back to step-by-step
+// launches (nb_step, nb_batch_run).
+std::shared_mutex &capture_gate();
+
+inline bool is_capture_error(cudaError_t e)
+{
+    return e >= cudaErrorStreamCaptureUnsupported && e <= cudaErrorStreamCaptureWrongThread;
+}
+
+template <class T>
+inline cudaError_t dmalloc(T **p, size_t bytes)
+{
+    std::unique_lock<std::shared_mutex> g(capture_gate());
+    return cudaMalloc((void **)p, bytes);
+}
+template <class T>
+inline cudaError_t dmalloc_managed(T **p, size_t bytes)
+{
+    std::unique_lock<std::shared_mutex> g(capture_gate());
+    return cudaMallocManaged((void **)p, bytes, cudaMemAttachGlobal);
+}
+template <class T>
+inline cudaError_t hmalloc(T **p, size_t bytes)
+{
+    std::unique_lock<std::shared_mutex> g(capture_gate());
+    return cudaMallocHost((void **)p, bytes);
+}
+inline cudaError_t dfree(void *p)
+{
+    if (!p) return cudaSuccess;
+    std::unique_lock<std::shared_mutex> g(capture_gate());
+    return cudaFree(p);
+}
+inline cudaError_t hfree(void *p)
+{
+    if (!p) return cudaSuccess;
+    std::unique_lock<std::shared_mutex> g(capture_gate());
+    return cudaFreeHost(p);
+}
+inline cudaError_t device_sync()
+{
+    std::unique_lock<std::shared_mutex> g(capture_gate());
+    return cudaDeviceSynchronize();
+}
+inline cudaError_t dmemcpy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind)
+{
+    std::unique_lock<std::shared_mutex> g(capture_gate());
+    return cudaMemcpy(dst, src, bytes, kind);
+}
+// graph instantiation and destruction may allocate or free device memory
+inline cudaError_t graph_instantiate(cudaGraphExec_t *out, cudaGraph_t g)
+{
+    std::unique_lock<std::shared_mutex> lk(capture_gate());
+    return cudaGraphInstantiate(out, g, 0);
+}
+inline cudaError_t graph_exec_destroy(cudaGraphExec_t g)
+{
+    if (!g) return cudaSuccess;
+    std::unique_lock<std::shared_mutex> lk(capture_gate());
+    return cudaGraphExecDestroy(g);
+}
 
 // ---------------------------------------------------------------------------
 // packed f32x2 arithmetic (sm_100+ FFMA2 / FADD2 / FMUL2)

@@ -74,7 +74,9 @@ class NBodySystem:
     # ------------------------------------------------------------------
     def close(self):
         if getattr(self, "handle", None):
-            self.lib.nb_destroy(self.handle)
+            # a refused destroy (another thread is capturing a graph) keeps the
+            # context, and the handle with it, for a later close()
+            N.check(self.lib.nb_destroy(self.handle), "nb_destroy")
             self.handle = None
 
     def __del__(self):
@@ -284,7 +286,7 @@ class NBodyBatch:
 
     def close(self):
         if getattr(self, "handle", None):
-            self.lib.nb_batch_destroy(self.handle)
+            N.check(self.lib.nb_batch_destroy(self.handle), "nb_batch_destroy")
             self.handle = None
 
     def __del__(self):
