@@ -5,6 +5,7 @@
 // (oracle/nbody_oracle.c) and records what the task handed over.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -25,10 +26,21 @@ struct Record {
     int streams_created = 0, streams_destroyed = 0;
 } g_rec;
 
+struct BatchRecord {
+    int creates = 0, runs = 0, nsys = 0, destroys = 0, precision = -1, algo = -1;
+    void *stream = nullptr;
+} g_batch;
+
 }  // namespace
 
 struct nb_ctx {
     nb_params p;
+};
+
+struct nb_batch {
+    nb_params p;
+    std::vector<int> sizes;
+    std::vector<double> x, v;
 };
 
 extern "C" {
@@ -119,7 +131,108 @@ int nb_run_host(nb_ctx *c, const void *pos, const void *vel, int loops, int out_
     return NB_OK;
 }
 
+// ---- the timing events and the batch calls of a task group ----
+cudaError_t cudaEventCreate(cudaEvent_t *e)
+{
+    *e = reinterpret_cast<cudaEvent_t>(&g_fake_stream_object);
+    return cudaSuccess;
+}
+cudaError_t cudaEventRecord(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
+cudaError_t cudaEventSynchronize(cudaEvent_t) { return cudaSuccess; }
+cudaError_t cudaEventElapsedTime(float *ms, cudaEvent_t, cudaEvent_t)
+{
+    *ms = 1.0f;
+    return cudaSuccess;
+}
+cudaError_t cudaEventDestroy(cudaEvent_t) { return cudaSuccess; }
+
+int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **out)
+{
+    *out = nullptr;
+    for (int i = 0; i < nsys; ++i)
+        if (sizes[i] == 3) {  // planted failure: every member must report it
+            g_err = "mock: a system of 3 bodies is refused";
+            return NB_ERR_INVALID;
+        }
+    nb_batch *b = new nb_batch();
+    b->p = *p;
+    b->sizes.assign(sizes, sizes + nsys);
+    size_t total = 0;
+    for (int n : b->sizes) total += 4 * (size_t)n;
+    b->x.resize(total);
+    b->v.resize(total);
+    g_batch.creates++;
+    g_batch.nsys = nsys;
+    g_batch.precision = p->precision;
+    g_batch.algo = p->algo;
+    *out = b;
+    return NB_OK;
+}
+
+int nb_batch_destroy(nb_batch *b)
+{
+    if (b) g_batch.destroys++;
+    delete b;
+    return NB_OK;
+}
+
+int nb_batch_set_state(nb_batch *b, const void *pos, const void *vel, int, void *)
+{
+    const size_t m = b->x.size(), w = b->p.precision == NB_F64 ? 8 : 4;
+    for (size_t k = 0; k < m; ++k) {  // kept as double: exact for either state type
+        b->x[k] = w == 8 ? ((const double *)pos)[k] : (double)((const float *)pos)[k];
+        b->v[k] = w == 8 ? ((const double *)vel)[k] : (double)((const float *)vel)[k];
+    }
+    return NB_OK;
+}
+
+int nb_batch_get_state(nb_batch *b, void *pos, void *vel, int, void *)
+{
+    const size_t m = b->x.size();
+    for (size_t k = 0; k < m; ++k) {
+        if (b->p.precision == NB_F64) {
+            if (pos) ((double *)pos)[k] = b->x[k];
+            if (vel) ((double *)vel)[k] = b->v[k];
+        } else {
+            if (pos) ((float *)pos)[k] = (float)b->x[k];
+            if (vel) ((float *)vel)[k] = (float)b->v[k];
+        }
+    }
+    return NB_OK;
+}
+
+// each system stepped alone by the oracle, in the state's precision
+int nb_batch_run(nb_batch *b, int steps, void *stream)
+{
+    const nb_params &p = b->p;
+    g_batch.runs++;
+    g_batch.stream = stream;
+    size_t o = 0;
+    for (int n : b->sizes) {
+        const size_t m = 4 * (size_t)n;
+        if (p.precision == NB_F64) {
+            orc_step_f64(n, &b->x[o], &b->v[o], p.eps2, p.damping, p.dt, steps, p.kick, p.G, 1);
+        } else {
+            std::vector<float> x(b->x.begin() + o, b->x.begin() + o + m), v(b->v.begin() + o, b->v.begin() + o + m);
+            orc_step_f32(n, x.data(), v.data(), (float)p.eps2, (float)p.damping, (float)p.dt, steps, p.kick,
+                         (float)p.G, 1);
+            std::copy(x.begin(), x.end(), b->x.begin() + o);
+            std::copy(v.begin(), v.end(), b->v.begin() + o);
+        }
+        o += m;
+    }
+    return NB_OK;
+}
+
 // ---- what the test reads back ----
+void mock_batch_record(int *ints6, void **stream)
+{
+    const int v[6] = {g_batch.creates, g_batch.runs, g_batch.nsys, g_batch.destroys, g_batch.precision,
+                      g_batch.algo};
+    std::memcpy(ints6, v, sizeof(v));
+    *stream = g_batch.stream;
+}
+void mock_batch_reset(void) { g_batch = BatchRecord(); }
 void *mock_fake_stream(void) { return g_fake_stream; }
 void mock_record(void **stream, int *ints9, double *dbl3)
 {

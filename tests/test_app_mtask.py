@@ -56,3 +56,20 @@ def test_mtask_many_tasks_at_once(cuda, state):
                            capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
         assert "status" not in r.stderr and "Test complete !!!" in r.stdout
+
+
+@pytest.mark.parametrize("state", ["double", "float"])
+def test_mtask_grouped_tasks_equal_the_batch(cuda, tmp_path, state):
+    # -B 2: one task per system, the tasks joined in one BodyTaskGroup, whose
+    # run is the same batch as -B 1: the frames agree bit for bit
+    n, ntasks, loops, oi = 512, 6, 40, 20
+    extra = ["-F"] if state == "float" else []
+    out = {}
+    for mode in ("1", "2"):
+        path = str(tmp_path / f"out{mode}.txt")
+        r = subprocess.run([APP, "-v", "-n", str(n), "-T", str(ntasks), "-l", str(loops), "-o", str(oi),
+                            "-O", path, "-B", mode] + extra, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "Test complete !!!" in r.stdout
+        out[mode] = open(path).read()
+    assert out["1"] == out["2"]

@@ -92,3 +92,76 @@ def test_task_reports_a_failing_call(mock_task):
                                frames.ctypes.data, 0, -1, 0)
     assert rc == 1  # NB_ERR_INVALID from nb_create, kept as the task's status
     assert (frames == -7.0).all() and (rt == 0).all()
+
+
+# ---- BodyTaskGroup: tasks whose runs go as one batch ----
+
+def group_run(lib, dtype, sizes, eps2s, loops, oi, members=None, timeout=30.0, damping=0.999, dt=0.005):
+    n_sys = len(sizes)
+    states = [oracle.randomize(1, n, dtype, seed=1 + k) for k, n in enumerate(sizes)]
+    pos = [p for p, _ in states]
+    vel = [v for _, v in states]
+    frames = [np.full((loops // oi + 1, n, 4), -7.0, dtype) for n in sizes]  # one spare frame each
+    ptr = C.c_void_p * n_sys
+    st = np.full(n_sys, -1, np.int32)
+    rt = np.zeros((n_sys, 4), np.float64)
+    fn = lib.nbt_group_run_f64 if dtype == np.float64 else lib.nbt_group_run_f32
+    T = C.c_double if dtype == np.float64 else C.c_float
+    fn.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, T, T, C.c_int, C.c_int,
+                   C.c_int, C.c_double, C.c_void_p, C.c_void_p]
+    sz = np.asarray(sizes, np.int32)
+    e = np.asarray(eps2s, dtype)
+    lib.mock_batch_reset()
+    rc = fn(n_sys, sz.ctypes.data, ptr(*[p.ctypes.data for p in pos]), ptr(*[v.ctypes.data for v in vel]),
+            ptr(*[f.ctypes.data for f in frames]), e.ctypes.data, damping, dt, loops, oi,
+            members or n_sys, timeout, st.ctypes.data, rt.ctypes.data)
+    return rc, st, pos, vel, frames, rt
+
+
+def batch_record(lib):
+    ints = np.zeros(6, np.int32)
+    s = C.c_void_p()
+    lib.mock_batch_record(ints.ctypes.data_as(C.c_void_p), C.byref(s))
+    return ints, s.value
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_group_runs_every_member_as_one_batch(mock_task, dtype):
+    sizes, loops, oi = [64, 100, 36], 12, 4
+    rc, st, pos, vel, frames, rt = group_run(mock_task, dtype, sizes, [0.01] * 3, loops, oi)
+    assert rc == 0 and list(st) == [0, 0, 0]
+    for k, n in enumerate(sizes):
+        p, v = oracle.randomize(1, n, dtype, seed=1 + k)
+        assert np.array_equal(pos[k], p) and np.array_equal(vel[k], v)  # inputs not updated
+        for f in range(loops // oi):
+            p, v = oracle.step(p, v, dtype(0.01), dtype(0.999), dtype(0.005), oi)
+            assert np.array_equal(frames[k][f], p), (k, f)
+        assert (frames[k][-1] == -7.0).all()
+    (creates, runs, nsys, destroys, prec, algo), stream = batch_record(mock_task)
+    assert (creates, runs, nsys, destroys) == (1, loops // oi, 3, 1)  # one batch, one run per frame
+    assert prec == (1 if dtype == np.float64 else 0) and algo == 2
+    assert stream == mock_task.mock_fake_stream()  # the batch's own stream
+    # every member gets the batch's timers: 3 frames x 1 ms kernel, 1 ms copy-in, 3 x 1 ms copy-out
+    for r in rt:
+        assert r[0] > 0 and np.allclose(r[1:], [3e-3, 1e-3, 3e-3])
+
+
+def test_group_refuses_members_that_differ(mock_task):
+    rc, st, _, _, frames, _ = group_run(mock_task, np.float64, [64, 64], [0.01, 0.02], 8, 4)
+    assert list(st) == [1, 1]  # NB_ERR_INVALID for every member
+    assert all((f == -7.0).all() for f in frames)
+    assert batch_record(mock_task)[0][0] == 0  # no batch made
+
+
+def test_group_reports_a_failing_batch_to_every_member(mock_task):
+    rc, st, _, _, frames, _ = group_run(mock_task, np.float32, [64, 3, 40], [0.01] * 3, 8, 4)
+    assert list(st) == [1, 1, 1]  # the planted nb_batch_create failure
+    assert all((f == -7.0).all() for f in frames)
+
+
+def test_group_that_does_not_fill_times_out(mock_task):
+    # a group of three with two tasks: the round ends at the timeout
+    rc, st, _, _, frames, _ = group_run(mock_task, np.float64, [64, 64], [0.01] * 2, 8, 4, members=3, timeout=0.3)
+    assert list(st) == [4, 4]  # NB_ERR_STATE
+    assert all((f == -7.0).all() for f in frames)
+    assert batch_record(mock_task)[0][0] == 0

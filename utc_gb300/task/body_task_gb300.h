@@ -26,8 +26,16 @@
 #ifndef UTC_GB300_BODY_TASK_GB300_H_
 #define UTC_GB300_BODY_TASK_GB300_H_
 
+#include <condition_variable>
+#include <mutex>
+#include <string>
+#include <vector>
+
 #include "nbody_gb300.h"
 #include "utc_standin.h"
+
+template <typename T>
+class BodyTaskGroup;
 
 template <typename T>
 class BodySystemGB300 : public UserTaskBase {
@@ -40,6 +48,7 @@ private:
     int m_algo = -1;  // -1: default for T
     int m_kick = NB_KICK_REFERENCE;
     int m_status = NB_OK;
+    BodyTaskGroup<T> *m_group = nullptr;
 
 public:
     void initImpl(unsigned int numBodies, T softeningSquared, T damping, T *pos, T *vel);
@@ -50,10 +59,68 @@ public:
     /* extensions (not in the reference): force algorithm and kick mode */
     void setAlgo(int algo) { m_algo = algo; }
     void setKick(int kick) { m_kick = kick; }
+    /* run as a member of a group (below); nullptr: run alone */
+    void setGroup(BodyTaskGroup<T> *group) { m_group = group; }
     int lastStatus() const { return m_status; }
+};
+
+/* What a task hands to its group: its system, its run's arguments and
+ * where its results go. */
+template <typename T>
+struct BodyTaskGroupMember {
+    unsigned int n;
+    T eps2, damping, dt;
+    const T *pos, *vel;
+    int loops, outInterval, algo, kick;
+    T *outbuffer;
+    double *runtime;
+    int status = NB_OK;
+    std::string error;   // the message behind a failing status
+    bool taken = false;  // a member's round has started running
+    bool done = false;   // ... and has finished
+};
+
+/* Extension (not in the reference): tasks whose runs go as one batch.  The
+ * reference's multi-task app (benchapps/nbody/utc/nbody_mtask.cc:199-231)
+ * runs one Task<BodySystemSGPU> per system, each on its own stream.  Tasks
+ * given the same group meet in runImpl; the last to arrive runs every
+ * member's system as one nb_batch (one launch pair per step for all
+ * systems, each frame's steps one CUDA graph) on its own stream, then
+ * writes every member's frames and timers, and the others return with it.
+ * Members may differ in N; they must share eps2, damping, dt, loops,
+ * outInterval, algorithm and kick mode, else every member of that round
+ * gets NB_ERR_INVALID.  A member waits at most timeout_s for the group to
+ * fill; a round that does not fill in time ends with NB_ERR_STATE for the
+ * members that came, whose outbuffers stay untouched.  memtype and
+ * blocksize do not apply (the batch copies from the caller's arrays and
+ * chooses its own launch shape).  A group serves any number of rounds of
+ * `members` runs each. */
+template <typename T>
+class BodyTaskGroup {
+public:
+    explicit BodyTaskGroup(int members, double timeout_s = 600.0)
+        : m_members(members > 0 ? members : 1), m_timeout(timeout_s)
+    {
+    }
+    int members() const { return m_members; }
+    /* called by runImpl on the member's task thread; returns its status */
+    int join(BodyTaskGroupMember<T> *m);
+
+private:
+    int runBatch(const std::vector<BodyTaskGroupMember<T> *> &ms);
+
+    const int m_members;
+    const double m_timeout;
+    std::mutex m_mu;
+    std::condition_variable m_cv;
+    std::vector<BodyTaskGroupMember<T> *> m_arrived;
+    long long m_round = 0;  // rounds finished or abandoned
+    bool m_running = false;
 };
 
 extern template class BodySystemGB300<float>;
 extern template class BodySystemGB300<double>;
+extern template class BodyTaskGroup<float>;
+extern template class BodyTaskGroup<double>;
 
 #endif
