@@ -102,3 +102,48 @@ def test_threads_many_small_contexts(cuda):
     assert not errors, errors
     for a, t in zip(alone, together):
         assert a[0].tobytes() == t[0].tobytes() and a[1].tobytes() == t[1].tobytes()
+
+
+def test_destroy_keeps_the_context_while_another_thread_captures(cuda):
+    # a thread outside the library captures a graph in global mode; the
+    # device cannot be synchronised meanwhile, so nb_destroy refuses and
+    # keeps the context, which stays usable and is destroyed afterwards
+    import torch
+
+    from utc_gb300 import _native as N
+
+    n = 1024
+    pos, vel = start("f32", n, 3)
+    s = NBodySystem(n, "f32", "sym", kick="physical", eps2=np.float32(1e-3), damping=1.0, dt=np.float32(1e-3))
+    s.set_state(pos, vel)
+    started, release = threading.Event(), threading.Event()
+    seen = []
+
+    def capture():
+        st = torch.cuda.Stream()
+        x = torch.zeros(16, device="cuda")
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(st):
+            g.capture_begin(capture_error_mode="global")
+            x.add_(1)
+            started.set()
+            release.wait(30)
+            try:
+                g.capture_end()
+            except Exception as e:  # a refused call elsewhere may void the capture
+                seen.append(repr(e))
+
+    t = threading.Thread(target=capture)
+    t.start()
+    assert started.wait(30)
+    rc = s.lib.nb_destroy(s.handle)
+    msg = s.lib.nb_last_error().decode()
+    release.set()
+    t.join(60)
+    if rc == N.NB_OK:
+        s.handle = None  # destroyed after all: nothing of it may be used below
+    assert rc == N.NB_ERR_CUDA and "captures a graph" in msg, (rc, msg)
+    s.step(2)  # kept and usable
+    s.get_state()
+    s.close()
