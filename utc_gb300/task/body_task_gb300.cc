@@ -8,6 +8,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <type_traits>
 
 #include <cuda_runtime.h>
@@ -28,6 +29,15 @@ void BodySystemGB300<T>::initImpl(unsigned int numBodies, T softeningSquared, T 
         m_vel = vel;
     }
     intra_Barrier();
+}
+
+// nb_destroy / nb_batch_destroy keep what they were given while another
+// thread of the process is capturing a graph (the device cannot be
+// synchronised then): try again for up to ten seconds for that capture to end
+template <typename F>
+static void destroy_when_possible(F destroy)
+{
+    for (int k = 0; k < 1000 && destroy() != NB_OK; ++k) std::this_thread::sleep_for(std::chrono::milliseconds(10));
 }
 
 template <typename T>
@@ -63,7 +73,7 @@ void BodySystemGB300<T>::runImpl(double *runtime, int loops, int outInterval, in
                          (void *)__streamId);
     if (st != NB_OK)
         std::fprintf(stderr, "BodySystemGB300::runImpl: status %d: %s\n", st, nb_last_error());
-    nb_destroy(ctx);
+    if (ctx) destroy_when_possible([ctx] { return nb_destroy(ctx); });
     m_status = st;
     if (runtime)
         for (int k = 0; k < 4; ++k) runtime[k] = t[k];
@@ -188,7 +198,7 @@ int BodyTaskGroup<T>::runBatch(const std::vector<BodyTaskGroupMember<T> *> &ms)
     for (auto &x : e)
         if (x) cudaEventDestroy(x);
     if (s) cudaStreamDestroy(s);
-    if (b) nb_batch_destroy(b);
+    if (b) destroy_when_possible([b] { return nb_batch_destroy(b); });
     const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     for (auto *x : ms) {
         x->status = st;
