@@ -119,6 +119,12 @@ def task_lib():
         t.nbt_randomize_f64.argtypes = [I, vp, vp, F, F, I, U]
         t.nbt_randomize_f32.restype = I
         t.nbt_randomize_f64.restype = I
+        # nsys, sizes, pos[], vel[], out[], eps2[], damping, dt, loops, outInterval, members, timeout,
+        # status[], runtime[4 nsys]
+        t.nbt_group_run_f32.argtypes = [I, vp, vp, vp, vp, vp, F, F, I, I, I, D, vp, vp]
+        t.nbt_group_run_f64.argtypes = [I, vp, vp, vp, vp, vp, D, D, I, I, I, D, vp, vp]
+        t.nbt_group_run_f32.restype = I
+        t.nbt_group_run_f64.restype = I
         _task = t
     return _task
 
