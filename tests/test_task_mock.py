@@ -165,3 +165,21 @@ def test_group_that_does_not_fill_times_out(mock_task):
     assert list(st) == [4, 4]  # NB_ERR_STATE
     assert all((f == -7.0).all() for f in frames)
     assert batch_record(mock_task)[0][0] == 0
+
+
+def test_group_refuses_a_null_outbuffer(mock_task):
+    sizes = [64, 64]
+    states = [oracle.randomize(1, n, np.float64, seed=5 + k) for k, n in enumerate(sizes)]
+    good = np.full((3, 64, 4), -7.0)
+    ptr = C.c_void_p * 2
+    st = np.full(2, -1, np.int32)
+    e = np.full(2, 0.01)
+    fn = mock_task.nbt_group_run_f64
+    fn.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                   C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p]
+    mock_task.mock_batch_reset()
+    fn(2, np.asarray(sizes, np.int32).ctypes.data, ptr(*[p.ctypes.data for p, _ in states]),
+       ptr(*[v.ctypes.data for _, v in states]), ptr(good.ctypes.data, None), e.ctypes.data, 0.999, 0.005,
+       8, 4, 2, 30.0, st.ctypes.data, None)
+    assert list(st) == [1, 1] and (good == -7.0).all()
+    assert batch_record(mock_task)[0][0] == 0

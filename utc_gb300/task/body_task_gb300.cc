@@ -131,6 +131,11 @@ int BodyTaskGroup<T>::runBatch(const std::vector<BodyTaskGroupMember<T> *> &ms)
         st = NB_ERR_INVALID;
         msg = "task group: loops must be >= 0 and outInterval > 0";
     }
+    for (auto *x : ms)
+        if (!st && x->n > 0 && (!x->pos || !x->vel || (a.loops >= a.outInterval && !x->outbuffer))) {
+            st = NB_ERR_INVALID;
+            msg = "task group: a member's pos, vel or outbuffer is NULL";
+        }
     const int nsys = (int)ms.size();
     std::vector<int> sizes(nsys);
     std::vector<size_t> off(nsys + 1, 0);
