@@ -11,6 +11,9 @@ interaction (benchapps/nbody/seq/bodysystem.h:75-95).
 
 Under torchrun each rank runs an independent replica of the workload
 (weak scaling, no data-path collective); rank 0 prints one JSON line.
+`e2e` times nb_run_host (the C-ABI call the task makes) from pinned host
+buffers; `e2e.through_task` times the drop-in UTC task itself
+(BodySystemGB300<float>: init, run, wait, from pageable arrays).
 
 Extension workloads, one JSON line each (not the headline):
   --workload precision  N=1,048,576 Plummer, 20 steps of dt=1e-4, plain FP32
