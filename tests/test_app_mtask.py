@@ -73,3 +73,18 @@ def test_mtask_grouped_tasks_equal_the_batch(cuda, tmp_path, state):
         assert "Test complete !!!" in r.stdout
         out[mode] = open(path).read()
     assert out["1"] == out["2"]
+
+
+@pytest.mark.parametrize("mode,algo,ok", [("0", "1", True), ("0", "0", True), ("2", "0", True), ("2", "1", False)])
+def test_mtask_algorithm_flag_reaches_the_tasks(cuda, tmp_path, mode, algo, ok):
+    # -a goes to every task with -B 0 and -B 2; a group runs one batch, which
+    # has no reference-exact kernel, so -B 2 -a 1 ends with that status
+    path = str(tmp_path / "out.txt")
+    r = subprocess.run([APP, "-F", "-n", "256", "-T", "3", "-l", "10", "-o", "5", "-O", path, "-B", mode, "-a", algo],
+                       capture_output=True, text=True, timeout=300)
+    if ok:
+        assert r.returncode == 0, r.stdout + r.stderr
+        frames = frames_of(path, 3, 256, 3)
+        assert np.isfinite(frames).all()
+    else:
+        assert r.returncode == 2 and "batches run NB_F32" in r.stderr, r.stdout + r.stderr

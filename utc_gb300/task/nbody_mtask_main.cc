@@ -18,7 +18,8 @@
  *   -F      float state (the reference fixes FTYPE=double)
  *   -a 0|2  batched force algorithm for float state: 0 directed, 2 symmetric
  *           (default); double-state batches run the float-float symmetric
- *           kernel
+ *           kernel.  With -B 0 and -B 2 the value goes to every task
+ *           (setAlgo; -a 1 and -a 3 also serve single tasks there)
  *   -O file write every system's frames (system 0's frames, then system
  *           1's, ...) in the app's text format; the reference parses -O
  *           and writes nothing
@@ -147,6 +148,7 @@ static int run_app(bool printTime, int paraSelect, int iteration, int outInterva
         for (int i = 0; i < ntasks; ++i) {
             auto *t = new Task<BodySystemGB300<FTYPE>>(ProcList(0), TaskType::gpu_task);
             if (mode == 2) t->userObject()->setGroup(&group);
+            if (algo >= 0) t->userObject()->setAlgo(algo);
             t->init((unsigned)numBodies, (FTYPE)activeParams.m_softening * (FTYPE)activeParams.m_softening,
                     (FTYPE)activeParams.m_damping, pos[i], vel[i]);
             tasks.push_back(t);
