@@ -156,6 +156,32 @@ int BodyTaskGroup<T>::runBatch(const std::vector<BodyTaskGroupMember<T> *> &ms)
         std::memcpy(&P[off[i]], ms[i]->pos, 4 * (size_t)ms[i]->n * sizeof(T));
         std::memcpy(&V[off[i]], ms[i]->vel, 4 * (size_t)ms[i]->n * sizeof(T));
     }
+    const bool batchable = p.algo == NB_ALGO_SYM || (p.precision == NB_F32 && p.algo == NB_ALGO_FAST);
+    if (!st && !batchable) {
+        // the reference-exact and FP64-pipe kernels have no batched form:
+        // the members' systems run one after another, each as runImpl runs
+        // it alone, each member with its own timers
+        cudaStream_t s1 = nullptr;
+        if (cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking) != cudaSuccess) {
+            st = NB_ERR_CUDA;
+            msg = "task group: cannot create the run's stream";
+        }
+        for (auto *x : ms) {
+            double t[4] = {0, 0, 0, 0};
+            nb_params q = p;
+            q.n = (int)x->n;
+            nb_ctx *ctx = nullptr;
+            int sx = st ? st : nb_create(&q, &ctx);
+            if (!sx) sx = nb_run_host(ctx, x->pos, x->vel, a.loops, a.outInterval, x->outbuffer, t, (void *)s1);
+            x->status = sx;
+            x->error = sx && !st ? nb_last_error() : msg;
+            if (ctx) destroy_when_possible([ctx] { return nb_destroy(ctx); });
+            if (x->runtime && !sx)
+                for (int k = 0; k < 4; ++k) x->runtime[k] = t[k];
+        }
+        if (s1) cudaStreamDestroy(s1);
+        return st;
+    }
     nb_batch *b = nullptr;
     cudaStream_t s = nullptr;
     cudaEvent_t e[4] = {};

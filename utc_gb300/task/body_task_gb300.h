@@ -87,6 +87,8 @@ struct BodyTaskGroupMember {
  * member's system as one nb_batch (one launch pair per step for all
  * systems, each frame's steps one CUDA graph) on its own stream, then
  * writes every member's frames and timers, and the others return with it.
+ * Algorithms without a batched kernel (NB_ALGO_EXACT, NB_ALGO_SYM_FP64) run
+ * the members' systems one after another instead, each as it runs alone.
  * Members may differ in N; they must share eps2, damping, dt, loops,
  * outInterval, algorithm and kick mode, else every member of that round
  * gets NB_ERR_INVALID.  A member waits at most timeout_s for the group to
