@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -23,8 +24,9 @@ struct Record {
     void *stream = nullptr;
     int calls = 0, n = 0, loops = 0, out_interval = 0, precision = -1, algo = -1, memtype = -1, kick = -1;
     double eps2 = 0, damping = 0, dt = 0;
-    int streams_created = 0, streams_destroyed = 0;
 } g_rec;
+// every task worker makes and frees a stream: counted from many threads
+std::atomic<int> g_streams_created{0}, g_streams_destroyed{0};
 
 struct BatchRecord {
     int creates = 0, runs = 0, nsys = 0, destroys = 0, precision = -1, algo = -1;
@@ -55,10 +57,10 @@ cudaError_t cudaSetDevice(int) { return cudaSuccess; }
 cudaError_t cudaStreamCreateWithFlags(cudaStream_t *s, unsigned int)
 {
     *s = g_fake_stream;
-    ++g_rec.streams_created;
+    ++g_streams_created;
     return cudaSuccess;
 }
-cudaError_t cudaStreamDestroy(cudaStream_t) { ++g_rec.streams_destroyed; return cudaSuccess; }
+cudaError_t cudaStreamDestroy(cudaStream_t) { ++g_streams_destroyed; return cudaSuccess; }
 
 // ---- the C ABI calls of the task ----
 void nb_params_default(nb_params *p)
@@ -238,7 +240,7 @@ void mock_record(void **stream, int *ints9, double *dbl3)
 {
     *stream = g_rec.stream;
     const int v[9] = {g_rec.calls, g_rec.n, g_rec.loops, g_rec.out_interval, g_rec.precision, g_rec.algo,
-                      g_rec.memtype, g_rec.streams_created, g_rec.streams_destroyed};
+                      g_rec.memtype, g_streams_created.load(), g_streams_destroyed.load()};
     std::memcpy(ints9, v, sizeof(v));
     dbl3[0] = g_rec.eps2;
     dbl3[1] = g_rec.damping;
