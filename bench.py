@@ -34,6 +34,9 @@ Extension workloads, one JSON line each (not the headline):
                         throughput, force error against the FP64 oracle
                         (512-body subsample), final positions against the
                         reference-exact run
+  --workload frames     N=65536, 200 steps through nb_run_host with a frame
+                        every 200, 20, 5 and 1 steps, pageable and pinned
+                        host memory: wall time against one frame
 """
 from __future__ import annotations
 
@@ -852,6 +855,47 @@ def run_batched(args):
     return 0
 
 
+def run_frames(args):
+    """Frame copy-out (body_task_sgpu.cu:116-125): nb_run_host with a frame
+    every `oi` steps, pageable and pinned host memory, against the same run
+    with one frame at the end.  Each frame is a device snapshot copied to the
+    host on a second stream while the next steps run."""
+    from utc_gb300 import _native as N
+    from utc_gb300 import ics
+    from utc_gb300.nbody import NBodySystem
+
+    n = args.n or 65536
+    loops = 200
+    p, v = ics.plummer(n, seed=0)
+    pos, vel = ics.f32(p), ics.f32(v)
+    frame_bytes = n * 16
+    out = {"workload": "frames", "n": n, "loops": loops, "algo": "sym", "eps2": 1e-4, "dt": 1e-4,
+           "data": "synthetic (seeded Plummer sphere, float32)", "runs": []}
+    for mname, mt in (("pageable", N.NB_MEM_PAGEABLE), ("pinned", N.NB_MEM_PINNED)):
+        with NBodySystem(n, "f32", "sym", kick="physical", eps2=np.float32(1e-4), damping=1.0,
+                         dt=np.float32(1e-4), memtype=mt) as s:
+            s.run_host(pos, vel, 20, 20)  # warm-up: graphs, staging, snapshots
+            base = None
+            for oi in (loops, 20, 5, 1):
+                reps = []
+                for _ in range(3):
+                    t0 = time.perf_counter()
+                    frames, t = s.run_host(pos, vel, loops, oi)
+                    reps.append(time.perf_counter() - t0)
+                wall = statistics.median(reps)
+                if oi == loops:
+                    base = wall
+                k = loops // oi
+                out["runs"].append({"memtype": mname, "out_interval": oi, "frames": k, "wall_ms": wall * 1e3,
+                                    "G_interactions_per_s": float(n) ** 2 * loops / wall / 1e9,
+                                    "frame_GB_per_s": k * frame_bytes / wall / 1e9,
+                                    "slowdown_vs_one_frame": wall / base})
+    out["note"] = ("wall clock of nb_run_host from host arrays (state in, frames out); slowdown_vs_one_frame "
+                   "near 1 means the copies hide behind the steps")
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -859,7 +903,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "precision", "adjoint", "batched", "double"])
+    ap.add_argument("--workload", default="plain",
+                    choices=["plain", "precision", "adjoint", "batched", "double", "frames"])
     ap.add_argument("--algo", default="sym", choices=["fast", "sym"],
                     help="force algorithm (plain, adjoint and batched workloads)")
     ap.add_argument("--n", type=int, default=0, help="body count override for extension workloads")
@@ -877,6 +922,8 @@ def main():
         return run_batched(args)
     if args.workload == "double":
         return run_double(args)
+    if args.workload == "frames":
+        return run_frames(args)
     return run_ours(args)
 
 
