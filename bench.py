@@ -37,6 +37,9 @@ Extension workloads, one JSON line each (not the headline):
   --workload frames     N=65536, 200 steps through nb_run_host with a frame
                         every 200, 20, 5 and 1 steps, pageable and pinned
                         host memory: wall time against one frame
+  --workload ics        initial conditions drawn on the GPU (cube, Plummer,
+                        the app's shell) at N=2^20 and 2^24: bodies/s and
+                        store bandwidth, beside the host generator
 """
 from __future__ import annotations
 
@@ -896,6 +899,45 @@ def run_frames(args):
     return 0
 
 
+def run_ics(args):
+    """Initial conditions drawn on the GPU (nb_ics_generate, randomizeBodies at
+    nbody.h:89-250 for large inputs): bodies per second and the store rate
+    against the measured HBM copy bandwidth, beside the host generator
+    (numpy, FP64) on the same sizes."""
+    import torch
+
+    from utc_gb300 import ics
+    from utc_gb300.nbody import gpu_initial_conditions
+
+    peaks = measured_peaks()
+    out = {"workload": "ics", "data": "synthetic (seeded counter-based draws)", "runs": []}
+    for n in (1 << 20, 1 << 24):
+        for kind in ("cube", "plummer", "shell"):
+            gpu_initial_conditions(kind, n, seed=1)  # warm-up, allocator
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = 5
+            e0.record()
+            for r in range(reps):
+                gpu_initial_conditions(kind, n, seed=2 + r)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            stored = 32.0 * n  # pos and vel, float4 each
+            run = {"kind": kind, "n": n, "ms": ms, "G_bodies_per_s": n / ms / 1e6,
+                   "store_GB_per_s": stored / ms / 1e6,
+                   "hbm_frac": (stored / ms / 1e6) / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None}
+            if n == 1 << 20 and kind in ("cube", "plummer"):
+                t0 = time.perf_counter()
+                (ics.uniform_cube if kind == "cube" else ics.plummer)(n, seed=2)
+                run["host_numpy_ms"] = (time.perf_counter() - t0) * 1e3
+            out["runs"].append(run)
+    out["note"] = ("ms per call by CUDA events over 5 calls (each call also allocates its outputs from "
+                   "torch's cache); plummer and shell add an FP64 recentering reduction")
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -904,7 +946,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="plain",
-                    choices=["plain", "precision", "adjoint", "batched", "double", "frames"])
+                    choices=["plain", "precision", "adjoint", "batched", "double", "frames", "ics"])
     ap.add_argument("--algo", default="sym", choices=["fast", "sym"],
                     help="force algorithm (plain, adjoint and batched workloads)")
     ap.add_argument("--n", type=int, default=0, help="body count override for extension workloads")
@@ -924,6 +966,8 @@ def main():
         return run_double(args)
     if args.workload == "frames":
         return run_frames(args)
+    if args.workload == "ics":
+        return run_ics(args)
     return run_ours(args)
 
 
