@@ -132,13 +132,16 @@ __global__ void ics_kernel(int kind, int n, unsigned long long seed, double a, d
         return;
     }
     // Plummer sphere
+    // x1^(-2/3) as rcbrt(x1)^2, (1 - q^2)^3.5 as t^3 sqrt(t) and
+    // (r^2 + a^2)^(-1/4) as rsqrt(sqrt(.)): the same quantities without pow,
+    // whose FP64 log/exp dominated the sampler on a part with a slow FP64 pipe
     const double x1 = fmax(0.999 * u01(seed, id, 0), 1e-300);
-    const double r = a / sqrt(pow(x1, -2.0 / 3.0) - 1.0);
+    const double c1 = rcbrt(x1);
+    const double r = a / sqrt(c1 * c1 - 1.0);
     double ct = 2.0 * u01(seed, id, 1) - 1.0;
     double st = sqrt(fmax(0.0, 1.0 - ct * ct));
-    double ph = 6.283185307179586 * u01(seed, id, 2);
     double sp, cp;
-    sincos(ph, &sp, &cp);
+    sincospi(2.0 * u01(seed, id, 2), &sp, &cp);
     pos[i] = mk4<V4>(r * st * cp, r * st * sp, r * ct, M / n);
     // speed fraction q by rejection from g(q) = q^2 (1 - q^2)^3.5 (max < 0.1);
     // each try is accepted with probability 7 pi / 512 / 0.1 = 0.43, so all 64
@@ -148,23 +151,25 @@ __global__ void ics_kernel(int kind, int n, unsigned long long seed, double a, d
     for (unsigned t = 0; t < 64; ++t) {
         const double qq = u01(seed, id, 8 + 2 * t);
         const double yy = 0.1 * u01(seed, id, 9 + 2 * t);
-        if (yy < qq * qq * pow(1.0 - qq * qq, 3.5)) {
+        const double t1 = 1.0 - qq * qq;
+        if (yy < qq * qq * (t1 * t1 * t1 * sqrt(t1))) {
             q = qq;
             break;
         }
     }
-    const double vesc = sqrt(2.0 * G * M) * pow(r * r + a * a, -0.25);
+    const double vesc = sqrt(2.0 * G * M) * rsqrt(sqrt(r * r + a * a));
     ct = 2.0 * u01(seed, id, 3) - 1.0;
     st = sqrt(fmax(0.0, 1.0 - ct * ct));
-    ph = 6.283185307179586 * u01(seed, id, 4);
-    sincos(ph, &sp, &cp);
+    sincospi(2.0 * u01(seed, id, 4), &sp, &cp);
     const double v = q * vesc;
     vel[i] = mk4<V4>(v * st * cp, v * st * sp, v * ct, 1.0);
 }
 
 // centre of mass / velocity (mass-weighted) in FP64: block partials, then
-// one block sums them in order
+// one block of 7 x 128 threads sums them in a fixed order (thread (q, j)
+// takes partials j, j + 128, ...; then a tree over j)
 constexpr int kIcsBlock = 256;
+constexpr int kIcsFinal = 128;
 
 template <typename V4>
 __global__ void ics_moments_kernel(int n, const V4 *__restrict__ pos, const V4 *__restrict__ vel,
@@ -193,12 +198,21 @@ __global__ void ics_moments_kernel(int n, const V4 *__restrict__ pos, const V4 *
     if (threadIdx.x < 7) part[(size_t)blockIdx.x * 7 + threadIdx.x] = red[threadIdx.x][0];
 }
 
-__global__ void ics_moments_final(const double *__restrict__ part, int nblocks, double *__restrict__ out)
+__global__ void __launch_bounds__(7 * kIcsFinal)
+    ics_moments_final(const double *__restrict__ part, int nblocks, double *__restrict__ out)
 {
-    if (threadIdx.x >= 7) return;
+    __shared__ double red[7][kIcsFinal];
+    const int q = threadIdx.x / kIcsFinal, j = threadIdx.x % kIcsFinal;
     double s = 0;
-    for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * 7 + threadIdx.x];
-    out[threadIdx.x] = s;
+#pragma unroll 8
+    for (int b = j; b < nblocks; b += kIcsFinal) s += part[(size_t)b * 7 + q];
+    red[q][j] = s;
+    __syncthreads();
+    for (int w = kIcsFinal / 2; w > 0; w >>= 1) {
+        if (j < w) red[q][j] += red[q][j + w];
+        __syncthreads();
+    }
+    if (j == 0) out[q] = red[q][0];
 }
 
 template <typename V4>
@@ -226,7 +240,7 @@ static int ics_launch(int kind, int n, unsigned long long seed, double a, double
     if (kind == 1) {
         ics_moments_kernel<V4><<<blocks, kIcsBlock, 0, s>>>(n, pos, vel, scratch + 8);
         NB_LAUNCH_CHECK("ics_moments_kernel launch");
-        ics_moments_final<<<1, 32, 0, s>>>(scratch + 8, blocks, scratch);
+        ics_moments_final<<<1, 7 * kIcsFinal, 0, s>>>(scratch + 8, blocks, scratch);
         NB_LAUNCH_CHECK("ics_moments_final launch");
         ics_recenter_kernel<V4><<<blocks, kIcsBlock, 0, s>>>(n, pos, vel, scratch);
         NB_LAUNCH_CHECK("ics_recenter_kernel launch");
