@@ -103,10 +103,11 @@ __global__ void ics_kernel(int kind, int n, unsigned long long seed, double a, d
     if (kind == 3) {  // reference shell
         double x, y, z, len;
         ball_point(seed, id, 8, x, y, z, len);
-        if (len > 1e-6) {
-            x /= len;
-            y /= len;
-            z /= len;
+        if (len > 1e-6) {  // one FP64 division instead of three
+            const double il = 1.0 / len;
+            x *= il;
+            y *= il;
+            z *= il;
         }
         const double inner = 2.5 * a, outer = 4.0 * a;
         const double px = x * (inner + (outer - inner) * u01(seed, id, 128));
@@ -114,10 +115,10 @@ __global__ void ics_kernel(int kind, int n, unsigned long long seed, double a, d
         const double pz = z * (inner + (outer - inner) * u01(seed, id, 130));
         double ax = 0.0, ay = 0.0, az = 1.0;
         if (1.0 - z < 1e-6) {
-            const double l = sqrt(y * y + x * x + 1.0);
-            ax = y / l;
-            ay = x / l;
-            az = 1.0 / l;
+            const double il = rsqrt(y * y + x * x + 1.0);
+            ax = y * il;
+            ay = x * il;
+            az = il;
         }
         const double vs = a * vmax;
         pos[i] = mk4<V4>(px, py, pz, 1.0);
