@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define NB_ABI_VERSION 1
+#define NB_ABI_VERSION 2
 
 /* Largest system (and batch) size: indices stay within 32-bit arithmetic. */
 #define NB_MAX_BODIES (1 << 30)
@@ -190,10 +190,18 @@ int nb_energy(nb_ctx *ctx, double *out5, void *accphi_dev, void *stream);
  * recomputing each segment's trajectory from its checkpoint.  The recompute
  * of the next segment runs on a stream of the context's own, ordered against
  * `stream` by events: the results are complete once `stream` has reached the
- * end of the call.  NB_F32 fast or symmetric contexts; both kick modes. */
-int nb_adj_forward(nb_ctx *ctx, int steps, int ckpt_every, void *stream);
-int nb_adj_backward(nb_ctx *ctx, const void *gx_T, const void *gv_T, void *gx0, void *gv0,
-                    void *gm, void *stream);
+ * end of the call.  NB_F32 fast or symmetric contexts; both kick modes.
+ * Each nb_adj_forward gets a new generation number (from 1, increasing per
+ * context), written to *generation (may be NULL).  nb_adj_backward takes the
+ * generation of the forward pass whose gradients it is asked for and returns
+ * NB_ERR_STATE when the context no longer holds that pass (a later
+ * nb_adj_forward replaced it, or nb_set_params / nb_autotune dropped it), so
+ * a caller that records several trajectories on one context gets an error
+ * instead of another trajectory's gradients. */
+int nb_adj_forward(nb_ctx *ctx, int steps, int ckpt_every, void *stream,
+                   unsigned long long *generation);
+int nb_adj_backward(nb_ctx *ctx, unsigned long long generation, const void *gx_T, const void *gv_T,
+                    void *gx0, void *gv0, void *gm, void *stream);
 
 /* The whole task run with host buffers, as BodySystemSGPU::runImpl
  * (body_task_sgpu.cu:40-137): copy pos/vel in, run `loops` steps, and after
@@ -270,9 +278,10 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks);
  * nb_adj_backward over the concatenated bodies of all systems (no
  * counterpart in the reference). */
 int nb_batch_set_params(nb_batch *b, double eps2, double damping, double dt, double G);
-int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream);
-int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void *gx0, void *gv0,
-                          void *gm, void *stream);
+int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream,
+                         unsigned long long *generation);
+int nb_batch_adj_backward(nb_batch *b, unsigned long long generation, const void *gx_T,
+                          const void *gv_T, void *gx0, void *gv0, void *gm, void *stream);
 
 /* Seeded initial conditions generated on the GPU, one thread per body
  * (counter-based: a body's draw depends only on (seed, index)).  kind 0:

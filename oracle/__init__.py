@@ -21,8 +21,6 @@ import threading
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SEQ_DEFAULT = "/root/reference/utc-0.1/benchapps/nbody/seq"
-REF_CUDA_DEFAULT = "/root/reference/utc-0.1/benchapps/nbody/cuda"
 REF_CUBIN = os.path.join(HERE, "_ref", "ref_kernel_sm103a.cubin")
 
 KICK_REFERENCE = 0
@@ -37,16 +35,24 @@ _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 
 
+def ref_root() -> str | None:
+    """The reference checkout's utc-0.1 directory, from $NB_REF_ROOT (None
+    when unset or absent: the reference builds are then skipped)."""
+    root = os.environ.get("NB_REF_ROOT")
+    return root if root and os.path.isdir(root) else None
+
+
 def build(ref: bool | None = None) -> None:
-    """Compile liboracle.so, and _ref/libnbref.so when the reference is present."""
+    """Compile liboracle.so, and the reference's own code into _ref/ when
+    $NB_REF_ROOT names the reference checkout."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    root = ref_root()
     if ref is None:
-        ref = os.path.isdir(os.environ.get("NB_REF_SEQ", REF_SEQ_DEFAULT))
+        ref = root is not None
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", "ref-gpu",
-                        "REF_SEQ=" + os.environ.get("NB_REF_SEQ", REF_SEQ_DEFAULT),
-                        "REF_CUDA=" + os.environ.get("NB_REF_CUDA", REF_CUDA_DEFAULT)],
-                       check=True)
+        if root is None:
+            raise RuntimeError("oracle.build(ref=True) needs NB_REF_ROOT (the reference's utc-0.1 directory)")
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "ref-gpu", "NB_REF_ROOT=" + root], check=True)
 
 
 def _declare(lib):

@@ -1,9 +1,9 @@
 """Generate the committed golden fixtures (tests/golden/*.json).
 
-Run in a checkout that has the reference tree (its path in REF_ROOT below or
-$NB_REF_ROOT) and a built oracle/_ref/libnbref.so (``make -C oracle ref``):
+Run with $NB_REF_ROOT naming the reference checkout's utc-0.1 directory and
+a built oracle/_ref/libnbref.so (``make -C oracle ref NB_REF_ROOT=...``):
 
-    python tests/golden/make_golden.py
+    NB_REF_ROOT=<reference>/utc-0.1 python tests/golden/make_golden.py
 
 What it records, all as SHA-256 digests plus summary numbers (no reference
 data is copied):
@@ -34,7 +34,7 @@ sys.path.insert(0, REPO)
 
 import oracle  # noqa: E402
 
-REF_ROOT = os.environ.get("NB_REF_ROOT", "/root/reference/utc-0.1")
+REF_ROOT = os.environ.get("NB_REF_ROOT", "")
 
 # (config, n, steps, dtype, para_select) of the pinned reference runs
 REF_RUN_CASES = [
@@ -127,6 +127,8 @@ def ref_runs():
 
 
 def main():
+    if not REF_ROOT or not os.path.isdir(REF_ROOT):
+        sys.exit("set NB_REF_ROOT to the reference checkout's utc-0.1 directory")
     oracle.build(ref=True)
     with open(os.path.join(HERE, "kat_shell_n1024.json"), "w") as f:
         json.dump(kat(), f, indent=1)

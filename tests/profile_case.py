@@ -1,6 +1,6 @@
 """Fixed small runs of the kernels for profilers.
 
-    python -m utc_gb300.profile_case --n 65536 --steps 4 [--algo fast|sym|exact]
+    python tests/profile_case.py --n 65536 --steps 4 [--algo fast|sym|exact]
         [--precision f32|f32comp|f64] [--case step|adjoint|batch]
         [--block B --bpt K] [--kick physical|reference] [--systems S]
 
@@ -12,11 +12,17 @@ case adjoint: a checkpointed forward of `steps` steps (one segment) and the
 case batch:   `steps` batched steps of `systems` Plummer systems with sizes
               log-uniform in [128, n] (float state, or double with
               --precision f64).
-Prints the launch plan; used as the command under ncu.
+Prints the launch plan; used as the command under ncu (the commands in
+profiles/*.md).  Kept with the tests: it is a measurement harness, not part
+of the package.
 """
 import argparse
+import os
+import sys
 
 import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 
 
 def main():
@@ -33,8 +39,8 @@ def main():
     a = ap.parse_args()
     import torch
 
-    from . import ics
-    from .nbody import NBodyBatch, NBodySystem
+    from utc_gb300 import ics
+    from utc_gb300.nbody import NBodyBatch, NBodySystem
 
     if a.case == "batch":
         sizes = ics.batch_sizes(a.systems, lo=128, hi=a.n, seed=0)

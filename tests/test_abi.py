@@ -25,7 +25,7 @@ def test_library_exports_every_header_symbol(built):
     lib = N.lib()
     for s in syms:
         assert hasattr(lib, s)
-    assert lib.nb_abi_version() == 1
+    assert lib.nb_abi_version() == 2
 
 
 def test_task_library_exports(built):

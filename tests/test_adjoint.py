@@ -137,3 +137,79 @@ def test_second_backward_recomputes_every_segment(cuda, algo, kick):
         b = [t.cpu().numpy() for t in s.adj_backward(gx, gv)]
     for x, y in zip(a, b):
         assert x.tobytes() == y.tobytes()
+
+
+def test_stale_forward_pass_is_refused(cuda):
+    """Two trajectories recorded on one system before the first backward: the
+    first graph's backward raises (NB_ERR_STATE) instead of returning the
+    second trajectory's gradients; the second graph's backward still gives
+    the gradients of its own trajectory.  The same check through the C ABI
+    with explicit generation numbers."""
+    import torch
+
+    from utc_gb300 import _native as N
+    from utc_gb300.autograd import trajectory
+
+    n, steps, every = 128, 8, 4
+    p64, v64 = ics.uniform_cube(n, seed=30)
+    p32, v32 = ics.f32(p64), ics.f32(v64)
+    y = torch.tensor(ics.gaussian_targets(n, seed=31), dtype=torch.float32, device="cuda")
+    kw = dict(kick="physical", eps2=np.float32(1e-2), damping=1.0, dt=np.float32(1e-3))
+
+    def leaves(scale):
+        return (torch.tensor(p32[:, :3] * scale, device="cuda", requires_grad=True),
+                torch.tensor(v32[:, :3], device="cuda", requires_grad=True),
+                torch.tensor(p32[:, 3], device="cuda", requires_grad=True))
+
+    with NBodySystem(n, "f32", "sym", **kw) as s:
+        a = leaves(1.0)
+        b = leaves(0.5)
+        xa, _ = trajectory(*a, s, steps, every)
+        xb, _ = trajectory(*b, s, steps, every)
+        with pytest.raises(RuntimeError, match="no longer holds"):
+            ((xa - y) ** 2).sum().backward()
+        ((xb - y) ** 2).sum().backward()
+        got = b[0].grad.cpu().numpy()
+    with NBodySystem(n, "f32", "sym", **kw) as s2:
+        c = leaves(0.5)
+        xc, _ = trajectory(*c, s2, steps, every)
+        ((xc - y) ** 2).sum().backward()
+    assert np.array_equal(got, c[0].grad.cpu().numpy())
+
+    with NBodySystem(n, "f32", "fast", **kw) as s:
+        s.set_state(p32, v32)
+        g1 = s.adj_forward(steps, every)
+        g2 = s.adj_forward(steps, every)
+        assert g2 == g1 + 1
+        gx = torch.randn((n, 4), device="cuda")
+        z = [torch.zeros((n, 4), device="cuda"), torch.zeros((n, 4), device="cuda"),
+             torch.zeros((n,), device="cuda")]
+        import ctypes as C
+        rc = s.lib.nb_adj_backward(s.handle, C.c_ulonglong(g1), C.c_void_p(gx.data_ptr()), None,
+                                   *[C.c_void_p(t.data_ptr()) for t in z], None)
+        assert rc == N.NB_ERR_STATE
+        s.set_params(np.float32(2e-2), 1.0, np.float32(1e-3))
+        with pytest.raises(RuntimeError):
+            s.adj_backward(gx, generation=g2)  # nb_set_params dropped the pass
+
+
+def test_batch_stale_forward_pass_is_refused(cuda):
+    import torch
+
+    from utc_gb300.nbody import NBodyBatch
+
+    sizes = np.array([64, 100, 37], dtype=np.int32)
+    ps, vs = zip(*[ics.uniform_cube(int(k), seed=40 + i) for i, k in enumerate(sizes)])
+    pos, vel = ics.f32(np.concatenate(ps)), ics.f32(np.concatenate(vs))
+    with NBodyBatch(sizes, kick="physical", eps2=np.float32(1e-2), dt=np.float32(1e-3)) as b:
+        b.set_state(pos, vel)
+        g1 = b.adj_forward(6, 3)
+        gx = torch.randn((b.nbody, 4), device="cuda")
+        first = [t.cpu().numpy() for t in b.adj_backward(gx, generation=g1)]
+        b.set_state(pos, vel)
+        g2 = b.adj_forward(6, 3)
+        with pytest.raises(RuntimeError, match="no longer holds"):
+            b.adj_backward(gx, generation=g1)
+        again = [t.cpu().numpy() for t in b.adj_backward(gx, generation=g2)]
+    for x, y in zip(first, again):
+        assert x.tobytes() == y.tobytes()

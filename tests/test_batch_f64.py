@@ -138,6 +138,6 @@ def test_f64_batched_matches_per_system_and_autotune(cuda, tmp_path):
 def test_f64_batch_refuses_adjoint_and_exact(cuda):
     with NBodyBatch([10, 20], precision="f64") as b:
         b.set_state(*make_batch([10, 20]))
-        assert b.lib.nb_batch_adj_forward(b.handle, 4, 2, None) == N.NB_ERR_UNSUPPORTED
+        assert b.lib.nb_batch_adj_forward(b.handle, 4, 2, None, None) == N.NB_ERR_UNSUPPORTED
     with pytest.raises(RuntimeError):
         NBodyBatch([10, 20], precision="f64", algo="exact")

@@ -80,7 +80,7 @@ def test_adjoint_needs_a_float_fast_context(cuda, prec, algo):
     p, v = ics.plummer(32, seed=2)
     with NBodySystem(32, prec, algo) as s:
         s.set_state(p.astype(dt_), v.astype(dt_))
-        assert s.lib.nb_adj_forward(s.handle, 4, 2, None) == N.NB_ERR_UNSUPPORTED
+        assert s.lib.nb_adj_forward(s.handle, 4, 2, None, None) == N.NB_ERR_UNSUPPORTED
 
 
 def test_batch_argument_checks(cuda):

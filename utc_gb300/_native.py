@@ -56,8 +56,8 @@ def _declare(lib):
         "nb_accel": (I, [vp, vp, vp]),
         "nb_step_timed": (I, [vp, I, P(C.c_float), P(C.c_float), vp]),
         "nb_energy": (I, [vp, P(D), vp, vp]),
-        "nb_adj_forward": (I, [vp, I, I, vp]),
-        "nb_adj_backward": (I, [vp, vp, vp, vp, vp, vp, vp]),
+        "nb_adj_forward": (I, [vp, I, I, vp, P(C.c_ulonglong)]),
+        "nb_adj_backward": (I, [vp, C.c_ulonglong, vp, vp, vp, vp, vp, vp]),
         "nb_autotune": (I, [vp, I, C.c_char_p, vp, P(I)]),
         "nb_step_f32_noalloc": (I, [vp, vp, vp, I, C.c_float, C.c_float, C.c_float, I, C.c_float, vp]),
         "nb_run_host": (I, [vp, vp, vp, I, I, vp, P(D), vp]),
@@ -77,9 +77,9 @@ def _declare(lib):
         "nb_batch_plan_info": (I, [vp, P(C.c_longlong)]),
         "nb_batch_launches_per_step": (I, [vp]),
         "nb_batch_step_per_system": (I, [vp, I, vp]),
-        "nb_batch_adj_forward": (I, [vp, I, I, vp]),
+        "nb_batch_adj_forward": (I, [vp, I, I, vp, P(C.c_ulonglong)]),
         "nb_batch_step_tasks": (I, [vp, I, I]),
-        "nb_batch_adj_backward": (I, [vp, vp, vp, vp, vp, vp, vp]),
+        "nb_batch_adj_backward": (I, [vp, C.c_ulonglong, vp, vp, vp, vp, vp, vp]),
         "nb_ics_generate": (I, [I, I, C.c_ulonglong, D, D, D, D, I, vp, vp, vp, vp]),
         "nb_ics_scratch_bytes": (C.c_size_t, [I]),
         "nb_last_error": (C.c_char_p, []),

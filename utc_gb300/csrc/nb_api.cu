@@ -116,6 +116,9 @@ struct nb_ctx {
         nb::SymPlan splan;
         float4 *sym_t = nullptr, *sym_s = nullptr;
         bool ready = false;
+        // number of the recorded forward pass (nb_adj_forward counts from 1);
+        // nb_adj_backward refuses any other
+        unsigned long long generation = 0;
         // the forward pass left the last segment's states in seg_pos/seg_acc
         bool live_last = false;
         // second segment buffer: segment s-1 is recomputed on rstream while
@@ -803,8 +806,9 @@ static int adj_reserve(nb_ctx *c, int nckpt, int every)
     return NB_OK;
 }
 
-int nb_adj_forward(nb_ctx *c, int steps, int ckpt_every, void *stream)
+int nb_adj_forward(nb_ctx *c, int steps, int ckpt_every, void *stream, unsigned long long *generation)
 {
+    if (generation) *generation = 0;
     if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
     if (!uses_fast(c)) return set_error(NB_ERR_UNSUPPORTED, "the adjoint needs an NB_F32 fast context");
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
@@ -859,14 +863,19 @@ int nb_adj_forward(nb_ctx *c, int steps, int ckpt_every, void *stream)
     A.nckpt = nckpt;
     A.ready = true;
     A.live_last = n > 0;
+    A.generation += 1;
+    if (generation) *generation = A.generation;
     return NB_OK;
 }
 
-int nb_adj_backward(nb_ctx *c, const void *gx_T, const void *gv_T, void *gx0, void *gv0, void *gm,
-                    void *stream)
+int nb_adj_backward(nb_ctx *c, unsigned long long generation, const void *gx_T, const void *gv_T,
+                    void *gx0, void *gv0, void *gm, void *stream)
 {
     if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
     if (!c->adj.ready) return set_error(NB_ERR_STATE, "nb_adj_backward needs a preceding nb_adj_forward");
+    if (generation != c->adj.generation)
+        return set_error(NB_ERR_STATE, "nb_adj_backward: the context no longer holds that forward pass "
+                                       "(a later nb_adj_forward replaced it)");
     if (c->p.n == 0) return NB_OK;
     if (!gx_T || !gx0 || !gv0 || !gm) return set_error(NB_ERR_INVALID, "NULL gradient buffer");
     auto &A = c->adj;

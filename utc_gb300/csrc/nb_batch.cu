@@ -977,6 +977,7 @@ struct nb_batch {
     bool adj_live_last = false;       // last segment's states left by the forward
     int adj_steps = 0, adj_every = 0, adj_nckpt = 0, cap_ckpt = 0, cap_seg = 0;
     bool adj_ready = false;
+    unsigned long long adj_generation = 0;  // number of the recorded forward pass
     float4 *ckpt_pos = nullptr, *ckpt_vel = nullptr, *seg_pos = nullptr, *seg_acc = nullptr;
     // second segment buffer and stream: segment s-1 is recomputed on rstream
     // while the reverse pass runs through segment s
@@ -1819,8 +1820,10 @@ int nb_batch_launches_per_step(nb_batch *b)
 // checkpoint every ckpt_every steps, then the reverse pass for all systems
 // at once (same contract as nb_adj_forward / nb_adj_backward, over the
 // concatenated bodies).
-int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream)
+int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream,
+                         unsigned long long *generation)
 {
+    if (generation) *generation = 0;
     if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
     if (b->f64) return set_error(NB_ERR_UNSUPPORTED, "the batched adjoint runs NB_F32 batches");
     if (!b->has_state) return set_error(NB_ERR_STATE, "no state loaded");
@@ -1885,15 +1888,20 @@ int nb_batch_adj_forward(nb_batch *b, int steps, int ckpt_every, void *stream)
     b->adj_nckpt = nckpt;
     b->adj_ready = true;
     b->adj_live_last = n > 0;
+    b->adj_generation += 1;
+    if (generation) *generation = b->adj_generation;
     return NB_OK;
 }
 
-int nb_batch_adj_backward(nb_batch *b, const void *gx_T, const void *gv_T, void *gx0, void *gv0,
-                          void *gm, void *stream)
+int nb_batch_adj_backward(nb_batch *b, unsigned long long generation, const void *gx_T,
+                          const void *gv_T, void *gx0, void *gv0, void *gm, void *stream)
 {
     if (!b) return set_error(NB_ERR_INVALID, "batch is NULL");
     if (b->f64) return set_error(NB_ERR_UNSUPPORTED, "the batched adjoint runs NB_F32 batches");
     if (!b->adj_ready) return set_error(NB_ERR_STATE, "nb_batch_adj_backward needs a preceding nb_batch_adj_forward");
+    if (generation != b->adj_generation)
+        return set_error(NB_ERR_STATE, "nb_batch_adj_backward: the batch no longer holds that forward pass "
+                                       "(a later nb_batch_adj_forward replaced it)");
     if (b->nbody == 0) return NB_OK;
     if (!gx_T || !gx0 || !gv0 || !gm) return set_error(NB_ERR_INVALID, "NULL gradient buffer");
     const size_t n = (size_t)b->nbody;

@@ -183,14 +183,21 @@ class NBodySystem:
         return e
 
     def adj_forward(self, steps, ckpt_every, stream=None):
-        """Advance `steps` steps keeping a checkpoint every `ckpt_every` steps."""
+        """Advance `steps` steps keeping a checkpoint every `ckpt_every` steps.
+        Returns the generation number of this recorded forward pass (also kept
+        as self.adj_generation, the default of adj_backward)."""
         s = current_stream_handle() if stream is None else stream
-        N.check(self.lib.nb_adj_forward(self.handle, int(steps), int(ckpt_every), C.c_void_p(s)),
-                "nb_adj_forward")
+        gen = C.c_ulonglong(0)
+        N.check(self.lib.nb_adj_forward(self.handle, int(steps), int(ckpt_every), C.c_void_p(s),
+                                        C.byref(gen)), "nb_adj_forward")
+        self.adj_generation = int(gen.value)
+        return self.adj_generation
 
-    def adj_backward(self, gx_T, gv_T=None, stream=None):
+    def adj_backward(self, gx_T, gv_T=None, stream=None, generation=None):
         """Cotangents of the final (n,4) positions / velocities (torch CUDA
-        float32; gv_T may be None) -> (dL/dx0 (n,4), dL/dv0 (n,4), dL/dm (n,))."""
+        float32; gv_T may be None) -> (dL/dx0 (n,4), dL/dv0 (n,4), dL/dm (n,)).
+        `generation` names the forward pass (default: the last adj_forward
+        of this object); a pass the context no longer holds raises."""
         torch = _torch()
         gx0 = torch.zeros((self.n, 4), dtype=torch.float32, device="cuda")
         gv0 = torch.zeros((self.n, 4), dtype=torch.float32, device="cuda")
@@ -199,7 +206,8 @@ class NBodySystem:
         gx = _device_buffer(gx_T, (self.n, 4), torch.float32, "gx_T")
         gv = _device_buffer(gv_T, (self.n, 4), torch.float32, "gv_T") if gv_T is not None else None
         gv_ptr = C.c_void_p(gv.data_ptr()) if gv is not None else C.c_void_p(0)
-        N.check(self.lib.nb_adj_backward(self.handle, C.c_void_p(gx.data_ptr()), gv_ptr,
+        gen = getattr(self, "adj_generation", 0) if generation is None else int(generation)
+        N.check(self.lib.nb_adj_backward(self.handle, C.c_ulonglong(gen), C.c_void_p(gx.data_ptr()), gv_ptr,
                                          C.c_void_p(gx0.data_ptr()), C.c_void_p(gv0.data_ptr()),
                                          C.c_void_p(gm.data_ptr()), C.c_void_p(s)),
                 "nb_adj_backward")
@@ -359,12 +367,17 @@ class NBodyBatch:
         return int(out[0]), int(out[1])
 
     def adj_forward(self, steps, ckpt_every, stream=None):
+        """As NBodySystem.adj_forward, for all systems; returns the generation."""
         s = current_stream_handle() if stream is None else stream
-        N.check(self.lib.nb_batch_adj_forward(self.handle, int(steps), int(ckpt_every), C.c_void_p(s)),
-                "nb_batch_adj_forward")
+        gen = C.c_ulonglong(0)
+        N.check(self.lib.nb_batch_adj_forward(self.handle, int(steps), int(ckpt_every), C.c_void_p(s),
+                                              C.byref(gen)), "nb_batch_adj_forward")
+        self.adj_generation = int(gen.value)
+        return self.adj_generation
 
-    def adj_backward(self, gx_T, gv_T=None, stream=None):
-        """Cotangents (nbody, 4) torch CUDA float32 -> (dL/dx0, dL/dv0, dL/dm)."""
+    def adj_backward(self, gx_T, gv_T=None, stream=None, generation=None):
+        """Cotangents (nbody, 4) torch CUDA float32 -> (dL/dx0, dL/dv0, dL/dm);
+        `generation` as in NBodySystem.adj_backward."""
         torch = _torch()
         gx0 = torch.zeros((self.nbody, 4), dtype=torch.float32, device="cuda")
         gv0 = torch.zeros((self.nbody, 4), dtype=torch.float32, device="cuda")
@@ -372,8 +385,9 @@ class NBodyBatch:
         s = current_stream_handle() if stream is None else stream
         gx = _device_buffer(gx_T, (self.nbody, 4), torch.float32, "gx_T")
         gv = _device_buffer(gv_T, (self.nbody, 4), torch.float32, "gv_T") if gv_T is not None else None
+        gen = getattr(self, "adj_generation", 0) if generation is None else int(generation)
         N.check(self.lib.nb_batch_adj_backward(
-            self.handle, C.c_void_p(gx.data_ptr()),
+            self.handle, C.c_ulonglong(gen), C.c_void_p(gx.data_ptr()),
             C.c_void_p(gv.data_ptr() if gv is not None else 0),
             C.c_void_p(gx0.data_ptr()), C.c_void_p(gv0.data_ptr()), C.c_void_p(gm.data_ptr()),
             C.c_void_p(s)), "nb_batch_adj_backward")
