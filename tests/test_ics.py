@@ -1,15 +1,75 @@
-"""Initial conditions drawn on the GPU (nb_ics_generate): deterministic per
-seed, and distributed as specified (checked against the analytic Plummer
-mass profile and the virial ratio, and the cube's ranges)."""
+"""Initial conditions drawn on the GPU (nb_ics_generate): equal to the host
+restatement of the generator (oracle/ics.py) -- bit for bit for the cube,
+random and expand configurations, within a few units in the last place for
+the shell and the Plummer sphere, whose arithmetic the compiler may fuse or
+whose cbrt/rsqrt/sincospi differ from numpy's -- deterministic per seed, and
+distributed as specified (the analytic Plummer mass profile and the virial
+ratio, the cube's ranges).  The restatement's SplitMix64 is pinned by the
+published known-answer sequence."""
 import numpy as np
 import pytest
 
 import oracle
+from oracle import ics as ics_oracle
 from utc_gb300.nbody import NBodySystem, gpu_initial_conditions
 
-pytestmark = pytest.mark.gpu
+gpu = pytest.mark.gpu
 
 
+def test_splitmix64_known_answers():
+    """SplitMix64 from state 1234567: the first five outputs of the published
+    reference sequence (each output mixes the state after one increment)."""
+    want = [6457827717110365317, 3203168211198807973, 9817491932198370423,
+            4593380528125082431, 16408922859458223821]
+    state = 1234567
+    got = []
+    for _ in range(5):
+        got.append(int(ics_oracle.splitmix64(np.uint64(state))))
+        state = (state + 0x9E3779B97F4A7C15) % (1 << 64)
+    assert got == want
+
+
+def test_restatement_streams_are_per_body():
+    """A body's draws depend only on (seed, index, stream): the restated
+    cube of 1000 bodies is the head of the one of 3000 (masses aside)."""
+    a, _ = ics_oracle.generate("cube", 1000, seed=5, precision="f64")
+    b, _ = ics_oracle.generate("cube", 3000, seed=5, precision="f64")
+    assert np.array_equal(a[:, :3], b[:1000, :3])
+    u = ics_oracle.u01(9, np.arange(100000, dtype=np.uint64), 3)
+    assert 0.0 <= u.min() and u.max() < 1.0 and abs(u.mean() - 0.5) < 0.01
+
+
+def _ulps_close(got, want, rel):
+    """Per body: |got - want| <= rel * (|want| + median |want|), all four
+    components."""
+    got = np.asarray(got, np.float64)
+    want = np.asarray(want, np.float64)
+    scale = np.abs(want) + np.median(np.abs(want))
+    return float((np.abs(got - want) / scale).max()) <= rel
+
+
+@gpu
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+@pytest.mark.parametrize("kind", ["cube", "random", "expand", "shell", "plummer"])
+@pytest.mark.parametrize("n,seed", [(100003, 7), (4099, (1 << 63) + 5)])
+def test_gpu_generator_matches_restatement(cuda, kind, precision, n, seed):
+    a, vmax = (1.0, 0.01) if kind in ("cube", "plummer") else (1.54, 8.0)
+    gp, gv = [t.cpu().numpy() for t in gpu_initial_conditions(kind, n, seed=seed, a=a, vmax=vmax,
+                                                               precision=precision)]
+    wp, wv = ics_oracle.generate(kind, n, seed, a=a, vmax=vmax, precision=precision)
+    if kind in ("cube", "random", "expand"):
+        assert gp.tobytes() == wp.tobytes() and gv.tobytes() == wv.tobytes()
+        return
+    # shell: fused multiply-adds in the radius and velocity; Plummer: CUDA's
+    # rcbrt / rsqrt / sincospi against numpy's cbrt / sqrt / sin(pi x), then
+    # the recentring.  FP64 within 1e-12; float within two float ulps, since
+    # a double near a rounding midpoint may round either way
+    rel = 1e-12 if precision == "f64" else 2.5e-7
+    assert _ulps_close(gp, wp, rel) and _ulps_close(gv, wv, rel)
+    assert np.array_equal(gp[:, 3], wp[:, 3]) and np.array_equal(gv[:, 3], wv[:, 3])
+
+
+@gpu
 def test_deterministic_and_seeded(cuda):
     a = gpu_initial_conditions("plummer", 5000, seed=3)
     b = gpu_initial_conditions("plummer", 5000, seed=3)
@@ -23,6 +83,7 @@ def test_deterministic_and_seeded(cuda):
     assert d[:, :3].tobytes() == e[:1000, :3].tobytes()
 
 
+@gpu
 def test_cube_ranges(cuda):
     n = 20000
     p, v = [t.cpu().numpy() for t in gpu_initial_conditions("cube", n, seed=1, vmax=0.01)]
@@ -32,6 +93,7 @@ def test_cube_ranges(cuda):
     assert np.all(v[:, 3] == 1.0)
 
 
+@gpu
 @pytest.mark.parametrize("precision", ["f32", "f64"])
 def test_plummer_profile_and_virial(cuda, precision):
     n = 100000
@@ -51,6 +113,7 @@ def test_plummer_profile_and_virial(cuda, precision):
     assert abs(-e[0] / e[1] - 0.5) < 0.03
 
 
+@gpu
 @pytest.mark.parametrize("kind", ["random", "shell", "expand"])
 def test_reference_configurations(cuda, kind):
     """The reference app's three initial configurations drawn on the GPU:
