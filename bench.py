@@ -192,16 +192,172 @@ def integrate_bytes(n, algo, plan):
 
 
 def committed_traffic():
-    """Per-launch DRAM bytes of the top kernels from the committed ncu summary."""
+    """Per-launch DRAM bytes and pipe counters of the top kernels from the
+    committed ncu summaries (profiles/traffic.json)."""
     try:
         return json.load(open(os.path.join(REPO, "profiles", "traffic.json")))
     except (OSError, ValueError):
         return {}
 
 
+# Algorithmic bytes of the integrator per body (FP32, split integrator
+# kernel): read pos 16 + vel 16 + acceleration 16, write pos 16 + vel 16.
+INTEGRATOR_BYTES_PER_BODY = 80
+
+
+def _device_free_bytes():
+    import torch
+
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info()[0]
+
+
+def sub_n1m_forward(peak_flops):
+    """The forward target at N=1,048,576 (Plummer, eps2 = dt = 1e-4): the
+    default FP32 symmetric kernel, 3 leapfrog steps after one untimed step,
+    per-kernel CUDA events; the context's device footprint beside it."""
+    from utc_gb300 import ics
+    from utc_gb300.nbody import NBodySystem
+
+    n = 1 << 20
+    p, v = ics.plummer(n, seed=0)
+    p32, v32 = ics.f32(p), ics.f32(v)
+    free0 = _device_free_bytes()
+    with NBodySystem(n, "f32", "sym", kick="physical", eps2=np.float32(EPS2), damping=1.0,
+                     dt=np.float32(DT)) as s:
+        footprint = free0 - _device_free_bytes()
+        s.set_state(p32, v32)
+        s.step(1)
+        s.set_state(p32, v32)
+        steps = 3
+        f, g = s.step_timed(steps)
+        plan = s.plan_info()
+    inter = float(n) ** 2 * steps
+    return {"workload": f"plain forward, Plummer N={n}, {steps} leapfrog steps, eps2={EPS2}, dt={DT}",
+            "G_interactions_per_s": inter / ((f + g) * 1e-3) / 1e9,
+            "force_kernel_G_interactions_per_s": inter / (f * 1e-3) / 1e9,
+            "force_ms_per_launch": f / steps, "integrate_ms_per_launch": g / steps,
+            "tflops_20flop": FLOP_PER_INTERACTION * inter / (f * 1e-3) / 1e12,
+            "frac_of_fp32_peak_20flop": FLOP_PER_INTERACTION * inter / (f * 1e-3) / peak_flops,
+            "device_footprint_bytes": int(footprint), "plan": plan}
+
+
+def sub_adjoint(reps=3):
+    """The adjoint workload (N=16384 uniform cube, 200 steps, checkpoints
+    every 20, default symmetric kernels): medians of the plain forward, the
+    checkpointed forward and the backward (recompute + VJP)."""
+    import torch
+
+    from utc_gb300 import ics
+    from utc_gb300.nbody import NBodySystem
+
+    n, T, K = 16384, 200, 20
+    p64, v64 = ics.uniform_cube(n, seed=0)
+    y = torch.tensor(ics.gaussian_targets(n, seed=1, sigma=0.5), dtype=torch.float32, device="cuda")
+    p32, v32 = ics.f32(p64), ics.f32(v64)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    ts = {"forward": [], "adj_forward": [], "adj_backward": []}
+    with NBodySystem(n, "f32", "sym", kick="physical", eps2=np.float32(1e-2), damping=1.0,
+                     dt=np.float32(1e-3)) as s:
+        pT = torch.empty((n, 4), device="cuda")
+        vT = torch.empty((n, 4), device="cuda")
+        for r in range(reps + 1):
+            s.set_state(p32, v32)
+            tf = timed(lambda: s.step(T))
+            s.set_state(p32, v32)
+            ta = timed(lambda: s.adj_forward(T, K))
+            s.get_state_device(pT, vT)
+            gx = torch.zeros((n, 4), device="cuda")
+            gx[:, :3] = 2.0 * (pT[:, :3] - y)
+            tb = timed(lambda: s.adj_backward(gx))
+            if r:  # the first round is the warm-up
+                ts["forward"].append(tf)
+                ts["adj_forward"].append(ta)
+                ts["adj_backward"].append(tb)
+    med = {k: float(np.median(v)) for k, v in ts.items()}
+    return {"workload": f"adjoint, uniform cube N={n}, {T} steps, checkpoints every {K}, symmetric kernels",
+            "ms_median": med,
+            "backward_over_forward": med["adj_backward"] / med["forward"],
+            "backward_plus_ckpt_forward_over_forward": (med["adj_backward"] + med["adj_forward"]) / med["forward"]}
+
+
+def sub_batched():
+    """The batched workload (512 Plummer systems, N log-uniform in
+    [128, 16384], eps2 = dt = 1e-3, 50 steps): the autotuned batched launch
+    in a CUDA graph against this library's plain per-system launches."""
+    import torch
+
+    from utc_gb300 import ics
+    from utc_gb300.nbody import NBodyBatch
+
+    sizes = ics.batch_sizes(512, lo=128, hi=16384, seed=0)
+    steps = 50
+    ps, vs = [], []
+    for k, nn in enumerate(sizes):
+        p, v = ics.plummer(int(nn), seed=1000 + k)
+        ps.append(ics.f32(p))
+        vs.append(ics.f32(v))
+    pos, vel = np.concatenate(ps), np.concatenate(vs)
+    pairs = float(np.sum(sizes.astype(np.float64) ** 2)) * steps
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    res = {}
+    with torch.cuda.stream(stream), NBodyBatch(sizes, kick="physical", eps2=np.float32(1e-3),
+                                               dt=np.float32(1e-3)) as b:
+        b.set_state(pos, vel, stream=sh)
+        shape = b.autotune(reps=1, stream=sh)
+        for name, fn in (("graph", lambda: b.run(steps, sh)),
+                         ("per_system", lambda: b.step_per_system(steps, sh))):
+            b.set_state(pos, vel, stream=sh)
+            fn()  # warm-up (captures the graph)
+            b.set_state(pos, vel, stream=sh)
+            stream.synchronize()
+            a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            c.record(stream)
+            c.synchronize()
+            res[name] = a.elapsed_time(c)
+    return {"workload": f"batched, {sizes.size} Plummer systems N in [128, 16384] ({int(sizes.sum())} "
+                        f"bodies), {steps} steps, eps2=dt=1e-3",
+            "autotuned_shape": list(shape), "ms_batched_graph": res["graph"],
+            "ms_per_system_launches": res["per_system"],
+            "speedup_vs_per_system": res["per_system"] / res["graph"],
+            "G_interactions_per_s_batched": pairs / (res["graph"] * 1e-3) / 1e9,
+            "G_interactions_per_s_per_system": pairs / (res["per_system"] * 1e-3) / 1e9,
+            "reference_kernel_per_system": "timed in tests/test_reference_gpu_kernel.py "
+                                           "(the reference's kernel is test infrastructure)"}
+
+
 # ---------------------------------------------------------------------------
 # CPU baseline (oracle port of the reference's sequential BodySystem<float>)
 # ---------------------------------------------------------------------------
+def cpu_single_thread(pos, vel):
+    """One leapfrog step of the workload by the oracle port on ONE host
+    thread, as the reference's sequential nbody runs
+    (benchapps/nbody/seq/nbody_main.cc:177-190, bodysystem.cc:103-133)."""
+    import oracle
+
+    t0 = time.perf_counter()
+    oracle.step(pos, vel, np.float32(EPS2), np.float32(1.0), np.float32(DT), 1,
+                kick_mode=oracle.KICK_PHYSICAL, G=np.float32(1.0), nthreads=1)
+    dt = time.perf_counter() - t0
+    return {"value": float(N_BODIES) ** 2 / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+            "nproc": os.cpu_count(),
+            "sample": f"1 of the {LEAPFROG_STEPS} leapfrog steps at N={N_BODIES} ({dt:.1f} s on 1 host "
+                      f"thread of {os.cpu_count()}; the reference's CPU nbody is sequential)"}
+
+
 def cpu_baseline(pos, vel, min_seconds=10.0, max_steps=3, threads=None):
     import oracle
 
@@ -221,7 +377,8 @@ def cpu_baseline(pos, vel, min_seconds=10.0, max_steps=3, threads=None):
     return {"value": rate, "unit": UNIT, "cores": threads, "kind": kind,
             "sample": f"{steps} of the {LEAPFROG_STEPS} leapfrog steps at N={N_BODIES} "
                       f"({dt:.1f} s on {threads} host threads; oracle restatement of "
-                      f"BodySystem<float>, targets split across threads, bit-identical per body)"}
+                      f"BodySystem<float>, targets split across threads, bit-identical per body)",
+            "threads_1": cpu_single_thread(pos, vel)}
 
 
 def run_reference_arm(args):
@@ -254,7 +411,8 @@ def run_reference_arm(args):
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} single leapfrog steps at N={N_BODIES} on "
                                    f"{threads} host threads (reference sequential algorithm, "
-                                   f"oracle restatement; the compiled reference is x86-only here)"},
+                                   f"oracle restatement; the compiled reference is x86-only here)",
+                         "threads_1": cpu_single_thread(pos, vel)},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -389,7 +547,9 @@ def run_ours(args):
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         nominal_tf = sms * 128 * 2 * (clk.get("sm_max_mhz") or 2070.0) * 1e6 / 1e12
         traffic = committed_traffic()
-        integ_bytes = integrate_bytes(N_BODIES, args.algo, plan)
+        integ_bytes = INTEGRATOR_BYTES_PER_BODY * N_BODIES
+        integ_moved = integrate_bytes(N_BODIES, args.algo, plan)
+        integ_traffic = traffic.get("integrate_bytes_per_launch") if args.algo == "sym" else None
         hbm = peaks.get("hbm_gbs")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -401,7 +561,7 @@ def run_ours(args):
                        "kick": "physical (G=1)", "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "flushed between timed steps (256 MB write outside the event pair)",
                        "plan": plan},
-            "fp32_pipe_pct": 100.0 * achieved_tf / fp32_peak_tf,
+            "fp32_pct_20flop_convention": 100.0 * achieved_tf / fp32_peak_tf,
             "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak_tf,
                          "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak_tf,
                          "traffic": traffic.get("force_bytes_per_launch" if args.algo == "sym"
@@ -411,17 +571,30 @@ def run_ours(args):
                          "avg_launch_ms": force_avg_s * 1e3,
                          "peak_source": "packed-FMA probe measured in this run "
                                         "(MEASURED_PEAKS.json has no FP32 figure)",
-                         "nominal_peak": nominal_tf},
+                         "nominal_peak": nominal_tf,
+                         "flop_convention": "20 FLOP per interaction (bodysystem.h:75-95); the "
+                                            "symmetric kernel issues 16 FP32 operations per PAIR of "
+                                            "interactions, so this rate can exceed the pipe's own use",
+                         "ncu_fma_pipe_active": traffic.get("force_fma_pipe_active")
+                         if args.algo == "sym" else traffic.get("directed_force_fma_pipe_active"),
+                         "ncu_issue_active": traffic.get("force_issue_active")
+                         if args.algo == "sym" else traffic.get("directed_force_issue_active"),
+                         "ncu_source": traffic.get("force_source") if args.algo == "sym"
+                         else traffic.get("directed_force_source")},
             "roofline_integrator": {"bound": "hbm",
                                     "kernel": "sym_integrate_kernel" if args.algo == "sym" else "sk_integrate_kernel",
                                     "achieved": integ_bytes / integ_avg_s / 1e9, "peak": hbm,
                                     "unit": "GB/s",
                                     "frac": (integ_bytes / integ_avg_s / 1e9) / hbm if hbm else None,
-                                    "bytes_per_launch": integ_bytes,
+                                    "algorithmic_bytes_per_launch": integ_bytes,
                                     "avg_launch_ms": integ_avg_s * 1e3,
-                                    "traffic": traffic.get("integrate_bytes_per_launch") if args.algo == "sym" else None,
-                                    "note": "state (64 B/body) + every partial entry the kernel adds "
-                                            "(16 B each); at N=65536 these are mostly L2-resident"},
+                                    "traffic": integ_traffic,
+                                    "traffic_over_algorithmic": integ_traffic / integ_bytes if integ_traffic else None,
+                                    "bytes_moved_per_launch": integ_moved,
+                                    "moved_rate_GB_per_s": integ_moved / integ_avg_s / 1e9,
+                                    "note": f"algorithmic: {INTEGRATOR_BYTES_PER_BODY} B/body (pos, vel, acc "
+                                            "read; pos, vel written); moved: the state plus every partial "
+                                            "entry the kernel adds (16 B each)"},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * state_bytes,
                     "d2h_bytes_per_step": state_bytes,
                     "through_task": {"value": e2e_task_val, "unit": UNIT,
@@ -433,6 +606,12 @@ def run_ours(args):
             "clocks": clk,
             "wall_s_timed_region": wall,
         }
+        if world == 1 and not args.no_extras:
+            # the other stated targets, measured in the same run (outside the
+            # timed region above; each has its own CUDA-event timing)
+            line["n1m_forward"] = sub_n1m_forward(fp32_flops)
+            line["adjoint_n16384"] = sub_adjoint()
+            line["batched_512"] = sub_batched()
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(pos, vel)
         print(json.dumps(line), flush=True)
@@ -945,6 +1124,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the N=1M, adjoint and batched sub-records of the default line")
     ap.add_argument("--workload", default="plain",
                     choices=["plain", "precision", "adjoint", "batched", "double", "frames", "ics"])
     ap.add_argument("--algo", default="sym", choices=["fast", "sym"],
