@@ -234,6 +234,32 @@ int nb_step_f32_noalloc(const float *pos_old, float *pos_new, float *vel, int n,
                         float damping, float dt, int kick, float G, void *stream);
 
 /* ------------------------------------------------------------------------
+ * Target partition across GPUs: replaces the multi-GPU task
+ * BodySystemMGPU<T> (benchapps/nbody/utc-snode-mgpu/mgpu/body_task_mgpu.cu:
+ * 14-163), whose threads each own a range of targets, copy every body's
+ * positions in before each step and their own range out after it.
+ *
+ * nb_create_shard makes a context (on the current device) for shard `rank`
+ * of `nranks`: it holds every body's state and, per step, updates only its
+ * own targets against all sources.  NB_F32 with NB_ALGO_FAST: whole target
+ * blocks of the directed kernel's plan per shard (the remainder to the first
+ * ranks), and the shard launches exactly the CTAs of the single-GPU launch
+ * that cover its blocks, so the shards' results put together equal a
+ * single-GPU NB_ALGO_FAST context's bit for bit.  NB_ALGO_EXACT (NB_F32 or
+ * NB_F64): the reference's split, n / nranks bodies each and one more for
+ * the first n % nranks ranks; bit-identical to the sequential reference.
+ * With nranks > 1, nb_step / nb_step_timed take one step per call: between
+ * steps the caller brings the other shards' new positions into this
+ * context's current position buffer (nb_state_ptrs; an all-gather of every
+ * shard's range [first, first + count) of that buffer, e.g. by NCCL).  Velocities
+ * are valid in the shard's own range only.  nb_accel, nb_energy, the adjoint,
+ * nb_run_host and nb_autotune are refused (NB_ERR_UNSUPPORTED) on such a
+ * shard.  nb_shard_info: {first body, body count, rank, nranks}.
+ * ---------------------------------------------------------------------- */
+int nb_create_shard(const nb_params *p, int rank, int nranks, nb_ctx **out);
+int nb_shard_info(nb_ctx *ctx, int *info4);
+
+/* ------------------------------------------------------------------------
  * Batches: many independent systems of uneven size advanced together, one
  * persistent launch per step for all of them.  Replaces running one
  * Task<BodySystemSGPU<T>> per system (benchapps/nbody/utc/nbody_mtask.cc:

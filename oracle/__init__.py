@@ -64,6 +64,7 @@ def _declare(lib):
         "orc_accel_phi_subset_f64": (I, [I, _f64p, I, _i32p, D, _f64p, _f64p, I]),
         "orc_step_f32": (I, [I, _f32p, _f32p, F, F, F, I, I, F, I]),
         "orc_step_f64": (I, [I, _f64p, _f64p, D, D, D, I, I, D, I]),
+        "orc_step_range_f32": (I, [I, _f32p, _f32p, _f32p, I, I, F, F, F, I, F, I]),
         "orc_energy_f64": (I, [I, _f64p, _f64p, D, D, _f64p, I]),
         "orc_adjoint_f64": (I, [I, _f64p, _f64p, D, D, D, I, I, D, _f64p,
                                 C.POINTER(D), _f64p, _f64p, _f64p, I]),
@@ -184,6 +185,17 @@ def step(pos, vel, eps2, damping, dt, steps, kick_mode=KICK_REFERENCE, G=1.0, nt
         _check(lib().orc_step_f64(n, pos.reshape(-1), vel.reshape(-1), float(eps2), float(damping),
                                   float(dt), steps, kick_mode, float(G), nt), "step_f64")
     return pos, vel
+
+
+def step_range(pos_old, pos_new, vel, i0, i1, eps2, damping, dt, kick_mode=KICK_REFERENCE, G=1.0,
+               nthreads=None):
+    """One float step of targets [i0, i1) against every body of pos_old,
+    written into pos_new[i0:i1] and vel[i0:i1] in place (float32 (n, 4)
+    C-contiguous arrays): the share of one shard of a target partition."""
+    n = pos_old.shape[0]
+    _check(lib().orc_step_range_f32(n, pos_old.reshape(-1), pos_new.reshape(-1), vel.reshape(-1), int(i0),
+                                    int(i1), np.float32(eps2), np.float32(damping), np.float32(dt),
+                                    kick_mode, np.float32(G), nthreads or default_threads()), "step_range_f32")
 
 
 def energy(pos, vel, eps2, G=1.0, nthreads=None):

@@ -287,6 +287,48 @@ int orc_step_f64(int n, double *pos, double *vel, double eps2, double damping,
     return 0;
 }
 
+/* One step of the targets [i0, i1) only, against all n sources at pos_old:
+ * the part of a step one thread of the reference's multi-GPU task computes
+ * (benchapps/nbody/utc-snode-mgpu/mgpu/body_task_mgpu.cu:102-151: every
+ * body's positions in, the local range's new positions out).  Writes the
+ * range's positions to pos_new and its velocities in place; the other
+ * entries of pos_new and vel are left as they are. */
+typedef struct {
+    int n, i0;
+    const float *pos;
+    float eps2;
+    float *acc;
+} accel_rng_ctx;
+
+static void accel_rng_range(void *vp, int lo, int hi)
+{
+    accel_rng_ctx *c = (accel_rng_ctx *)vp;
+    for (int t = lo; t < hi; ++t) {
+        float a[3] = {0.f, 0.f, 0.f};
+        const float *pi = c->pos + 4 * (size_t)(c->i0 + t);
+        for (int j = 0; j < c->n; ++j) pair_f32(a, pi, c->pos + 4 * (size_t)j, c->eps2);
+        c->acc[3 * (size_t)t + 0] = a[0];
+        c->acc[3 * (size_t)t + 1] = a[1];
+        c->acc[3 * (size_t)t + 2] = a[2];
+    }
+}
+
+int orc_step_range_f32(int n, const float *pos_old, float *pos_new, float *vel, int i0, int i1,
+                       float eps2, float damping, float dt, int kick_mode, float G, int nthreads)
+{
+    if (n < 0 || i0 < 0 || i1 < i0 || i1 > n || (n > 0 && (!pos_old || !pos_new || !vel))) return 1;
+    if (kick_mode != ORC_KICK_REFERENCE && kick_mode != ORC_KICK_PHYSICAL) return 1;
+    const int m = i1 - i0;
+    float *force = (float *)malloc(sizeof(float) * 3 * (size_t)(m > 0 ? m : 1));
+    if (!force) return 2;
+    accel_rng_ctx c = {n, i0, pos_old, eps2, force};
+    parallel_for(m, nthreads, accel_rng_range, &c);
+    memcpy(pos_new + 4 * (size_t)i0, pos_old + 4 * (size_t)i0, sizeof(float) * 4 * (size_t)m);
+    integrate_f32(m, pos_new + 4 * (size_t)i0, vel + 4 * (size_t)i0, force, damping, dt, kick_mode, G);
+    free(force);
+    return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* energy and momentum                                                 */
 /* ------------------------------------------------------------------ */

@@ -57,6 +57,10 @@ int orc_step_f32(int n, float *pos, float *vel, float eps2, float damping,
                  float dt, int steps, int kick_mode, float G, int nthreads);
 int orc_step_f64(int n, double *pos, double *vel, double eps2, double damping,
                  double dt, int steps, int kick_mode, double G, int nthreads);
+/* One step of targets [i0, i1) against all n sources (a shard of the
+ * multi-GPU target partition); pos_new/vel receive that range only. */
+int orc_step_range_f32(int n, const float *pos_old, float *pos_new, float *vel, int i0, int i1,
+                       float eps2, float damping, float dt, int kick_mode, float G, int nthreads);
 
 /* Total energy and momentum of a state in double:
  * out[0] = kinetic  sum_i 0.5 m_i |v_i|^2

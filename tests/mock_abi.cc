@@ -54,6 +54,11 @@ cudaError_t cudaGetDevice(int *dev)
     return cudaSuccess;
 }
 cudaError_t cudaSetDevice(int) { return cudaSuccess; }
+cudaError_t cudaGetDeviceCount(int *count)
+{
+    *count = 1;
+    return cudaSuccess;
+}
 cudaError_t cudaStreamCreateWithFlags(cudaStream_t *s, unsigned int)
 {
     *s = g_fake_stream;

@@ -113,7 +113,8 @@ def test_batch_vs_reference_kernel_per_system(ref_kernel, capsys):
                                 vt.data_ptr() + o, int(nn), 1e-3, 1e-3, 1.0, 128, sh)
 
     torch.cuda.synchronize()
-    ref_steps(2)  # warm-up
+    ref_steps(2)  # warm-up, on `stream`
+    stream.synchronize()  # before the default stream rewrites its buffers
     bufs[0].copy_(torch.from_numpy(pos))
     vt.copy_(torch.from_numpy(vel))
     torch.cuda.synchronize()

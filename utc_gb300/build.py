@@ -2,7 +2,8 @@
 
 Produces, next to this file:
   libnbody_gb300.so  -- the CUDA kernels behind the C ABI (include/nbody_gb300.h)
-  libnbody_task.so   -- BodySystemGB300<T> (the UTC-task drop-in) + Task stand-in
+  libnbody_task.so   -- BodySystemGB300<T> (the UTC-task drop-in), BodySystemMGPU_GB300<T>
+                        (the multi-GPU task drop-in) + Task stand-in
   nbody_main         -- the app driver with the reference's flags
   nbody_mtask        -- the multi-task app driver (many systems, batched)
 
@@ -84,7 +85,7 @@ def build(force: bool = False, verbose: bool = False) -> None:
              os.path.join(BUILD_DIR, "link.log"))
 
     # C++ drop-in task + stand-in runtime + app driver (host code only)
-    task_srcs = [os.path.join(TASK, "body_task_gb300.cc")]
+    task_srcs = [os.path.join(TASK, "body_task_gb300.cc"), os.path.join(TASK, "body_task_mgpu_gb300.cc")]
     task_hdrs = glob.glob(os.path.join(TASK, "*.h")) + [os.path.join(INCLUDE, "nbody_gb300.h")]
     cxx = os.environ.get("CXX", "g++")
     # -ffp-contract=off: NbodyInit restates the reference's float arithmetic,

@@ -100,6 +100,10 @@ struct nb_ctx {
     // steps (one per starting ping-pong buffer): small systems are otherwise
     // bound by the per-kernel launch cost
     cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
+    // shard of a multi-GPU target partition (nb_create_shard): this context
+    // updates targets [shard_lo, shard_hi) of all n bodies; shard_count 1 is
+    // a whole system
+    int shard_rank = 0, shard_count = 1, shard_lo = 0, shard_hi = 0;
     // adjoint: checkpoints of the last nb_adj_forward and reverse-pass buffers
     struct Adj {
         int steps = 0, every = 0, nckpt = 0;
@@ -367,7 +371,66 @@ int nb_create(const nb_params *p, nb_ctx **out)
             return st;
         }
     }
+    c->shard_lo = 0;
+    c->shard_hi = p->n;
     *out = c;
+    return NB_OK;
+}
+
+int nb_create_shard(const nb_params *p, int rank, int nranks, nb_ctx **out)
+{
+    if (!out) return set_error(NB_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!p) return set_error(NB_ERR_INVALID, "params is NULL");
+    if (nranks < 1 || rank < 0 || rank >= nranks)
+        return set_error(NB_ERR_INVALID, "nb_create_shard: rank must be in [0, nranks), nranks >= 1");
+    const bool fast = p->precision == NB_F32 && p->algo == NB_ALGO_FAST;
+    const bool exact = (p->precision == NB_F32 || p->precision == NB_F64) && p->algo == NB_ALGO_EXACT;
+    if (!fast && !exact)
+        return set_error(NB_ERR_UNSUPPORTED, "nb_create_shard: shards run the directed kernel (NB_F32, "
+                                             "NB_ALGO_FAST) or the reference-exact one (NB_ALGO_EXACT)");
+    int st = nb_create(p, out);
+    if (st) return st;
+    nb_ctx *c = *out;
+    c->shard_rank = rank;
+    c->shard_count = nranks;
+    if (fast) {
+        // whole target blocks per shard, so that the shard's CTAs write the
+        // partial slots the single-GPU launch writes for those targets
+        if ((st = nb::fast_shard(&c->plan, rank, nranks))) {
+            free_ctx(c);
+            *out = nullptr;
+            return st;
+        }
+        c->shard_lo = c->plan.i_lo;
+        c->shard_hi = c->plan.i_hi;
+    } else {
+        // the reference's split (body_task_mgpu.cu:41-49): n / nranks bodies
+        // each, one more for the first n % nranks ranks
+        const int q = p->n / nranks, r = p->n % nranks;
+        c->shard_lo = rank < r ? rank * (q + 1) : rank * q + r;
+        c->shard_hi = c->shard_lo + q + (rank < r ? 1 : 0);
+    }
+    return NB_OK;
+}
+
+int nb_shard_info(nb_ctx *c, int *info4)
+{
+    if (!c || !info4) return set_error(NB_ERR_INVALID, "ctx/info is NULL");
+    info4[0] = c->shard_lo;
+    info4[1] = c->shard_hi - c->shard_lo;
+    info4[2] = c->shard_rank;
+    info4[3] = c->shard_count;
+    return NB_OK;
+}
+
+// Calls that need every body's fresh state, refused on a shard of a
+// multi-rank partition (its other ranks' bodies are stale between steps).
+static int refuse_shard(const nb_ctx *c, const char *what)
+{
+    if (c && c->shard_count > 1)
+        return set_error(NB_ERR_UNSUPPORTED, std::string(what) +
+                                                 ": not available on a shard of a multi-rank partition");
     return NB_OK;
 }
 
@@ -484,10 +547,12 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
                                      (const double4 *)c->sym_t, (const double4 *)c->sym_s, p.damping, p.dt,
                                      p.kick, p.G, (double4 *)acc_out, s, ff_sym(c) ? c->ff_range : nullptr);
     } else if (p.precision == NB_F64) {
-        st = nb::exact_step_f64(p.n, (const double4 *)po, (double4 *)pn, (double4 *)c->vel, p.eps2,
+        st = nb::exact_step_f64(p.n, c->shard_lo, c->shard_hi, (const double4 *)po, (double4 *)pn,
+                                (double4 *)c->vel, p.eps2,
                                 p.damping, p.dt, p.kick, p.G, (double4 *)acc_out, p.block, s);
     } else if (p.algo == NB_ALGO_EXACT) {
-        st = nb::exact_step_f32(p.n, (const float4 *)po, (float4 *)pn, (float4 *)c->vel,
+        st = nb::exact_step_f32(p.n, c->shard_lo, c->shard_hi, (const float4 *)po, (float4 *)pn,
+                                (float4 *)c->vel,
                                 (float)p.eps2, (float)p.damping, (float)p.dt, p.kick, (float)p.G,
                                 (float4 *)acc_out, p.block, s);
     } else if (p.algo == NB_ALGO_SYM) {
@@ -558,6 +623,9 @@ int nb_step(nb_ctx *c, int steps, void *stream)
     if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
     if (steps < 0) return set_error(NB_ERR_INVALID, "steps must be >= 0");
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
+    if (c->shard_count > 1 && steps > 1)
+        return set_error(NB_ERR_INVALID, "nb_step: a shard steps once per call (the other shards' "
+                                         "positions are exchanged between steps)");
     cudaStream_t s = (cudaStream_t)stream;
     int st;
     // the legacy default stream cannot be captured: launch step by step there,
@@ -606,6 +674,8 @@ int nb_step_timed(nb_ctx *c, int steps, float *ms_force, float *ms_integrate, vo
 {
     if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
     if (steps < 0) return set_error(NB_ERR_INVALID, "steps must be >= 0");
+    if (c->shard_count > 1 && steps > 1)
+        return set_error(NB_ERR_INVALID, "nb_step_timed: a shard steps once per call");
     if (!ms_force || !ms_integrate) return set_error(NB_ERR_INVALID, "ms outputs are NULL");
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
     cudaStream_t s = (cudaStream_t)stream;
@@ -635,6 +705,7 @@ int nb_step_timed(nb_ctx *c, int steps, float *ms_force, float *ms_integrate, vo
 
 int nb_accel(nb_ctx *c, void *acc_dev, void *stream)
 {
+    if (int rs = refuse_shard(c, "nb_accel")) return rs;
     if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
     if (c->p.n == 0) return NB_OK;
@@ -644,6 +715,7 @@ int nb_accel(nb_ctx *c, void *acc_dev, void *stream)
 
 int nb_energy(nb_ctx *c, double *out5, void *accphi_dev, void *stream)
 {
+    if (int rs = refuse_shard(c, "nb_energy")) return rs;
     if (!c || !out5) return set_error(NB_ERR_INVALID, "ctx/out is NULL");
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
     if (!(c->p.eps2 > 0.0)) return set_error(NB_ERR_INVALID, "nb_energy needs eps2 > 0");
@@ -809,6 +881,7 @@ static int adj_reserve(nb_ctx *c, int nckpt, int every)
 int nb_adj_forward(nb_ctx *c, int steps, int ckpt_every, void *stream, unsigned long long *generation)
 {
     if (generation) *generation = 0;
+    if (int rs = refuse_shard(c, "nb_adj_forward")) return rs;
     if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
     if (!uses_fast(c)) return set_error(NB_ERR_UNSUPPORTED, "the adjoint needs an NB_F32 fast context");
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
@@ -993,6 +1066,7 @@ int nb_launches_per_step(nb_ctx *c)
 // and kept, so no step reallocates afterwards.
 int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *chosen2)
 {
+    if (int rs = refuse_shard(c, "nb_autotune")) return rs;
     if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
     if (reps < 1) reps = 3;
@@ -1218,6 +1292,7 @@ int nb_plan_info(nb_ctx *c, int *info5)
 int nb_run_host(nb_ctx *c, const void *pos, const void *vel, int loops, int out_interval,
                 void *outbuffer, double *timings, void *stream)
 {
+    if (int rs = refuse_shard(c, "nb_run_host")) return rs;
     if (!c) return set_error(NB_ERR_INVALID, "ctx is NULL");
     if (loops < 0) return set_error(NB_ERR_INVALID, "loops must be >= 0");
     if (out_interval <= 0) return set_error(NB_ERR_INVALID, "out_interval must be >= 1");

@@ -28,20 +28,23 @@ __device__ __forceinline__ double e_mul(double a, double b) { return __dmul_rn(a
 __device__ __forceinline__ float e_rinvsqrt(float x) { return __frcp_rn(__fsqrt_rn(x)); }
 __device__ __forceinline__ double e_rinvsqrt(double x) { return __drcp_rn(__dsqrt_rn(x)); }
 
+// Targets i_begin <= i < i_end against all n sources: a target's result does
+// not depend on which other targets a launch covers (a shard of the targets
+// gives the full launch's bits).
 template <typename T>
 __global__ void exact_step_kernel(const typename vec4_of<T>::type *__restrict__ pos_old,
                                   typename vec4_of<T>::type *__restrict__ pos_new,
-                                  typename vec4_of<T>::type *__restrict__ vel, int n, T eps2,
-                                  T damping, T dt, int kick, T G,
+                                  typename vec4_of<T>::type *__restrict__ vel, int n, int i_begin,
+                                  int i_end, T eps2, T damping, T dt, int kick, T G,
                                   typename vec4_of<T>::type *__restrict__ acc_out)
 {
     typedef typename vec4_of<T>::type V4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V4 *sp = reinterpret_cast<V4 *>(smem_raw);
     const int nt = blockDim.x;
-    const int i = blockIdx.x * nt + threadIdx.x;
+    const int i = i_begin + blockIdx.x * nt + threadIdx.x;
     V4 pi;
-    if (i < n) {
+    if (i < i_end) {
         pi = pos_old[i];
     } else {
         pi.x = pi.y = pi.z = pi.w = T(0);
@@ -67,7 +70,7 @@ __global__ void exact_step_kernel(const typename vec4_of<T>::type *__restrict__ 
             az = e_add(az, e_mul(r2, s));
         }
     }
-    if (i >= n) return;
+    if (i >= i_end) return;
     if (acc_out) {
         V4 a;
         a.x = ax;
@@ -93,12 +96,13 @@ __global__ void exact_step_kernel(const typename vec4_of<T>::type *__restrict__ 
 }
 
 template <typename T>
-static int exact_launch(int n, const typename vec4_of<T>::type *pos_old,
+static int exact_launch(int n, int i_begin, int i_end, const typename vec4_of<T>::type *pos_old,
                         typename vec4_of<T>::type *pos_new, typename vec4_of<T>::type *vel,
                         T eps2, T damping, T dt, int kick, T G,
                         typename vec4_of<T>::type *acc_out, int block, cudaStream_t s)
 {
-    if (n == 0) return NB_OK;
+    const int nt = i_end - i_begin;  // targets of this launch
+    if (n == 0 || nt <= 0) return NB_OK;
     if (block <= 0) block = 256;
     if (block % 32 != 0 || block > 1024)
         return set_error(NB_ERR_INVALID, "exact kernel block size must be a multiple of 32, <= 1024");
@@ -111,32 +115,33 @@ static int exact_launch(int n, const typename vec4_of<T>::type *pos_old,
     NB_CUDA(cudaGetDevice(&dev));
     NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     auto load = [&](int b) {
-        const long long grid = ((long long)n + b - 1) / b;
+        const long long grid = ((long long)nt + b - 1) / b;
         return ((grid + sms - 1) / sms) * (b / 32);
     };
     for (int b = block / 2; b >= 32 && b % 32 == 0; b /= 2)
         if (load(b) < load(block)) block = b;
     const size_t smem = sizeof(typename vec4_of<T>::type) * block;
-    exact_step_kernel<T><<<(n + block - 1) / block, block, smem, s>>>(pos_old, pos_new, vel, n, eps2,
-                                                                     damping, dt, kick, G, acc_out);
+    exact_step_kernel<T><<<(nt + block - 1) / block, block, smem, s>>>(pos_old, pos_new, vel, n, i_begin,
+                                                                      i_end, eps2, damping, dt, kick, G,
+                                                                      acc_out);
     NB_LAUNCH_CHECK("exact_step_kernel launch");
     return NB_OK;
 }
 
-int exact_step_f32(int n, const float4 *pos_old, float4 *pos_new, float4 *vel, float eps2,
-                   float damping, float dt, int kick, float G, float4 *acc_out, int block,
+int exact_step_f32(int n, int i_begin, int i_end, const float4 *pos_old, float4 *pos_new, float4 *vel,
+                   float eps2, float damping, float dt, int kick, float G, float4 *acc_out, int block,
                    cudaStream_t s)
 {
-    return exact_launch<float>(n, pos_old, pos_new, vel, eps2, damping, dt, kick, G, acc_out,
-                               block, s);
+    return exact_launch<float>(n, i_begin, i_end, pos_old, pos_new, vel, eps2, damping, dt, kick, G,
+                               acc_out, block, s);
 }
 
-int exact_step_f64(int n, const double4 *pos_old, double4 *pos_new, double4 *vel, double eps2,
-                   double damping, double dt, int kick, double G, double4 *acc_out, int block,
-                   cudaStream_t s)
+int exact_step_f64(int n, int i_begin, int i_end, const double4 *pos_old, double4 *pos_new,
+                   double4 *vel, double eps2, double damping, double dt, int kick, double G,
+                   double4 *acc_out, int block, cudaStream_t s)
 {
-    return exact_launch<double>(n, pos_old, pos_new, vel, eps2, damping, dt, kick, G, acc_out,
-                                block, s);
+    return exact_launch<double>(n, i_begin, i_end, pos_old, pos_new, vel, eps2, damping, dt, kick, G,
+                                acc_out, block, s);
 }
 
 }  // namespace nb

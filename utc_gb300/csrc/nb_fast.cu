@@ -42,11 +42,16 @@ __device__ __forceinline__ void f2_two_sum(f2 a, f2 b, f2 &s, f2 &e)
 // compensated (hi, lo) pair with a two-sum, and write both (lo at
 // partial + lo_offset); SK_PHI -- also accumulate the potential
 // sum_j m_j / sqrt(r^2 + eps2) in w.
+// CTA blockIdx.x is CTA cta_base + blockIdx.x of a plan of grid_full CTAs,
+// and works only on iterations inside [it_lo, it_hi): a launch of the CTAs
+// that cover a range of target blocks computes those blocks' partial slots
+// exactly as the full launch does (a shard of the targets, same bits).
 template <int NT, int NPAIR, int FLAGS>
 __global__ void __launch_bounds__(NT) sk_force_kernel(const float4 *__restrict__ pos, int n,
                                                       float eps2, float4 *__restrict__ partial,
                                                       long long total, int ngroups,
-                                                      long long lo_offset)
+                                                      long long lo_offset, int cta_base, int grid_full,
+                                                      long long it_lo, long long it_hi)
 {
     constexpr bool COMP = (FLAGS & SK_COMP) != 0;
     constexpr bool PHI = (FLAGS & SK_PHI) != 0;
@@ -55,9 +60,11 @@ __global__ void __launch_bounds__(NT) sk_force_kernel(const float4 *__restrict__
     __shared__ __align__(16) float4 sA[NT];  // (x, x, y, y)
     __shared__ __align__(16) float4 sB[NT];  // (z, z, m, m)
     const int t = threadIdx.x;
-    const int c = blockIdx.x;
-    long long it = sk_start(c, total, gridDim.x);
-    const long long end = sk_start(c + 1, total, gridDim.x);
+    const int c = cta_base + blockIdx.x;
+    long long it = sk_start(c, total, grid_full);
+    long long end = sk_start(c + 1, total, grid_full);
+    if (it < it_lo) it = it_lo;
+    if (end > it_hi) end = it_hi;
     const f2 EPS2 = f2_pack(eps2, eps2);
     const f2 ZERO = f2_pack(0.f, 0.f);
     const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
@@ -175,15 +182,15 @@ __global__ void __launch_bounds__(NT) sk_force_kernel(const float4 *__restrict__
 
 // Sum the partial slots of each target in CTA order, then the reference's
 // kick / damping / drift with unfused IEEE operations in its order
-// (bodysystem_kernel.cu:115-126).
+// (bodysystem_kernel.cu:115-126).  Targets i_begin <= i < i_end.
 __global__ void sk_integrate_kernel(const float4 *__restrict__ pos_old, float4 *__restrict__ pos_new,
                                     float4 *__restrict__ vel, const float4 *__restrict__ partial,
-                                    int n, int tbsize, long long total, int ngroups, int grid,
-                                    float damping, float dt, int kick, float G,
+                                    int i_begin, int i_end, int tbsize, long long total, int ngroups,
+                                    int grid, float damping, float dt, int kick, float G,
                                     float4 *__restrict__ acc_out)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int i = i_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= i_end) return;
     const int tb = i / tbsize;
     const int li = i - tb * tbsize;
     const long long first = (long long)tb * ngroups;
@@ -219,7 +226,8 @@ __global__ void sk_integrate_kernel(const float4 *__restrict__ pos_old, float4 *
 // ---------------------------------------------------------------------------
 // dispatch over the compiled (threads per CTA, target pairs per thread) shapes
 // ---------------------------------------------------------------------------
-typedef void (*sk_kernel_t)(const float4 *, int, float, float4 *, long long, int, long long);
+typedef void (*sk_kernel_t)(const float4 *, int, float, float4 *, long long, int, long long, int, int,
+                            long long, long long);
 
 // Compiled shapes (threads per CTA x bodies per thread): plain kernel
 // 128|256 x 2|4|8; compensated and potential variants 256 x 4|8.
@@ -277,6 +285,22 @@ int fast_plan(int n, int block, int bpt, int ctas_per_sm, int device, SkPlan *pl
     return NB_OK;
 }
 
+int fast_shard(SkPlan *p, int rank, int nranks)
+{
+    if (nranks < 1 || rank < 0 || rank >= nranks)
+        return set_error(NB_ERR_INVALID, "shard rank must be in [0, nranks)");
+    // whole target blocks per rank, the remainder to the first ranks
+    const int q = p->ntb / nranks, r = p->ntb % nranks;
+    const int tb0 = rank * q + (rank < r ? rank : r);
+    const int tb1 = tb0 + q + (rank < r ? 1 : 0);
+    p->ranged = true;
+    p->it_lo = (long long)tb0 * p->ngroups;
+    p->it_hi = (long long)tb1 * p->ngroups;
+    p->i_lo = std::min(tb0 * p->tbsize, p->n);
+    p->i_hi = std::min(tb1 * p->tbsize, p->n);
+    return NB_OK;
+}
+
 int fast_force(const SkPlan &p, const float4 *pos, float eps2, float4 *partial, cudaStream_t s,
                int flags)
 {
@@ -284,7 +308,16 @@ int fast_force(const SkPlan &p, const float4 *pos, float eps2, float4 *partial, 
     sk_kernel_t k = sk_kernel_for(p.block, p.bpt, flags);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "fast kernel shape not compiled for this variant");
     const long long lo_offset = (long long)p.slots * p.tbsize;
-    k<<<p.grid, p.block, 0, s>>>(pos, p.n, eps2, partial, p.total, p.ngroups, lo_offset);
+    long long lo = 0, hi = p.total;
+    int base = 0, ctas = p.grid;
+    if (p.ranged) {  // only the CTAs that cover the shard's iterations
+        lo = p.it_lo;
+        hi = p.it_hi;
+        if (hi <= lo) return NB_OK;
+        base = sk_owner(lo, p.total, p.grid);
+        ctas = sk_owner(hi - 1, p.total, p.grid) - base + 1;
+    }
+    k<<<ctas, p.block, 0, s>>>(pos, p.n, eps2, partial, p.total, p.ngroups, lo_offset, base, p.grid, lo, hi);
     NB_LAUNCH_CHECK("sk_force_kernel launch");
     return NB_OK;
 }
@@ -293,11 +326,12 @@ int fast_integrate(const SkPlan &p, const float4 *pos_old, float4 *pos_new, floa
                    const float4 *partial, float damping, float dt, int kick, float G,
                    float4 *acc_out, cudaStream_t s)
 {
-    if (p.n == 0) return NB_OK;
+    const int i0 = p.ranged ? p.i_lo : 0, i1 = p.ranged ? p.i_hi : p.n;
+    if (i1 <= i0) return NB_OK;
     const int bs = 256;
-    sk_integrate_kernel<<<(p.n + bs - 1) / bs, bs, 0, s>>>(pos_old, pos_new, vel, partial, p.n,
-                                                           p.tbsize, p.total, p.ngroups, p.grid,
-                                                           damping, dt, kick, G, acc_out);
+    sk_integrate_kernel<<<(i1 - i0 + bs - 1) / bs, bs, 0, s>>>(pos_old, pos_new, vel, partial, i0, i1,
+                                                               p.tbsize, p.total, p.ngroups, p.grid,
+                                                               damping, dt, kick, G, acc_out);
     NB_LAUNCH_CHECK("sk_integrate_kernel launch");
     return NB_OK;
 }

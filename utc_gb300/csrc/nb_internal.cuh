@@ -195,6 +195,11 @@ struct SkPlan {
     long long total = 0;
     int grid = 0;      // persistent CTAs
     int slots = 0;     // grid + ntb - 1
+    // a shard of the targets (fast_shard): whole target blocks; iterations
+    // [it_lo, it_hi) and targets [i_lo, i_hi) of the full plan above
+    bool ranged = false;
+    long long it_lo = 0, it_hi = 0;
+    int i_lo = 0, i_hi = 0;
 };
 
 __host__ __device__ __forceinline__ long long sk_start(long long c, long long total, int grid)
@@ -216,6 +221,9 @@ enum : int { SK_COMP = 1, SK_PHI = 2 };
 int fast_plan(int n, int block, int bpt, int ctas_per_sm, int device, SkPlan *plan,
               int flags = 0);
 bool fast_shape_supported(int block, int bpt, int flags);
+// Restrict a plan to the target blocks of shard `rank` of `nranks` (whole
+// blocks each, the remainder to the first ranks).
+int fast_shard(SkPlan *plan, int rank, int nranks);
 int fast_force(const SkPlan &plan, const float4 *pos, float eps2, float4 *partial,
                cudaStream_t s, int flags = 0);
 // Reduce the partial slots and integrate (acc_out != nullptr: write the bare
@@ -384,13 +392,13 @@ int adj_update_sym(const SymPlan &p, const float4 *tpart, const float4 *spart, c
                    const float4 *acc, float4 *lx, float4 *lv, float *gm, float4 *gbuf, float damping,
                    float dt, int kick, float G, int want_next_g, cudaStream_t s);
 
-// Exact-path entry points (nb_exact.cu)
-int exact_step_f32(int n, const float4 *pos_old, float4 *pos_new, float4 *vel, float eps2,
-                   float damping, float dt, int kick, float G, float4 *acc_out, int block,
+// Exact-path entry points (nb_exact.cu): targets [i_begin, i_end) of n
+int exact_step_f32(int n, int i_begin, int i_end, const float4 *pos_old, float4 *pos_new, float4 *vel,
+                   float eps2, float damping, float dt, int kick, float G, float4 *acc_out, int block,
                    cudaStream_t s);
-int exact_step_f64(int n, const double4 *pos_old, double4 *pos_new, double4 *vel, double eps2,
-                   double damping, double dt, int kick, double G, double4 *acc_out, int block,
-                   cudaStream_t s);
+int exact_step_f64(int n, int i_begin, int i_end, const double4 *pos_old, double4 *pos_new,
+                   double4 *vel, double eps2, double damping, double dt, int kick, double G,
+                   double4 *acc_out, int block, cudaStream_t s);
 
 // FMA peak probe (nb_fast.cu)
 int probe_fma(int iters, int packed, double *flops, float *ms, cudaStream_t s);

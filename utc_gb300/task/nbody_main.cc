@@ -2,7 +2,7 @@
  * nbody_main.cc -- the nbody app driver on the GB300 task, with the
  * reference's flags and flow (benchapps/nbody/utc/nbody_main.cc:68-271):
  *
- *   -v print timers      -t threads (must be 1)   -p processes (must be 1)
+ *   -v print timers      -t threads               -p processes (must be 1)
  *   -m 0|1|2 memtype     -i preset 0..6           -l iterations
  *   -o output interval   -O output file           -n bodies
  *   -b block size (exact kernel CTA size; N is rounded up to a multiple)
@@ -14,22 +14,28 @@
  *
  * Bodies come from NbodyInit (SHELL), run through Task<BodySystemGB300<T>>,
  * frames go through Task<Output<T>>; timers are printed as the reference
- * prints them.
+ * prints them.  With -t N > 1 the bodies run through the multi-GPU task
+ * Task<BodySystemMGPU_GB300<T>>(ProcList(N, 0)), as the reference's
+ * multi-GPU app does (benchapps/nbody/utc-snode-mgpu/nbody_main.cc:209-236:
+ * one thread per GPU, timers averaged over the threads).
  */
+#include <array>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 #include <iomanip>
 #include <iostream>
 #include <unistd.h>
 
 #include "body_task_gb300.h"
+#include "body_task_mgpu_gb300.h"
 #include "nbody_init.h"
 
 using namespace iUtc;
 
 template <typename FTYPE>
 static int run_app(bool printTime, int paraSelect, int iteration, int outInterval, int numBodies,
-                   const char *outfilename, int blocksize, MemType memtype, int algo)
+                   const char *outfilename, int blocksize, MemType memtype, int algo, int nthreads)
 {
     NBodyParams activeParams = nbody_demo_params(paraSelect, numBodies);
     FTYPE *body_pos = new FTYPE[(size_t)numBodies * 4];
@@ -47,7 +53,20 @@ static int run_app(bool printTime, int paraSelect, int iteration, int outInterva
 
     double runtime[4] = {0, 0, 0, 0};
     int status;
-    {
+    if (nthreads > 1) {
+        std::vector<std::array<double, 4>> runtime_m(nthreads);
+        Task<BodySystemMGPU_GB300<FTYPE>> nbody(ProcList(nthreads, 0), TaskType::gpu_task);
+        if (algo >= 0) nbody.userObject()->setAlgo(algo);
+        nbody.init((unsigned)numBodies,
+                   (FTYPE)activeParams.m_softening * (FTYPE)activeParams.m_softening,
+                   (FTYPE)activeParams.m_damping, body_pos, body_vel);
+        nbody.run(reinterpret_cast<double(*)[4]>(runtime_m.data()), iteration, outInterval, blocksize,
+                  (FTYPE)activeParams.m_timestep, body_outBuffer + (size_t)numBodies * 4, memtype);
+        nbody.wait();
+        status = nbody.userObject()->lastStatus();
+        for (int i = 0; i < nthreads; i++)
+            for (int j = 0; j < 4; j++) runtime[j] += runtime_m[i][j] / nthreads;
+    } else {
         Task<BodySystemGB300<FTYPE>> nbody(ProcList(0), TaskType::gpu_task);
         if (algo >= 0) nbody.userObject()->setAlgo(algo);
         nbody.init((unsigned)numBodies,
@@ -126,8 +145,8 @@ int main(int argc, char **argv)
         std::cerr << "process number not match with arguments '-p' !!!\n";
         return 1;
     }
-    if (nthreads != 1) {
-        std::cerr << "require one thread !!!\n";
+    if (nthreads < 1) {
+        std::cerr << "require at least one thread !!!\n";
         return 1;
     }
     MemType memtype = MemType::pageable;
@@ -143,7 +162,7 @@ int main(int argc, char **argv)
     }
     if (useFloat)
         return run_app<float>(printTime, paraSelect, iteration, outInterval, numBodies, outfilename,
-                              blocksize, memtype, algo);
+                              blocksize, memtype, algo, nthreads);
     return run_app<double>(printTime, paraSelect, iteration, outInterval, numBodies, outfilename,
-                           blocksize, memtype, algo);
+                           blocksize, memtype, algo, nthreads);
 }
