@@ -351,12 +351,14 @@ int nb_create(const nb_params *p, nb_ctx **out)
         if (uses_sym(c) || comp_sym(c)) {
             const size_t halves = comp_sym(c) ? 2 : 1;  // compensated: hi and lo blocks
             if ((st = nb::sym_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan,
-                                   comp_sym(c) ? 1 : 0)) ||
+                                   comp_sym(c) ? 1 : 0, comp_sym(c) ? 0 : 1)) ||
                 (st = dev_alloc((void **)&c->sym_t,
                                 halves * c->splan.slots * c->splan.rb * sizeof(float4),
                                 "symmetric scratch allocation")) ||
                 (st = dev_alloc((void **)&c->sym_s, halves * c->splan.spart_size * sizeof(float4),
-                                "symmetric source-side array (about N^2/(2 rb) entries; NB_ALGO_FAST needs O(N) scratch)"))) {
+                                comp_sym(c) ? "symmetric source-side array (about N^2/(2 rb) entries; NB_ALGO_FAST "
+                                              "needs O(N) scratch)"
+                                            : "symmetric source-side accumulators (48 B per body)"))) {
                 free_ctx(c);
                 return st;
             }
@@ -469,6 +471,12 @@ int nb_set_state(nb_ctx *c, const void *pos, const void *vel, int where, void *s
     } else if (sb) {
         NB_CUDA(cudaMemcpyAsync(c->pos[0], pos, sb, cudaMemcpyDefault, s));
         NB_CUDA(cudaMemcpyAsync(c->vel, vel, sb, cudaMemcpyDefault, s));
+        // symmetric contexts: zeroed source-side accumulators and the sum of
+        // |m| their scale comes from
+        if (uses_sym(c)) {
+            int st = nb::sym_fx_prepare(c->splan, (const float4 *)c->pos[0], c->sym_s, s);
+            if (st) return st;
+        }
         if (where == NB_HOST) NB_CUDA(cudaStreamSynchronize(s));
     }
     c->has_state = true;
@@ -507,7 +515,10 @@ int nb_state_ptrs(nb_ctx *c, void **pos_dev, void **vel_dev)
 
 // One step; when ev != nullptr, records ev[0] before the first kernel,
 // ev[1] between the force and the integrate kernel and ev[2] at the end.
-static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev = nullptr)
+// acc_keep (symmetric FP32 contexts only): also the step's bare
+// accelerations, read from the same force launch before the step consumes it.
+static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev = nullptr,
+                     float4 *acc_keep = nullptr)
 {
     const nb_params &p = c->p;
     void *po = c->pos[c->cur], *pn = c->pos[c->cur ^ 1];
@@ -558,9 +569,13 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
     } else if (p.algo == NB_ALGO_SYM) {
         st = nb::sym_force(c->splan, (const float4 *)po, (float)p.eps2, c->sym_t, c->sym_s, s);
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
+        if (!st && acc_keep)
+            st = nb::sym_integrate(c->splan, (const float4 *)po, nullptr, nullptr, c->sym_t, c->sym_s,
+                                   (float)p.eps2, (float)p.damping, (float)p.dt, p.kick, (float)p.G, acc_keep,
+                                   s, 0);
         if (!st)
             st = nb::sym_integrate(c->splan, (const float4 *)po, (float4 *)pn, (float4 *)c->vel,
-                                   c->sym_t, c->sym_s, (float)p.damping, (float)p.dt, p.kick,
+                                   c->sym_t, c->sym_s, (float)p.eps2, (float)p.damping, (float)p.dt, p.kick,
                                    (float)p.G, (float4 *)acc_out, s);
     } else {
         st = nb::fast_force(c->plan, (const float4 *)po, (float)p.eps2, c->partial, s);
@@ -915,19 +930,15 @@ int nb_adj_forward(nb_ctx *c, int steps, int ckpt_every, void *stream, unsigned 
             NB_CUDA(cudaMemcpyAsync(A.seg_pos, c->pos[c->cur], n * sizeof(float4),
                                     cudaMemcpyDeviceToDevice, s));
         const float4 *xk = (const float4 *)c->pos[c->cur];
-        if ((st = step_once(c, s, nullptr))) return st;
+        // reference kick: the bare acceleration at x_k from the step's own
+        // force launch (the symmetric step reads it before consuming the
+        // source-side sums; the directed partials stay in the scratch)
+        float4 *ak = (keep && p.kick == NB_KICK_REFERENCE) ? A.seg_acc + k * n : nullptr;
+        if ((st = step_once(c, s, nullptr, nullptr, uses_sym(c) ? ak : nullptr))) return st;
         if (!keep) continue;
-        if (p.kick == NB_KICK_REFERENCE) {
-            // the step's partial sums are still in the scratch: reduce them to
-            // the bare acceleration at x_k
-            float4 *ak = A.seg_acc + k * n;
-            if (uses_sym(c))
-                st = nb::sym_integrate(c->splan, xk, nullptr, nullptr, c->sym_t, c->sym_s,
-                                       (float)p.damping, (float)p.dt, p.kick, (float)p.G, ak, s);
-            else
-                st = nb::fast_reduce(c->plan, c->partial, 0, xk, (float)p.eps2, ak, nullptr, s);
-            if (st) return st;
-        }
+        if (ak && !uses_sym(c) &&
+            (st = nb::fast_reduce(c->plan, c->partial, 0, xk, (float)p.eps2, ak, nullptr, s)))
+            return st;
         NB_CUDA(cudaMemcpyAsync(A.seg_pos + (k + 1) * n, c->pos[c->cur], n * sizeof(float4),
                                 cudaMemcpyDeviceToDevice, s));
     }
@@ -979,10 +990,10 @@ int nb_adj_backward(nb_ctx *c, unsigned long long generation, const void *gx_T, 
             if (uses_sym(c)) {
                 if ((st2 = nb::sym_force(c->splan, xk, eps2, c->sym_t, c->sym_s, rs))) return st2;
                 if (p.kick == NB_KICK_REFERENCE &&
-                    (st2 = nb::sym_integrate(c->splan, xk, nullptr, nullptr, c->sym_t, c->sym_s, D, dt,
-                                             p.kick, G, sa + (size_t)k * n, rs)))
+                    (st2 = nb::sym_integrate(c->splan, xk, nullptr, nullptr, c->sym_t, c->sym_s, eps2, D, dt,
+                                             p.kick, G, sa + (size_t)k * n, rs, 0)))
                     return st2;
-                if ((st2 = nb::sym_integrate(c->splan, xk, xn, vt, c->sym_t, c->sym_s, D, dt, p.kick, G,
+                if ((st2 = nb::sym_integrate(c->splan, xk, xn, vt, c->sym_t, c->sym_s, eps2, D, dt, p.kick, G,
                                              nullptr, rs)))
                     return st2;
                 continue;
@@ -1106,7 +1117,7 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
         if (symm) {
             if (ff_sym(c)) return nb::symff_plan(p.n, a, b, c->device, sp);
             if (f64_sym(c)) return nb::sym64_plan(p.n, a, b, c->device, sp);
-            return nb::sym_plan(p.n, a, b, c->device, sp, comp_sym(c) ? 1 : 0);
+            return nb::sym_plan(p.n, a, b, c->device, sp, comp_sym(c) ? 1 : 0, comp_sym(c) ? 0 : 1);
         }
         return nb::fast_plan(p.n, a, b, p.ctas_per_sm, c->device, fp, is_comp(c) ? nb::SK_COMP : 0);
     };
@@ -1213,6 +1224,11 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
         nb::dfree(c->sym_s);
         c->sym_t = (float4 *)m[0];
         c->sym_s = (float4 *)m[1];
+        // a fixed-point source side starts zeroed, with its mass record
+        if (e == cudaSuccess && uses_sym(c)) {
+            int sp_st = nb::sym_fx_prepare(c->splan, (const float4 *)pos_now, c->sym_s, s);
+            if (sp_st) e = cudaErrorUnknown;
+        }
     } else {
         nb::dfree(c->partial);
         c->partial = (float4 *)m[0];

@@ -27,6 +27,26 @@
 // The integrate kernel adds, per body, its target-side slots (CTA order) and
 // its source-side entries spart[0..I_b-1][b] (row order): deterministic.
 //
+// Fixed-point source side (plans with fixed = 1, the default for FP32
+// contexts).  The triangular array holds about N^2 / (2 rb) float4 (67 MB at
+// N = 65536, 3.4 GB at N = 1M), which the integrator reads back: 15 times
+// the state's own bytes at N = 65536.  Instead, each warp adds its reaction
+// on a chunk body straight into per-body 64-bit integer accumulators with
+// integer atomics.  Integer addition is associative, so the sums are the
+// same whatever order the CTAs run in: the step stays deterministic, and
+// the source side takes 48 B per body.  Every reaction v (a float) is split
+// into two integers, hi = round(v / 2^(e-61)) and lo = round((v - hi
+// 2^(e-61)) / 2^(e-83)), both exact for |v| >= 2^(e-60) (the float's 24
+// significant bits fit), and within 2^(e-84) otherwise.  The exponent e
+// comes from a bound on every partial and total reaction: a body at distance
+// r adds at most m r / (r^2 + eps2)^(3/2) <= (2 / (3 sqrt 3)) m / eps2, so
+// B = 0.385 sum|m| / eps2 bounds them all, and 2^e > 2 B keeps the hi sums
+// below 2^62 (the lo sums stay below 2^22 per reaction).  So the source
+// side is summed essentially exactly: more accurately than float partial
+// sums, for any eps2 > 0.  sum|m| is recorded at nb_set_state
+// (sym_fx_prepare); the integrator zeroes the accumulators after reading
+// them.
+//
 // Compensated variant (COMP): each target's per-chunk partial sum (32
 // sources) is folded into a two-sum (hi, lo) pair, the W warps' reactions on
 // a chunk body are combined with two-sums, and both halves are written (lo
@@ -45,12 +65,68 @@
 
 namespace nb {
 
+// Scale of the fixed-point source side for msum = sum |m| and eps2 (see the
+// header): powers of two 2^(61-e), 2^(e-61), 2^(83-e).
+struct FxScale {
+    int e;
+    float inv_hi, lsb_hi, inv_lo;
+};
+
+__device__ __forceinline__ FxScale fx_scale(float msum, float eps2)
+{
+    const float b = 0.38490018f * msum / eps2;  // 2 / (3 sqrt 3) sum|m| / eps2
+    int e = -40;
+    if (b > 0.f && b <= 3.0e38f) {
+        frexpf(b, &e);  // b < 2^e
+        e += 1;         // 2^e > 2 b
+    } else if (b > 0.f) {
+        e = 120;        // eps2 = 0 (the self pair makes every result NaN anyway)
+    }
+    e = max(-40, min(120, e));
+    FxScale f;
+    f.e = e;
+    f.inv_hi = __int_as_float((127 + 61 - e) << 23);
+    f.lsb_hi = __int_as_float((127 + e - 61) << 23);
+    f.inv_lo = __int_as_float((127 + 83 - e) << 23);
+    return f;
+}
+
+// v added to the accumulators hi_p (units 2^(e-61)) and lo_p (2^(e-83)).
+// The products with powers of two are exact; rem is exact (|v / 2^(e-61)|
+// < 2^23 makes (float)h exact, otherwise v / 2^(e-61) is an integer and
+// rem = 0).  The adds compile to fire-and-forget reductions.
+__device__ __forceinline__ void fx_add(unsigned long long *hi_p, unsigned long long *lo_p, float v,
+                                       const FxScale &f)
+{
+    const long long h = __float2ll_rn(v * f.inv_hi);
+    const float rem = fmaf(-(float)h, f.lsb_hi, v);
+    const long long l = __float2ll_rn(rem * f.inv_lo);
+    atomicAdd(hi_p, (unsigned long long)h);
+    atomicAdd(lo_p, (unsigned long long)l);
+}
+
+// This warp's reaction (fx, fy, fz on chunk body jb + lane) into the
+// fixed-point accumulators: six reductions per lane and chunk.
+__device__ __forceinline__ void fx_emit(unsigned long long *acc, int n, int j, float fx, float fy, float fz,
+                                        const FxScale &f)
+{
+    if (j >= n) return;
+    const long long nn = n;
+    fx_add(acc + j, acc + 3 * nn + j, fx, f);
+    fx_add(acc + nn + j, acc + 4 * nn + j, fy, f);
+    fx_add(acc + 2 * nn + j, acc + 5 * nn + j, fz, f);
+}
+
+// fxacc != nullptr: the fixed-point source side (accumulators fxacc, sum
+// |m| at *fxmsum); otherwise the triangular array spart.
 template <int W, int BPT, int MINB, bool COMP>
 __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *__restrict__ pos, int n,
                                                            float eps2, float4 *__restrict__ tpart,
                                                            float4 *__restrict__ spart,
                                                            long long total, int nc, int nrb,
-                                                           long long tlo, long long slo)
+                                                           long long tlo, long long slo,
+                                                           unsigned long long *__restrict__ fxacc,
+                                                           const float *__restrict__ fxmsum)
 {
     constexpr int WB = 32 * BPT;
     constexpr int RB = W * WB;
@@ -63,6 +139,8 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
     long long it = sk_start(c, total, gridDim.x);
     const long long end = sk_start(c + 1, total, gridDim.x);
     const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
+    FxScale fxs{};
+    if (fxacc) fxs = fx_scale(*fxmsum, eps2);
 
     while (it < end) {
         const int I = sym_row_of(it, nc, RC, nrb);
@@ -141,6 +219,9 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
                     fz = __shfl_sync(0xffffffffu, fz, from);
                 }
                 // lane l now holds the reaction on chunk body l from this warp
+                if (!COMP && fxacc) {
+                    fx_emit(fxacc, n, jb + lane, fx, fy, fz, fxs);
+                } else {
                 sF[0][wid][lane] = fx;
                 sF[1][wid][lane] = fy;
                 sF[2][wid][lane] = fz;
@@ -170,6 +251,7 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
                         }
                         spart[so] = make_float4(sx, sy, sz, 0.f);
                     }
+                }
                 }
             }
             if constexpr (COMP) {
@@ -212,7 +294,9 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__re
                                                               float eps2, float4 *__restrict__ tpart,
                                                               float4 *__restrict__ spart,
                                                               long long total, int nc, int nrb,
-                                                              long long, long long)
+                                                              long long, long long,
+                                                              unsigned long long *__restrict__ fxacc,
+                                                              const float *__restrict__ fxmsum)
 {
     constexpr int BPT = 2 * NP;
     constexpr int WB = 32 * BPT;
@@ -228,6 +312,8 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__re
     const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
     const f2 EPS2 = f2_pack(eps2, eps2);
     const f2 ZERO = f2_pack(0.f, 0.f);
+    FxScale fxs{};
+    if (fxacc) fxs = fx_scale(*fxmsum, eps2);
 
     while (it < end) {
         const int I = sym_row_of(it, nc, RC, nrb);
@@ -301,7 +387,9 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__re
                     fz = __shfl_sync(0xffffffffu, fz, from);
                 }
             }
-            if (!diag) {
+            if (!diag && fxacc) {
+                fx_emit(fxacc, n, jb + lane, fx, fy, fz, fxs);
+            } else if (!diag) {
                 sF[0][wid][lane] = fx;
                 sF[1][wid][lane] = fy;
                 sF[2][wid][lane] = fz;
@@ -341,10 +429,14 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__re
 // four ways it is a quarter as long.
 constexpr int kSymIntegBlock = 256;
 
+// fxacc != nullptr: the fixed-point source side; thread 0 of the quad adds
+// its total to the target-side sum in FP64 (one rounding) and, with
+// consume, zeroes the body's six accumulators for the next force launch.
 __global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
     const float4 *__restrict__ pos_old, float4 *__restrict__ pos_new, float4 *__restrict__ vel,
     const float4 *__restrict__ tpart, const float4 *__restrict__ spart, int n, int rb, int nc, int nrb,
-    long long total, int grid, float damping, float dt, int kick, float G, float4 *__restrict__ acc_out)
+    long long total, int grid, float damping, float dt, int kick, float G, float4 *__restrict__ acc_out,
+    unsigned long long *__restrict__ fxacc, const float *__restrict__ fxmsum, float eps2, int consume)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int i = (int)(t >> 2), q = (int)(t & 3);
@@ -362,12 +454,14 @@ __global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
             ay = __fadd_rn(ay, v4.y);
             az = __fadd_rn(az, v4.z);
         }
+        if (!fxacc) {
 #pragma unroll 4
-        for (int r = q; r < I; r += 4) {
-            const float4 v4 = spart[sym_soff(r, n, rb) + (i - (long long)(r + 1) * rb)];
-            ax = __fadd_rn(ax, v4.x);
-            ay = __fadd_rn(ay, v4.y);
-            az = __fadd_rn(az, v4.z);
+            for (int r = q; r < I; r += 4) {
+                const float4 v4 = spart[sym_soff(r, n, rb) + (i - (long long)(r + 1) * rb)];
+                ax = __fadd_rn(ax, v4.x);
+                ay = __fadd_rn(ay, v4.y);
+                az = __fadd_rn(az, v4.z);
+            }
         }
     }
     ax = __fadd_rn(ax, __shfl_xor_sync(0xffffffffu, ax, 1));
@@ -377,6 +471,20 @@ __global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
     ay = __fadd_rn(ay, __shfl_xor_sync(0xffffffffu, ay, 2));
     az = __fadd_rn(az, __shfl_xor_sync(0xffffffffu, az, 2));
     if (!live || q != 0) return;
+    if (fxacc) {
+        const FxScale f = fx_scale(*fxmsum, eps2);
+        const double lhi = __longlong_as_double((long long)(1023 + f.e - 61) << 52);
+        const double llo = __longlong_as_double((long long)(1023 + f.e - 83) << 52);
+        const long long nn = n;
+        unsigned long long *a = fxacc + i;
+        const double sx = (double)(long long)a[0] * lhi + (double)(long long)a[3 * nn] * llo;
+        const double sy = (double)(long long)a[nn] * lhi + (double)(long long)a[4 * nn] * llo;
+        const double sz = (double)(long long)a[2 * nn] * lhi + (double)(long long)a[5 * nn] * llo;
+        ax = (float)((double)ax + sx);
+        ay = (float)((double)ay + sy);
+        az = (float)((double)az + sz);
+        if (consume) a[0] = a[nn] = a[2 * nn] = a[3 * nn] = a[4 * nn] = a[5 * nn] = 0ull;
+    }
     if (acc_out) {
         acc_out[i] = make_float4(ax, ay, az, 0.f);
         return;
@@ -398,7 +506,7 @@ __global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
 }
 
 typedef void (*sym_kernel_t)(const float4 *, int, float, float4 *, float4 *, long long, int, int,
-                             long long, long long);
+                             long long, long long, unsigned long long *, const float *);
 
 // bpt > 0: scalar kernel with bpt bodies per lane (the third template
 // argument asks for that many resident CTAs per SM); bpt < 0: packed f32x2
@@ -430,8 +538,9 @@ static sym_kernel_t sym_kernel_for(int w, int bpt, int comp)
     return nullptr;
 }
 
-int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp)
+int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int fixed)
 {
+    if (comp) fixed = 0;  // the compensated kernel keeps its (hi, lo) triangular array
     if (warps == 0 && bpt == 0) {
         // plain: one-warp CTAs x 16 targets (row block 512); then 4 x 20
         // (2560), 8 x 24 (6144) while the source-side array is over budget.
@@ -442,9 +551,9 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp)
         const int(*shapes)[2] = comp ? compd : plain;
         const long long halves = comp ? 2 : 1;
         int s = 0;
-        while (s < 2 && halves * sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) *
-                                (long long)sizeof(float4) >
-                            kSymSpartBudget)
+        while (!fixed && s < 2 &&
+               halves * sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) * (long long)sizeof(float4) >
+                   kSymSpartBudget)
             ++s;
         warps = shapes[s][0];
         bpt = shapes[s][1];
@@ -483,33 +592,86 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp)
     if (p.total > 0 && grid > p.total) grid = p.total;
     p.grid = p.total > 0 ? (int)grid : 0;
     p.slots = p.total > 0 ? p.grid + p.nrb - 1 : 0;
-    p.spart_size = sym_spart_entries(n, p.rb);
+    p.fixed = fixed;
+    p.spart_size = fixed ? sym_fx_entries(n) : sym_spart_entries(n, p.rb);
     *pl = p;
     return NB_OK;
 }
 
+// Sum of |m| of bodies off[b] .. off[b+1] - 1 by block b, in a fixed order
+// (per-thread strided sums, then a tree): the record of a fixed-point plan.
+// off == nullptr: one system of n bodies.
+constexpr int kFxMassBlock = 1024;
+
+__global__ void __launch_bounds__(kFxMassBlock) fx_mass_kernel(const float4 *__restrict__ pos, int n,
+                                                               const int *__restrict__ off,
+                                                               float *__restrict__ out, int stride)
+{
+    __shared__ float red[kFxMassBlock];
+    const int lo = off ? off[blockIdx.x] : 0, hi = off ? off[blockIdx.x + 1] : n;
+    float sum = 0.f;
+    for (int i = lo + (int)threadIdx.x; i < hi; i += kFxMassBlock) sum += fabsf(pos[i].w);
+    red[threadIdx.x] = sum;
+    __syncthreads();
+    for (int w = kFxMassBlock / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[(size_t)blockIdx.x * stride] = red[0];
+}
+
+int sym_fx_prepare(const SymPlan &p, const float4 *pos, float4 *spart, cudaStream_t s)
+{
+    if (!p.fixed || p.n == 0) return NB_OK;
+    NB_CUDA(cudaMemsetAsync(spart, 0, 6 * sizeof(unsigned long long) * (size_t)p.n, s));
+    float *rec = reinterpret_cast<float *>(reinterpret_cast<unsigned long long *>(spart) + 6ll * p.n);
+    fx_mass_kernel<<<1, kFxMassBlock, 0, s>>>(pos, p.n, nullptr, rec, 1);
+    NB_LAUNCH_CHECK("fx_mass_kernel launch");
+    return NB_OK;
+}
+
+int sym_fx_masses(int nsys, const int *off, const float4 *pos, float *msum, cudaStream_t s)
+{
+    if (nsys <= 0) return NB_OK;
+    fx_mass_kernel<<<nsys, kFxMassBlock, 0, s>>>(pos, 0, off, msum, 1);
+    NB_LAUNCH_CHECK("fx_mass_kernel launch");
+    return NB_OK;
+}
+
+// The fixed-point accumulators and the record of a fixed plan's spart.
+static unsigned long long *fx_acc(const SymPlan &p, const float4 *spart)
+{
+    return p.fixed ? reinterpret_cast<unsigned long long *>(const_cast<float4 *>(spart)) : nullptr;
+}
+static const float *fx_rec(const SymPlan &p, const float4 *spart, const float *msum)
+{
+    if (!p.fixed) return nullptr;
+    return msum ? msum : reinterpret_cast<const float *>(reinterpret_cast<const unsigned long long *>(spart) + 6ll * p.n);
+}
+
 int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, float4 *spart,
-              cudaStream_t s)
+              cudaStream_t s, const float *msum)
 {
     if (p.total == 0) return NB_OK;
     sym_kernel_t k = sym_kernel_for(p.warps, p.bpt, p.comp);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "symmetric kernel shape not compiled");
     // lo blocks (compensated plans) follow the hi blocks
     const long long tlo = (long long)p.slots * p.rb, slo = p.spart_size;
-    k<<<p.grid, 32 * p.warps, 0, s>>>(pos, p.n, eps2, tpart, spart, p.total, p.nc, p.nrb, tlo, slo);
+    k<<<p.grid, 32 * p.warps, 0, s>>>(pos, p.n, eps2, tpart, spart, p.total, p.nc, p.nrb, tlo, slo,
+                                      fx_acc(p, spart), fx_rec(p, spart, msum));
     NB_LAUNCH_CHECK("sym_force_kernel launch");
     return NB_OK;
 }
 
 int sym_integrate(const SymPlan &p, const float4 *pos_old, float4 *pos_new, float4 *vel,
-                  const float4 *tpart, const float4 *spart, float damping, float dt, int kick,
-                  float G, float4 *acc_out, cudaStream_t s)
+                  const float4 *tpart, const float4 *spart, float eps2, float damping, float dt,
+                  int kick, float G, float4 *acc_out, cudaStream_t s, int consume, const float *msum)
 {
     if (p.n == 0) return NB_OK;
     const long long threads = 4ll * p.n;  // a quad of threads per body
     sym_integrate_kernel<<<(unsigned)((threads + kSymIntegBlock - 1) / kSymIntegBlock), kSymIntegBlock, 0, s>>>(
         pos_old, pos_new, vel, tpart, spart, p.n, p.rb, p.nc, p.nrb, p.total, p.grid, damping, dt, kick,
-        G, acc_out);
+        G, acc_out, fx_acc(p, spart), fx_rec(p, spart, msum), eps2, consume);
     NB_LAUNCH_CHECK("sym_integrate_kernel launch");
     return NB_OK;
 }
