@@ -161,10 +161,10 @@ def measured_peaks():
 
 def integrate_bytes(n, algo, plan):
     """Bytes the integrate kernel has to move per launch: the state read and
-    written (pos and vel, 64 B per body) plus every partial-sum entry it adds,
-    16 B each: the target-side slots of the CTAs that worked on the body's
-    block and, on the symmetric path, one source-side entry per earlier row
-    block."""
+    written (pos and vel, 64 B per body) plus every target-side partial entry
+    it adds (16 B each: the slots of the CTAs that worked on the body's
+    block) and, on the symmetric path, the body's fixed-point source-side
+    accumulators (six 64-bit words read and zeroed: 96 B)."""
     grid, rb = plan["grid"], plan["tbsize"]
     nblk = (n + rb - 1) // rb
     if algo == "sym":
@@ -186,9 +186,8 @@ def integrate_bytes(n, algo, plan):
     for b in range(nblk):
         rows = min(rb, n - b * rb)
         entries += (owner(first(b + 1) - 1) - owner(first(b)) + 1) * rows
-        if algo == "sym":
-            entries += b * rows  # source-side rows 0..b-1
-    return 64.0 * n + 16.0 * entries
+    source_side = 96.0 * n if algo == "sym" else 0.0
+    return 64.0 * n + 16.0 * entries + source_side
 
 
 def committed_traffic():
@@ -593,8 +592,9 @@ def run_ours(args):
                                     "bytes_moved_per_launch": integ_moved,
                                     "moved_rate_GB_per_s": integ_moved / integ_avg_s / 1e9,
                                     "note": f"algorithmic: {INTEGRATOR_BYTES_PER_BODY} B/body (pos, vel, acc "
-                                            "read; pos, vel written); moved: the state plus every partial "
-                                            "entry the kernel adds (16 B each)"},
+                                            "read; pos, vel written); moved: the state, every target-side "
+                                            "partial entry the kernel adds (16 B each) and, symmetric, the "
+                                            "fixed-point source-side words read and zeroed (96 B/body)"},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * state_bytes,
                     "d2h_bytes_per_step": state_bytes,
                     "through_task": {"value": e2e_task_val, "unit": UNIT,

@@ -89,16 +89,49 @@ def test_sym_adjoint_matches_directed_adjoint(cuda):
         assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("n,shape", [(65536, (32, 16)), (1048576, (128, 20)), (1024, (32, 4)),
+@pytest.mark.parametrize("n,shape", [(65536, (32, 16)), (1048576, (32, 16)), (1024, (32, 4)),
                                      (4096, (32, 8)), (16384, (32, 16))])
 def test_sym_default_shape(cuda, n, shape):
-    """One-warp CTAs x 16 targets unless the source-side array (about
-    N^2 / (2 rb) float4) would pass 8 GiB, then 4 warps x 20 targets; small
-    systems drop to 8 or 4 targets per lane to keep four (row, chunk) items
-    per SM."""
+    """One-warp CTAs x 16 targets at any size (the fixed-point source side
+    takes 48 B per body whatever the row block); small systems drop to 8 or
+    4 targets per lane to keep four (row, chunk) items per SM."""
     with NBodySystem(n, "f32", "sym") as s:
         info = s.plan_info()
     assert (info["block"], info["bpt"]) == shape
+
+
+@pytest.mark.parametrize("n", [4096, 65536])
+def test_sym_fixed_point_source_side_is_exact_and_deterministic(cuda, n):
+    """The source side summed in fixed point: accelerations of every shape
+    within 2e-5 of the FP64 oracle; a second context (a different CTA order
+    at run time) gives the same bits; so do two runs of one context, and
+    steps after nb_set_state with heavier masses (a new scale record)."""
+    p, _ = ics.plummer(n, seed=n + 3)
+    p32 = ics.f32(p)
+    v = np.zeros_like(p32)
+    tidx = np.random.default_rng(2).choice(n, 256, replace=False).astype(np.int32)
+    ref = oracle.accel_subset_f64(p32.astype(np.float64), tidx, float(np.float32(1e-4)))
+    outs = []
+    for shape in [(32, 16), (32, 16), (64, 16), (128, 20), (256, 24)]:
+        with NBodySystem(n, "f32", "sym", eps2=np.float32(1e-4), block=shape[0], bpt=shape[1]) as s:
+            s.set_state(p32, v)
+            a = s.accel()
+            again = s.accel()
+            assert a.tobytes() == again.tobytes()
+            outs.append(a)
+        d = np.linalg.norm(a[tidx].astype(np.float64) - ref, axis=1)
+        w = np.linalg.norm(ref, axis=1)
+        assert (d <= 2e-5 * (w + w.mean())).all(), shape
+    assert outs[0].tobytes() == outs[1].tobytes()
+    heavy = p32.copy()
+    heavy[:, 3] *= 1e6
+    with NBodySystem(n, "f32", "sym", eps2=np.float32(1e-4)) as s:
+        s.set_state(heavy, v)
+        a = s.accel()
+    ref_h = oracle.accel_subset_f64(heavy.astype(np.float64), tidx, float(np.float32(1e-4)))
+    d = np.linalg.norm(a[tidx].astype(np.float64) - ref_h, axis=1)
+    w = np.linalg.norm(ref_h, axis=1)
+    assert (d <= 2e-5 * (w + w.mean())).all()
 
 
 F64_SYM = ["sym", "sym64"]  # float-float pair arithmetic; FP64 arithmetic throughout
