@@ -37,6 +37,11 @@ struct BatchRecord {
 
 struct nb_ctx {
     nb_params p;
+    // shard contexts (nb_create_shard): every body's state in host memory,
+    // two position buffers, the shard's range and its steps so far
+    int rank = 0, nranks = 1, lo = 0, hi = 0, cur = 0, steps = 0;
+    std::vector<double> x[2], v;
+    std::vector<float> xf[2], vf;
 };
 
 struct nb_batch {
@@ -137,6 +142,103 @@ int nb_run_host(nb_ctx *c, const void *pos, const void *vel, int loops, int out_
         for (int k = 0; k < 4; ++k) timings[k] = 1.0 + k;  // total, kernel, copy-in, copy-out
     return NB_OK;
 }
+
+// ---- shard contexts of the multi-GPU task (host memory stands for each
+// "device"; planted failures: n == 5 refuses rank 1 at creation, n == 7 fails
+// rank 1's fifth step) ----
+int nb_create_shard(const nb_params *p, int rank, int nranks, nb_ctx **out)
+{
+    *out = nullptr;
+    if (p->n == 5 && rank == 1) {
+        g_err = "mock: shard 1 of a 5-body system is refused";
+        return NB_ERR_INVALID;
+    }
+    nb_ctx *c = new nb_ctx{*p};
+    c->rank = rank;
+    c->nranks = nranks;
+    const int q = p->n / nranks, r = p->n % nranks;
+    c->lo = rank < r ? rank * (q + 1) : rank * q + r;
+    c->hi = c->lo + q + (rank < r ? 1 : 0);
+    *out = c;
+    return NB_OK;
+}
+
+int nb_shard_info(nb_ctx *c, int *info4)
+{
+    info4[0] = c->lo;
+    info4[1] = c->hi - c->lo;
+    info4[2] = c->rank;
+    info4[3] = c->nranks;
+    return NB_OK;
+}
+
+int nb_set_state(nb_ctx *c, const void *pos, const void *vel, int, void *)
+{
+    const size_t m = 4 * (size_t)c->p.n;
+    if (c->p.precision == NB_F64) {
+        c->x[0].assign((const double *)pos, (const double *)pos + m);
+        c->x[1] = c->x[0];
+        c->v.assign((const double *)vel, (const double *)vel + m);
+    } else {
+        c->xf[0].assign((const float *)pos, (const float *)pos + m);
+        c->xf[1] = c->xf[0];
+        c->vf.assign((const float *)vel, (const float *)vel + m);
+    }
+    c->cur = 0;
+    return NB_OK;
+}
+
+// One step of the shard's range: the oracle's step of every body, of which
+// the range is kept (a target's result does not depend on the others'
+// velocities or on the partition)
+int nb_step(nb_ctx *c, int steps, void *)
+{
+    if (steps != 1) {
+        g_err = "mock: a shard steps once per call";
+        return NB_ERR_INVALID;
+    }
+    if (c->p.n == 7 && c->rank == 1 && ++c->steps == 5) {
+        g_err = "mock: planted failure of shard 1's fifth step";
+        return NB_ERR_CUDA;
+    }
+    const nb_params &p = c->p;
+    const size_t a = 4 * (size_t)c->lo, b = 4 * (size_t)c->hi;
+    if (p.precision == NB_F64) {
+        std::vector<double> x = c->x[c->cur], v = c->v;
+        orc_step_f64(p.n, x.data(), v.data(), p.eps2, p.damping, p.dt, 1, p.kick, p.G, 1);
+        std::copy(x.begin() + a, x.begin() + b, c->x[c->cur ^ 1].begin() + a);
+        std::copy(v.begin() + a, v.begin() + b, c->v.begin() + a);
+    } else {
+        std::vector<float> x = c->xf[c->cur], v = c->vf;
+        orc_step_f32(p.n, x.data(), v.data(), (float)p.eps2, (float)p.damping, (float)p.dt, 1, p.kick,
+                     (float)p.G, 1);
+        std::copy(x.begin() + a, x.begin() + b, c->xf[c->cur ^ 1].begin() + a);
+        std::copy(v.begin() + a, v.begin() + b, c->vf.begin() + a);
+    }
+    c->cur ^= 1;
+    return NB_OK;
+}
+
+int nb_state_ptrs(nb_ctx *c, void **pos_dev, void **vel_dev)
+{
+    const bool f64 = c->p.precision == NB_F64;
+    if (pos_dev) *pos_dev = f64 ? (void *)c->x[c->cur].data() : (void *)c->xf[c->cur].data();
+    if (vel_dev) *vel_dev = f64 ? (void *)c->v.data() : (void *)c->vf.data();
+    return NB_OK;
+}
+
+cudaError_t cudaMemcpyPeerAsync(void *dst, int, const void *src, int, size_t bytes, cudaStream_t)
+{
+    std::memcpy(dst, src, bytes);
+    return cudaSuccess;
+}
+cudaError_t cudaMemcpyAsync(void *dst, const void *src, size_t bytes, cudaMemcpyKind, cudaStream_t)
+{
+    std::memcpy(dst, src, bytes);
+    return cudaSuccess;
+}
+cudaError_t cudaStreamSynchronize(cudaStream_t) { return cudaSuccess; }
+const char *cudaGetErrorString(cudaError_t) { return "mock CUDA error"; }
 
 // ---- the timing events and the batch calls of a task group ----
 cudaError_t cudaEventCreate(cudaEvent_t *e)

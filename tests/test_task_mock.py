@@ -26,7 +26,8 @@ def mock_task(tmp_path_factory):
     cuda_home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
     odir = os.path.join(REPO, "oracle")
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-shared", "-o", out,
-           os.path.join(REPO, "utc_gb300", "task", "body_task_gb300.cc"), os.path.join(REPO, "tests", "mock_abi.cc"),
+           os.path.join(REPO, "utc_gb300", "task", "body_task_gb300.cc"),
+           os.path.join(REPO, "utc_gb300", "task", "body_task_mgpu_gb300.cc"), os.path.join(REPO, "tests", "mock_abi.cc"),
            "-I", os.path.join(REPO, "include"), "-I", os.path.join(REPO, "utc_gb300", "task"), "-I", odir,
            "-I", os.path.join(cuda_home, "include"), "-L", odir, "-loracle", "-Wl,-rpath," + odir, "-lpthread",
            # bind the library's calls to its own mock definitions even when a real CUDA runtime (torch's)
@@ -40,6 +41,9 @@ def mock_task(tmp_path_factory):
     lib.nbt_run_f32.argtypes = [C.c_uint, C.c_float, C.c_float, vp, vp, vp, I, I, I, C.c_float, vp, I, I, I]
     lib.mock_fake_stream.restype = vp
     lib.mock_record.argtypes = [C.POINTER(vp), vp, vp]
+    lib.nbt_mgpu_run_f32.argtypes = [C.c_uint, C.c_float, C.c_float, vp, vp, vp, I, I, I, C.c_float, vp, I, I]
+    lib.nbt_mgpu_run_f64.argtypes = [C.c_uint, D, D, vp, vp, vp, I, I, I, D, vp, I, I]
+    lib.path = out
     return lib
 
 
@@ -183,3 +187,65 @@ def test_group_refuses_a_null_outbuffer(mock_task):
        8, 4, 2, 30.0, st.ctypes.data, None)
     assert list(st) == [1, 1] and (good == -7.0).all()
     assert batch_record(mock_task)[0][0] == 0
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("nthreads", [1, 3, 4])
+def test_mgpu_task_on_the_mock(mock_task, dtype, nthreads):
+    """The multi-GPU task (BodySystemMGPU_GB300<T>) with `nthreads` threads on
+    the mock: each thread steps its own range of targets (the reference's
+    split, uneven here), pushes it into the other threads' position buffers
+    after every step and writes its range of each frame; the frames equal
+    the oracle's run of the whole system bit for bit, the caller's arrays
+    are not updated and every thread fills its row of runtime."""
+    n, loops, oi = 101, 12, 4
+    pos, vel = oracle.randomize(1, n, dtype)
+    pos0, vel0 = pos.copy(), vel.copy()
+    eps2, damp, dt = 0.01, 0.999, 0.005
+    frames = np.full((loops // oi + 1, n, 4), -7.0, dtype)
+    rt = np.full((nthreads, 4), -1.0)
+    run = mock_task.nbt_mgpu_run_f64 if dtype == np.float64 else mock_task.nbt_mgpu_run_f32
+    rc = run(n, eps2, damp, pos.ctypes.data, vel.ctypes.data, rt.ctypes.data, loops, oi, 128, dt,
+             frames.ctypes.data, nthreads, -1)
+    assert rc == 0
+    assert np.array_equal(pos, pos0) and np.array_equal(vel, vel0)
+    p, v = pos0, vel0
+    for f in range(loops // oi):
+        p, v = oracle.step(p, v, dtype(eps2), dtype(damp), dtype(dt), oi)
+        assert np.array_equal(frames[f], p), f
+    assert (frames[-1] == -7.0).all()
+    assert (rt >= 0).all()
+
+
+def test_mgpu_task_failures_end_every_thread(mock_task):
+    """A thread whose shard cannot be made (n = 5: shard 1 refused), or whose
+    fifth step fails (n = 7), ends the run for every thread at the same
+    barrier: the call returns the failing status instead of hanging, and a
+    later run of the same task object works.  Run in a child process with a
+    time limit, so that a deadlock fails the test."""
+    import sys
+
+    code = f"""
+import ctypes as C, numpy as np
+lib = C.CDLL({mock_task.path!r})
+vp, I = C.c_void_p, C.c_int
+lib.nbt_mgpu_run_f32.argtypes = [C.c_uint, C.c_float, C.c_float, vp, vp, vp, I, I, I, C.c_float, vp, I, I]
+out = []
+for n in (5, 7, 8):
+    pos = np.zeros((n, 4), np.float32); pos[:, 0] = np.arange(n); pos[:, 3] = 1
+    vel = np.zeros((n, 4), np.float32)
+    frames = np.full((4, n, 4), -7.0, np.float32)
+    rt = np.zeros((3, 4))
+    rc = lib.nbt_mgpu_run_f32(n, 0.01, 1.0, pos.ctypes.data, vel.ctypes.data, rt.ctypes.data, 9, 3, 128, 0.001,
+                              frames.ctypes.data, 3, -1)
+    out.append((rc, bool((frames[0] == -7).all()), bool((frames[1] == -7).all())))
+print(out)
+"""
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    res = eval(r.stdout.strip().splitlines()[-1])
+    # n=5: refused at set-up, nothing written; n=7: the first frame (step 3)
+    # is out, the failure at step 5 stops the second; n=8 runs clean
+    assert res[0] == (1, True, True)
+    assert res[1][0] == 2 and res[1][1] is False and res[1][2] is True
+    assert res[2] == (0, False, False)

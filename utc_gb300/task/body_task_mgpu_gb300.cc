@@ -154,3 +154,39 @@ void BodySystemMGPU_GB300<T>::runImpl(double runtime[][4], int loops, int outInt
 
 template class BodySystemMGPU_GB300<float>;
 template class BodySystemMGPU_GB300<double>;
+
+// ---------------------------------------------------------------------------
+// flat entry points, so that non-C++ callers (the test harness) can drive the
+// multi-GPU task as the app does: `nthreads` threads, runtime[nthreads][4]
+// ---------------------------------------------------------------------------
+template <typename T>
+static int mgpu_run(unsigned n, T eps2, T damping, T *pos, T *vel, double *runtime, int loops, int outInterval,
+                    int blocksize, T dt, T *outbuffer, int nthreads, int algo)
+{
+    iUtc::Task<BodySystemMGPU_GB300<T>> nbody(iUtc::ProcList(nthreads, 0), iUtc::TaskType::gpu_task);
+    if (algo >= 0) nbody.userObject()->setAlgo(algo);
+    nbody.init(n, eps2, damping, pos, vel);
+    nbody.run(reinterpret_cast<double(*)[4]>(runtime), loops, outInterval, blocksize, dt, outbuffer,
+              iUtc::MemType::pageable);
+    nbody.wait();
+    return nbody.userObject()->lastStatus();
+}
+
+extern "C" {
+
+int nbt_mgpu_run_f32(unsigned n, float eps2, float damping, float *pos, float *vel, double *runtime, int loops,
+                     int outInterval, int blocksize, float dt, float *outbuffer, int nthreads, int algo)
+{
+    return mgpu_run<float>(n, eps2, damping, pos, vel, runtime, loops, outInterval, blocksize, dt, outbuffer,
+                           nthreads, algo);
+}
+
+int nbt_mgpu_run_f64(unsigned n, double eps2, double damping, double *pos, double *vel, double *runtime,
+                     int loops, int outInterval, int blocksize, double dt, double *outbuffer, int nthreads,
+                     int algo)
+{
+    return mgpu_run<double>(n, eps2, damping, pos, vel, runtime, loops, outInterval, blocksize, dt, outbuffer,
+                            nthreads, algo);
+}
+
+}  // extern "C"
