@@ -116,8 +116,22 @@ typedef struct nb_params {
     int bpt;          /* fast kernel bodies per thread (0 = tuned/auto) */
     int ctas_per_sm;  /* fast kernel persistent CTAs per SM (0 = occupancy) */
     int memtype;      /* nb_memtype, for nb_run_host staging */
-    int reserved[4];
+    int source_side;  /* nb_source_side: how NB_ALGO_SYM (NB_F32) sums the
+                         reactions on the source bodies */
+    int reserved[3];
 } nb_params;
+
+/* Source side of the symmetric FP32 kernel (nb_params.source_side).  Each
+ * row block's reactions on the bodies after it are either stored in a
+ * triangular array, about N^2 / (2 rb) float4 (67 MB at N = 65536, 3.4 GB at
+ * N = 1M with the shapes chosen there), and summed by the integrator in row
+ * order; or added at once into per-body 64-bit fixed-point accumulators with
+ * integer atomics, 48 B per body, summed essentially exactly and still
+ * deterministic (integer sums do not depend on their order), but measured
+ * 2-10 % slower on GB300.  NB_SOURCE_AUTO takes the triangular array unless
+ * it would pass 32 GiB at the largest row block (N above about 5e6).  Both
+ * are within the same tolerances of the FP64 oracle. */
+typedef enum { NB_SOURCE_AUTO = 0, NB_SOURCE_TRIANGULAR = 1, NB_SOURCE_FIXED = 2 } nb_source_side;
 
 typedef struct nb_ctx nb_ctx;
 

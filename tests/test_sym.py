@@ -89,22 +89,28 @@ def test_sym_adjoint_matches_directed_adjoint(cuda):
         assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("n,shape", [(65536, (32, 16)), (1048576, (32, 16)), (1024, (32, 4)),
+@pytest.mark.parametrize("n,shape", [(65536, (32, 16)), (1048576, (128, 20)), (1024, (32, 4)),
                                      (4096, (32, 8)), (16384, (32, 16))])
 def test_sym_default_shape(cuda, n, shape):
-    """One-warp CTAs x 16 targets at any size (the fixed-point source side
-    takes 48 B per body whatever the row block); small systems drop to 8 or
-    4 targets per lane to keep four (row, chunk) items per SM."""
+    """One-warp CTAs x 16 targets unless the triangular source-side array
+    (about N^2 / (2 rb) float4) would pass 8 GiB, then 4 warps x 20 targets;
+    small systems drop to 8 or 4 targets per lane to keep four (row, chunk)
+    items per SM.  With the fixed-point source side: one warp x 16 at any
+    size (48 B per body whatever the row block)."""
     with NBodySystem(n, "f32", "sym") as s:
         info = s.plan_info()
     assert (info["block"], info["bpt"]) == shape
+    with NBodySystem(n, "f32", "sym", source_side="fixed") as s:
+        info = s.plan_info()
+    assert (info["block"], info["bpt"]) == (32, min(shape[1], 16))
 
 
 @pytest.mark.parametrize("n", [4096, 65536])
 def test_sym_fixed_point_source_side_is_exact_and_deterministic(cuda, n):
-    """The source side summed in fixed point: accelerations of every shape
-    within 2e-5 of the FP64 oracle; a second context (a different CTA order
-    at run time) gives the same bits; so do two runs of one context, and
+    """The source side summed in fixed point (NB_SOURCE_FIXED): accelerations
+    of every fixed-point shape within 2e-5 of the FP64 oracle and closer to
+    it than the triangular array's; a second context (a different CTA order
+    at run time) gives the same bits; so do two calls of one context, and
     steps after nb_set_state with heavier masses (a new scale record)."""
     p, _ = ics.plummer(n, seed=n + 3)
     p32 = ics.f32(p)
@@ -112,8 +118,9 @@ def test_sym_fixed_point_source_side_is_exact_and_deterministic(cuda, n):
     tidx = np.random.default_rng(2).choice(n, 256, replace=False).astype(np.int32)
     ref = oracle.accel_subset_f64(p32.astype(np.float64), tidx, float(np.float32(1e-4)))
     outs = []
-    for shape in [(32, 16), (32, 16), (64, 16), (128, 20), (256, 24)]:
-        with NBodySystem(n, "f32", "sym", eps2=np.float32(1e-4), block=shape[0], bpt=shape[1]) as s:
+    for shape in [(32, 16), (32, 16), (32, 8), (32, 4)]:
+        with NBodySystem(n, "f32", "sym", eps2=np.float32(1e-4), block=shape[0], bpt=shape[1],
+                         source_side="fixed") as s:
             s.set_state(p32, v)
             a = s.accel()
             again = s.accel()
@@ -123,9 +130,16 @@ def test_sym_fixed_point_source_side_is_exact_and_deterministic(cuda, n):
         w = np.linalg.norm(ref, axis=1)
         assert (d <= 2e-5 * (w + w.mean())).all(), shape
     assert outs[0].tobytes() == outs[1].tobytes()
+    with NBodySystem(n, "f32", "sym", eps2=np.float32(1e-4), source_side="triangular") as s:
+        s.set_state(p32, v)
+        tri = s.accel()
+    w = np.linalg.norm(ref, axis=1)
+    e_fx = np.linalg.norm(outs[0][tidx].astype(np.float64) - ref, axis=1) / w
+    e_tri = np.linalg.norm(tri[tidx].astype(np.float64) - ref, axis=1) / w
+    assert np.median(e_fx) <= np.median(e_tri)
     heavy = p32.copy()
     heavy[:, 3] *= 1e6
-    with NBodySystem(n, "f32", "sym", eps2=np.float32(1e-4)) as s:
+    with NBodySystem(n, "f32", "sym", eps2=np.float32(1e-4), source_side="fixed") as s:
         s.set_state(heavy, v)
         a = s.accel()
     ref_h = oracle.accel_subset_f64(heavy.astype(np.float64), tidx, float(np.float32(1e-4)))
@@ -292,3 +306,43 @@ def test_gpu_scale_positions_after_100_steps_vs_fp64(cuda):
             got, _ = s.get_state()
         rel = np.linalg.norm(got[:, :3].astype(np.float64) - want[:, :3], axis=1) / scale
         assert rel.max() <= 1e-5, (algo, rel.max())
+
+
+def test_sym_fixed_point_steps_and_new_eps2(cuda):
+    """Steps with the fixed-point source side: positions after 40 steps within
+    1e-5 (|x| + 0.1) of the FP64 oracle, bitwise reruns through the captured
+    graph and step by step, and nb_set_params to a new eps2 (its scale is
+    rewritten before the next force launch) equal to a fresh context made
+    with that eps2."""
+    n, steps = 3000, 40
+    p, v = ics.plummer(n, seed=17)
+    p32, v32 = ics.f32(p), ics.f32(v)
+    kw = dict(kick="physical", damping=1.0, dt=np.float32(1e-4), source_side="fixed")
+    with NBodySystem(n, "f32", "sym", eps2=np.float32(1e-4), **kw) as s:
+        s.set_state(p32, v32)
+        s.step(steps)
+        got, _ = s.get_state()
+        s.set_state(p32, v32)
+        for _ in range(steps):
+            s.step(1)
+        again, _ = s.get_state()
+        s.set_params(np.float32(1e-2), 1.0, np.float32(1e-4))
+        s.set_state(p32, v32)
+        s.step(3)
+        newe, _ = s.get_state()
+        s.set_state(p32, v32)
+        s.set_params(np.float32(1e-3), 1.0, np.float32(1e-4))
+        s.step(3)
+        mid, _ = s.get_state()
+    with NBodySystem(n, "f32", "sym", eps2=np.float32(1e-3), **kw) as s:
+        s.set_state(p32, v32)
+        s.step(3)
+        fresh, _ = s.get_state()
+    want, _ = oracle.step(p32.astype(np.float64), v32.astype(np.float64), float(np.float32(1e-4)), 1.0,
+                          float(np.float32(1e-4)), steps, kick_mode=oracle.KICK_PHYSICAL)
+    rel = np.linalg.norm(got[:, :3].astype(np.float64) - want[:, :3], axis=1) / (
+        np.linalg.norm(want[:, :3], axis=1) + 0.1)
+    assert rel.max() <= 1e-5
+    assert got.tobytes() == again.tobytes()
+    assert mid.tobytes() == fresh.tobytes()
+    assert newe.tobytes() != mid.tobytes()

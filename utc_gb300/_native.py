@@ -21,6 +21,7 @@ NB_ALGO_FAST, NB_ALGO_EXACT, NB_ALGO_SYM, NB_ALGO_SYM_FP64 = 0, 1, 2, 3
 NB_KICK_REFERENCE, NB_KICK_PHYSICAL = 0, 1
 NB_HOST, NB_DEVICE = 0, 1
 NB_MEM_PAGEABLE, NB_MEM_PINNED, NB_MEM_UNIFIED = 0, 1, 2
+NB_SOURCE_AUTO, NB_SOURCE_TRIANGULAR, NB_SOURCE_FIXED = 0, 1, 2
 
 
 class NbParams(C.Structure):
@@ -28,7 +29,7 @@ class NbParams(C.Structure):
         ("n", C.c_int), ("precision", C.c_int), ("algo", C.c_int), ("kick", C.c_int),
         ("eps2", C.c_double), ("damping", C.c_double), ("dt", C.c_double), ("G", C.c_double),
         ("block", C.c_int), ("bpt", C.c_int), ("ctas_per_sm", C.c_int), ("memtype", C.c_int),
-        ("reserved", C.c_int * 4),
+        ("source_side", C.c_int), ("reserved", C.c_int * 3),
     ]
 
 

@@ -104,6 +104,8 @@ struct nb_ctx {
     // updates targets [shard_lo, shard_hi) of all n bodies; shard_count 1 is
     // a whole system
     int shard_rank = 0, shard_count = 1, shard_lo = 0, shard_hi = 0;
+    // fixed-point source side: eps2 changed since its scale was recorded
+    bool fx_dirty = false;
     // adjoint: checkpoints of the last nb_adj_forward and reverse-pass buffers
     struct Adj {
         int steps = 0, every = 0, nckpt = 0;
@@ -351,14 +353,14 @@ int nb_create(const nb_params *p, nb_ctx **out)
         if (uses_sym(c) || comp_sym(c)) {
             const size_t halves = comp_sym(c) ? 2 : 1;  // compensated: hi and lo blocks
             if ((st = nb::sym_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan,
-                                   comp_sym(c) ? 1 : 0, comp_sym(c) ? 0 : 1)) ||
+                                   comp_sym(c) ? 1 : 0, comp_sym(c) ? NB_SOURCE_AUTO : p->source_side)) ||
                 (st = dev_alloc((void **)&c->sym_t,
                                 halves * c->splan.slots * c->splan.rb * sizeof(float4),
                                 "symmetric scratch allocation")) ||
                 (st = dev_alloc((void **)&c->sym_s, halves * c->splan.spart_size * sizeof(float4),
-                                comp_sym(c) ? "symmetric source-side array (about N^2/(2 rb) entries; NB_ALGO_FAST "
-                                              "needs O(N) scratch)"
-                                            : "symmetric source-side accumulators (48 B per body)"))) {
+                                c->splan.fixed ? "symmetric source-side accumulators (48 B per body)"
+                                               : "symmetric source-side array (about N^2/(2 rb) entries; "
+                                                 "NB_SOURCE_FIXED or NB_ALGO_FAST need O(N) scratch)"))) {
                 free_ctx(c);
                 return st;
             }
@@ -436,6 +438,17 @@ static int refuse_shard(const nb_ctx *c, const char *what)
     return NB_OK;
 }
 
+// A fixed-point source side whose eps2 changed gets its scale rewritten on
+// the stream of the next stepping call, before that call's force launches
+// (and before any graph capture, which then does not contain it).
+static int fx_refresh(nb_ctx *c, cudaStream_t s)
+{
+    if (!c->fx_dirty || !c->has_state) return NB_OK;
+    int st = nb::sym_fx_rescale(c->splan, c->sym_s, (float)c->p.eps2, s);
+    if (!st) c->fx_dirty = false;
+    return st;
+}
+
 int nb_destroy(nb_ctx *c)
 {
     if (!c) return NB_OK;
@@ -474,7 +487,8 @@ int nb_set_state(nb_ctx *c, const void *pos, const void *vel, int where, void *s
         // symmetric contexts: zeroed source-side accumulators and the sum of
         // |m| their scale comes from
         if (uses_sym(c)) {
-            int st = nb::sym_fx_prepare(c->splan, (const float4 *)c->pos[0], c->sym_s, s);
+            int st = nb::sym_fx_prepare(c->splan, (const float4 *)c->pos[0], c->sym_s, (float)c->p.eps2, s);
+            if (!st) c->fx_dirty = false;
             if (st) return st;
         }
         if (where == NB_HOST) NB_CUDA(cudaStreamSynchronize(s));
@@ -571,11 +585,11 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
         if (!st && acc_keep)
             st = nb::sym_integrate(c->splan, (const float4 *)po, nullptr, nullptr, c->sym_t, c->sym_s,
-                                   (float)p.eps2, (float)p.damping, (float)p.dt, p.kick, (float)p.G, acc_keep,
+                                   (float)p.damping, (float)p.dt, p.kick, (float)p.G, acc_keep,
                                    s, 0);
         if (!st)
             st = nb::sym_integrate(c->splan, (const float4 *)po, (float4 *)pn, (float4 *)c->vel,
-                                   c->sym_t, c->sym_s, (float)p.eps2, (float)p.damping, (float)p.dt, p.kick,
+                                   c->sym_t, c->sym_s, (float)p.damping, (float)p.dt, p.kick,
                                    (float)p.G, (float4 *)acc_out, s);
     } else {
         st = nb::fast_force(c->plan, (const float4 *)po, (float)p.eps2, c->partial, s);
@@ -643,6 +657,7 @@ int nb_step(nb_ctx *c, int steps, void *stream)
                                          "positions are exchanged between steps)");
     cudaStream_t s = (cudaStream_t)stream;
     int st;
+    if ((st = fx_refresh(c, s))) return st;
     // the legacy default stream cannot be captured: launch step by step there,
     // and also on a stream the caller is capturing into a graph of its own
     // (the launches then go into the caller's graph)
@@ -676,6 +691,7 @@ int nb_set_params(nb_ctx *c, double eps2, double damping, double dt, double G)
             nb::graph_exec_destroy(g);
             g = nullptr;
         }
+    if (c->splan.fixed && eps2 != c->p.eps2) c->fx_dirty = true;  // rescaled before the next force launch
     c->p.eps2 = eps2;
     c->p.damping = damping;
     c->p.dt = dt;
@@ -694,6 +710,7 @@ int nb_step_timed(nb_ctx *c, int steps, float *ms_force, float *ms_integrate, vo
     if (!ms_force || !ms_integrate) return set_error(NB_ERR_INVALID, "ms outputs are NULL");
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
     cudaStream_t s = (cudaStream_t)stream;
+    if (int st = fx_refresh(c, s)) return st;
     const size_t need = 3 * (size_t)steps;
     while (c->events.size() < need) {
         cudaEvent_t e;
@@ -725,6 +742,7 @@ int nb_accel(nb_ctx *c, void *acc_dev, void *stream)
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
     if (c->p.n == 0) return NB_OK;
     if (!acc_dev) return set_error(NB_ERR_INVALID, "acc_dev is NULL");
+    if (int st = fx_refresh(c, (cudaStream_t)stream)) return st;
     return step_once(c, (cudaStream_t)stream, acc_dev);
 }
 
@@ -906,6 +924,7 @@ int nb_adj_forward(nb_ctx *c, int steps, int ckpt_every, void *stream, unsigned 
     int st = adj_reserve(c, nckpt, ckpt_every);
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
+    if ((st = fx_refresh(c, s))) return st;
     const size_t n = (size_t)c->p.n;
     auto &A = c->adj;
     const nb_params &p = c->p;
@@ -990,10 +1009,10 @@ int nb_adj_backward(nb_ctx *c, unsigned long long generation, const void *gx_T, 
             if (uses_sym(c)) {
                 if ((st2 = nb::sym_force(c->splan, xk, eps2, c->sym_t, c->sym_s, rs))) return st2;
                 if (p.kick == NB_KICK_REFERENCE &&
-                    (st2 = nb::sym_integrate(c->splan, xk, nullptr, nullptr, c->sym_t, c->sym_s, eps2, D, dt,
+                    (st2 = nb::sym_integrate(c->splan, xk, nullptr, nullptr, c->sym_t, c->sym_s, D, dt,
                                              p.kick, G, sa + (size_t)k * n, rs, 0)))
                     return st2;
-                if ((st2 = nb::sym_integrate(c->splan, xk, xn, vt, c->sym_t, c->sym_s, eps2, D, dt, p.kick, G,
+                if ((st2 = nb::sym_integrate(c->splan, xk, xn, vt, c->sym_t, c->sym_s, D, dt, p.kick, G,
                                              nullptr, rs)))
                     return st2;
                 continue;
@@ -1082,6 +1101,7 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
     if (!c->has_state) return set_error(NB_ERR_STATE, "no state loaded");
     if (reps < 1) reps = 3;
     cudaStream_t s = (cudaStream_t)stream;
+    if (int fst = fx_refresh(c, s)) return fst;
     const nb_params &p = c->p;
     const bool symm = uses_sym(c) || comp_sym(c) || f64_sym(c);
     const bool fast = !symm && (uses_fast(c) || is_comp(c));
@@ -1117,7 +1137,8 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
         if (symm) {
             if (ff_sym(c)) return nb::symff_plan(p.n, a, b, c->device, sp);
             if (f64_sym(c)) return nb::sym64_plan(p.n, a, b, c->device, sp);
-            return nb::sym_plan(p.n, a, b, c->device, sp, comp_sym(c) ? 1 : 0, comp_sym(c) ? 0 : 1);
+            return nb::sym_plan(p.n, a, b, c->device, sp, comp_sym(c) ? 1 : 0,
+                                comp_sym(c) ? NB_SOURCE_AUTO : (c->splan.fixed ? NB_SOURCE_FIXED : NB_SOURCE_TRIANGULAR));
         }
         return nb::fast_plan(p.n, a, b, p.ctas_per_sm, c->device, fp, is_comp(c) ? nb::SK_COMP : 0);
     };
@@ -1226,7 +1247,7 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
         c->sym_s = (float4 *)m[1];
         // a fixed-point source side starts zeroed, with its mass record
         if (e == cudaSuccess && uses_sym(c)) {
-            int sp_st = nb::sym_fx_prepare(c->splan, (const float4 *)pos_now, c->sym_s, s);
+            int sp_st = nb::sym_fx_prepare(c->splan, (const float4 *)pos_now, c->sym_s, (float)p.eps2, s);
             if (sp_st) e = cudaErrorUnknown;
         }
     } else {

@@ -957,7 +957,6 @@ struct nb_batch {
     int graph_steps = 0, graph_cur = -1;
     // scratch of the per-system baseline (target-side and source-side)
     float4 *sys_partial = nullptr, *sys_spart = nullptr;
-    float *sys_msum = nullptr;  // per-system sum of |m| (fixed-point source side of the baselines)
     // NB_F64 state (NB_ALGO_SYM): pos / vel / partial / spart hold double4
     // (twice the float4 entries), stepped by the float-float batched kernel
     // from the scaled grid split (3 nbody float4) and the batch's
@@ -1259,7 +1258,6 @@ static void free_batch(nb_batch *b)
     nb::dfree(b->d_sp_off);
     nb::dfree(b->sys_partial);
     nb::dfree(b->sys_spart);
-    nb::dfree(b->sys_msum);
     nb::dfree(b->ff_split);
     nb::dfree(b->ff_range);
     nb::dfree(b->d_it_off_v);
@@ -1670,7 +1668,7 @@ static int sys_plans_for(nb_batch *b, SysPlans *out)
         if (b->sym) {
             nb::SymPlan q;
             if ((st = b->f64 ? nb::symff_plan(b->sizes[i], 0, 0, b->device, &q)
-                             : nb::sym_plan(b->sizes[i], 0, 0, b->device, &q, 0, 1)))
+                             : nb::sym_plan(b->sizes[i], 0, 0, b->device, &q, 0, NB_SOURCE_TRIANGULAR)))
                 return st;
             sp.tpart = std::max(sp.tpart, (size_t)q.slots * q.rb * wide);
             sp.spart = std::max(sp.spart, (size_t)q.spart_size * wide);
@@ -1688,10 +1686,9 @@ static int sys_plans_for(nb_batch *b, SysPlans *out)
 
 // System i stepped on its own from pos[c] into pos[c ^ 1]: force + integrate
 // launches (float-float for FP64 state: its own scale record `range` and
-// its slice of the split buffer; float symmetric: the fixed-point source
-// side in spart, zero between steps, with system i's mass record msum[i]).
+// its slice of the split buffer).
 static int sys_step(const nb_batch *b, const SysPlans &sp, int i, int c, float4 *tpart, float4 *spart,
-                    unsigned long long *range, const float *msum, cudaStream_t s)
+                    unsigned long long *range, cudaStream_t s)
 {
     const nb_params &p = b->p;
     const int o = sp.off[i];
@@ -1708,9 +1705,9 @@ static int sys_step(const nb_batch *b, const SysPlans &sp, int i, int c, float4 
     const float4 *po = b->pos[c] + o;
     float4 *pn = b->pos[c ^ 1] + o, *vel = b->vel + o;
     if (b->sym) {
-        if ((st = nb::sym_force(sp.sym[i], po, (float)p.eps2, tpart, spart, s, msum + i))) return st;
-        return nb::sym_integrate(sp.sym[i], po, pn, vel, tpart, spart, (float)p.eps2, (float)p.damping,
-                                 (float)p.dt, p.kick, (float)p.G, nullptr, s, 1, msum + i);
+        if ((st = nb::sym_force(sp.sym[i], po, (float)p.eps2, tpart, spart, s))) return st;
+        return nb::sym_integrate(sp.sym[i], po, pn, vel, tpart, spart, (float)p.damping, (float)p.dt,
+                                 p.kick, (float)p.G, nullptr, s);
     }
     if ((st = nb::fast_force(sp.dir[i], po, (float)p.eps2, tpart, s, 0))) return st;
     return nb::fast_integrate(sp.dir[i], po, pn, vel, tpart, (float)p.damping, (float)p.dt, p.kick,
@@ -1742,22 +1739,9 @@ int nb_batch_step_per_system(nb_batch *b, int steps, void *stream)
         b->sys_partial = t;
         b->sys_spart = u;
     }
-    const bool fixed = b->sym && !b->f64;
-    if (fixed) {
-        // zeroed accumulators (each integrate leaves them zero for the next
-        // system) and every system's mass record, as its own context has
-        if (!b->sys_msum) {
-            cudaError_t e = nb::dmalloc((void **)&b->sys_msum, sizeof(float) * (size_t)std::max(b->nsys, 1));
-            if (e != cudaSuccess) return nb::cuda_error(e, "per-system baseline scratch allocation");
-        }
-        NB_CUDA(cudaMemsetAsync(b->sys_spart, 0, sp.spart * sizeof(float4), s));
-        if ((st = nb::sym_fx_masses(b->nsys, b->d_sys_off, b->pos[b->cur], b->sys_msum, s))) return st;
-    }
     for (int t = 0; t < steps; ++t) {
         for (int i = 0; i < b->nsys; ++i) {
-            if ((st = sys_step(b, sp, i, b->cur, b->sys_partial, b->sys_spart, b->ff_range,
-                               fixed ? b->sys_msum : nullptr, s)))
-                return st;
+            if ((st = sys_step(b, sp, i, b->cur, b->sys_partial, b->sys_spart, b->ff_range, s))) return st;
         }
         b->cur ^= 1;
     }
@@ -1790,36 +1774,16 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
             if (streams[t]) cudaStreamDestroy(streams[t]);
         }
     };
-    const bool fixed = b->sym && !b->f64;
     for (int t = 0; t < ntasks; ++t) {
         cudaError_t e = nb::dmalloc((void **)&tscratch[t], sp.tpart * sizeof(float4));
         if (e == cudaSuccess) e = nb::dmalloc((void **)&sscratch[t], sp.spart * sizeof(float4));
         if (e == cudaSuccess) e = nb::dmalloc((void **)&ranges[t], 2 * sizeof(unsigned long long));
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&streams[t], cudaStreamNonBlocking);
-        if (e == cudaSuccess && fixed) e = cudaMemsetAsync(sscratch[t], 0, sp.spart * sizeof(float4), streams[t]);
         if (e != cudaSuccess) {
             release();
             return nb::cuda_error(e, "per-system task baseline setup");
         }
     }
-    if (fixed) {  // every system's mass record, before the tasks start
-        if (!b->sys_msum) {
-            cudaError_t e = nb::dmalloc((void **)&b->sys_msum, sizeof(float) * (size_t)std::max(b->nsys, 1));
-            if (e != cudaSuccess) {
-                release();
-                return nb::cuda_error(e, "per-system task baseline setup");
-            }
-        }
-        int stm = nb::sym_fx_masses(b->nsys, b->d_sys_off, b->pos[b->cur], b->sys_msum, streams[0]);
-        if (!stm && cudaStreamSynchronize(streams[0]) != cudaSuccess) stm = NB_ERR_CUDA;
-        for (int t = 1; t < ntasks && !stm; ++t)
-            if (cudaStreamSynchronize(streams[t]) != cudaSuccess) stm = NB_ERR_CUDA;
-        if (stm) {
-            release();
-            return set_error(stm, "per-system task baseline: mass records");
-        }
-    }
-    const float *msum = fixed ? b->sys_msum : nullptr;
     const int cur = b->cur, dev = b->device;
     std::vector<int> status(ntasks, NB_OK);
     std::vector<std::thread> workers;
@@ -1829,7 +1793,7 @@ int nb_batch_step_tasks(nb_batch *b, int steps, int ntasks)
             for (int i = t; i < b->nsys && status[t] == NB_OK; i += ntasks) {
                 int c = cur;
                 for (int k = 0; k < steps && status[t] == NB_OK; ++k) {
-                    int st = sys_step(b, sp, i, c, tscratch[t], sscratch[t], ranges[t], msum, streams[t]);
+                    int st = sys_step(b, sp, i, c, tscratch[t], sscratch[t], ranges[t], streams[t]);
                     if (!st && cudaStreamSynchronize(streams[t]) != cudaSuccess) st = NB_ERR_CUDA;
                     status[t] = st;
                     c ^= 1;

@@ -289,7 +289,8 @@ __device__ __forceinline__ int sym_row_of(long long it, int nc, int rc, int nrb)
 struct SymPlan {
     int n = 0, warps = 0, bpt = 0;
     int comp = 0;        // compensated (hi, lo) partials: tpart and spart hold a lo block after the hi block
-    int fixed = 0;       // source side in 64-bit fixed point (sym_fx_*): spart holds 6 n integers and a record
+    int fixed = 0;       // plain plans: source side in 64-bit fixed point (sym_fx_*), spart then holds
+                         // 6 n integers and a record; otherwise the triangular array
     int rb = 0;          // bodies per row block (CTA targets)
     int nc = 0;          // 32-body chunks
     int nrb = 0;         // row blocks
@@ -309,29 +310,30 @@ inline long long sym_spart_entries(int n, int rb)
 // bigger row block.
 constexpr long long kSymSpartBudget = 8ll << 30;
 
+// Largest triangular array the automatic choice accepts at the largest row
+// block before it takes the fixed-point source side.
+constexpr long long kSymSpartMax = 32ll << 30;
 // float4 entries of the fixed-point source side: 6 n 64-bit accumulators
-// (hi x, y, z then lo x, y, z, each n long) and one float4 record whose x is
-// the sum of |m| over the bodies.
+// (hi x, y, z then lo x, y, z, each n long) and one float4 record: the sum of
+// |m| over the bodies and the scale factors (sym_fx_prepare).
 inline long long sym_fx_entries(int n) { return 3ll * n + 1; }
 
-int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp = 0, int fixed = 0);
-// msum (fixed plans; may be nullptr): the record to read instead of the one
-// at the end of spart (the batch's per-system runs keep one per system)
+// source_side: nb_source_side (NB_SOURCE_AUTO / TRIANGULAR / FIXED), for
+// plain plans; compensated plans are always triangular.
+int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp = 0, int source_side = 0);
 int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, float4 *spart,
-              cudaStream_t s, const float *msum = nullptr);
+              cudaStream_t s);
 // consume (fixed plans): zero the accumulators after reading them, ready for
 // the next force launch; 0 leaves them for a second reader of the same
 // force launch
 int sym_integrate(const SymPlan &p, const float4 *pos_old, float4 *pos_new, float4 *vel,
-                  const float4 *tpart, const float4 *spart, float eps2, float damping, float dt,
-                  int kick, float G, float4 *acc_out, cudaStream_t s, int consume = 1,
-                  const float *msum = nullptr);
-// Fixed plans: zero the accumulators and record the sum of |m| of pos (n
-// bodies) in spart's record; needed after every new state and new scratch.
-int sym_fx_prepare(const SymPlan &p, const float4 *pos, float4 *spart, cudaStream_t s);
-// The records of nsys systems at once (bodies off[i] .. off[i+1] - 1 of pos,
-// off on the device): msum[i] = sum of |m| of system i.
-int sym_fx_masses(int nsys, const int *off, const float4 *pos, float *msum, cudaStream_t s);
+                  const float4 *tpart, const float4 *spart, float damping, float dt, int kick,
+                  float G, float4 *acc_out, cudaStream_t s, int consume = 1);
+// Fixed plans: zero the accumulators and write the record (the sum of |m| of
+// pos and the scale it gives with eps2); after every new state and scratch.
+int sym_fx_prepare(const SymPlan &p, const float4 *pos, float4 *spart, float eps2, cudaStream_t s);
+// Fixed plans: the record's scale for a new eps2 (the masses unchanged).
+int sym_fx_rescale(const SymPlan &p, float4 *spart, float eps2, cudaStream_t s);
 
 // FP64 symmetric path (nb_sym64.cu): tpart / spart hold double4 entries.
 // sym64_integrate with ffrange (the float-float path's scale record) undoes

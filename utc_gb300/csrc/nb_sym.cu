@@ -27,25 +27,27 @@
 // The integrate kernel adds, per body, its target-side slots (CTA order) and
 // its source-side entries spart[0..I_b-1][b] (row order): deterministic.
 //
-// Fixed-point source side (plans with fixed = 1, the default for FP32
-// contexts).  The triangular array holds about N^2 / (2 rb) float4 (67 MB at
-// N = 65536, 3.4 GB at N = 1M), which the integrator reads back: 15 times
-// the state's own bytes at N = 65536.  Instead, each warp adds its reaction
-// on a chunk body straight into per-body 64-bit integer accumulators with
-// integer atomics.  Integer addition is associative, so the sums are the
-// same whatever order the CTAs run in: the step stays deterministic, and
-// the source side takes 48 B per body.  Every reaction v (a float) is split
-// into two integers, hi = round(v / 2^(e-61)) and lo = round((v - hi
-// 2^(e-61)) / 2^(e-83)), both exact for |v| >= 2^(e-60) (the float's 24
-// significant bits fit), and within 2^(e-84) otherwise.  The exponent e
-// comes from a bound on every partial and total reaction: a body at distance
-// r adds at most m r / (r^2 + eps2)^(3/2) <= (2 / (3 sqrt 3)) m / eps2, so
-// B = 0.385 sum|m| / eps2 bounds them all, and 2^e > 2 B keeps the hi sums
-// below 2^62 (the lo sums stay below 2^22 per reaction).  So the source
-// side is summed essentially exactly: more accurately than float partial
-// sums, for any eps2 > 0.  sum|m| is recorded at nb_set_state
-// (sym_fx_prepare); the integrator zeroes the accumulators after reading
-// them.
+// Fixed-point source side (template flag FX; plans with fixed = 1, chosen
+// by nb_params.source_side or when the triangular array would not fit: it
+// holds about N^2 / (2 rb) float4).  The CTA's reaction on a chunk body,
+// summed over its warps as above, is added straight into per-body 64-bit
+// integer accumulators with integer atomics.  Integer addition is
+// associative, so the sums do not depend on the order the CTAs run in: the
+// step stays deterministic, and the source side takes 48 B per body.  Each
+// reaction v is split into two integers, hi = round(v / 2^(e-61)) and
+// lo = round((v - hi 2^(e-61)) / 2^(e-83)), exact for |v| >= 2^(e-60) (the
+// float's 24 significant bits fit) and within 2^(e-84) below.  The exponent
+// comes from a bound on every partial and total reaction: a body at
+// distance r adds at most m r / (r^2 + eps2)^(3/2) <= (2 / (3 sqrt 3)) m /
+// eps2, so B = 0.385 sum|m| / eps2 bounds them all, and 2^e > 2 B keeps the
+// hi sums below 2^62 (the lo words stay below 2^22 per reaction).  The
+// source side is so summed essentially exactly, for any eps2 > 0.  The scale
+// sits in a record after the accumulators, written at nb_set_state (and for
+// a new eps2) by sym_fx_prepare / sym_fx_rescale; the integrator zeroes the
+// accumulators after reading them.  On GB300 this variant ran 2-10 % slower
+// than the triangular array at N = 65536 in every arrangement tried (the
+// pair loop's schedule shifts with the code around it), so it is used only
+// where the array would not fit or where a caller asks for it.
 //
 // Compensated variant (COMP): each target's per-chunk partial sum (32
 // sources) is folded into a two-sum (hi, lo) pair, the W warps' reactions on
@@ -65,68 +67,45 @@
 
 namespace nb {
 
-// Scale of the fixed-point source side for msum = sum |m| and eps2 (see the
-// header): powers of two 2^(61-e), 2^(e-61), 2^(83-e).
-struct FxScale {
-    int e;
-    float inv_hi, lsb_hi, inv_lo;
-};
-
-__device__ __forceinline__ FxScale fx_scale(float msum, float eps2)
+// Record after the fixed-point accumulators: x = sum |m|, y = 2^(61-e),
+// z = 2^(e-61), w = 2^(83-e).
+__device__ __forceinline__ const float4 *fx_record(const unsigned long long *acc, int n)
 {
-    const float b = 0.38490018f * msum / eps2;  // 2 / (3 sqrt 3) sum|m| / eps2
-    int e = -40;
-    if (b > 0.f && b <= 3.0e38f) {
-        frexpf(b, &e);  // b < 2^e
-        e += 1;         // 2^e > 2 b
-    } else if (b > 0.f) {
-        e = 120;        // eps2 = 0 (the self pair makes every result NaN anyway)
-    }
-    e = max(-40, min(120, e));
-    FxScale f;
-    f.e = e;
-    f.inv_hi = __int_as_float((127 + 61 - e) << 23);
-    f.lsb_hi = __int_as_float((127 + e - 61) << 23);
-    f.inv_lo = __int_as_float((127 + 83 - e) << 23);
-    return f;
+    return reinterpret_cast<const float4 *>(acc + 6ll * n);
 }
 
-// v added to the accumulators hi_p (units 2^(e-61)) and lo_p (2^(e-83)).
-// The products with powers of two are exact; rem is exact (|v / 2^(e-61)|
-// < 2^23 makes (float)h exact, otherwise v / 2^(e-61) is an integer and
+// v added to the accumulators hi_p (units z = 2^(e-61)) and lo_p (units
+// 1/w = 2^(e-83)).  The products with powers of two are exact; rem is exact
+// (|v y| < 2^23 makes (float)h exact, otherwise v y is an integer and
 // rem = 0).  The adds compile to fire-and-forget reductions.
 __device__ __forceinline__ void fx_add(unsigned long long *hi_p, unsigned long long *lo_p, float v,
-                                       const FxScale &f)
+                                       const float4 &r)
 {
-    const long long h = __float2ll_rn(v * f.inv_hi);
-    const float rem = fmaf(-(float)h, f.lsb_hi, v);
-    const long long l = __float2ll_rn(rem * f.inv_lo);
+    const long long h = __float2ll_rn(v * r.y);
+    const float rem = fmaf(-(float)h, r.z, v);
+    const long long l = __float2ll_rn(rem * r.w);
     atomicAdd(hi_p, (unsigned long long)h);
     atomicAdd(lo_p, (unsigned long long)l);
 }
 
-// This warp's reaction (fx, fy, fz on chunk body jb + lane) into the
-// fixed-point accumulators: six reductions per lane and chunk.
-__device__ __forceinline__ void fx_emit(unsigned long long *acc, int n, int j, float fx, float fy, float fz,
-                                        const FxScale &f)
+// A reaction (fx, fy, fz) on body j into the fixed-point accumulators.
+__device__ __forceinline__ void fx_emit(unsigned long long *acc, int n, int j, float fx, float fy, float fz)
 {
-    if (j >= n) return;
+    const float4 r = __ldg(fx_record(acc, n));
     const long long nn = n;
-    fx_add(acc + j, acc + 3 * nn + j, fx, f);
-    fx_add(acc + nn + j, acc + 4 * nn + j, fy, f);
-    fx_add(acc + 2 * nn + j, acc + 5 * nn + j, fz, f);
+    fx_add(acc + j, acc + 3 * nn + j, fx, r);
+    fx_add(acc + nn + j, acc + 4 * nn + j, fy, r);
+    fx_add(acc + 2 * nn + j, acc + 5 * nn + j, fz, r);
 }
 
-// fxacc != nullptr: the fixed-point source side (accumulators fxacc, sum
-// |m| at *fxmsum); otherwise the triangular array spart.
-template <int W, int BPT, int MINB, bool COMP>
+// FX: spart is the fixed-point accumulator buffer (with its record), not
+// the triangular array.
+template <int W, int BPT, int MINB, bool COMP, bool FX = false>
 __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *__restrict__ pos, int n,
                                                            float eps2, float4 *__restrict__ tpart,
                                                            float4 *__restrict__ spart,
                                                            long long total, int nc, int nrb,
-                                                           long long tlo, long long slo,
-                                                           unsigned long long *__restrict__ fxacc,
-                                                           const float *__restrict__ fxmsum)
+                                                           long long tlo, long long slo)
 {
     constexpr int WB = 32 * BPT;
     constexpr int RB = W * WB;
@@ -139,8 +118,6 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
     long long it = sk_start(c, total, gridDim.x);
     const long long end = sk_start(c + 1, total, gridDim.x);
     const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
-    FxScale fxs{};
-    if (fxacc) fxs = fx_scale(*fxmsum, eps2);
 
     while (it < end) {
         const int I = sym_row_of(it, nc, RC, nrb);
@@ -219,14 +196,20 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
                     fz = __shfl_sync(0xffffffffu, fz, from);
                 }
                 // lane l now holds the reaction on chunk body l from this warp
-                if (!COMP && fxacc) {
-                    fx_emit(fxacc, n, jb + lane, fx, fy, fz, fxs);
-                } else {
                 sF[0][wid][lane] = fx;
                 sF[1][wid][lane] = fy;
                 sF[2][wid][lane] = fz;
                 __syncthreads();
-                if (wid == 0 && jb + lane < n) {
+                if (FX && wid == 0 && jb + lane < n) {
+                    float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+                    for (int w = 0; w < W; ++w) {
+                        sx += sF[0][w][lane];
+                        sy += sF[1][w][lane];
+                        sz += sF[2][w][lane];
+                    }
+                    fx_emit(reinterpret_cast<unsigned long long *>(spart), n, jb + lane, sx, sy, sz);
+                } else if (wid == 0 && jb + lane < n) {
                     const long long so = sym_soff(I, n, RB) + (jb + lane - (I + 1) * RB);
                     if constexpr (COMP) {
                         float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f, e;
@@ -251,7 +234,6 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
                         }
                         spart[so] = make_float4(sx, sy, sz, 0.f);
                     }
-                }
                 }
             }
             if constexpr (COMP) {
@@ -294,9 +276,7 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__re
                                                               float eps2, float4 *__restrict__ tpart,
                                                               float4 *__restrict__ spart,
                                                               long long total, int nc, int nrb,
-                                                              long long, long long,
-                                                              unsigned long long *__restrict__ fxacc,
-                                                              const float *__restrict__ fxmsum)
+                                                              long long, long long)
 {
     constexpr int BPT = 2 * NP;
     constexpr int WB = 32 * BPT;
@@ -312,8 +292,6 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__re
     const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
     const f2 EPS2 = f2_pack(eps2, eps2);
     const f2 ZERO = f2_pack(0.f, 0.f);
-    FxScale fxs{};
-    if (fxacc) fxs = fx_scale(*fxmsum, eps2);
 
     while (it < end) {
         const int I = sym_row_of(it, nc, RC, nrb);
@@ -387,9 +365,7 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__re
                     fz = __shfl_sync(0xffffffffu, fz, from);
                 }
             }
-            if (!diag && fxacc) {
-                fx_emit(fxacc, n, jb + lane, fx, fy, fz, fxs);
-            } else if (!diag) {
+            if (!diag) {
                 sF[0][wid][lane] = fx;
                 sF[1][wid][lane] = fy;
                 sF[2][wid][lane] = fz;
@@ -436,7 +412,7 @@ __global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
     const float4 *__restrict__ pos_old, float4 *__restrict__ pos_new, float4 *__restrict__ vel,
     const float4 *__restrict__ tpart, const float4 *__restrict__ spart, int n, int rb, int nc, int nrb,
     long long total, int grid, float damping, float dt, int kick, float G, float4 *__restrict__ acc_out,
-    unsigned long long *__restrict__ fxacc, const float *__restrict__ fxmsum, float eps2, int consume)
+    unsigned long long *__restrict__ fxacc, int consume)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int i = (int)(t >> 2), q = (int)(t & 3);
@@ -472,9 +448,9 @@ __global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
     az = __fadd_rn(az, __shfl_xor_sync(0xffffffffu, az, 2));
     if (!live || q != 0) return;
     if (fxacc) {
-        const FxScale f = fx_scale(*fxmsum, eps2);
-        const double lhi = __longlong_as_double((long long)(1023 + f.e - 61) << 52);
-        const double llo = __longlong_as_double((long long)(1023 + f.e - 83) << 52);
+        // units 2^(e-61) and 2^(e-83) as doubles, from the record's 2^(e-61)
+        const float4 rec = *fx_record(fxacc, n);
+        const double lhi = (double)rec.z, llo = (double)rec.z * 0x1p-22;
         const long long nn = n;
         unsigned long long *a = fxacc + i;
         const double sx = (double)(long long)a[0] * lhi + (double)(long long)a[3 * nn] * llo;
@@ -506,14 +482,21 @@ __global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
 }
 
 typedef void (*sym_kernel_t)(const float4 *, int, float, float4 *, float4 *, long long, int, int,
-                             long long, long long, unsigned long long *, const float *);
+                             long long, long long);
 
 // bpt > 0: scalar kernel with bpt bodies per lane (the third template
 // argument asks for that many resident CTAs per SM); bpt < 0: packed f32x2
 // kernel with -bpt bodies per lane.  comp: the compensated kernel (scalar
 // shapes with up to 12 targets per lane: 13 registers per target).
-static sym_kernel_t sym_kernel_for(int w, int bpt, int comp)
+static sym_kernel_t sym_kernel_for(int w, int bpt, int comp, int fixed = 0)
 {
+    if (fixed) {  // fixed-point source side: one-warp shapes
+        if (comp) return nullptr;
+        if (w == 1 && bpt == 16) return sym_force_kernel<1, 16, 8, false, true>;
+        if (w == 1 && bpt == 8) return sym_force_kernel<1, 8, 8, false, true>;
+        if (w == 1 && bpt == 4) return sym_force_kernel<1, 4, 8, false, true>;
+        return nullptr;
+    }
     if (comp) {
         if (w == 1 && bpt == 12) return sym_force_kernel<1, 12, 8, true>;
         if (w == 4 && bpt == 12) return sym_force_kernel<4, 12, 2, true>;
@@ -538,9 +521,28 @@ static sym_kernel_t sym_kernel_for(int w, int bpt, int comp)
     return nullptr;
 }
 
-int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int fixed)
+int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int source_side)
 {
-    if (comp) fixed = 0;  // the compensated kernel keeps its (hi, lo) triangular array
+    if (source_side < NB_SOURCE_AUTO || source_side > NB_SOURCE_FIXED)
+        return set_error(NB_ERR_INVALID, "source_side is NB_SOURCE_AUTO, NB_SOURCE_TRIANGULAR or NB_SOURCE_FIXED");
+    if (comp && source_side == NB_SOURCE_FIXED)
+        return set_error(NB_ERR_UNSUPPORTED, "the compensated kernel keeps its triangular (hi, lo) source side");
+    int fixed = source_side == NB_SOURCE_FIXED ? 1 : 0;
+    const bool given = warps != 0 || bpt != 0;
+    if (!given && !fixed && !comp && source_side == NB_SOURCE_AUTO &&
+        sym_spart_entries(n, 8 * 32 * 24) * (long long)sizeof(float4) > kSymSpartMax)
+        fixed = 1;  // the triangular array would not fit even at the largest row block
+    if (!given && fixed) {
+        warps = 1;
+        bpt = 16;
+        int sms = 0;  // fewer targets per lane for small systems, as below
+        NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        while (bpt > 4 && n > 0) {
+            const int rb = 32 * bpt, nrb = (n + rb - 1) / rb, nc = (n + 31) / 32;
+            if (sym_prefix(nrb, nc, bpt) >= 4ll * sms) break;
+            bpt /= 2;
+        }
+    }
     if (warps == 0 && bpt == 0) {
         // plain: one-warp CTAs x 16 targets (row block 512); then 4 x 20
         // (2560), 8 x 24 (6144) while the source-side array is over budget.
@@ -551,9 +553,9 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int f
         const int(*shapes)[2] = comp ? compd : plain;
         const long long halves = comp ? 2 : 1;
         int s = 0;
-        while (!fixed && s < 2 &&
-               halves * sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) * (long long)sizeof(float4) >
-                   kSymSpartBudget)
+        while (s < 2 && halves * sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) *
+                                (long long)sizeof(float4) >
+                            kSymSpartBudget)
             ++s;
         warps = shapes[s][0];
         bpt = shapes[s][1];
@@ -573,13 +575,17 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int f
     }
     if (warps == 0) warps = 8;
     if (bpt == 0) bpt = 8;
-    sym_kernel_t k = sym_kernel_for(warps, bpt, comp);
-    if (!k) return set_error(NB_ERR_UNSUPPORTED, "symmetric kernel shape not compiled");
+    sym_kernel_t k = sym_kernel_for(warps, bpt, comp, fixed);
+    if (!k)
+        return set_error(NB_ERR_UNSUPPORTED, fixed ? "symmetric kernel shape not compiled with the fixed-point "
+                                                     "source side (one warp x 4, 8 or 16 targets)"
+                                                   : "symmetric kernel shape not compiled");
     SymPlan p;
     p.n = n;
     p.warps = warps;
     p.bpt = bpt;
     p.comp = comp;
+    p.fixed = fixed;
     p.rb = warps * 32 * (bpt < 0 ? -bpt : bpt);
     p.nc = (n + 31) / 32;
     p.nrb = (n + p.rb - 1) / p.rb;
@@ -592,86 +598,91 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int f
     if (p.total > 0 && grid > p.total) grid = p.total;
     p.grid = p.total > 0 ? (int)grid : 0;
     p.slots = p.total > 0 ? p.grid + p.nrb - 1 : 0;
-    p.fixed = fixed;
     p.spart_size = fixed ? sym_fx_entries(n) : sym_spart_entries(n, p.rb);
     *pl = p;
     return NB_OK;
 }
 
-// Sum of |m| of bodies off[b] .. off[b+1] - 1 by block b, in a fixed order
-// (per-thread strided sums, then a tree): the record of a fixed-point plan.
-// off == nullptr: one system of n bodies.
-constexpr int kFxMassBlock = 1024;
+// The record of a fixed plan: sum |m| of n bodies by one block in a fixed
+// order (per-thread strided sums, then a tree), then the scale for eps2
+// (with_sum 0: keep the recorded sum, a new eps2 only).
+constexpr int kFxBlock = 1024;
 
-__global__ void __launch_bounds__(kFxMassBlock) fx_mass_kernel(const float4 *__restrict__ pos, int n,
-                                                               const int *__restrict__ off,
-                                                               float *__restrict__ out, int stride)
+__global__ void __launch_bounds__(kFxBlock) fx_record_kernel(const float4 *__restrict__ pos, int n, float eps2,
+                                                             unsigned long long *__restrict__ acc, int with_sum)
 {
-    __shared__ float red[kFxMassBlock];
-    const int lo = off ? off[blockIdx.x] : 0, hi = off ? off[blockIdx.x + 1] : n;
-    float sum = 0.f;
-    for (int i = lo + (int)threadIdx.x; i < hi; i += kFxMassBlock) sum += fabsf(pos[i].w);
-    red[threadIdx.x] = sum;
-    __syncthreads();
-    for (int w = kFxMassBlock / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __shared__ float red[kFxBlock];
+    float4 *rec = reinterpret_cast<float4 *>(acc + 6ll * n);
+    float msum = 0.f;
+    if (with_sum) {
+        float sum = 0.f;
+        for (int i = (int)threadIdx.x; i < n; i += kFxBlock) sum += fabsf(pos[i].w);
+        red[threadIdx.x] = sum;
         __syncthreads();
+        for (int w = kFxBlock / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        msum = red[0];
+    } else {
+        msum = rec->x;
     }
-    if (threadIdx.x == 0) out[(size_t)blockIdx.x * stride] = red[0];
+    if (threadIdx.x != 0) return;
+    // B = 2 / (3 sqrt 3) sum|m| / eps2 bounds every reaction; 2^e > 2 B
+    const float b = 0.38490018f * msum / eps2;
+    int e = -40;
+    if (b > 0.f && b <= 3.0e38f) {
+        frexpf(b, &e);  // b < 2^e
+        e += 1;
+    } else if (b > 0.f) {
+        e = 120;  // eps2 = 0: the self pair makes every result NaN anyway
+    }
+    e = max(-40, min(120, e));
+    *rec = make_float4(msum, __int_as_float((127 + 61 - e) << 23), __int_as_float((127 + e - 61) << 23),
+                       __int_as_float((127 + 83 - e) << 23));
 }
 
-int sym_fx_prepare(const SymPlan &p, const float4 *pos, float4 *spart, cudaStream_t s)
+int sym_fx_prepare(const SymPlan &p, const float4 *pos, float4 *spart, float eps2, cudaStream_t s)
 {
     if (!p.fixed || p.n == 0) return NB_OK;
     NB_CUDA(cudaMemsetAsync(spart, 0, 6 * sizeof(unsigned long long) * (size_t)p.n, s));
-    float *rec = reinterpret_cast<float *>(reinterpret_cast<unsigned long long *>(spart) + 6ll * p.n);
-    fx_mass_kernel<<<1, kFxMassBlock, 0, s>>>(pos, p.n, nullptr, rec, 1);
-    NB_LAUNCH_CHECK("fx_mass_kernel launch");
+    fx_record_kernel<<<1, kFxBlock, 0, s>>>(pos, p.n, eps2, reinterpret_cast<unsigned long long *>(spart), 1);
+    NB_LAUNCH_CHECK("fx_record_kernel launch");
     return NB_OK;
 }
 
-int sym_fx_masses(int nsys, const int *off, const float4 *pos, float *msum, cudaStream_t s)
+int sym_fx_rescale(const SymPlan &p, float4 *spart, float eps2, cudaStream_t s)
 {
-    if (nsys <= 0) return NB_OK;
-    fx_mass_kernel<<<nsys, kFxMassBlock, 0, s>>>(pos, 0, off, msum, 1);
-    NB_LAUNCH_CHECK("fx_mass_kernel launch");
+    if (!p.fixed || p.n == 0) return NB_OK;
+    fx_record_kernel<<<1, kFxBlock, 0, s>>>(nullptr, p.n, eps2, reinterpret_cast<unsigned long long *>(spart), 0);
+    NB_LAUNCH_CHECK("fx_record_kernel launch");
     return NB_OK;
-}
-
-// The fixed-point accumulators and the record of a fixed plan's spart.
-static unsigned long long *fx_acc(const SymPlan &p, const float4 *spart)
-{
-    return p.fixed ? reinterpret_cast<unsigned long long *>(const_cast<float4 *>(spart)) : nullptr;
-}
-static const float *fx_rec(const SymPlan &p, const float4 *spart, const float *msum)
-{
-    if (!p.fixed) return nullptr;
-    return msum ? msum : reinterpret_cast<const float *>(reinterpret_cast<const unsigned long long *>(spart) + 6ll * p.n);
 }
 
 int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, float4 *spart,
-              cudaStream_t s, const float *msum)
+              cudaStream_t s)
 {
     if (p.total == 0) return NB_OK;
-    sym_kernel_t k = sym_kernel_for(p.warps, p.bpt, p.comp);
+    sym_kernel_t k = sym_kernel_for(p.warps, p.bpt, p.comp, p.fixed);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "symmetric kernel shape not compiled");
     // lo blocks (compensated plans) follow the hi blocks
     const long long tlo = (long long)p.slots * p.rb, slo = p.spart_size;
-    k<<<p.grid, 32 * p.warps, 0, s>>>(pos, p.n, eps2, tpart, spart, p.total, p.nc, p.nrb, tlo, slo,
-                                      fx_acc(p, spart), fx_rec(p, spart, msum));
+    k<<<p.grid, 32 * p.warps, 0, s>>>(pos, p.n, eps2, tpart, spart, p.total, p.nc, p.nrb, tlo, slo);
     NB_LAUNCH_CHECK("sym_force_kernel launch");
     return NB_OK;
 }
 
 int sym_integrate(const SymPlan &p, const float4 *pos_old, float4 *pos_new, float4 *vel,
-                  const float4 *tpart, const float4 *spart, float eps2, float damping, float dt,
-                  int kick, float G, float4 *acc_out, cudaStream_t s, int consume, const float *msum)
+                  const float4 *tpart, const float4 *spart, float damping, float dt, int kick, float G,
+                  float4 *acc_out, cudaStream_t s, int consume)
 {
     if (p.n == 0) return NB_OK;
     const long long threads = 4ll * p.n;  // a quad of threads per body
+    unsigned long long *fxacc =
+        p.fixed ? reinterpret_cast<unsigned long long *>(const_cast<float4 *>(spart)) : nullptr;
     sym_integrate_kernel<<<(unsigned)((threads + kSymIntegBlock - 1) / kSymIntegBlock), kSymIntegBlock, 0, s>>>(
         pos_old, pos_new, vel, tpart, spart, p.n, p.rb, p.nc, p.nrb, p.total, p.grid, damping, dt, kick,
-        G, acc_out, fx_acc(p, spart), fx_rec(p, spart, msum), eps2, consume);
+        G, acc_out, fxacc, consume);
     NB_LAUNCH_CHECK("sym_integrate_kernel launch");
     return NB_OK;
 }

@@ -52,7 +52,7 @@ def _device_buffer(x, shape, dtype, name):
 class NBodySystem:
     def __init__(self, n, precision="f32", algo="fast", kick="reference", eps2=0.00125,
                  damping=0.995, dt=0.016, G=1.0, block=0, bpt=0, ctas_per_sm=0,
-                 memtype=N.NB_MEM_PAGEABLE):
+                 memtype=N.NB_MEM_PAGEABLE, source_side="auto"):
         self.lib = N.lib()
         p = N.NbParams()
         self.lib.nb_params_default(C.byref(p))
@@ -62,6 +62,9 @@ class NBodySystem:
         p.kick = _KICK[kick]
         p.eps2, p.damping, p.dt, p.G = float(eps2), float(damping), float(dt), float(G)
         p.block, p.bpt, p.ctas_per_sm, p.memtype = int(block), int(bpt), int(ctas_per_sm), int(memtype)
+        # symmetric FP32 kernel: "triangular" array or "fixed"-point accumulators
+        p.source_side = {"auto": N.NB_SOURCE_AUTO, "triangular": N.NB_SOURCE_TRIANGULAR,
+                         "fixed": N.NB_SOURCE_FIXED}[source_side]
         self.params = p
         self.n = int(n)
         self.precision = precision
