@@ -13,8 +13,15 @@ from utc_gb300.nbody import NBodyBatch, NBodySystem
 
 pytestmark = pytest.mark.gpu
 
-MODES = [("f32", "fast"), ("f32", "sym"), ("f32", "exact"), ("f64", "exact"), ("f64", "sym"),
+# "symfx": the symmetric FP32 kernel with its fixed-point source side
+MODES = [("f32", "fast"), ("f32", "sym"), ("f32", "symfx"), ("f32", "exact"), ("f64", "exact"), ("f64", "sym"),
          ("f64", "sym64"), ("f32comp", "fast"), ("f32comp", "sym")]
+
+
+def system(n, prec, algo, **kw):
+    if algo == "symfx":
+        return NBodySystem(n, prec, "sym", source_side="fixed", **kw)
+    return NBodySystem(n, prec, algo, **kw)
 
 
 def dtype_of(prec):
@@ -24,7 +31,7 @@ def dtype_of(prec):
 @pytest.mark.parametrize("prec,algo", MODES)
 def test_empty_system_every_mode(cuda, prec, algo):
     dt = dtype_of(prec)
-    with NBodySystem(0, prec, algo) as s:
+    with system(0, prec, algo) as s:
         s.set_state(np.zeros((0, 4), dt), np.zeros((0, 4), dt))
         s.step(3)
         p, v = s.get_state()
@@ -39,7 +46,7 @@ def test_one_body_drifts_freely(cuda, prec, algo):
     dt_ = dtype_of(prec)
     pos = np.array([[0.25, -0.5, 0.125, 2.0]], dt_)
     vel = np.array([[0.5, 0.25, -1.0, 1.0]], dt_)
-    with NBodySystem(1, prec, algo, kick="physical", eps2=1e-2, damping=1.0, dt=1e-3) as s:
+    with system(1, prec, algo, kick="physical", eps2=1e-2, damping=1.0, dt=1e-3) as s:
         s.set_state(pos, vel)
         s.step(5)
         p, v = s.get_state()
@@ -51,7 +58,7 @@ def test_one_body_drifts_freely(cuda, prec, algo):
 
 @pytest.mark.parametrize("prec,algo", MODES)
 def test_status_codes_every_mode(cuda, prec, algo):
-    with NBodySystem(64, prec, algo) as s:
+    with system(64, prec, algo) as s:
         assert s.lib.nb_step(s.handle, 1, None) == N.NB_ERR_STATE
         assert s.lib.nb_accel(s.handle, None, None) == N.NB_ERR_STATE
         assert s.lib.nb_step(s.handle, -1, None) == N.NB_ERR_INVALID
@@ -69,7 +76,7 @@ def test_status_codes_every_mode(cuda, prec, algo):
 @pytest.mark.parametrize("prec,algo", [("f64", "fast"), ("f32comp", "exact")])
 def test_rejected_combinations(cuda, prec, algo):
     with pytest.raises(N.NbError) as e:
-        NBodySystem(16, prec, algo)
+        system(16, prec, algo)
     assert e.value.status == N.NB_ERR_UNSUPPORTED
 
 
@@ -78,7 +85,7 @@ def test_rejected_combinations(cuda, prec, algo):
 def test_adjoint_needs_a_float_fast_context(cuda, prec, algo):
     dt_ = dtype_of(prec)
     p, v = ics.plummer(32, seed=2)
-    with NBodySystem(32, prec, algo) as s:
+    with system(32, prec, algo) as s:
         s.set_state(p.astype(dt_), v.astype(dt_))
         assert s.lib.nb_adj_forward(s.handle, 4, 2, None, None) == N.NB_ERR_UNSUPPORTED
 
@@ -131,7 +138,7 @@ def test_graph_replay_equals_single_steps(cuda, prec, algo):
     p, v = ics.plummer(n, seed=5)
     p, v = p.astype(dt_), v.astype(dt_)
     side = torch.cuda.Stream()
-    with NBodySystem(n, prec, algo, kick="physical", eps2=1e-3, damping=1.0, dt=1e-3) as s:
+    with system(n, prec, algo, kick="physical", eps2=1e-3, damping=1.0, dt=1e-3) as s:
         s.set_state(p, v)
         for _ in range(71):
             s.step(1)
@@ -185,7 +192,7 @@ def test_set_params_equals_a_fresh_context(cuda, prec, algo):
     p, v = p.astype(dt_), v.astype(dt_)
     side = torch.cuda.Stream()
     kw = dict(kick="physical", eps2=1e-3, damping=1.0, dt=1e-3)
-    with NBodySystem(n, prec, algo, **kw) as s:
+    with system(n, prec, algo, **kw) as s:
         s.set_state(p, v)
         torch.cuda.synchronize()
         with torch.cuda.stream(side):
@@ -197,7 +204,7 @@ def test_set_params_equals_a_fresh_context(cuda, prec, algo):
             s.step(40, stream=side.cuda_stream)
             side.synchronize()
         got = s.get_state()
-    with NBodySystem(n, prec, algo, kick="physical", eps2=2e-3, damping=0.99, dt=5e-4) as f:
+    with system(n, prec, algo, kick="physical", eps2=2e-3, damping=0.99, dt=5e-4) as f:
         f.set_state(*mid)
         for _ in range(40):
             f.step(1)
@@ -339,7 +346,7 @@ def test_coincident_bodies_every_mode(cuda, prec, algo):
     dt = dtype_of(prec)
     host = pos.astype(dt)
     eps2 = 1e-3 if dt == np.float64 else np.float32(1e-3)
-    with NBodySystem(pos.shape[0], prec, algo, kick="physical", eps2=eps2, damping=1.0) as s:
+    with system(pos.shape[0], prec, algo, kick="physical", eps2=eps2, damping=1.0) as s:
         s.set_state(host, np.zeros_like(host))
         a = s.accel().astype(np.float64)
     want = oracle.accel(host.astype(np.float64), float(eps2))
@@ -359,12 +366,12 @@ def test_zero_softening_is_nan_like_the_reference(cuda, prec, algo):
     dt = dtype_of(prec)
     host = p.astype(dt)
     assert np.isnan(oracle.accel(host, 0.0)).all()
-    with NBodySystem(64, prec, algo, kick="physical", eps2=0.0, damping=1.0) as s:
+    with system(64, prec, algo, kick="physical", eps2=0.0, damping=1.0) as s:
         s.set_state(host, np.zeros_like(host))
         assert np.isnan(s.accel()).all()
 
 
-TOL = {("f32", "fast"): 2e-5, ("f32", "sym"): 2e-5, ("f32", "exact"): 2e-5, ("f64", "exact"): 1e-14,
+TOL = {("f32", "fast"): 2e-5, ("f32", "sym"): 2e-5, ("f32", "symfx"): 2e-5, ("f32", "exact"): 2e-5, ("f64", "exact"): 1e-14,
        ("f64", "sym"): 1e-13, ("f64", "sym64"): 1e-13, ("f32comp", "fast"): 2e-6, ("f32comp", "sym"): 2e-6}
 
 
@@ -379,7 +386,7 @@ def test_small_sizes_every_mode(cuda, prec, algo, n):
     pos = p.astype(np.float32).astype(dt) if prec == "f32" else p.astype(dt)
     vel = v.astype(np.float32).astype(dt) if prec == "f32" else v.astype(dt)
     eps2 = 1e-2 if dt == np.float64 else np.float32(1e-2)
-    with NBodySystem(n, prec, algo, kick="physical", eps2=eps2, damping=1.0, dt=1e-3 if dt == np.float64
+    with system(n, prec, algo, kick="physical", eps2=eps2, damping=1.0, dt=1e-3 if dt == np.float64
                      else np.float32(1e-3)) as s:
         s.set_state(pos, vel)
         a = np.asarray(s.accel(), np.float64)
@@ -406,7 +413,7 @@ def test_energy_tiny_systems_every_mode(cuda, prec, algo, n):
     p, v = ics.plummer(max(n, 1), seed=7)
     pos, vel = p[:n].astype(dt), v[:n].astype(dt)
     eps2 = 1e-2 if dt == np.float64 else np.float32(1e-2)
-    with NBodySystem(n, prec, algo, kick="physical", eps2=eps2) as s:
+    with system(n, prec, algo, kick="physical", eps2=eps2) as s:
         s.set_state(pos, vel)
         e = s.energy()
     if n == 0:

@@ -116,6 +116,24 @@ def test_exact_shards_equal_the_oracle(cuda, precision, n, nranks):
     assert got_v.tobytes() == want_v.tobytes()
 
 
+@pytest.mark.parametrize("algo,precision", [("fast", "f32"), ("exact", "f32"), ("exact", "f64")])
+@pytest.mark.parametrize("n,nranks", [(2, 3), (1, 2), (5, 8)])
+def test_more_shards_than_bodies(cuda, algo, precision, n, nranks):
+    """Shards left without targets step nothing and still take part in the
+    exchange; the partition equals the single run bit for bit."""
+    dtype = np.float64 if precision == "f64" else np.float32
+    p, v = ics.plummer(n, seed=31 + n)
+    pos, vel = p.astype(dtype), v.astype(dtype)
+    kw = dict(kick="physical", eps2=float(dtype(1e-2)), damping=1.0, dt=float(dtype(1e-3)))
+    got_p, got_v, ranges = run_shards(n, nranks, 3, precision, algo, pos, vel, **kw)
+    assert sum(c for _, c in ranges) == n and any(c == 0 for _, c in ranges)
+    with NBodySystem(n, precision, algo, **kw) as s:
+        s.set_state(pos, vel)
+        s.step(3)
+        want_p, want_v = s.get_state()
+    assert got_p.tobytes() == want_p.tobytes() and got_v.tobytes() == want_v.tobytes()
+
+
 def test_shard_refusals(cuda):
     lib = N.lib()
     p = N.NbParams()
