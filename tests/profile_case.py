@@ -3,6 +3,7 @@
     python tests/profile_case.py --n 65536 --steps 4 [--algo fast|sym|exact]
         [--precision f32|f32comp|f64] [--case step|adjoint|batch]
         [--block B --bpt K] [--kick physical|reference] [--systems S]
+        [--source-side auto|triangular|fixed]
 
 case step:    `steps` steps of a seeded Plummer sphere (eps2=1e-4, dt=1e-4)
               through the C ABI;
@@ -36,6 +37,8 @@ def main():
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--bpt", type=int, default=0)
     ap.add_argument("--systems", type=int, default=64)
+    ap.add_argument("--source-side", default="auto", choices=["auto", "triangular", "fixed"],
+                    help="source side of the symmetric FP32 kernel")
     a = ap.parse_args()
     import torch
 
@@ -72,7 +75,7 @@ def main():
     p, v = ics.plummer(a.n, seed=0)
     eps2 = 1e-4 if a.precision in ("f32comp", "f64") else np.float32(1e-4)
     with NBodySystem(a.n, a.precision, a.algo, kick=a.kick, eps2=eps2, damping=1.0,
-                     dt=np.float32(1e-4), block=a.block, bpt=a.bpt) as s:
+                     dt=np.float32(1e-4), block=a.block, bpt=a.bpt, source_side=a.source_side) as s:
         if a.precision in ("f32comp", "f64"):
             s.set_state(p, v)
         else:
