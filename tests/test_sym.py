@@ -283,13 +283,14 @@ def test_sym_f64_steps_vs_oracle(cuda, kick, algo):
     assert got.tobytes() == again.tobytes()
 
 
-def test_gpu_scale_positions_after_100_steps_vs_fp64(cuda):
+def test_gpu_scale_positions_after_100_steps_vs_fp64(cuda, capsys):
     """The GPU-scale workload as the bench runs it (N=65536 Plummer,
     eps2 = dt = 1e-4, 100 leapfrog steps): float positions from the symmetric
-    and directed kernels within 1e-5 (|x| + 0.1) of an FP64 run of the same
-    float-rounded start.  The FP64 run is the float-float symmetric kernel
-    for FP64 state, itself held to 1e-13 of the FP64 oracle (test_sym_f64_*);
-    the CPU oracle would need minutes for this size."""
+    kernel (both source sides) and the directed kernel within 1e-5 (|x| + 0.1)
+    of an FP64 run of the same float-rounded start.  The FP64 run is the
+    float-float symmetric kernel for FP64 state, itself held to 1e-13 of the
+    FP64 oracle (test_sym_f64_*); the CPU oracle would need 4-8 minutes for
+    the 4.3e11 FP64 pair terms of this run."""
     n, steps = 65536, 100
     p, v = ics.plummer(n, seed=0)
     p32, v32 = ics.f32(p), ics.f32(v)
@@ -299,14 +300,19 @@ def test_gpu_scale_positions_after_100_steps_vs_fp64(cuda):
         s.step(steps)
         want, _ = s.get_state()
     scale = np.linalg.norm(want[:, :3], axis=1) + 0.1
-    for algo in ("sym", "fast"):
+    worst = {}
+    for algo, side in (("sym", "auto"), ("sym", "fixed"), ("fast", "auto")):
         with NBodySystem(n, "f32", algo, kick="physical", eps2=np.float32(1e-4), damping=1.0,
-                         dt=np.float32(1e-4)) as s:
+                         dt=np.float32(1e-4), source_side=side) as s:
             s.set_state(p32, v32)
             s.step(steps)
             got, _ = s.get_state()
         rel = np.linalg.norm(got[:, :3].astype(np.float64) - want[:, :3], axis=1) / scale
-        assert rel.max() <= 1e-5, (algo, rel.max())
+        worst[f"{algo}/{side}"] = float(rel.max())
+        assert rel.max() <= 1e-5, (algo, side, rel.max())
+    with capsys.disabled():
+        print("\n[N=65536, 100 steps] max |dx|/(|x|+0.1) against the FP64-accurate run: "
+              + ", ".join(f"{k} {v:.1e}" for k, v in worst.items()))
 
 
 def test_sym_fixed_point_steps_and_new_eps2(cuda):
