@@ -10,8 +10,15 @@ from utc_gb300.nbody import NBodySystem
 
 pytestmark = pytest.mark.gpu
 
-MODES = [("f32", "sym"), ("f32", "fast"), ("f32comp", "sym"), ("f32comp", "fast"), ("f64", "sym"),
-         ("f64", "sym64"), ("f32", "exact")]
+# "symfx": the symmetric FP32 kernel with its fixed-point source side
+MODES = [("f32", "sym"), ("f32", "symfx"), ("f32", "fast"), ("f32comp", "sym"), ("f32comp", "fast"),
+         ("f64", "sym"), ("f64", "sym64"), ("f32", "exact")]
+
+
+def system(n, prec, algo, **kw):
+    if algo == "symfx":
+        return NBodySystem(n, prec, "sym", source_side="fixed", **kw)
+    return NBodySystem(n, prec, algo, **kw)
 
 
 def state(prec, n):
@@ -29,7 +36,7 @@ def test_autotune_every_mode(cuda, tmp_path, prec, algo):
     dt = np.float32(1e-3) if prec == "f32" else 1e-3
     cache = str(tmp_path / "tune.txt")
     kw = dict(kick="physical", eps2=eps2, damping=1.0, dt=dt)
-    with NBodySystem(n, prec, algo, **kw) as s:
+    with system(n, prec, algo, **kw) as s:
         s.set_state(pos, vel)
         before = s.get_state()
         shape = s.autotune(reps=1, cache_path=cache)
@@ -41,16 +48,23 @@ def test_autotune_every_mode(cuda, tmp_path, prec, algo):
         assert (info["block"], info["bpt"]) == shape
         s.step(3)
         tuned = s.get_state()
-    with NBodySystem(n, prec, algo, block=shape[0], bpt=shape[1], **kw) as f:
+    with system(n, prec, algo, block=shape[0], bpt=shape[1], **kw) as f:
         f.set_state(pos, vel)
         f.step(3)
         fresh = f.get_state()
     assert tuned[0].tobytes() == fresh[0].tobytes() and tuned[1].tobytes() == fresh[1].tobytes()
     # the cache gives the next context the same shape
-    with NBodySystem(n, prec, algo, **kw) as s2:
+    with system(n, prec, algo, **kw) as s2:
         s2.set_state(pos, vel)
         assert s2.autotune(reps=1, cache_path=cache) == shape
     assert len(open(cache).read().splitlines()) == 1
+    if algo == "sym" and prec == "f32":
+        # a context with the other source side keeps its own cache entry
+        with system(n, prec, "symfx", **kw) as s3:
+            s3.set_state(pos, vel)
+            w, b = s3.autotune(reps=1, cache_path=cache)
+        assert w == 32 and b in (4, 8, 16)
+        assert len(open(cache).read().splitlines()) == 2
 
 
 def test_autotune_drops_a_recorded_adjoint_forward(cuda):

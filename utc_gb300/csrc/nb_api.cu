@@ -1153,6 +1153,7 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
     std::ostringstream key;
     key << "single|" << prop.name << "|sms" << prop.multiProcessorCount << "|prec" << p.precision << "|algo"
         << p.algo << "|n" << p.n;
+    if (c->splan.fixed) key << "|fixedsource";  // its own compiled shapes
     std::string k = key.str();
     for (char &ch : k)
         if (ch == ' ') ch = '_';
