@@ -40,6 +40,9 @@ Extension workloads, one JSON line each (not the headline):
   --workload ics        initial conditions drawn on the GPU (cube, Plummer,
                         the app's shell) at N=2^20 and 2^24: bodies/s and
                         store bandwidth, beside the host generator
+  --workload sharded    one N=1,048,576 system split over the ranks (the
+                        multi-GPU target partition, one all-gather per step),
+                        10 leapfrog steps per bench step: strong scaling
 """
 from __future__ import annotations
 
@@ -1042,6 +1045,62 @@ def run_batched(args):
     return 0
 
 
+def run_sharded(args):
+    """One system split over the ranks (the target partition: directed
+    shards, one all-gather of positions per step, `utc_gb300/shard.py`):
+    N=1,048,576 Plummer, eps2 = dt = 1e-4, 10 leapfrog steps per bench step,
+    timed across ranks (barrier, max over ranks).  Strong scaling: the total
+    work is fixed as ranks are added.  On one GPU the exchange is empty."""
+    import torch
+    import torch.distributed as dist
+
+    from utc_gb300 import ics
+    from utc_gb300.shard import ShardedNBodySystem
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    os.environ.setdefault("NCCL_NVLS_ENABLE", "0")
+    if not dist.is_initialized():
+        if world > 1:
+            dist.init_process_group("nccl", device_id=dev)
+        else:
+            dist.init_process_group("nccl", init_method="tcp://127.0.0.1:29561", rank=0, world_size=1)
+    n = args.n or (1 << 20)
+    leap = 10
+    p, v = ics.plummer(n, seed=0)
+    p32, v32 = ics.f32(p), ics.f32(v)
+    with ShardedNBodySystem(n, "f32", "fast", kick="physical", eps2=float(np.float32(EPS2)), damping=1.0,
+                            dt=float(np.float32(DT))) as s:
+        for _ in range(args.warmup):
+            s.set_state(p32, v32)
+            s.step(leap)
+        torch.cuda.synchronize()
+        dist.barrier()
+        stream = torch.cuda.current_stream()
+        ms = 0.0
+        for _ in range(args.steps):
+            s.set_state(p32, v32)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            s.step(leap)
+            b.record(stream)
+            b.synchronize()
+            ms += a.elapsed_time(b)
+        dist.barrier()
+        ms_max = max_over_ranks(ms, world, dev)
+        counts = [c for _, c in s.ranges]
+    val = float(n) ** 2 * leap * args.steps / (ms_max * 1e-3) / 1e9
+    if rank == 0:
+        print(json.dumps({"workload": "sharded", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world,
+                          "n": n, "leapfrog_steps_per_bench_step": leap, "steps": args.steps,
+                          "ms_per_step": ms_max / args.steps, "scaling": "strong",
+                          "bodies_per_rank": counts, "kernel": "sk_force_kernel shards + all-gather"}),
+              flush=True)
+    dist.destroy_process_group()
+    return 0
+
+
 def run_frames(args):
     """Frame copy-out (body_task_sgpu.cu:116-125): nb_run_host with a frame
     every `oi` steps, pageable and pinned host memory, against the same run
@@ -1132,7 +1191,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the N=1M, adjoint and batched sub-records of the default line")
     ap.add_argument("--workload", default="plain",
-                    choices=["plain", "precision", "adjoint", "batched", "double", "frames", "ics"])
+                    choices=["plain", "precision", "adjoint", "batched", "double", "frames", "ics", "sharded"])
     ap.add_argument("--algo", default="sym", choices=["fast", "sym"],
                     help="force algorithm (plain, adjoint and batched workloads)")
     ap.add_argument("--n", type=int, default=0, help="body count override for extension workloads")
@@ -1154,6 +1213,8 @@ def main():
         return run_frames(args)
     if args.workload == "ics":
         return run_ics(args)
+    if args.workload == "sharded":
+        return run_sharded(args)
     return run_ours(args)
 
 
