@@ -341,7 +341,11 @@ int nb_ics_generate(int kind, int n, unsigned long long seed, double a, double G
                     void *stream);
 size_t nb_ics_scratch_bytes(int n);
 
-/* Device pointers of the current state (valid until the next nb_step). */
+/* Device pointers of the current state (valid until the next nb_step).
+ * A context with the fixed-point source side (nb_params.source_side) takes
+ * the masses into its scale at nb_set_state: after changing pos.w through
+ * these pointers, load the state again with nb_set_state (NB_DEVICE) before
+ * stepping.  Positions and velocities may be written freely. */
 int nb_state_ptrs(nb_ctx *ctx, void **pos_dev, void **vel_dev);
 
 /* Resolved launch shape of the context's force kernel: {block, bpt, grid,
