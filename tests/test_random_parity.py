@@ -58,3 +58,55 @@ def test_random_case(cuda, c):
     scale = np.abs(wdx).max() + 1e-300
     dtol = {"f32": 1e-3, "f32comp": 1e-6, "f64": 1e-10}[prec]
     assert np.abs(dx - wdx).max() <= dtol * scale + 4 * np.finfo(T).eps * (np.abs(wp[:, :3]).max())
+
+
+def cases_more(count=24, seed=4049):
+    """A second sweep over the paths added later: the fixed-point source side
+    of the symmetric kernel, and target partitions of 2 to 5 shards (the
+    directed kernel's and the reference-exact ones, float and double)."""
+    rng = np.random.default_rng(seed)
+    modes = [("symfx", "f32"), ("shard-fast", "f32"), ("shard-exact", "f32"), ("shard-exact", "f64")]
+    for k in range(count):
+        mode, prec = modes[k % len(modes)]
+        yield dict(k=k, mode=mode, prec=prec, n=int(np.exp(rng.uniform(0, np.log(6000)))),
+                   nranks=int(rng.integers(2, 6)), kick=["reference", "physical"][int(rng.integers(2))],
+                   eps2=float(10 ** rng.uniform(-4, -1)), damping=float(rng.choice([1.0, 0.999, 0.995])),
+                   dt=float(10 ** rng.uniform(-4, -2)), G=float(rng.uniform(0.5, 2.0)),
+                   steps=int(rng.integers(1, 5)), ic=["plummer", "cube"][int(rng.integers(2))],
+                   seed=int(rng.integers(1 << 30)))
+
+
+@pytest.mark.parametrize("c", list(cases_more()), ids=lambda c: f"{c['k']}-{c['mode']}-{c['prec']}-n{c['n']}")
+def test_random_case_more(cuda, c):
+    from test_shard_gpu import run_shards
+
+    n, T = c["n"], np.float64 if c["prec"] == "f64" else np.float32
+    p, v = (ics.plummer if c["ic"] == "plummer" else ics.uniform_cube)(n, seed=c["seed"])
+    pos, vel = p.astype(T), v.astype(T)
+    eps2, damp, dt, G = T(c["eps2"]), T(c["damping"]), T(c["dt"]), T(c["G"])
+    km = oracle.KICK_REFERENCE if c["kick"] == "reference" else oracle.KICK_PHYSICAL
+    kw = dict(kick=c["kick"], eps2=float(eps2), damping=float(damp), dt=float(dt))
+    if c["mode"] == "symfx":
+        with NBodySystem(n, "f32", "sym", G=float(G), source_side="fixed", **kw) as s:
+            s.set_state(pos, vel)
+            s.step(c["steps"])
+            gp, _ = s.get_state()
+        wp, _ = oracle.step(np.asarray(pos, np.float64), np.asarray(vel, np.float64), float(eps2), float(damp),
+                            float(dt), c["steps"], kick_mode=km, G=float(G))
+        rel = np.linalg.norm(np.asarray(gp, np.float64)[:, :3] - wp[:, :3], axis=1) / (
+            np.linalg.norm(wp[:, :3], axis=1) + 0.1)
+        assert rel.max() <= 1e-5, rel.max()
+        return
+    algo = "fast" if c["mode"] == "shard-fast" else "exact"
+    if c["kick"] == "physical" and float(G) != 1.0:
+        kw["kick"] = "reference"  # the shard helper takes no G; the reference kick needs none
+        km = oracle.KICK_REFERENCE
+    gp, gv, _ = run_shards(n, c["nranks"], c["steps"], c["prec"], algo, pos, vel, **kw)
+    if algo == "exact":
+        wp, wv = oracle.step(pos, vel, eps2, damp, dt, c["steps"], kick_mode=km)
+    else:
+        with NBodySystem(n, "f32", "fast", **kw) as s:
+            s.set_state(pos, vel)
+            s.step(c["steps"])
+            wp, wv = s.get_state()
+    assert gp.tobytes() == wp.tobytes() and gv.tobytes() == wv.tobytes()
