@@ -4,7 +4,7 @@
   first n % nranks ranks, benchapps/nbody/utc-snode-mgpu/mgpu/
   body_task_mgpu.cu:41-49) and the whole-block split of the directed kernel
   cover 0..n-1 once, in rank order.
-* Two gloo ranks, each advancing only its own targets with the oracle
+* Two and three gloo ranks, each advancing only its own targets with the oracle
   (oracle.step_range, the share of one thread of the reference's multi-GPU
   task) and exchanging positions with ShardExchange after every step, end
   with every body's state equal to the single-process oracle run bit for
@@ -66,15 +66,15 @@ def _rank(rank, world, port, n, steps, outdir):
     dist.destroy_process_group()
 
 
-@pytest.mark.parametrize("n", [1024, 1001])
-def test_two_gloo_ranks_equal_the_single_run(tmp_path, n):
+@pytest.mark.parametrize("n,world", [(1024, 2), (1001, 2), (1001, 3)])
+def test_gloo_ranks_equal_the_single_run(tmp_path, n, world):
     import oracle
 
     oracle.build()
     steps = 5
     ctx = mp.get_context("spawn")
-    port = 29530 + (n % 7)
-    procs = [ctx.Process(target=_rank, args=(r, 2, port, n, steps, str(tmp_path))) for r in range(2)]
+    port = 29530 + (n % 7) + 10 * world
+    procs = [ctx.Process(target=_rank, args=(r, world, port, n, steps, str(tmp_path))) for r in range(world)]
     for p in procs:
         p.start()
     for p in procs:
@@ -82,7 +82,7 @@ def test_two_gloo_ranks_equal_the_single_run(tmp_path, n):
         assert p.exitcode == 0
     pos, vel = oracle.randomize(1, n, np.float32)
     want_p, want_v = oracle.step(pos, vel, np.float32(0.01), np.float32(0.999), np.float32(0.016), steps)
-    for r in range(2):
+    for r in range(world):
         got_p = np.load(tmp_path / f"pos{r}.npy")
         got_v = np.load(tmp_path / f"vel{r}.npy")
         assert got_p.tobytes() == want_p.tobytes()
