@@ -117,7 +117,9 @@ typedef struct nb_params {
     int ctas_per_sm;  /* fast kernel persistent CTAs per SM (0 = occupancy) */
     int memtype;      /* nb_memtype, for nb_run_host staging */
     int source_side;  /* nb_source_side: how NB_ALGO_SYM (NB_F32) sums the
-                         reactions on the source bodies */
+                         reactions on the source bodies; other contexts and
+                         batches ignore it (a value outside the enum is
+                         NB_ERR_INVALID everywhere) */
     int reserved[3];
 } nb_params;
 

@@ -30,7 +30,8 @@ def test_library_exports_every_header_symbol(built):
 
 def test_task_library_exports(built):
     ex = exported(N.TASK_LIB_PATH)
-    for s in ("nbt_run_f32", "nbt_run_f64", "nbt_randomize_f32", "nbt_randomize_f64"):
+    for s in ("nbt_run_f32", "nbt_run_f64", "nbt_randomize_f32", "nbt_randomize_f64", "nbt_mgpu_run_f32",
+              "nbt_mgpu_run_f64"):
         assert s in ex
     N.task_lib()
 
@@ -51,6 +52,8 @@ def _params(**kw):
     (dict(n=8, kick=3), N.NB_ERR_INVALID),
     (dict(n=8, memtype=5), N.NB_ERR_INVALID),
     (dict(n=8, dt=float("nan")), N.NB_ERR_INVALID),
+    (dict(n=8, source_side=3), N.NB_ERR_INVALID),
+    (dict(n=8, source_side=-1, precision=N.NB_F64, algo=N.NB_ALGO_EXACT), N.NB_ERR_INVALID),
     (dict(n=8, precision=N.NB_F64, algo=N.NB_ALGO_FAST), N.NB_ERR_UNSUPPORTED),
     (dict(n=8, precision=N.NB_F32, algo=N.NB_ALGO_SYM_FP64), N.NB_ERR_UNSUPPORTED),
 ])
@@ -67,6 +70,7 @@ def test_create_rejects_bad_params(built, kw, status):
     (dict(eps2=float("inf")), N.NB_ERR_INVALID),
     (dict(dt=float("nan")), N.NB_ERR_INVALID),
     (dict(kick=3), N.NB_ERR_INVALID),
+    (dict(source_side=7), N.NB_ERR_INVALID),
     (dict(precision=N.NB_F64), N.NB_ERR_UNSUPPORTED),
     (dict(algo=N.NB_ALGO_EXACT), N.NB_ERR_UNSUPPORTED),
 ])

@@ -155,6 +155,8 @@ static int validate(const nb_params *p)
         return set_error(NB_ERR_INVALID, "unknown kick mode");
     if (p->memtype < NB_MEM_PAGEABLE || p->memtype > NB_MEM_UNIFIED)
         return set_error(NB_ERR_INVALID, "unknown memtype");
+    if (p->source_side < NB_SOURCE_AUTO || p->source_side > NB_SOURCE_FIXED)
+        return set_error(NB_ERR_INVALID, "unknown source_side");
     if (!std::isfinite(p->eps2) || !std::isfinite(p->damping) || !std::isfinite(p->dt) ||
         !std::isfinite(p->G))
         return set_error(NB_ERR_INVALID, "eps2, damping, dt and G must be finite");

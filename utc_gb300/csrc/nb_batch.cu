@@ -1297,6 +1297,10 @@ int nb_batch_create(const nb_params *p, int nsys, const int *sizes, nb_batch **o
                          "batches run NB_F32 with the fast or symmetric algorithm, or NB_F64 with the symmetric one");
     if (p->kick != NB_KICK_REFERENCE && p->kick != NB_KICK_PHYSICAL)
         return set_error(NB_ERR_INVALID, "unknown kick mode");
+    // batches always keep the triangular source side; the field is checked
+    // only for a valid value
+    if (p->source_side < NB_SOURCE_AUTO || p->source_side > NB_SOURCE_FIXED)
+        return set_error(NB_ERR_INVALID, "unknown source_side");
     if (!std::isfinite(p->eps2) || !std::isfinite(p->damping) || !std::isfinite(p->dt) || !std::isfinite(p->G))
         return set_error(NB_ERR_INVALID, "eps2, damping, dt and G must be finite");
     long long nbody = 0;
