@@ -130,9 +130,11 @@ typedef struct nb_params {
  * order; or added at once into per-body 64-bit fixed-point accumulators with
  * integer atomics, 48 B per body, summed essentially exactly and still
  * deterministic (integer sums do not depend on their order), but measured
- * 2-10 % slower on GB300.  NB_SOURCE_AUTO takes the triangular array unless
- * it would pass 32 GiB at the largest row block (N above about 5e6).  Both
- * are within the same tolerances of the FP64 oracle. */
+ * 2-10 % slower on GB300 at the same launch shape.  NB_SOURCE_AUTO takes
+ * the triangular array while it fits in 8 GiB with 4 warps x 20 targets per
+ * lane (N up to about 1.66e6), and the fixed-point side beyond (3 % faster
+ * there than the one shape whose array would still fit, and 48 B per body).
+ * Both are within the same tolerances of the FP64 oracle. */
 typedef enum { NB_SOURCE_AUTO = 0, NB_SOURCE_TRIANGULAR = 1, NB_SOURCE_FIXED = 2 } nb_source_side;
 
 typedef struct nb_ctx nb_ctx;

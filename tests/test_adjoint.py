@@ -19,12 +19,20 @@ def rel(a, b):
     return float(np.linalg.norm(np.asarray(a, np.float64) - b) / (np.linalg.norm(b) + 1e-300))
 
 
+def system(n, algo, **kw):
+    """algo "fast": directed forward and VJP kernels; "sym": symmetric ones;
+    "symfx": symmetric ones, the forward with its fixed-point source side
+    (the automatic choice for N above about 1.66e6)."""
+    if algo == "symfx":
+        return NBodySystem(n, "f32", "sym", source_side="fixed", **kw)
+    return NBodySystem(n, "f32", algo, **kw)
+
+
 def gpu_grads(pos32, vel32, y, kick, eps2, dt, damping, steps, every, G=1.0, algo="fast"):
-    """algo "fast": directed forward and VJP kernels; "sym": symmetric ones."""
     import torch
 
     n = pos32.shape[0]
-    with NBodySystem(n, "f32", algo, kick=kick, eps2=eps2, damping=damping, dt=dt, G=G) as s:
+    with system(n, algo, kick=kick, eps2=eps2, damping=damping, dt=dt, G=G) as s:
         s.set_state(pos32, vel32)
         s.adj_forward(steps, every)
         pT, _ = s.get_state()
@@ -35,7 +43,7 @@ def gpu_grads(pos32, vel32, y, kick, eps2, dt, damping, steps, every, G=1.0, alg
         return pT, gx0[:, :3].cpu().numpy(), gv0[:, :3].cpu().numpy(), gm.cpu().numpy()
 
 
-@pytest.mark.parametrize("algo", ["fast", "sym"])
+@pytest.mark.parametrize("algo", ["fast", "sym", "symfx"])
 @pytest.mark.parametrize("kick", ["physical", "reference"])
 @pytest.mark.parametrize("n,steps,every", [(96, 30, 7), (1000, 20, 20), (257, 12, 1), (3000, 6, 4)])
 def test_adjoint_matches_fp64_reference(cuda, algo, kick, n, steps, every):
@@ -54,7 +62,7 @@ def test_adjoint_matches_fp64_reference(cuda, algo, kick, n, steps, every):
     assert rel(gm, rm) <= 1e-4
 
 
-@pytest.mark.parametrize("algo", ["fast", "sym"])
+@pytest.mark.parametrize("algo", ["fast", "sym", "symfx"])
 def test_checkpoint_interval_does_not_change_gradients(cuda, algo):
     n, steps = 300, 24
     p64, v64 = ics.uniform_cube(n, seed=3)
@@ -114,7 +122,7 @@ def test_autograd_function_loss_gradients(cuda):
     assert torch.equal(m.grad, dm)
 
 
-@pytest.mark.parametrize("algo", ["fast", "sym"])
+@pytest.mark.parametrize("algo", ["fast", "sym", "symfx"])
 @pytest.mark.parametrize("kick", ["physical", "reference"])
 def test_second_backward_recomputes_every_segment(cuda, algo, kick):
     """The forward pass leaves the last segment's states in place and the first
@@ -127,8 +135,7 @@ def test_second_backward_recomputes_every_segment(cuda, algo, kick):
     if kick == "reference":
         p64[:, 3] *= n
     p32, v32 = ics.f32(p64), ics.f32(v64)
-    with NBodySystem(n, "f32", algo, kick=kick, eps2=np.float32(1e-2), damping=0.999,
-                     dt=np.float32(1e-3)) as s:
+    with system(n, algo, kick=kick, eps2=np.float32(1e-2), damping=0.999, dt=np.float32(1e-3)) as s:
         s.set_state(p32, v32)
         s.adj_forward(steps, every)
         gx = torch.randn((n, 4), device="cuda")

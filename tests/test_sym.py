@@ -90,16 +90,17 @@ def test_sym_adjoint_matches_directed_adjoint(cuda):
 
 
 @pytest.mark.parametrize("n,shape", [(65536, (32, 16)), (1048576, (128, 20)), (1024, (32, 4)),
-                                     (4096, (32, 8)), (16384, (32, 16)), (6000000, (32, 16))])
+                                     (4096, (32, 8)), (16384, (32, 16)), (1600000, (128, 20)),
+                                     (1700000, (32, 16)), (2097152, (32, 16)), (6000000, (32, 16))])
 def test_sym_default_shape(cuda, n, shape):
     """One-warp CTAs x 16 targets unless the triangular source-side array
     (about N^2 / (2 rb) float4) would pass 8 GiB, then 4 warps x 20 targets;
     small systems drop to 8 or 4 targets per lane to keep four (row, chunk)
     items per SM.  With the fixed-point source side: one warp x 16 at any
-    size (48 B per body whatever the row block).  At N = 6e6 the triangular
-    array would pass 32 GiB even at the largest row block (8 x 24: 44 GiB),
-    so the automatic choice is the fixed-point source side: the context then
-    holds well under 1 GB."""
+    size (48 B per body whatever the row block).  Once the 4 x 20 array
+    would pass 8 GiB too (N above about 1.66e6: 8.0 GB at 1.6e6, 9.0 GB at
+    1.7e6), the automatic choice is the fixed-point source side: the context
+    then holds well under 1 GB."""
     import torch
 
     torch.cuda.synchronize()
@@ -108,7 +109,7 @@ def test_sym_default_shape(cuda, n, shape):
         info = s.plan_info()
         used = free0 - torch.cuda.mem_get_info()[0]
     assert (info["block"], info["bpt"]) == shape
-    if n == 6000000:
+    if n > 1650000:
         assert used < 1 << 30, used
     with NBodySystem(n, "f32", "sym", source_side="fixed") as s:
         info = s.plan_info()

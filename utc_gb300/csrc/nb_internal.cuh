@@ -307,12 +307,9 @@ inline long long sym_spart_entries(int n, int rb)
     return nrb > 1 ? sym_soff(nrb - 1, n, rb) : 0;
 }
 // Largest source-side array a default shape accepts before it moves to a
-// bigger row block.
+// bigger row block (or, for the automatic source side of the plain kernel,
+// to the fixed-point one).
 constexpr long long kSymSpartBudget = 8ll << 30;
-
-// Largest triangular array the automatic choice accepts at the largest row
-// block before it takes the fixed-point source side.
-constexpr long long kSymSpartMax = 32ll << 30;
 // float4 entries of the fixed-point source side: 6 n 64-bit accumulators
 // (hi x, y, z then lo x, y, z, each n long) and one float4 record: the sum of
 // |m| over the bodies and the scale factors (sym_fx_prepare).

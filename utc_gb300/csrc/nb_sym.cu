@@ -28,8 +28,8 @@
 // its source-side entries spart[0..I_b-1][b] (row order): deterministic.
 //
 // Fixed-point source side (template flag FX; plans with fixed = 1, chosen
-// by nb_params.source_side or when the triangular array would not fit: it
-// holds about N^2 / (2 rb) float4).  The CTA's reaction on a chunk body,
+// by nb_params.source_side or for large N, where the triangular array,
+// about N^2 / (2 rb) float4, would need a slow shape to stay in budget).  The CTA's reaction on a chunk body,
 // summed over its warps as above, is added straight into per-body 64-bit
 // integer accumulators with integer atomics.  Integer addition is
 // associative, so the sums do not depend on the order the CTAs run in: the
@@ -45,9 +45,12 @@
 // sits in a record after the accumulators, written at nb_set_state (and for
 // a new eps2) by sym_fx_prepare / sym_fx_rescale; the integrator zeroes the
 // accumulators after reading them.  On GB300 this variant ran 2-10 % slower
-// than the triangular array at N = 65536 in every arrangement tried (the
-// pair loop's schedule shifts with the code around it), so it is used only
-// where the array would not fit or where a caller asks for it.
+// than the triangular array of the same shape (the pair loop's schedule
+// shifts with the code around it), 4 % slower than the 4 x 20 triangular
+// shape at N = 2^21, but 3 % faster than the 8 x 24 one, the only shape
+// whose array stays within budget there.  So it is the automatic choice
+// where 4 x 20 would pass the budget (N above about 1.66e6), and otherwise
+// only where a caller asks for it.
 //
 // Compensated variant (COMP): each target's per-chunk partial sum (32
 // sources) is folded into a two-sum (hi, lo) pair, the W warps' reactions on
@@ -529,9 +532,15 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int s
         return set_error(NB_ERR_UNSUPPORTED, "the compensated kernel keeps its triangular (hi, lo) source side");
     int fixed = source_side == NB_SOURCE_FIXED ? 1 : 0;
     const bool given = warps != 0 || bpt != 0;
+    // automatic: the triangular array while the 4 x 20 shape keeps it within
+    // budget; beyond that (N above about 1.66e6) the fixed-point source side
+    // with one warp x 16 targets, which ran 3 % faster on GB300 than the
+    // 8 x 24 shape that would keep the array within budget (3510 against
+    // 3405 G interactions/s at N = 2^21, 3514 against 3394 at 2^22) and
+    // takes 48 B per body
     if (!given && !fixed && !comp && source_side == NB_SOURCE_AUTO &&
-        sym_spart_entries(n, 8 * 32 * 24) * (long long)sizeof(float4) > kSymSpartMax)
-        fixed = 1;  // the triangular array would not fit even at the largest row block
+        sym_spart_entries(n, 4 * 32 * 20) * (long long)sizeof(float4) > kSymSpartBudget)
+        fixed = 1;
     if (!given && fixed) {
         warps = 1;
         bpt = 16;
@@ -545,7 +554,8 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int s
     }
     if (warps == 0 && bpt == 0) {
         // plain: one-warp CTAs x 16 targets (row block 512); then 4 x 20
-        // (2560), 8 x 24 (6144) while the source-side array is over budget.
+        // (2560), 8 x 24 (6144) while the source-side array is over budget
+        // (8 x 24 only when the triangular side is asked for).
         // Compensated (hi and lo halves): 1 x 12 (384), 4 x 12 (1536),
         // 8 x 12 (3072).
         static const int plain[3][2] = {{1, 16}, {4, 20}, {8, 24}};
