@@ -163,10 +163,14 @@ int nb_set_state(nb_ctx *ctx, const void *pos, const void *vel, int where, void 
 int nb_get_state(nb_ctx *ctx, void *pos, void *vel, int where, void *stream);
 
 /* Advance `steps` steps on `stream` (asynchronous).  Replaces the launch
- * loop of BodySystemSGPU::runImpl, body_task_sgpu.cu:85-127.  On a stream
- * other than the legacy default stream, bulk steps replay a captured CUDA
- * graph; a capture that another thread's device-wide call invalidates is
- * dropped and those steps are launched one by one (same results). */
+ * loop of BodySystemSGPU::runImpl, body_task_sgpu.cu:85-127.  Bulk steps
+ * (32 or more in one call) replay a captured CUDA graph; on the legacy
+ * default stream, which cannot be captured, they run on a stream of the
+ * context's own, after an event recorded on the caller's stream, and the
+ * caller's stream waits for their end (so the call stays ordered like any
+ * other work on it).  A capture that another thread's device-wide call
+ * invalidates is dropped and those steps are launched one by one (same
+ * results). */
 int nb_step(nb_ctx *ctx, int steps, void *stream);
 
 /* Change eps2 (the softening squared), damping, dt and G of a context (or of

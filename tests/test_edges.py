@@ -127,10 +127,13 @@ def test_batch_of_single_bodies(cuda, algo):
 
 
 @pytest.mark.parametrize("prec,algo", MODES)
-def test_graph_replay_equals_single_steps(cuda, prec, algo):
-    """nb_step on a non-default stream replays a captured graph of steps; the
-    result must equal stepping one launch pair at a time, from either
-    ping-pong buffer."""
+@pytest.mark.parametrize("where", ["side", "legacy"])
+def test_graph_replay_equals_single_steps(cuda, prec, algo, where):
+    """nb_step replays a captured graph of steps, on a non-default stream
+    directly and from the legacy default stream through the context's own
+    stream (ordered by events both ways, so the calls around it on the legacy
+    stream need no synchronisation); the result must equal stepping one
+    launch pair at a time, from either ping-pong buffer."""
     import torch
 
     dt_ = dtype_of(prec)
@@ -145,38 +148,48 @@ def test_graph_replay_equals_single_steps(cuda, prec, algo):
         want = s.get_state()
         s.set_state(p, v)
         s.step(1)  # odd start: the graph begins from the second buffer
-        torch.cuda.synchronize()
-        with torch.cuda.stream(side):
-            s.step(70, stream=side.cuda_stream)
-            side.synchronize()
+        if where == "side":
+            torch.cuda.synchronize()
+            with torch.cuda.stream(side):
+                s.step(70, stream=side.cuda_stream)
+                side.synchronize()
+        else:
+            s.step(70, stream=0)
         got = s.get_state()
     assert got[0].tobytes() == want[0].tobytes() and got[1].tobytes() == want[1].tobytes()
 
 
 def test_graph_replay_speeds_up_small_systems(cuda, capsys):
+    """Calls of fewer than 32 steps launch kernel by kernel; longer ones
+    replay graphs, on a non-default stream and from the legacy one."""
     import torch
 
     n, steps = 1024, 320
     p, v = ics.plummer(n, seed=6)
     side = torch.cuda.Stream()
+    legacy = torch.cuda.default_stream()
     with NBodySystem(n, "f32", "sym", kick="physical", eps2=np.float32(1e-3), dt=np.float32(1e-3)) as s:
         s.set_state(ics.f32(p), ics.f32(v))
         times = {}
-        for name, st in (("launches", None), ("graph", side.cuda_stream)):
-            with torch.cuda.stream(side if st else torch.cuda.current_stream()):
-                cur = torch.cuda.current_stream()
-                s.step(steps, stream=cur.cuda_stream if st else 0)  # warm-up (captures the graph)
-                cur.synchronize()
+        for name, st, per_call in (("launches", legacy, 16), ("graph", side, steps),
+                                   ("graph_legacy", legacy, steps)):
+            with torch.cuda.stream(st):
+                h = 0 if st is legacy else st.cuda_stream
+                s.step(steps, stream=h)  # warm-up (captures the graph)
+                st.synchronize()
                 a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(cur)
-                s.step(steps, stream=cur.cuda_stream if st else 0)
-                b.record(cur)
+                a.record(st)
+                for _ in range(steps // per_call):
+                    s.step(per_call, stream=h)
+                b.record(st)
                 b.synchronize()
                 times[name] = a.elapsed_time(b) / steps
     with capsys.disabled():
         print(f"\n[small N] N={n}: {times['launches'] * 1e3:.1f} us/step launched, "
-              f"{times['graph'] * 1e3:.1f} us/step from the graph")
+              f"{times['graph'] * 1e3:.1f} us/step from the graph, "
+              f"{times['graph_legacy'] * 1e3:.1f} from the legacy stream")
     assert times["graph"] < times["launches"]
+    assert times["graph_legacy"] < times["launches"]
 
 
 @pytest.mark.parametrize("prec,algo", MODES)

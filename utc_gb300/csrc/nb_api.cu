@@ -100,6 +100,11 @@ struct nb_ctx {
     // steps (one per starting ping-pong buffer): small systems are otherwise
     // bound by the per-kernel launch cost
     cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
+    // nb_step on the legacy default stream, which cannot be captured: the
+    // steps run on this non-blocking stream instead, after an event recorded
+    // on the caller's stream, and the caller's stream waits for a second one
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t side_ev[2] = {nullptr, nullptr};
     // shard of a multi-GPU target partition (nb_create_shard): this context
     // updates targets [shard_lo, shard_hi) of all n bodies; shard_count 1 is
     // a whole system
@@ -222,6 +227,9 @@ static void free_ctx(nb_ctx *c)
         if (c->ev_c1[k]) cudaEventDestroy(c->ev_c1[k]);
     }
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    for (cudaEvent_t e : c->side_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->side_stream) cudaStreamDestroy(c->side_stream);
     delete c;
 }
 
@@ -647,6 +655,26 @@ static void capture_step_graph(nb_ctx *c, cudaStream_t s, cudaGraphExec_t *out)
     (void)cudaGetLastError();  // a capture that did not take leaves its error behind
 }
 
+// The side stream of nb_step and its two events, made on first use; all or
+// nothing, so that a failed call leaves nothing half set up.
+static int make_side_stream(nb_ctx *c)
+{
+    cudaStream_t ss = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaError_t e = cudaStreamCreateWithFlags(&ss, cudaStreamNonBlocking);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        if (ss) cudaStreamDestroy(ss);
+        return nb::cuda_error(e, "nb_step: side stream setup");
+    }
+    c->side_ev[0] = ev[0];
+    c->side_ev[1] = ev[1];
+    c->side_stream = ss;
+    return NB_OK;
+}
+
 extern "C" {
 
 int nb_step(nb_ctx *c, int steps, void *stream)
@@ -660,10 +688,26 @@ int nb_step(nb_ctx *c, int steps, void *stream)
     cudaStream_t s = (cudaStream_t)stream;
     int st;
     if ((st = fx_refresh(c, s))) return st;
-    // the legacy default stream cannot be captured: launch step by step there,
-    // and also on a stream the caller is capturing into a graph of its own
-    // (the launches then go into the caller's graph)
-    bool graphs = s != nullptr && s != cudaStreamLegacy && c->p.n > 0;
+    const bool legacy = s == nullptr || s == cudaStreamLegacy;
+    if (legacy && c->p.n > 0 && steps >= 2 * kGraphSteps) {
+        // the legacy default stream cannot be captured: enough steps for a
+        // graph run on the side stream, ordered after the caller's earlier
+        // work, and the caller's later work waits for them
+        if (!c->side_stream && (st = make_side_stream(c))) return st;
+        NB_CUDA(cudaEventRecord(c->side_ev[0], s));
+        NB_CUDA(cudaStreamWaitEvent(c->side_stream, c->side_ev[0], 0));
+        st = nb_step(c, steps, (void *)c->side_stream);
+        // joined also after a failure, for whatever the steps launched
+        cudaError_t e = cudaEventRecord(c->side_ev[1], c->side_stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->side_ev[1], 0);
+        if (st) return st;
+        if (e != cudaSuccess) return nb::cuda_error(e, "nb_step: ordering the caller's stream after the steps");
+        return NB_OK;
+    }
+    // launch step by step on the legacy default stream (a few steps), and
+    // also on a stream the caller is capturing into a graph of its own (the
+    // launches then go into the caller's graph)
+    bool graphs = !legacy && c->p.n > 0;
     if (graphs) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         NB_CUDA(cudaStreamIsCapturing(s, &cs));
