@@ -120,7 +120,13 @@ typedef struct nb_params {
                          reactions on the source bodies; other contexts and
                          batches ignore it (a value outside the enum is
                          NB_ERR_INVALID everywhere) */
-    int reserved[3];
+    int bands;        /* NB_ALGO_SYM with the triangular source side (NB_F32
+                         and NB_F64): 0 = cut the rows into bands only where
+                         the array would pass 8 GiB; k > 1 = about k bands
+                         (smaller scratch; for tests and tight memory);
+                         other values NB_ERR_INVALID; other contexts and
+                         batches ignore it */
+    int reserved[2];
 } nb_params;
 
 /* Source side of the symmetric FP32 kernel (nb_params.source_side).  Each
@@ -360,6 +366,12 @@ int nb_state_ptrs(nb_ctx *ctx, void **pos_dev, void **vel_dev);
  * target block size, slots}; for the symmetric kernels block = warps per
  * CTA * 32, bpt = targets per lane and the target block is the row block. */
 int nb_plan_info(nb_ctx *ctx, int *info5);
+
+/* Source side of a symmetric context: info4 = {source side (NB_SOURCE_FIXED
+ * or NB_SOURCE_TRIANGULAR), bands of the triangular array (1 = one pass),
+ * MiB of scratch the source side holds (the largest band's share),
+ * 0 (reserved)}.  Other contexts give {0, 1, 0, 0}. */
+int nb_source_info(nb_ctx *ctx, int *info4);
 
 /* Time every compiled launch shape of the context's force kernel on its
  * current state (`reps` steps each; the state is restored) and keep the

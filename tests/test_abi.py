@@ -53,6 +53,9 @@ def _params(**kw):
     (dict(n=8, memtype=5), N.NB_ERR_INVALID),
     (dict(n=8, dt=float("nan")), N.NB_ERR_INVALID),
     (dict(n=8, source_side=3), N.NB_ERR_INVALID),
+    (dict(n=8, bands=1), N.NB_ERR_INVALID),
+    (dict(n=8, bands=-1), N.NB_ERR_INVALID),
+    (dict(n=8, bands=513), N.NB_ERR_INVALID),
     (dict(n=8, source_side=-1, precision=N.NB_F64, algo=N.NB_ALGO_EXACT), N.NB_ERR_INVALID),
     (dict(n=8, precision=N.NB_F64, algo=N.NB_ALGO_FAST), N.NB_ERR_UNSUPPORTED),
     (dict(n=8, precision=N.NB_F32, algo=N.NB_ALGO_SYM_FP64), N.NB_ERR_UNSUPPORTED),

@@ -10,14 +10,17 @@ from utc_gb300.nbody import NBodySystem
 
 pytestmark = pytest.mark.gpu
 
-# "symfx": the symmetric FP32 kernel with its fixed-point source side
-MODES = [("f32", "sym"), ("f32", "symfx"), ("f32", "fast"), ("f32comp", "sym"), ("f32comp", "fast"),
-         ("f64", "sym"), ("f64", "sym64"), ("f32", "exact")]
+# "symfx": the symmetric FP32 kernel with its fixed-point source side;
+# "symband": the symmetric kernel with its triangular array in three bands
+MODES = [("f32", "sym"), ("f32", "symfx"), ("f32", "symband"), ("f32", "fast"), ("f32comp", "sym"),
+         ("f32comp", "fast"), ("f64", "sym"), ("f64", "sym64"), ("f32", "exact")]
 
 
 def system(n, prec, algo, **kw):
     if algo == "symfx":
         return NBodySystem(n, prec, "sym", source_side="fixed", **kw)
+    if algo == "symband":
+        return NBodySystem(n, prec, "sym", bands=3, **kw)
     return NBodySystem(n, prec, algo, **kw)
 
 

@@ -89,31 +89,87 @@ def test_sym_adjoint_matches_directed_adjoint(cuda):
         assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("n,shape", [(65536, (32, 16)), (1048576, (128, 20)), (1024, (32, 4)),
-                                     (4096, (32, 8)), (16384, (32, 16)), (1600000, (128, 20)),
-                                     (1700000, (32, 16)), (2097152, (32, 16)), (6000000, (32, 16))])
-def test_sym_default_shape(cuda, n, shape):
+@pytest.mark.parametrize("n,shape,bands", [(65536, (32, 16), 1), (1048576, (128, 20), 1), (1024, (32, 4), 1),
+                                           (4096, (32, 8), 1), (16384, (32, 16), 1), (1600000, (128, 20), 1),
+                                           (1700000, (128, 20), 2), (2097152, (128, 20), 2),
+                                           (6000000, (128, 20), 14)])
+def test_sym_default_shape(cuda, n, shape, bands):
     """One-warp CTAs x 16 targets unless the triangular source-side array
     (about N^2 / (2 rb) float4) would pass 8 GiB, then 4 warps x 20 targets;
     small systems drop to 8 or 4 targets per lane to keep four (row, chunk)
-    items per SM.  With the fixed-point source side: one warp x 16 at any
-    size (48 B per body whatever the row block).  Once the 4 x 20 array
-    would pass 8 GiB too (N above about 1.66e6: 8.0 GB at 1.6e6, 9.0 GB at
-    1.7e6), the automatic choice is the fixed-point source side: the context
-    then holds well under 1 GB."""
+    items per SM.  Once the 4 x 20 array would pass 8 GiB too (N above about
+    1.66e6: 8.0 GB at 1.6e6, 9.0 GB at 1.7e6), it is cut into bands of at
+    most 8 GiB (112 GB in 14 bands at N = 6e6), so the context stays within
+    about 9 GB.  With the fixed-point source side: one warp x 16 at any size
+    (48 B per body whatever the row block)."""
     import torch
 
     torch.cuda.synchronize()
     free0 = torch.cuda.mem_get_info()[0]
     with NBodySystem(n, "f32", "sym") as s:
         info = s.plan_info()
+        src = s.source_info()
         used = free0 - torch.cuda.mem_get_info()[0]
     assert (info["block"], info["bpt"]) == shape
-    if n > 1650000:
-        assert used < 1 << 30, used
+    assert src["side"] == "triangular" and src["bands"] == bands, src
+    assert src["mib"] <= 8192
+    assert used < 10 << 30, used
     with NBodySystem(n, "f32", "sym", source_side="fixed") as s:
         info = s.plan_info()
     assert (info["block"], info["bpt"]) == (32, min(shape[1], 16))
+
+
+@pytest.mark.parametrize("n", [700, 4097, 20000])
+@pytest.mark.parametrize("bands", [2, 3, 7])
+@pytest.mark.parametrize("shape", [(0, 0), (128, 20), (32, 8)])
+def test_sym_bands_vs_fp64(cuda, n, bands, shape):
+    """The triangular source side cut into bands (nb_params.bands): the
+    force kernel runs band by band and a fold kernel adds each band's
+    target-side slots and source-side rows into one sum per body.
+    Accelerations within 2e-5 of the FP64 oracle for every banded shape;
+    reruns and a second context give the same bits; the scratch of the
+    source side shrinks with the band count."""
+    p, _ = ics.plummer(n, seed=n + 11)
+    pos = ics.f32(p)
+    z = np.zeros_like(pos)
+    want = oracle.accel(pos.astype(np.float64), float(np.float32(1e-3)))
+    outs = []
+    for _ in range(2):
+        with NBodySystem(n, "f32", "sym", eps2=np.float32(1e-3), block=shape[0], bpt=shape[1],
+                         bands=bands) as s:
+            info = s.source_info()
+            rb = s.plan_info()["tbsize"]
+            s.set_state(pos, z)
+            a = s.accel()
+            assert a.tobytes() == s.accel().tobytes()
+            outs.append(a)
+    nrb = -(-n // rb)
+    # about `bands` bands: whole row blocks each, so a few more where rows are long
+    assert info["side"] == "triangular" and 1 <= info["bands"] <= nrb, info
+    if nrb > bands:
+        assert info["bands"] > 1, info
+    assert close(outs[0], want)
+    assert outs[0].tobytes() == outs[1].tobytes()
+
+
+@pytest.mark.parametrize("kick", ["reference", "physical"])
+def test_sym_bands_steps_vs_oracle(cuda, kick):
+    """Leapfrog steps with a banded plan (graph replay included) against the
+    FP64 oracle, as test_sym_steps_vs_oracle does for one pass."""
+    n, steps = 4096, 40
+    p, v = ics.uniform_cube(n, seed=7)
+    pos, vel = ics.f32(p), ics.f32(v)
+    km = oracle.KICK_REFERENCE if kick == "reference" else oracle.KICK_PHYSICAL
+    with NBodySystem(n, "f32", "sym", kick=kick, eps2=np.float32(1e-2), damping=1.0, dt=np.float32(1e-3),
+                     bands=4) as s:
+        assert s.source_info()["bands"] > 1
+        s.set_state(pos, vel)
+        s.step(steps)
+        got, _ = s.get_state()
+    want, _ = oracle.step(pos.astype(np.float64), vel.astype(np.float64), float(np.float32(1e-2)), 1.0,
+                          float(np.float32(1e-3)), steps, kick_mode=km)
+    rel = np.linalg.norm(got[:, :3] - want[:, :3], axis=1) / (np.linalg.norm(want[:, :3], axis=1) + 0.1)
+    assert rel.max() <= 1e-5
 
 
 @pytest.mark.parametrize("n", [4096, 65536])

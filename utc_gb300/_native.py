@@ -29,7 +29,7 @@ class NbParams(C.Structure):
         ("n", C.c_int), ("precision", C.c_int), ("algo", C.c_int), ("kick", C.c_int),
         ("eps2", C.c_double), ("damping", C.c_double), ("dt", C.c_double), ("G", C.c_double),
         ("block", C.c_int), ("bpt", C.c_int), ("ctas_per_sm", C.c_int), ("memtype", C.c_int),
-        ("source_side", C.c_int), ("reserved", C.c_int * 3),
+        ("source_side", C.c_int), ("bands", C.c_int), ("reserved", C.c_int * 2),
     ]
 
 
@@ -64,6 +64,7 @@ def _declare(lib):
         "nb_run_host": (I, [vp, vp, vp, I, I, vp, P(D), vp]),
         "nb_state_ptrs": (I, [vp, P(vp), P(vp)]),
         "nb_plan_info": (I, [vp, P(I)]),
+        "nb_source_info": (I, [vp, P(I)]),
         "nb_launches_per_step": (I, [vp]),
         "nb_probe_fma_peak": (I, [I, I, P(D), P(C.c_float), vp]),
         "nb_create_shard": (I, [P(NbParams), I, I, P(vp)]),

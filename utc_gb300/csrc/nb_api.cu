@@ -92,6 +92,9 @@ struct nb_ctx {
     // symmetric algorithm: plan and its two partial arrays
     nb::SymPlan splan;
     float4 *sym_t = nullptr, *sym_s = nullptr;
+    // banded plans: the per-body sums the fold kernel builds band by band
+    // (float4, or double4 for FP64 state)
+    void *sym_acc = nullptr;
     // float-float path for FP64 state: scaled three-float positions (3 n
     // float4) and the per-step scale record
     float4 *ff_split = nullptr;
@@ -162,6 +165,8 @@ static int validate(const nb_params *p)
         return set_error(NB_ERR_INVALID, "unknown memtype");
     if (p->source_side < NB_SOURCE_AUTO || p->source_side > NB_SOURCE_FIXED)
         return set_error(NB_ERR_INVALID, "unknown source_side");
+    if (p->bands < 0 || p->bands == 1 || p->bands > nb::SymPlan::kMaxBands)
+        return set_error(NB_ERR_INVALID, "bands is 0 (automatic) or 2..512");
     if (!std::isfinite(p->eps2) || !std::isfinite(p->damping) || !std::isfinite(p->dt) ||
         !std::isfinite(p->G))
         return set_error(NB_ERR_INVALID, "eps2, damping, dt and G must be finite");
@@ -217,6 +222,7 @@ static void free_ctx(nb_ctx *c)
     if (c->adj.ev_go) cudaEventDestroy(c->adj.ev_go);
     nb::dfree(c->sym_t);
     nb::dfree(c->sym_s);
+    nb::dfree(c->sym_acc);
     nb::dfree(c->ff_split);
     nb::dfree(c->ff_range);
     for (int k = 0; k < 2; ++k) {
@@ -363,10 +369,13 @@ int nb_create(const nb_params *p, nb_ctx **out)
         if (uses_sym(c) || comp_sym(c)) {
             const size_t halves = comp_sym(c) ? 2 : 1;  // compensated: hi and lo blocks
             if ((st = nb::sym_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan,
-                                   comp_sym(c) ? 1 : 0, comp_sym(c) ? NB_SOURCE_AUTO : p->source_side)) ||
+                                   comp_sym(c) ? 1 : 0, comp_sym(c) ? NB_SOURCE_AUTO : p->source_side,
+                                   comp_sym(c) ? -1 : p->bands)) ||
                 (st = dev_alloc((void **)&c->sym_t,
                                 halves * c->splan.slots * c->splan.rb * sizeof(float4),
                                 "symmetric scratch allocation")) ||
+                (c->splan.nbands > 1 &&
+                 (st = dev_alloc(&c->sym_acc, n * sizeof(float4), "per-body sums of the banded source side"))) ||
                 (st = dev_alloc((void **)&c->sym_s, halves * c->splan.spart_size * sizeof(float4),
                                 c->splan.fixed ? "symmetric source-side accumulators (48 B per body)"
                                                : "symmetric source-side array (about N^2/(2 rb) entries; "
@@ -549,7 +558,7 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
     int st;
     if (ev) NB_CUDA(cudaEventRecord(ev[0], s));
     if (comp_sym(c)) {
-        st = nb::sym_force(c->splan, c->pos32, (float)p.eps2, c->sym_t, c->sym_s, s);
+        st = nb::sym_force(c->splan, c->pos32, (float)p.eps2, c->sym_t, c->sym_s, nullptr, s);
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
         if (!st)
             st = nb::sym_comp_integrate(c->splan, c->sym_t, c->sym_s, (double4 *)c->pos[0], c->pos32,
@@ -591,16 +600,18 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
                                 (float)p.eps2, (float)p.damping, (float)p.dt, p.kick, (float)p.G,
                                 (float4 *)acc_out, p.block, s);
     } else if (p.algo == NB_ALGO_SYM) {
-        st = nb::sym_force(c->splan, (const float4 *)po, (float)p.eps2, c->sym_t, c->sym_s, s);
+        st = nb::sym_force(c->splan, (const float4 *)po, (float)p.eps2, c->sym_t, c->sym_s,
+                           (float4 *)c->sym_acc, s);
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
         if (!st && acc_keep)
             st = nb::sym_integrate(c->splan, (const float4 *)po, nullptr, nullptr, c->sym_t, c->sym_s,
+                                   (const float4 *)c->sym_acc,
                                    (float)p.damping, (float)p.dt, p.kick, (float)p.G, acc_keep,
                                    s, 0);
         if (!st)
             st = nb::sym_integrate(c->splan, (const float4 *)po, (float4 *)pn, (float4 *)c->vel,
-                                   c->sym_t, c->sym_s, (float)p.damping, (float)p.dt, p.kick,
-                                   (float)p.G, (float4 *)acc_out, s);
+                                   c->sym_t, c->sym_s, (const float4 *)c->sym_acc, (float)p.damping,
+                                   (float)p.dt, p.kick, (float)p.G, (float4 *)acc_out, s);
     } else {
         st = nb::fast_force(c->plan, (const float4 *)po, (float)p.eps2, c->partial, s);
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
@@ -1053,13 +1064,15 @@ int nb_adj_backward(nb_ctx *c, unsigned long long generation, const void *gx_T, 
             const float4 *xk = sp + (size_t)k * n;
             float4 *xn = sp + (size_t)(k + 1) * n;
             if (uses_sym(c)) {
-                if ((st2 = nb::sym_force(c->splan, xk, eps2, c->sym_t, c->sym_s, rs))) return st2;
+                if ((st2 = nb::sym_force(c->splan, xk, eps2, c->sym_t, c->sym_s, (float4 *)c->sym_acc, rs)))
+                    return st2;
                 if (p.kick == NB_KICK_REFERENCE &&
-                    (st2 = nb::sym_integrate(c->splan, xk, nullptr, nullptr, c->sym_t, c->sym_s, D, dt,
+                    (st2 = nb::sym_integrate(c->splan, xk, nullptr, nullptr, c->sym_t, c->sym_s,
+                                             (const float4 *)c->sym_acc, D, dt,
                                              p.kick, G, sa + (size_t)k * n, rs, 0)))
                     return st2;
-                if ((st2 = nb::sym_integrate(c->splan, xk, xn, vt, c->sym_t, c->sym_s, D, dt, p.kick, G,
-                                             nullptr, rs)))
+                if ((st2 = nb::sym_integrate(c->splan, xk, xn, vt, c->sym_t, c->sym_s,
+                                             (const float4 *)c->sym_acc, D, dt, p.kick, G, nullptr, rs)))
                     return st2;
                 continue;
             }
@@ -1131,7 +1144,10 @@ int nb_launches_per_step(nb_ctx *c)
 {
     if (!c) return -1;
     if (c->p.n == 0) return 0;
-    if (ff_sym(c)) return 4;  // scale reduction, split, force, integrate
+    // a banded symmetric plan: a force and a fold launch per band
+    const int bands = (uses_sym(c) || f64_sym(c)) && c->splan.nbands > 1 ? c->splan.nbands : 0;
+    if (ff_sym(c)) return 4 + (bands ? 2 * bands - 1 : 0);  // scale reduction, split, force, integrate
+    if (bands) return 2 * bands + 1;
     return (uses_fast(c) || is_comp(c) || f64_sym(c)) ? 2 : 1;
 }
 
@@ -1184,7 +1200,8 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
             if (ff_sym(c)) return nb::symff_plan(p.n, a, b, c->device, sp);
             if (f64_sym(c)) return nb::sym64_plan(p.n, a, b, c->device, sp);
             return nb::sym_plan(p.n, a, b, c->device, sp, comp_sym(c) ? 1 : 0,
-                                comp_sym(c) ? NB_SOURCE_AUTO : (c->splan.fixed ? NB_SOURCE_FIXED : NB_SOURCE_TRIANGULAR));
+                                comp_sym(c) ? NB_SOURCE_AUTO : (c->splan.fixed ? NB_SOURCE_FIXED : NB_SOURCE_TRIANGULAR),
+                                comp_sym(c) ? -1 : p.bands);
         }
         return nb::fast_plan(p.n, a, b, p.ctas_per_sm, c->device, fp, is_comp(c) ? nb::SK_COMP : 0);
     };
@@ -1240,6 +1257,14 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
     if (viable.empty()) {
         report(symm ? cur_a * 32 : cur_a, cur_b);
         return NB_OK;
+    }
+    // banded candidates fold into per-body sums: the context keeps a buffer
+    // for them once one is timed
+    bool banded = false;
+    for (const Cand &v : viable) banded = banded || (symm && v.sp.nbands > 1);
+    if (banded && !c->sym_acc) {
+        cudaError_t ea = nb::dmalloc(&c->sym_acc, (size_t)p.n * ent);
+        if (ea != cudaSuccess) return nb::cuda_error(ea, "autotune scratch allocation");
     }
     if (!symm) {  // the directed scratch also serves the energy pass
         need_t = std::max(need_t, mult * (size_t)c->eplan.slots * c->eplan.tbsize * sizeof(float4));
@@ -1370,6 +1395,23 @@ int nb_plan_info(nb_ctx *c, int *info5)
     info5[2] = c->plan.grid;
     info5[3] = c->plan.tbsize;
     info5[4] = c->plan.slots;
+    return NB_OK;
+}
+
+int nb_source_info(nb_ctx *c, int *info4)
+{
+    if (!c || !info4) return set_error(NB_ERR_INVALID, "ctx/info is NULL");
+    info4[0] = 0;
+    info4[1] = 1;
+    info4[2] = 0;
+    info4[3] = 0;
+    if (uses_sym(c) || comp_sym(c) || f64_sym(c)) {
+        const size_t ent = c->p.precision == NB_F64 ? sizeof(double4) : sizeof(float4);
+        const size_t halves = comp_sym(c) ? 2 : 1;
+        info4[0] = c->splan.fixed ? NB_SOURCE_FIXED : NB_SOURCE_TRIANGULAR;
+        info4[1] = c->splan.nbands;
+        info4[2] = (int)((halves * (size_t)c->splan.spart_size * ent) >> 20);
+    }
     return NB_OK;
 }
 

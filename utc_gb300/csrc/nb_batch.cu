@@ -1672,7 +1672,7 @@ static int sys_plans_for(nb_batch *b, SysPlans *out)
         if (b->sym) {
             nb::SymPlan q;
             if ((st = b->f64 ? nb::symff_plan(b->sizes[i], 0, 0, b->device, &q)
-                             : nb::sym_plan(b->sizes[i], 0, 0, b->device, &q, 0, NB_SOURCE_TRIANGULAR)))
+                             : nb::sym_plan(b->sizes[i], 0, 0, b->device, &q, 0, NB_SOURCE_TRIANGULAR, -1)))
                 return st;
             sp.tpart = std::max(sp.tpart, (size_t)q.slots * q.rb * wide);
             sp.spart = std::max(sp.spart, (size_t)q.spart_size * wide);
@@ -1709,8 +1709,8 @@ static int sys_step(const nb_batch *b, const SysPlans &sp, int i, int c, float4 
     const float4 *po = b->pos[c] + o;
     float4 *pn = b->pos[c ^ 1] + o, *vel = b->vel + o;
     if (b->sym) {
-        if ((st = nb::sym_force(sp.sym[i], po, (float)p.eps2, tpart, spart, s))) return st;
-        return nb::sym_integrate(sp.sym[i], po, pn, vel, tpart, spart, (float)p.damping, (float)p.dt,
+        if ((st = nb::sym_force(sp.sym[i], po, (float)p.eps2, tpart, spart, nullptr, s))) return st;
+        return nb::sym_integrate(sp.sym[i], po, pn, vel, tpart, spart, nullptr, (float)p.damping, (float)p.dt,
                                  p.kick, (float)p.G, nullptr, s);
     }
     if ((st = nb::fast_force(sp.dir[i], po, (float)p.eps2, tpart, s, 0))) return st;

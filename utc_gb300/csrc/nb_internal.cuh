@@ -297,8 +297,17 @@ struct SymPlan {
     long long total = 0; // (row, chunk) items
     int grid = 0;
     int slots = 0;       // grid + nrb - 1 target-side slots of rb float4
-    long long spart_size = 0;  // float4 entries of the source-side array
+    long long spart_size = 0;  // float4 entries of the source-side array (of the largest band)
     int sms = 0;         // SMs of the device planned for
+    // Triangular plans whose source-side array would pass the budget are cut
+    // into bands of consecutive row blocks: the force kernel runs band by
+    // band over the band's (row, chunk) items, every band's source-side
+    // entries reusing one buffer, and after each band a fold kernel adds its
+    // target-side slots and source-side rows into one sum per body (accsum),
+    // which the integrator then reads.  nbands = 1: one pass, no fold.
+    static constexpr int kMaxBands = 512;
+    int nbands = 1;
+    int band_row[kMaxBands + 1] = {};  // band k: row blocks [band_row[k], band_row[k + 1])
 };
 // float4 entries of the source-side array for row blocks of rb bodies
 inline long long sym_spart_entries(int n, int rb)
@@ -307,25 +316,60 @@ inline long long sym_spart_entries(int n, int rb)
     return nrb > 1 ? sym_soff(nrb - 1, n, rb) : 0;
 }
 // Largest source-side array a default shape accepts before it moves to a
-// bigger row block (or, for the automatic source side of the plain kernel,
-// to the fixed-point one).
+// bigger row block or to bands.
 constexpr long long kSymSpartBudget = 8ll << 30;
+
+// Cuts the row blocks of a triangular plan into bands whose source-side
+// entries stay within cap (want > 0: about `want` bands of equal size
+// instead); fills rows[0..k] and the largest band's entry count and returns
+// the band count k, or 0 when more than SymPlan::kMaxBands would be needed.
+// A row's entries are n - (r + 1) rb (none for the last row block).
+inline int sym_make_bands(int n, int rb, long long cap, int want, int *rows, long long *max_entries)
+{
+    const int nrb = (n + rb - 1) / rb;
+    if (want > 0) {
+        const long long total = sym_spart_entries(n, rb);
+        cap = (total + want - 1) / want;
+        if (cap < 1) cap = 1;
+    }
+    int k = 0;
+    long long acc = 0, mx = 0;
+    rows[0] = 0;
+    for (int r = 0; r < nrb; ++r) {
+        const long long e = r < nrb - 1 ? (long long)n - (long long)(r + 1) * rb : 0;
+        if (acc > 0 && acc + e > cap) {
+            if (k + 1 >= SymPlan::kMaxBands) return 0;
+            rows[++k] = r;
+            mx = acc > mx ? acc : mx;
+            acc = 0;
+        }
+        acc += e;
+    }
+    mx = acc > mx ? acc : mx;
+    rows[++k] = nrb;
+    *max_entries = mx;
+    return k;
+}
 // float4 entries of the fixed-point source side: 6 n 64-bit accumulators
 // (hi x, y, z then lo x, y, z, each n long) and one float4 record: the sum of
 // |m| over the bodies and the scale factors (sym_fx_prepare).
 inline long long sym_fx_entries(int n) { return 3ll * n + 1; }
 
 // source_side: nb_source_side (NB_SOURCE_AUTO / TRIANGULAR / FIXED), for
-// plain plans; compensated plans are always triangular.
-int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp = 0, int source_side = 0);
+// plain plans; compensated plans are always triangular.  bands: 0 = bands
+// only where the triangular array would pass the budget, k > 0 = about k
+// bands, -1 = never (the shape grows instead, as compensated plans do).
+int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp = 0, int source_side = 0,
+             int bands = 0);
+// accsum: n float4, the per-body sums of banded plans (unused otherwise)
 int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, float4 *spart,
-              cudaStream_t s);
+              float4 *accsum, cudaStream_t s);
 // consume (fixed plans): zero the accumulators after reading them, ready for
 // the next force launch; 0 leaves them for a second reader of the same
 // force launch
 int sym_integrate(const SymPlan &p, const float4 *pos_old, float4 *pos_new, float4 *vel,
-                  const float4 *tpart, const float4 *spart, float damping, float dt, int kick,
-                  float G, float4 *acc_out, cudaStream_t s, int consume = 1);
+                  const float4 *tpart, const float4 *spart, const float4 *accsum, float damping, float dt,
+                  int kick, float G, float4 *acc_out, cudaStream_t s, int consume = 1);
 // Fixed plans: zero the accumulators and write the record (the sum of |m| of
 // pos and the scale it gives with eps2); after every new state and scratch.
 int sym_fx_prepare(const SymPlan &p, const float4 *pos, float4 *spart, float eps2, cudaStream_t s);

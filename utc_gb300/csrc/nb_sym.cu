@@ -102,13 +102,16 @@ __device__ __forceinline__ void fx_emit(unsigned long long *acc, int n, int j, f
 }
 
 // FX: spart is the fixed-point accumulator buffer (with its record), not
-// the triangular array.
-template <int W, int BPT, int MINB, bool COMP, bool FX = false>
+// the triangular array.  BAND: one band of a banded plan, items
+// [it0, it0 + total) covering row blocks from r0 on: target-side slot
+// c + I - r0, source-side entries offset by soff0 (the band's first entry).
+template <int W, int BPT, int MINB, bool COMP, bool FX = false, bool BAND = false>
 __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *__restrict__ pos, int n,
                                                            float eps2, float4 *__restrict__ tpart,
                                                            float4 *__restrict__ spart,
                                                            long long total, int nc, int nrb,
-                                                           long long tlo, long long slo)
+                                                           long long tlo, long long slo, long long it0,
+                                                           int r0, long long soff0)
 {
     constexpr int WB = 32 * BPT;
     constexpr int RB = W * WB;
@@ -119,7 +122,11 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
     const int wid = threadIdx.x >> 5;
     const int c = blockIdx.x;
     long long it = sk_start(c, total, gridDim.x);
-    const long long end = sk_start(c + 1, total, gridDim.x);
+    long long end = sk_start(c + 1, total, gridDim.x);
+    if constexpr (BAND) {
+        it += it0;
+        end += it0;
+    }
     const float4 pad = make_float4(kPadCoord, kPadCoord, kPadCoord, 0.f);
 
     while (it < end) {
@@ -213,7 +220,8 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
                     }
                     fx_emit(reinterpret_cast<unsigned long long *>(spart), n, jb + lane, sx, sy, sz);
                 } else if (wid == 0 && jb + lane < n) {
-                    const long long so = sym_soff(I, n, RB) + (jb + lane - (I + 1) * RB);
+                    long long so = sym_soff(I, n, RB) + (jb + lane - (I + 1) * RB);
+                    if constexpr (BAND) so -= soff0;
                     if constexpr (COMP) {
                         float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f, e;
 #pragma unroll
@@ -254,7 +262,7 @@ __global__ void __launch_bounds__(32 * W, MINB) sym_force_kernel(const float4 *_
                 }
             }
         }
-        float4 *dst = tpart + (size_t)(c + I) * RB + wid * WB;
+        float4 *dst = tpart + (size_t)(c + I - (BAND ? r0 : 0)) * RB + wid * WB;
 #pragma unroll
         for (int k = 0; k < BPT; ++k) {
             if constexpr (COMP) {
@@ -279,7 +287,8 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__re
                                                               float eps2, float4 *__restrict__ tpart,
                                                               float4 *__restrict__ spart,
                                                               long long total, int nc, int nrb,
-                                                              long long, long long)
+                                                              long long, long long, long long, int,
+                                                              long long)
 {
     constexpr int BPT = 2 * NP;
     constexpr int WB = 32 * BPT;
@@ -411,17 +420,25 @@ constexpr int kSymIntegBlock = 256;
 // fxacc != nullptr: the fixed-point source side; thread 0 of the quad adds
 // its total to the target-side sum in FP64 (one rounding) and, with
 // consume, zeroes the body's six accumulators for the next force launch.
+// accsum != nullptr (banded plans): the folded sums, taken as they are.
 __global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
     const float4 *__restrict__ pos_old, float4 *__restrict__ pos_new, float4 *__restrict__ vel,
     const float4 *__restrict__ tpart, const float4 *__restrict__ spart, int n, int rb, int nc, int nrb,
     long long total, int grid, float damping, float dt, int kick, float G, float4 *__restrict__ acc_out,
-    unsigned long long *__restrict__ fxacc, int consume)
+    unsigned long long *__restrict__ fxacc, int consume, const float4 *__restrict__ accsum)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int i = (int)(t >> 2), q = (int)(t & 3);
     const bool live = i < n;  // dead threads still take part in the shuffles
     float ax = 0.f, ay = 0.f, az = 0.f;
-    if (live) {
+    if (live && accsum) {
+        if (q == 0) {
+            const float4 a4 = accsum[i];
+            ax = a4.x;
+            ay = a4.y;
+            az = a4.z;
+        }
+    } else if (live) {
         const int rc = rb / 32;
         const int I = i / rb;
         const int c0 = sk_owner(sym_prefix(I, nc, rc), total, grid);
@@ -484,15 +501,68 @@ __global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
     vel[i] = v;
 }
 
+// After band [r0, r1) of a banded plan (items [it0, it0 + bt) over gb CTAs):
+// per body, the running sum (zero before the first band) plus, if the body's
+// row block is in the band, its target-side slots in CTA order, then the
+// band's source-side rows before the body's row block in row order.  Fixed
+// order throughout: deterministic.
+__global__ void __launch_bounds__(256) sym_fold_kernel(const float4 *__restrict__ tpart,
+                                                       const float4 *__restrict__ spart,
+                                                       float4 *__restrict__ accsum, int n, int rb, int nc,
+                                                       long long it0, long long bt, int gb, int r0, int r1,
+                                                       long long soff0, int first)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int I = i / rb;
+    if (I < r0) return;  // rows before the band get nothing from it (r0 = 0 for the first band)
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    if (!first) {
+        const float4 a4 = accsum[i];
+        ax = a4.x;
+        ay = a4.y;
+        az = a4.z;
+    }
+    if (I < r1) {
+        const int rc = rb / 32;
+        const int c0 = sk_owner(sym_prefix(I, nc, rc) - it0, bt, gb);
+        const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1 - it0, bt, gb);
+        const int li = i - I * rb;
+        for (int c = c0; c <= c1; ++c) {
+            const float4 v4 = tpart[(size_t)(c + I - r0) * rb + li];
+            ax = __fadd_rn(ax, v4.x);
+            ay = __fadd_rn(ay, v4.y);
+            az = __fadd_rn(az, v4.z);
+        }
+    }
+    const int rend = I < r1 ? I : r1;
+#pragma unroll 4
+    for (int r = r0; r < rend; ++r) {
+        const float4 v4 = spart[sym_soff(r, n, rb) - soff0 + (i - (long long)(r + 1) * rb)];
+        ax = __fadd_rn(ax, v4.x);
+        ay = __fadd_rn(ay, v4.y);
+        az = __fadd_rn(az, v4.z);
+    }
+    accsum[i] = make_float4(ax, ay, az, 0.f);
+}
+
 typedef void (*sym_kernel_t)(const float4 *, int, float, float4 *, float4 *, long long, int, int,
-                             long long, long long);
+                             long long, long long, long long, int, long long);
 
 // bpt > 0: scalar kernel with bpt bodies per lane (the third template
 // argument asks for that many resident CTAs per SM); bpt < 0: packed f32x2
 // kernel with -bpt bodies per lane.  comp: the compensated kernel (scalar
 // shapes with up to 12 targets per lane: 13 registers per target).
-static sym_kernel_t sym_kernel_for(int w, int bpt, int comp, int fixed = 0)
+static sym_kernel_t sym_kernel_for(int w, int bpt, int comp, int fixed = 0, int band = 0)
 {
+    if (band) {  // banded triangular plans: the default shapes
+        if (comp || fixed) return nullptr;
+        if (w == 1 && bpt == 16) return sym_force_kernel<1, 16, 8, false, false, true>;
+        if (w == 4 && bpt == 20) return sym_force_kernel<4, 20, 2, false, false, true>;
+        if (w == 1 && bpt == 8) return sym_force_kernel<1, 8, 8, false, false, true>;
+        if (w == 1 && bpt == 4) return sym_force_kernel<1, 4, 8, false, false, true>;
+        return nullptr;
+    }
     if (fixed) {  // fixed-point source side: one-warp shapes
         if (comp) return nullptr;
         if (w == 1 && bpt == 16) return sym_force_kernel<1, 16, 8, false, true>;
@@ -524,7 +594,7 @@ static sym_kernel_t sym_kernel_for(int w, int bpt, int comp, int fixed = 0)
     return nullptr;
 }
 
-int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int source_side)
+int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int source_side, int bands)
 {
     if (source_side < NB_SOURCE_AUTO || source_side > NB_SOURCE_FIXED)
         return set_error(NB_ERR_INVALID, "source_side is NB_SOURCE_AUTO, NB_SOURCE_TRIANGULAR or NB_SOURCE_FIXED");
@@ -532,49 +602,15 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int s
         return set_error(NB_ERR_UNSUPPORTED, "the compensated kernel keeps its triangular (hi, lo) source side");
     int fixed = source_side == NB_SOURCE_FIXED ? 1 : 0;
     const bool given = warps != 0 || bpt != 0;
-    // automatic: the triangular array while the 4 x 20 shape keeps it within
-    // budget; beyond that (N above about 1.66e6) the fixed-point source side
-    // with one warp x 16 targets, which ran 3 % faster on GB300 than the
-    // 8 x 24 shape that would keep the array within budget (3510 against
-    // 3405 G interactions/s at N = 2^21, 3514 against 3394 at 2^22) and
-    // takes 48 B per body
-    if (!given && !fixed && !comp && source_side == NB_SOURCE_AUTO &&
-        sym_spart_entries(n, 4 * 32 * 20) * (long long)sizeof(float4) > kSymSpartBudget)
-        fixed = 1;
-    if (!given && fixed) {
-        warps = 1;
-        bpt = 16;
-        int sms = 0;  // fewer targets per lane for small systems, as below
-        NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        while (bpt > 4 && n > 0) {
-            const int rb = 32 * bpt, nrb = (n + rb - 1) / rb, nc = (n + 31) / 32;
-            if (sym_prefix(nrb, nc, bpt) >= 4ll * sms) break;
-            bpt /= 2;
-        }
-    }
-    if (warps == 0 && bpt == 0) {
-        // plain: one-warp CTAs x 16 targets (row block 512); then 4 x 20
-        // (2560), 8 x 24 (6144) while the source-side array is over budget
-        // (8 x 24 only when the triangular side is asked for).
-        // Compensated (hi and lo halves): 1 x 12 (384), 4 x 12 (1536),
-        // 8 x 12 (3072).
-        static const int plain[3][2] = {{1, 16}, {4, 20}, {8, 24}};
-        static const int compd[3][2] = {{1, 12}, {4, 12}, {8, 12}};
-        const int(*shapes)[2] = comp ? compd : plain;
-        const long long halves = comp ? 2 : 1;
-        int s = 0;
-        while (s < 2 && halves * sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) *
-                                (long long)sizeof(float4) >
-                            kSymSpartBudget)
-            ++s;
-        warps = shapes[s][0];
-        bpt = shapes[s][1];
-        // small systems: fewer targets per lane until there are at least
-        // four (row, chunk) items per resident warp slot of an SM, so the
-        // launch is not a few long items (at N=1024, 16 targets per lane give
-        // 48 items)
-        if (!comp && warps == 1) {
-            int sms = 0;
+    // plain triangular plans go to bands where the array would pass the
+    // budget; compensated plans and bands = -1 grow the row block instead
+    const bool may_band = !comp && !fixed && bands >= 0;
+    SymPlan p;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (!given && fixed) {
+            warps = 1;
+            bpt = 16;
+            int sms = 0;  // fewer targets per lane for small systems, as below
             NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
             while (bpt > 4 && n > 0) {
                 const int rb = 32 * bpt, nrb = (n + rb - 1) / rb, nc = (n + 31) / 32;
@@ -582,33 +618,88 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int s
                 bpt /= 2;
             }
         }
+        if (warps == 0 && bpt == 0) {
+            // plain: one-warp CTAs x 16 targets (row block 512), then 4 x 20
+            // (2560) while the source-side array is over budget, and beyond
+            // that 4 x 20 in bands (without bands: 8 x 24, 6144).
+            // Compensated (hi and lo halves): 1 x 12 (384), 4 x 12 (1536),
+            // 8 x 12 (3072).
+            static const int plain[3][2] = {{1, 16}, {4, 20}, {8, 24}};
+            static const int compd[3][2] = {{1, 12}, {4, 12}, {8, 12}};
+            const int(*shapes)[2] = comp ? compd : plain;
+            const long long halves = comp ? 2 : 1;
+            const int last = may_band ? 1 : 2;
+            int s = 0;
+            while (s < last && halves * sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) *
+                                   (long long)sizeof(float4) >
+                               kSymSpartBudget)
+                ++s;
+            warps = shapes[s][0];
+            bpt = shapes[s][1];
+            // small systems: fewer targets per lane until there are at least
+            // four (row, chunk) items per resident warp slot of an SM, so the
+            // launch is not a few long items (at N=1024, 16 targets per lane
+            // give 48 items)
+            if (!comp && warps == 1) {
+                int sms = 0;
+                NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+                while (bpt > 4 && n > 0) {
+                    const int rb = 32 * bpt, nrb = (n + rb - 1) / rb, nc = (n + 31) / 32;
+                    if (sym_prefix(nrb, nc, bpt) >= 4ll * sms) break;
+                    bpt /= 2;
+                }
+            }
+        }
+        if (warps == 0) warps = 8;
+        if (bpt == 0) bpt = 8;
+        p = SymPlan();
+        p.n = n;
+        p.warps = warps;
+        p.bpt = bpt;
+        p.comp = comp;
+        p.fixed = fixed;
+        p.rb = warps * 32 * (bpt < 0 ? -bpt : bpt);
+        p.nc = (n + 31) / 32;
+        p.nrb = (n + p.rb - 1) / p.rb;
+        p.spart_size = fixed ? sym_fx_entries(n) : sym_spart_entries(n, p.rb);
+        p.band_row[0] = 0;
+        p.band_row[1] = p.nrb;
+        if (may_band && !fixed && n > 0 && (bands > 1 || p.spart_size * (long long)sizeof(float4) > kSymSpartBudget)) {
+            long long mx = 0;
+            const int k = sym_make_bands(n, p.rb, kSymSpartBudget / (long long)sizeof(float4), bands > 1 ? bands : 0,
+                                         p.band_row, &mx);
+            if (k == 0) {
+                // more bands than a plan holds (N above about 3.6e7 with the
+                // 4 x 20 shape): the automatic choice takes the fixed-point
+                // source side instead
+                if (given || source_side != NB_SOURCE_AUTO)
+                    return set_error(NB_ERR_UNSUPPORTED, "the triangular source side would need more than 512 bands");
+                fixed = 1;
+                warps = bpt = 0;
+                continue;
+            }
+            p.nbands = k;
+            p.spart_size = mx;
+        }
+        break;
     }
-    if (warps == 0) warps = 8;
-    if (bpt == 0) bpt = 8;
-    sym_kernel_t k = sym_kernel_for(warps, bpt, comp, fixed);
+    sym_kernel_t k = sym_kernel_for(p.warps, p.bpt, comp, p.fixed, p.nbands > 1);
     if (!k)
-        return set_error(NB_ERR_UNSUPPORTED, fixed ? "symmetric kernel shape not compiled with the fixed-point "
-                                                     "source side (one warp x 4, 8 or 16 targets)"
-                                                   : "symmetric kernel shape not compiled");
-    SymPlan p;
-    p.n = n;
-    p.warps = warps;
-    p.bpt = bpt;
-    p.comp = comp;
-    p.fixed = fixed;
-    p.rb = warps * 32 * (bpt < 0 ? -bpt : bpt);
-    p.nc = (n + 31) / 32;
-    p.nrb = (n + p.rb - 1) / p.rb;
+        return set_error(NB_ERR_UNSUPPORTED, p.fixed ? "symmetric kernel shape not compiled with the fixed-point "
+                                                       "source side (one warp x 4, 8 or 16 targets)"
+                                         : p.nbands > 1 ? "symmetric kernel shape not compiled for bands (one warp "
+                                                          "x 4, 8 or 16 targets, 4 warps x 20)"
+                                                        : "symmetric kernel shape not compiled");
     p.total = n > 0 ? sym_prefix(p.nrb, p.nc, p.rb / 32) : 0;
     int sms = 0, occ = 0;
     NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * warps, 0));
+    NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * p.warps, 0));
     if (occ < 1) return set_error(NB_ERR_UNSUPPORTED, "symmetric kernel does not fit on an SM");
     long long grid = (long long)sms * occ;
     if (p.total > 0 && grid > p.total) grid = p.total;
     p.grid = p.total > 0 ? (int)grid : 0;
     p.slots = p.total > 0 ? p.grid + p.nrb - 1 : 0;
-    p.spart_size = fixed ? sym_fx_entries(n) : sym_spart_entries(n, p.rb);
+    p.sms = sms;
     *pl = p;
     return NB_OK;
 }
@@ -670,29 +761,46 @@ int sym_fx_rescale(const SymPlan &p, float4 *spart, float eps2, cudaStream_t s)
 }
 
 int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, float4 *spart,
-              cudaStream_t s)
+              float4 *accsum, cudaStream_t s)
 {
     if (p.total == 0) return NB_OK;
-    sym_kernel_t k = sym_kernel_for(p.warps, p.bpt, p.comp, p.fixed);
+    sym_kernel_t k = sym_kernel_for(p.warps, p.bpt, p.comp, p.fixed, p.nbands > 1);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "symmetric kernel shape not compiled");
     // lo blocks (compensated plans) follow the hi blocks
     const long long tlo = (long long)p.slots * p.rb, slo = p.spart_size;
-    k<<<p.grid, 32 * p.warps, 0, s>>>(pos, p.n, eps2, tpart, spart, p.total, p.nc, p.nrb, tlo, slo);
-    NB_LAUNCH_CHECK("sym_force_kernel launch");
+    if (p.nbands <= 1) {
+        k<<<p.grid, 32 * p.warps, 0, s>>>(pos, p.n, eps2, tpart, spart, p.total, p.nc, p.nrb, tlo, slo, 0, 0, 0);
+        NB_LAUNCH_CHECK("sym_force_kernel launch");
+        return NB_OK;
+    }
+    if (!accsum) return set_error(NB_ERR_INVALID, "sym_force: a banded plan needs its per-body sums");
+    const int rc = p.rb / 32;
+    for (int b = 0; b < p.nbands; ++b) {
+        const int r0 = p.band_row[b], r1 = p.band_row[b + 1];
+        const long long it0 = sym_prefix(r0, p.nc, rc), bt = sym_prefix(r1, p.nc, rc) - it0;
+        const long long soff0 = sym_soff(r0, p.n, p.rb);
+        const int gb = (int)(bt < p.grid ? bt : p.grid);
+        k<<<gb, 32 * p.warps, 0, s>>>(pos, p.n, eps2, tpart, spart, bt, p.nc, p.nrb, tlo, slo, it0, r0, soff0);
+        NB_LAUNCH_CHECK("sym_force_kernel launch");
+        sym_fold_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(tpart, spart, accsum, p.n, p.rb, p.nc, it0, bt, gb, r0, r1,
+                                                          soff0, b == 0);
+        NB_LAUNCH_CHECK("sym_fold_kernel launch");
+    }
     return NB_OK;
 }
 
 int sym_integrate(const SymPlan &p, const float4 *pos_old, float4 *pos_new, float4 *vel,
-                  const float4 *tpart, const float4 *spart, float damping, float dt, int kick, float G,
-                  float4 *acc_out, cudaStream_t s, int consume)
+                  const float4 *tpart, const float4 *spart, const float4 *accsum, float damping, float dt,
+                  int kick, float G, float4 *acc_out, cudaStream_t s, int consume)
 {
     if (p.n == 0) return NB_OK;
+    if (p.nbands > 1 && !accsum) return set_error(NB_ERR_INVALID, "sym_integrate: a banded plan needs its per-body sums");
     const long long threads = 4ll * p.n;  // a quad of threads per body
     unsigned long long *fxacc =
         p.fixed ? reinterpret_cast<unsigned long long *>(const_cast<float4 *>(spart)) : nullptr;
     sym_integrate_kernel<<<(unsigned)((threads + kSymIntegBlock - 1) / kSymIntegBlock), kSymIntegBlock, 0, s>>>(
         pos_old, pos_new, vel, tpart, spart, p.n, p.rb, p.nc, p.nrb, p.total, p.grid, damping, dt, kick,
-        G, acc_out, fxacc, consume);
+        G, acc_out, fxacc, consume, p.nbands > 1 ? accsum : nullptr);
     NB_LAUNCH_CHECK("sym_integrate_kernel launch");
     return NB_OK;
 }

@@ -52,7 +52,7 @@ def _device_buffer(x, shape, dtype, name):
 class NBodySystem:
     def __init__(self, n, precision="f32", algo="fast", kick="reference", eps2=0.00125,
                  damping=0.995, dt=0.016, G=1.0, block=0, bpt=0, ctas_per_sm=0,
-                 memtype=N.NB_MEM_PAGEABLE, source_side="auto"):
+                 memtype=N.NB_MEM_PAGEABLE, source_side="auto", bands=0):
         self.lib = N.lib()
         p = N.NbParams()
         self.lib.nb_params_default(C.byref(p))
@@ -65,6 +65,9 @@ class NBodySystem:
         # symmetric FP32 kernel: "triangular" array or "fixed"-point accumulators
         p.source_side = {"auto": N.NB_SOURCE_AUTO, "triangular": N.NB_SOURCE_TRIANGULAR,
                          "fixed": N.NB_SOURCE_FIXED}[source_side]
+        # symmetric kernels with the triangular array: 0 = bands only where it
+        # would pass 8 GiB, k > 1 = about k bands
+        p.bands = int(bands)
         self.params = p
         self.n = int(n)
         self.precision = precision
@@ -241,6 +244,14 @@ class NBodySystem:
         info = (C.c_int * 5)()
         N.check(self.lib.nb_plan_info(self.handle, info), "nb_plan_info")
         return dict(zip(["block", "bpt", "grid", "tbsize", "slots"], list(info)))
+
+    def source_info(self):
+        """Symmetric contexts: {"side": "fixed" or "triangular", "bands": k,
+        "mib": scratch of the source side in MiB}."""
+        info = (C.c_int * 4)()
+        N.check(self.lib.nb_source_info(self.handle, info), "nb_source_info")
+        side = {N.NB_SOURCE_FIXED: "fixed", N.NB_SOURCE_TRIANGULAR: "triangular"}.get(info[0])
+        return {"side": side, "bands": info[1], "mib": info[2]}
 
     def launches_per_step(self):
         return self.lib.nb_launches_per_step(self.handle)
