@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 # "symfx": the symmetric FP32 kernel with its fixed-point source side;
 # "symband": the symmetric kernel with its triangular array in three bands
 MODES = [("f32", "sym"), ("f32", "symfx"), ("f32", "symband"), ("f32", "fast"), ("f32comp", "sym"),
-         ("f32comp", "fast"), ("f64", "sym"), ("f64", "sym64"), ("f32", "exact")]
+         ("f32comp", "fast"), ("f64", "sym"), ("f64", "symband"), ("f64", "sym64"), ("f32", "exact")]
 
 
 def system(n, prec, algo, **kw):

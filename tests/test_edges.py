@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 # "symfx": the symmetric FP32 kernel with its fixed-point source side;
 # "symband": the symmetric kernel with its triangular array in three bands
 MODES = [("f32", "fast"), ("f32", "sym"), ("f32", "symfx"), ("f32", "symband"), ("f32", "exact"), ("f64", "exact"),
-         ("f64", "sym"), ("f64", "sym64"), ("f32comp", "fast"), ("f32comp", "sym")]
+         ("f64", "sym"), ("f64", "symband"), ("f64", "sym64"), ("f32comp", "fast"), ("f32comp", "sym")]
 
 
 def system(n, prec, algo, **kw):

@@ -85,15 +85,18 @@ def test_compensated_steps_vs_fp64_oracle(cuda, algo):
 
 
 @pytest.mark.parametrize("precision,algo", [("f32", "fast"), ("f32", "sym"), ("f32", "exact"), ("f32comp", "fast"),
-                                            ("f32comp", "sym"), ("f64", "sym"), ("f64", "sym64"),
-                                            ("f64", "exact")])
+                                            ("f32comp", "sym"), ("f64", "sym"), ("f64", "symband"),
+                                            ("f64", "sym64"), ("f64", "exact")])
 def test_energy_momentum_vs_fp64(cuda, precision, algo):
+    """"symband": the float-float energy pass with its triangular array in
+    three bands (the potential folded with the forces)."""
     n = 4096
     p, v = ics.plummer(n, seed=4)
     if precision == "f32":
         p, v = p.astype(np.float32), v.astype(np.float32)
     eps2 = np.float32(1e-3)
-    with NBodySystem(n, precision, algo, kick="physical", eps2=eps2) as s:
+    kw = {"bands": 3} if algo == "symband" else {}
+    with NBodySystem(n, precision, algo.replace("symband", "sym"), kick="physical", eps2=eps2, **kw) as s:
         s.set_state(p, v)
         e, bodies = s.energy(with_bodies=True)
     p64 = np.asarray(p, np.float64)

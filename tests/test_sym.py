@@ -172,6 +172,22 @@ def test_sym_bands_steps_vs_oracle(cuda, kick):
     assert rel.max() <= 1e-5
 
 
+@pytest.mark.parametrize("n,bands", [(65536, 1), (185000, 1), (190000, 2), (300000, 3)])
+def test_sym_f64_default_plan(cuda, n, bands):
+    """FP64 state: one warp x 2 targets at every size, the triangular array
+    (N^2 / 4 bytes) cut into bands of at most 8 GiB past N = 185k."""
+    import torch
+
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    with NBodySystem(n, "f64", "sym") as s:
+        info, src = s.plan_info(), s.source_info()
+        used = free0 - torch.cuda.mem_get_info()[0]
+    assert (info["block"], info["bpt"]) == (32, 2)
+    assert src["bands"] == bands and src["mib"] <= 8192, src
+    assert used < 10 << 30, used
+
+
 @pytest.mark.parametrize("n", [4096, 65536])
 def test_sym_fixed_point_source_side_is_exact_and_deterministic(cuda, n):
     """The source side summed in fixed point (NB_SOURCE_FIXED): accelerations
@@ -216,7 +232,15 @@ def test_sym_fixed_point_source_side_is_exact_and_deterministic(cuda, n):
     assert (d <= 2e-5 * (w + w.mean())).all()
 
 
-F64_SYM = ["sym", "sym64"]  # float-float pair arithmetic; FP64 arithmetic throughout
+# float-float pair arithmetic (its triangular array in one pass, or in three
+# bands); FP64 arithmetic throughout
+F64_SYM = ["sym", "symband", "sym64"]
+
+
+def f64sys(n, algo, **kw):
+    if algo == "symband":
+        return NBodySystem(n, "f64", "sym", bands=3, **kw)
+    return NBodySystem(n, "f64", algo, **kw)
 
 
 @pytest.mark.parametrize("algo", F64_SYM)
@@ -228,13 +252,14 @@ def test_sym_f64_accel_vs_oracle(cuda, n, algo):
     step on the FP32 rsqrt) and the FP64 one (FP64 rsqrt approximation and two
     Newton steps)."""
     p, _ = ics.plummer(n, seed=n)
-    with NBodySystem(n, "f64", algo, eps2=1e-3) as s:
+    with f64sys(n, algo, eps2=1e-3) as s:
         s.set_state(p, np.zeros_like(p))
         a = s.accel()
     assert close(a, oracle.accel(p, 1e-3), tol=1e-13)
 
 
 @pytest.mark.parametrize("algo,shape", [("sym", s) for s in [(32, 2), (32, 4), (128, 4), (256, 4), (256, 8)]] +
+                         [("symband", s) for s in [(32, 2), (32, 4)]] +
                          [("sym64", s) for s in [(32, 8), (32, 4), (128, 8), (256, 8)]])
 @pytest.mark.parametrize("n", [1000, 4097])
 def test_sym_f64_every_shape_vs_oracle(cuda, algo, shape, n):
@@ -242,7 +267,7 @@ def test_sym_f64_every_shape_vs_oracle(cuda, algo, shape, n):
     the multi-warp ones the default plan only picks for large N (their
     reactions are summed across the CTA's warps through shared memory)."""
     p, _ = ics.plummer(n, seed=n + 1)
-    with NBodySystem(n, "f64", algo, eps2=1e-3, block=shape[0], bpt=shape[1]) as s:
+    with f64sys(n, algo, eps2=1e-3, block=shape[0], bpt=shape[1]) as s:
         info = s.plan_info()
         assert (info["block"], info["bpt"]) == shape
         s.set_state(p, np.zeros_like(p))
@@ -267,7 +292,7 @@ def test_sym_f64_close_pairs_far_from_origin(cuda, algo):
     rad = np.where(np.arange(n) % 4 == 0, 0.05, 1.0) * rng.random(n) ** (1 / 3)
     p[:, :3] = np.array([3.0e3, -2.0e3, 5.0e2]) + u * rad[:, None]
     p[:, 3] = rng.uniform(0.5, 1.5, n) / n
-    with NBodySystem(n, "f64", algo, eps2=1e-4) as s:
+    with f64sys(n, algo, eps2=1e-4) as s:
         s.set_state(p, np.zeros_like(p))
         a = s.accel()
     assert close(a, oracle.accel(p, 1e-4), tol=1e-13)
@@ -288,7 +313,7 @@ def test_sym_f64_tight_binaries(cuda, algo):
     p[0::2, :3] = c - d / 2
     p[1::2, :3] = c + d / 2
     p[:, 3] = rng.uniform(0.5, 1.5, 2 * nb)
-    with NBodySystem(2 * nb, "f64", algo, eps2=1e-18) as s:
+    with f64sys(2 * nb, algo, eps2=1e-18) as s:
         s.set_state(p, np.zeros_like(p))
         a = s.accel()
     want = oracle.accel(p, 1e-18)
@@ -307,7 +332,7 @@ def test_sym_f64_si_units(cuda, algo):
     p = np.empty((n, 4))
     p[:, :3] = rng.normal(size=(n, 3)) * 1.5e11
     p[:, 3] = 10.0 ** rng.uniform(24, 30, n)
-    with NBodySystem(n, "f64", algo, eps2=1e14, G=6.674e-11) as s:
+    with f64sys(n, algo, eps2=1e14, G=6.674e-11) as s:
         s.set_state(p, np.zeros_like(p))
         a = s.accel()
     assert close(a, oracle.accel(p, 1e14), tol=1e-13)
@@ -325,7 +350,7 @@ def test_sym_f64_power_of_two_scale_invariance(cuda, algo):
     q[:, 3] *= 2.0 ** 5
     out = []
     for x, e in ((p, 1e-3), (q, 1e-3 * 2.0 ** 20)):
-        with NBodySystem(n, "f64", algo, eps2=e) as s:
+        with f64sys(n, algo, eps2=e) as s:
             s.set_state(x, np.zeros_like(x))
             out.append(s.accel())
     assert np.array_equal(out[1], out[0] * 2.0 ** -15)
@@ -337,7 +362,7 @@ def test_sym_f64_steps_vs_oracle(cuda, kick, algo):
     n, steps = 3000, 10
     p, v = ics.uniform_cube(n, seed=1)
     km = oracle.KICK_REFERENCE if kick == "reference" else oracle.KICK_PHYSICAL
-    with NBodySystem(n, "f64", algo, kick=kick, eps2=1e-2, damping=0.999, dt=1e-3) as s:
+    with f64sys(n, algo, kick=kick, eps2=1e-2, damping=0.999, dt=1e-3) as s:
         s.set_state(p, v)
         s.step(steps)
         got, gv = s.get_state()

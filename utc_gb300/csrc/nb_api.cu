@@ -338,14 +338,17 @@ int nb_create(const nb_params *p, nb_ctx **out)
         return st;
     }
     if (f64_sym(c) &&
-        ((st = ff_sym(c) ? nb::symff_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan)
+        ((st = ff_sym(c) ? nb::symff_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan,
+                                          p->bands)
                          : nb::sym64_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan)) ||
          (ff_sym(c) && (st = dev_alloc((void **)&c->ff_split, 3 * n * sizeof(float4), "split positions allocation"))) ||
          (ff_sym(c) && (st = dev_alloc((void **)&c->ff_range, 2 * sizeof(unsigned long long), "scale record allocation"))) ||
          (st = dev_alloc((void **)&c->sym_t, (size_t)c->splan.slots * c->splan.rb * sizeof(double4),
                          "symmetric scratch allocation")) ||
          (st = dev_alloc((void **)&c->sym_s, (size_t)c->splan.spart_size * sizeof(double4),
-                         "symmetric source-side array (about N^2/(2 rb) entries; NB_ALGO_EXACT needs none)")))) {
+                         "symmetric source-side array (about N^2/(2 rb) entries; NB_ALGO_EXACT needs none)")) ||
+         (c->splan.nbands > 1 &&
+          (st = dev_alloc(&c->sym_acc, n * sizeof(double4), "per-body sums of the banded source side"))))) {
         free_ctx(c);
         return st;
     }
@@ -582,14 +585,15 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
     }
     if (f64_sym(c)) {
         st = ff_sym(c) ? nb::symff_force(c->splan, (const double4 *)po, p.eps2, c->ff_split, c->ff_range,
-                                         (double4 *)c->sym_t, (double4 *)c->sym_s, s)
+                                         (double4 *)c->sym_t, (double4 *)c->sym_s, (double4 *)c->sym_acc, s)
                        : nb::sym64_force(c->splan, (const double4 *)po, p.eps2, (double4 *)c->sym_t,
                                          (double4 *)c->sym_s, s);
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
         if (!st)
             st = nb::sym64_integrate(c->splan, (const double4 *)po, (double4 *)pn, (double4 *)c->vel,
                                      (const double4 *)c->sym_t, (const double4 *)c->sym_s, p.damping, p.dt,
-                                     p.kick, p.G, (double4 *)acc_out, s, ff_sym(c) ? c->ff_range : nullptr);
+                                     p.kick, p.G, (double4 *)acc_out, s, ff_sym(c) ? c->ff_range : nullptr,
+                                     (const double4 *)c->sym_acc);
     } else if (p.precision == NB_F64) {
         st = nb::exact_step_f64(p.n, c->shard_lo, c->shard_hi, (const double4 *)po, (double4 *)pn,
                                 (double4 *)c->vel, p.eps2,
@@ -852,11 +856,11 @@ int nb_energy(nb_ctx *c, double *out5, void *accphi_dev, void *stream)
         // unscaled by the FP64 integrator into (acc, phi) per body
         const double4 *pos = (const double4 *)c->pos[c->cur];
         st = nb::symff_force(c->splan, pos, p.eps2, c->ff_split, c->ff_range, (double4 *)c->sym_t,
-                             (double4 *)c->sym_s, s, 1);
+                             (double4 *)c->sym_s, (double4 *)c->sym_acc, s, 1);
         if (!st)
             st = nb::sym64_integrate(c->splan, pos, nullptr, nullptr, (const double4 *)c->sym_t,
                                      (const double4 *)c->sym_s, p.damping, p.dt, p.kick, p.G,
-                                     (double4 *)c->acc_tmp, s, c->ff_range);
+                                     (double4 *)c->acc_tmp, s, c->ff_range, (const double4 *)c->sym_acc);
         if (!st)
             st = nb::energy_reduce(p.n, nullptr, pos, nullptr, nullptr, nullptr,
                                    (const double4 *)c->acc_tmp, p.G, c->e_blocks, c->e_out, s,
@@ -1197,7 +1201,7 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
     const int cur_a = symm ? c->splan.warps : c->plan.block, cur_b = symm ? c->splan.bpt : c->plan.bpt;
     auto make = [&](int a, int b, nb::SymPlan *sp, nb::SkPlan *fp) -> int {
         if (symm) {
-            if (ff_sym(c)) return nb::symff_plan(p.n, a, b, c->device, sp);
+            if (ff_sym(c)) return nb::symff_plan(p.n, a, b, c->device, sp, p.bands);
             if (f64_sym(c)) return nb::sym64_plan(p.n, a, b, c->device, sp);
             return nb::sym_plan(p.n, a, b, c->device, sp, comp_sym(c) ? 1 : 0,
                                 comp_sym(c) ? NB_SOURCE_AUTO : (c->splan.fixed ? NB_SOURCE_FIXED : NB_SOURCE_TRIANGULAR),

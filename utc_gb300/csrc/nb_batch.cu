@@ -1671,7 +1671,7 @@ static int sys_plans_for(nb_batch *b, SysPlans *out)
         int st;
         if (b->sym) {
             nb::SymPlan q;
-            if ((st = b->f64 ? nb::symff_plan(b->sizes[i], 0, 0, b->device, &q)
+            if ((st = b->f64 ? nb::symff_plan(b->sizes[i], 0, 0, b->device, &q, -1)
                              : nb::sym_plan(b->sizes[i], 0, 0, b->device, &q, 0, NB_SOURCE_TRIANGULAR, -1)))
                 return st;
             sp.tpart = std::max(sp.tpart, (size_t)q.slots * q.rb * wide);
@@ -1701,7 +1701,7 @@ static int sys_step(const nb_batch *b, const SysPlans &sp, int i, int c, float4 
         const double4 *po = (const double4 *)b->pos[c] + o;
         double4 *pn = (double4 *)b->pos[c ^ 1] + o, *vel = (double4 *)b->vel + o;
         if ((st = nb::symff_force(sp.sym[i], po, p.eps2, b->ff_split + 3 * (size_t)o, range, (double4 *)tpart,
-                                  (double4 *)spart, s)))
+                                  (double4 *)spart, nullptr, s)))
             return st;
         return nb::sym64_integrate(sp.sym[i], po, pn, vel, (const double4 *)tpart, (const double4 *)spart,
                                    p.damping, p.dt, p.kick, p.G, nullptr, s, range);

@@ -378,19 +378,24 @@ int sym_fx_rescale(const SymPlan &p, float4 *spart, float eps2, cudaStream_t s);
 
 // FP64 symmetric path (nb_sym64.cu): tpart / spart hold double4 entries.
 // sym64_integrate with ffrange (the float-float path's scale record) undoes
-// that path's power-of-two scaling of the sums.
+// that path's power-of-two scaling of the sums; with accsum (banded
+// float-float plans) it takes the folded per-body sums instead of the
+// partials.
 int sym64_plan(int n, int warps, int bpt, int device, SymPlan *pl);
 int sym64_force(const SymPlan &p, const double4 *pos, double eps2, double4 *tpart, double4 *spart,
                 cudaStream_t s);
 int sym64_integrate(const SymPlan &p, const double4 *pos_old, double4 *pos_new, double4 *vel,
                     const double4 *tpart, const double4 *spart, double damping, double dt, int kick,
-                    double G, double4 *acc_out, cudaStream_t s, const unsigned long long *ffrange = nullptr);
+                    double G, double4 *acc_out, cudaStream_t s, const unsigned long long *ffrange = nullptr,
+                    const double4 *accsum = nullptr);
 // Float-float symmetric path for FP64 state (nb_symff.cu): same layout and
 // double4 partials as the FP64 path; `split` holds 3 n float4 (the scaled
 // three-float positions), `range` 2 unsigned long long (the scale record).
-int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl);
+// bands as for sym_plan (0 = where the array would pass the budget, k > 1,
+// -1 = never: the shape grows instead); accsum: n double4 for banded plans.
+int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl, int bands = 0);
 int symff_force(const SymPlan &p, const double4 *pos, double eps2, float4 *split, unsigned long long *range,
-                double4 *tpart, double4 *spart, cudaStream_t s, int phi = 0);
+                double4 *tpart, double4 *spart, double4 *accsum, cudaStream_t s, int phi = 0);
 // The float-float paths' per-step preparation: range (2 unsigned long long)
 // <- bits of the largest |coordinate| and |mass|; H + M + L <- the positions
 // and masses scaled by those powers of two, split into three floats.

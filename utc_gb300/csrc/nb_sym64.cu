@@ -144,33 +144,42 @@ __global__ void sym64_integrate_kernel(const double4 *__restrict__ pos_old, doub
                                        const double4 *__restrict__ spart, int n, int rb, int nc, int nrb,
                                        long long total, int grid, double damping, double dt, int kick,
                                        double G, double4 *__restrict__ acc_out,
-                                       const unsigned long long *__restrict__ ffrange)
+                                       const unsigned long long *__restrict__ ffrange,
+                                       const double4 *__restrict__ accsum)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int rc = rb / 32;
-    const int I = i / rb;
-    const int c0 = sk_owner(sym_prefix(I, nc, rc), total, grid);
-    const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1, total, grid);
-    const int li = i - I * rb;
     // w: the potential sum_j m_j / sqrt(d2), j != i, when the force pass
     // recorded it (the float-float energy pass), else 0
     double ax = 0.0, ay = 0.0, az = 0.0, aw = 0.0;
-    for (int c = c0; c <= c1; ++c) {
-        const double4 q = tpart[(size_t)(c + I) * rb + li];
-        ax = __dadd_rn(ax, q.x);
-        ay = __dadd_rn(ay, q.y);
-        az = __dadd_rn(az, q.z);
-        aw = __dadd_rn(aw, q.w);
-    }
-    long long off = (long long)i - rb;  // row r at soff(r) + i - (r + 1) rb
-    for (int r = 0; r < I; ++r) {
-        const double4 q = spart[off];
-        off += (long long)n - (long long)(r + 2) * rb;
-        ax = __dadd_rn(ax, q.x);
-        ay = __dadd_rn(ay, q.y);
-        az = __dadd_rn(az, q.z);
-        aw = __dadd_rn(aw, q.w);
+    if (accsum) {  // banded plan: the fold kernel's sums
+        const double4 q = accsum[i];
+        ax = q.x;
+        ay = q.y;
+        az = q.z;
+        aw = q.w;
+    } else {
+        const int rc = rb / 32;
+        const int I = i / rb;
+        const int c0 = sk_owner(sym_prefix(I, nc, rc), total, grid);
+        const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1, total, grid);
+        const int li = i - I * rb;
+        for (int c = c0; c <= c1; ++c) {
+            const double4 q = tpart[(size_t)(c + I) * rb + li];
+            ax = __dadd_rn(ax, q.x);
+            ay = __dadd_rn(ay, q.y);
+            az = __dadd_rn(az, q.z);
+            aw = __dadd_rn(aw, q.w);
+        }
+        long long off = (long long)i - rb;  // row r at soff(r) + i - (r + 1) rb
+        for (int r = 0; r < I; ++r) {
+            const double4 q = spart[off];
+            off += (long long)n - (long long)(r + 2) * rb;
+            ax = __dadd_rn(ax, q.x);
+            ay = __dadd_rn(ay, q.y);
+            az = __dadd_rn(az, q.z);
+            aw = __dadd_rn(aw, q.w);
+        }
     }
     if (ffrange) {
         // float-float path: its sums are in units scaled by 2^kx (positions)
@@ -277,12 +286,14 @@ int sym64_force(const SymPlan &p, const double4 *pos, double eps2, double4 *tpar
 
 int sym64_integrate(const SymPlan &p, const double4 *pos_old, double4 *pos_new, double4 *vel,
                     const double4 *tpart, const double4 *spart, double damping, double dt, int kick,
-                    double G, double4 *acc_out, cudaStream_t s, const unsigned long long *ffrange)
+                    double G, double4 *acc_out, cudaStream_t s, const unsigned long long *ffrange,
+                    const double4 *accsum)
 {
     if (p.n == 0) return NB_OK;
+    if (p.nbands > 1 && !accsum) return set_error(NB_ERR_INVALID, "sym64_integrate: a banded plan needs its per-body sums");
     sym64_integrate_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(pos_old, pos_new, vel, tpart, spart, p.n, p.rb,
                                                              p.nc, p.nrb, p.total, p.grid, damping, dt, kick,
-                                                             G, acc_out, ffrange);
+                                                             G, acc_out, ffrange, p.nbands > 1 ? accsum : nullptr);
     NB_LAUNCH_CHECK("sym64_integrate_kernel launch");
     return NB_OK;
 }

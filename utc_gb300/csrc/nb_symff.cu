@@ -105,11 +105,15 @@ __global__ void ff_split_kernel(const double4 *__restrict__ pos, int n, const un
 
 // PHI: also the potential sum_j m_j inv (j != i) in the partials' w, the
 // reaction's included (energy pass).
-template <int W, int BPT, int MINB, bool PHI>
+// BAND: one band of a banded plan, as in sym_force_kernel: items
+// [it0, it0 + total) from row block r0 on, target-side slot c + I - r0,
+// source-side entries offset by soff0.
+template <int W, int BPT, int MINB, bool PHI, bool BAND = false>
 __global__ void __launch_bounds__(32 * W, MINB)
     symff_force_kernel(const float4 *__restrict__ H, const float4 *__restrict__ Mi, const float4 *__restrict__ Lo,
                        int n, double eps2, const unsigned long long *__restrict__ range,
-                       double4 *__restrict__ tpart, double4 *__restrict__ spart, long long total, int nc, int nrb)
+                       double4 *__restrict__ tpart, double4 *__restrict__ spart, long long total, int nc, int nrb,
+                       long long it0, int r0, long long soff0)
 {
     constexpr int WB = 32 * BPT;
     constexpr int RB = W * WB;
@@ -124,7 +128,11 @@ __global__ void __launch_bounds__(32 * W, MINB)
     const float eh = __double2float_rn(e2s), el = __double2float_rn(e2s - (double)eh);
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     long long it = sk_start(c, total, gridDim.x);
-    const long long end = sk_start(c + 1, total, gridDim.x);
+    long long end = sk_start(c + 1, total, gridDim.x);
+    if constexpr (BAND) {
+        it += it0;
+        end += it0;
+    }
 
     while (it < end) {
         const int I = sym_row_of(it, nc, RC, nrb);
@@ -227,7 +235,8 @@ __global__ void __launch_bounds__(32 * W, MINB)
                 // lane l now holds the reaction on chunk body l from this warp
                 const double fx = (double)Fxh + (double)Fxl, fy = (double)Fyh + (double)Fyl,
                              fz = (double)Fzh + (double)Fzl, fp = PHI ? (double)Fph + (double)Fpl : 0.0;
-                const long long so = sym_soff(I, n, RB) + (jb + lane - (I + 1) * RB);
+                long long so = sym_soff(I, n, RB) + (jb + lane - (I + 1) * RB);
+                if constexpr (BAND) so -= soff0;
                 if (W == 1) {
                     if (in) spart[so] = make_double4(fx, fy, fz, fp);
                 } else {
@@ -258,7 +267,7 @@ __global__ void __launch_bounds__(32 * W, MINB)
                 if (PHI) aphi[k] += (double)Aph[k] + (double)Apl[k];
             }
         }
-        double4 *dst = tpart + (size_t)(c + I) * RB + wid * WB;
+        double4 *dst = tpart + (size_t)(c + I - (BAND ? r0 : 0)) * RB + wid * WB;
 #pragma unroll
         for (int k = 0; k < BPT; ++k) dst[lane + 32 * k] = make_double4(ax[k], ay[k], az[k], aphi[k]);
         it = seg_end;
@@ -266,10 +275,18 @@ __global__ void __launch_bounds__(32 * W, MINB)
 }
 
 typedef void (*symff_kernel_t)(const float4 *, const float4 *, const float4 *, int, double,
-                               const unsigned long long *, double4 *, double4 *, long long, int, int);
+                               const unsigned long long *, double4 *, double4 *, long long, int, int, long long,
+                               int, long long);
 
-static symff_kernel_t symff_kernel_for(int w, int bpt, bool phi = false)
+static symff_kernel_t symff_kernel_for(int w, int bpt, bool phi = false, bool band = false)
 {
+    if (band) {  // banded plans: the one-warp shapes
+        if (w == 1 && bpt == 2)
+            return phi ? symff_force_kernel<1, 2, 16, true, true> : symff_force_kernel<1, 2, 16, false, true>;
+        if (w == 1 && bpt == 4)
+            return phi ? symff_force_kernel<1, 4, 8, true, true> : symff_force_kernel<1, 4, 8, false, true>;
+        return nullptr;
+    }
     if (w == 1 && bpt == 2) return phi ? symff_force_kernel<1, 2, 16, true> : symff_force_kernel<1, 2, 16, false>;
     if (w == 1 && bpt == 4) return phi ? symff_force_kernel<1, 4, 8, true> : symff_force_kernel<1, 4, 8, false>;
     if (w == 4 && bpt == 4) return phi ? symff_force_kernel<4, 4, 2, true> : symff_force_kernel<4, 4, 2, false>;
@@ -278,22 +295,23 @@ static symff_kernel_t symff_kernel_for(int w, int bpt, bool phi = false)
     return nullptr;
 }
 
-int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl)
+int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl, int bands)
 {
-    if (warps == 0 && bpt == 0) {
-        // one-warp CTAs x 2 targets (row block 64); then 1 x 4 (128), 4 x 4
-        // (512), 8 x 4 (1024), 8 x 8 (2048) while the source-side array
-        // (32 B entries) is over budget
+    const bool given = warps != 0 || bpt != 0;
+    if (!given) {
+        // one-warp CTAs x 2 targets (row block 64), its source-side array
+        // (32 B entries) in bands where it would pass the budget; without
+        // bands 1 x 4 (128), 4 x 4 (512), 8 x 4 (1024), 8 x 8 (2048) take
+        // over instead
         static const int shapes[5][2] = {{1, 2}, {1, 4}, {4, 4}, {8, 4}, {8, 8}};
         int s = 0;
-        while (s < 4 && sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) * (long long)sizeof(double4) >
-                            kSymSpartBudget)
-            ++s;
+        if (bands < 0)
+            while (s < 4 && sym_spart_entries(n, shapes[s][0] * 32 * shapes[s][1]) * (long long)sizeof(double4) >
+                                kSymSpartBudget)
+                ++s;
         warps = shapes[s][0];
         bpt = shapes[s][1];
     }
-    symff_kernel_t k = symff_kernel_for(warps, bpt);
-    if (!k) return set_error(NB_ERR_UNSUPPORTED, "float-float symmetric kernel shape not compiled");
     SymPlan p;
     p.n = n;
     p.warps = warps;
@@ -301,22 +319,79 @@ int symff_plan(int n, int warps, int bpt, int device, SymPlan *pl)
     p.rb = warps * 32 * bpt;
     p.nc = (n + 31) / 32;
     p.nrb = (n + p.rb - 1) / p.rb;
+    p.spart_size = sym_spart_entries(n, p.rb);
+    p.band_row[0] = 0;
+    p.band_row[1] = p.nrb;
+    if (bands >= 0 && n > 0 &&
+        (bands > 1 || p.spart_size * (long long)sizeof(double4) > kSymSpartBudget)) {
+        long long mx = 0;
+        const int k = sym_make_bands(n, p.rb, kSymSpartBudget / (long long)sizeof(double4), bands > 1 ? bands : 0,
+                                     p.band_row, &mx);
+        if (k == 0)
+            return set_error(NB_ERR_UNSUPPORTED, "the float-float source side would need more than 512 bands");
+        p.nbands = k;
+        p.spart_size = mx;
+    }
+    const bool band = p.nbands > 1;
+    symff_kernel_t k = symff_kernel_for(warps, bpt, false, band);
+    if (!k)
+        return set_error(NB_ERR_UNSUPPORTED, band ? "float-float symmetric kernel shape not compiled for bands "
+                                                    "(one warp x 2 or 4 targets)"
+                                                  : "float-float symmetric kernel shape not compiled");
     p.total = n > 0 ? sym_prefix(p.nrb, p.nc, p.rb / 32) : 0;
     int sms = 0, occ = 0;
     NB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * warps, 0));
     int occ_phi = 0;  // the energy pass runs on the same plan
-    NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_phi, symff_kernel_for(warps, bpt, true), 32 * warps, 0));
+    NB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_phi, symff_kernel_for(warps, bpt, true, band),
+                                                          32 * warps, 0));
     if (occ_phi < occ) occ = occ_phi;
     if (occ < 1) return set_error(NB_ERR_UNSUPPORTED, "float-float symmetric kernel does not fit on an SM");
     long long grid = (long long)sms * occ;
     if (p.total > 0 && grid > p.total) grid = p.total;
     p.grid = p.total > 0 ? (int)grid : 0;
     p.slots = p.total > 0 ? p.grid + p.nrb - 1 : 0;
-    p.spart_size = sym_spart_entries(n, p.rb);
     p.sms = sms;
     *pl = p;
     return NB_OK;
+}
+
+// After band [r0, r1) of a banded plan: the running per-body sums (x, y, z
+// and the potential in w), as sym_fold_kernel does for float partials.
+__global__ void __launch_bounds__(256) symff_fold_kernel(const double4 *__restrict__ tpart,
+                                                         const double4 *__restrict__ spart,
+                                                         double4 *__restrict__ accsum, int n, int rb, int nc,
+                                                         long long it0, long long bt, int gb, int r0, int r1,
+                                                         long long soff0, int first)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int I = i / rb;
+    if (I < r0) return;  // rows before the band get nothing from it (r0 = 0 for the first band)
+    double4 a = first ? make_double4(0.0, 0.0, 0.0, 0.0) : accsum[i];
+    if (I < r1) {
+        const int rc = rb / 32;
+        const int c0 = sk_owner(sym_prefix(I, nc, rc) - it0, bt, gb);
+        const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1 - it0, bt, gb);
+        const int li = i - I * rb;
+        for (int c = c0; c <= c1; ++c) {
+            const double4 q = tpart[(size_t)(c + I - r0) * rb + li];
+            a.x = __dadd_rn(a.x, q.x);
+            a.y = __dadd_rn(a.y, q.y);
+            a.z = __dadd_rn(a.z, q.z);
+            a.w = __dadd_rn(a.w, q.w);
+        }
+    }
+    const int rend = I < r1 ? I : r1;
+#pragma unroll 4
+    for (int r = r0; r < rend; ++r) {
+        const double4 q = spart[sym_soff(r, n, rb) - soff0 + (i - (long long)(r + 1) * rb)];
+        a.x = __dadd_rn(a.x, q.x);
+        a.y = __dadd_rn(a.y, q.y);
+        a.z = __dadd_rn(a.z, q.z);
+        a.w = __dadd_rn(a.w, q.w);
+    }
+    accsum[i] = a;
 }
 
 int ff_scale_split(const double4 *pos, int n, int sms, float4 *H, float4 *M, float4 *L, unsigned long long *range,
@@ -334,16 +409,32 @@ int ff_scale_split(const double4 *pos, int n, int sms, float4 *H, float4 *M, flo
 }
 
 int symff_force(const SymPlan &p, const double4 *pos, double eps2, float4 *split, unsigned long long *range,
-                double4 *tpart, double4 *spart, cudaStream_t s, int phi)
+                double4 *tpart, double4 *spart, double4 *accsum, cudaStream_t s, int phi)
 {
     if (p.n == 0) return NB_OK;
-    symff_kernel_t k = symff_kernel_for(p.warps, p.bpt, phi != 0);
+    symff_kernel_t k = symff_kernel_for(p.warps, p.bpt, phi != 0, p.nbands > 1);
     if (!k) return set_error(NB_ERR_UNSUPPORTED, "float-float symmetric kernel shape not compiled");
+    if (p.nbands > 1 && !accsum) return set_error(NB_ERR_INVALID, "symff_force: a banded plan needs its per-body sums");
     float4 *H = split, *M = split + p.n, *L = split + 2 * (size_t)p.n;
     int st = ff_scale_split(pos, p.n, p.sms, H, M, L, range, s);
     if (st) return st;
-    k<<<p.grid, 32 * p.warps, 0, s>>>(H, M, L, p.n, eps2, range, tpart, spart, p.total, p.nc, p.nrb);
-    NB_LAUNCH_CHECK("symff_force_kernel launch");
+    if (p.nbands <= 1) {
+        k<<<p.grid, 32 * p.warps, 0, s>>>(H, M, L, p.n, eps2, range, tpart, spart, p.total, p.nc, p.nrb, 0, 0, 0);
+        NB_LAUNCH_CHECK("symff_force_kernel launch");
+        return NB_OK;
+    }
+    const int rc = p.rb / 32;
+    for (int b = 0; b < p.nbands; ++b) {
+        const int r0 = p.band_row[b], r1 = p.band_row[b + 1];
+        const long long it0 = sym_prefix(r0, p.nc, rc), bt = sym_prefix(r1, p.nc, rc) - it0;
+        const long long soff0 = sym_soff(r0, p.n, p.rb);
+        const int gb = (int)(bt < p.grid ? bt : p.grid);
+        k<<<gb, 32 * p.warps, 0, s>>>(H, M, L, p.n, eps2, range, tpart, spart, bt, p.nc, p.nrb, it0, r0, soff0);
+        NB_LAUNCH_CHECK("symff_force_kernel launch");
+        symff_fold_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(tpart, spart, accsum, p.n, p.rb, p.nc, it0, bt, gb, r0,
+                                                            r1, soff0, b == 0);
+        NB_LAUNCH_CHECK("symff_fold_kernel launch");
+    }
     return NB_OK;
 }
 
