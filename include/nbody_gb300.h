@@ -136,11 +136,14 @@ typedef struct nb_params {
  * order; or added at once into per-body 64-bit fixed-point accumulators with
  * integer atomics, 48 B per body, summed essentially exactly and still
  * deterministic (integer sums do not depend on their order), but measured
- * 2-10 % slower on GB300 at the same launch shape.  NB_SOURCE_AUTO takes
- * the triangular array while it fits in 8 GiB with 4 warps x 20 targets per
- * lane (N up to about 1.66e6), and the fixed-point side beyond (3 % faster
- * there than the one shape whose array would still fit, and 48 B per body).
- * Both are within the same tolerances of the FP64 oracle. */
+ * 2-10 % slower on GB300 at the same launch shape.  Where the triangular
+ * array would pass 8 GiB even with 4 warps x 20 targets per lane (N above
+ * about 1.66e6), it is cut into bands of consecutive row blocks, stepped
+ * band by band through one 8 GiB buffer (nb_params.bands; the float-float
+ * kernel of NB_F64 state does the same past N = 185k).  NB_SOURCE_AUTO
+ * takes the triangular array (in bands where needed) and the fixed-point
+ * side only beyond 512 bands (N above about 3.6e7).  Both are within the
+ * same tolerances of the FP64 oracle. */
 typedef enum { NB_SOURCE_AUTO = 0, NB_SOURCE_TRIANGULAR = 1, NB_SOURCE_FIXED = 2 } nb_source_side;
 
 typedef struct nb_ctx nb_ctx;

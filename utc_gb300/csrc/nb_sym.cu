@@ -27,9 +27,22 @@
 // The integrate kernel adds, per body, its target-side slots (CTA order) and
 // its source-side entries spart[0..I_b-1][b] (row order): deterministic.
 //
+// Bands (template flag BAND; plans with nbands > 1, where the triangular
+// array, about N^2 / (2 rb) float4, would pass kSymSpartBudget, or on
+// request through nb_params.bands).  The row blocks are cut into bands of
+// consecutive rows whose entries fit the budget; the force kernel runs once
+// per band over the band's (row, chunk) items (stream-K over the band), all
+// bands reusing one source-side buffer and one set of target-side slots,
+// and after each band sym_fold_kernel adds, per body, the band's target-side
+// slots (if the body's row is in the band) and its source-side rows into a
+// running per-body sum, which the integrator then takes.  Fixed order
+// throughout, so still deterministic.  A band costs about 1.5 ms of tail
+// and fold at N = 2^20, so only sizes whose force pass takes seconds use
+// more than a few.
+//
 // Fixed-point source side (template flag FX; plans with fixed = 1, chosen
-// by nb_params.source_side or for large N, where the triangular array,
-// about N^2 / (2 rb) float4, would need a slow shape to stay in budget).  The CTA's reaction on a chunk body,
+// by nb_params.source_side, or where even bands would not do: more than
+// SymPlan::kMaxBands of them).  The CTA's reaction on a chunk body,
 // summed over its warps as above, is added straight into per-body 64-bit
 // integer accumulators with integer atomics.  Integer addition is
 // associative, so the sums do not depend on the order the CTAs run in: the
@@ -46,11 +59,8 @@
 // a new eps2) by sym_fx_prepare / sym_fx_rescale; the integrator zeroes the
 // accumulators after reading them.  On GB300 this variant ran 2-10 % slower
 // than the triangular array of the same shape (the pair loop's schedule
-// shifts with the code around it), 4 % slower than the 4 x 20 triangular
-// shape at N = 2^21, but 3 % faster than the 8 x 24 one, the only shape
-// whose array stays within budget there.  So it is the automatic choice
-// where 4 x 20 would pass the budget (N above about 1.66e6), and otherwise
-// only where a caller asks for it.
+// shifts with the code around it; 3513 against 3593 G interactions/s for
+// the banded 4 x 20 triangular plan at N = 2^21).
 //
 // Compensated variant (COMP): each target's per-chunk partial sum (32
 // sources) is folded into a two-sum (hi, lo) pair, the W warps' reactions on
@@ -65,7 +75,8 @@
 // SM) run 15 % faster than 8-warp CTAs with 8 targets per lane (80 registers,
 // 24 warps per SM) on GB300.  Small row blocks make the triangular
 // source-side array large (about N^2 / (2 rb) float4), so the default shape
-// grows the row block when that array would pass kSymSpartBudget.
+// grows to 4 warps x 20 targets when that array would pass kSymSpartBudget,
+// and is cut into bands beyond that.
 #include "nb_internal.cuh"
 
 namespace nb {

@@ -36,7 +36,12 @@
 // Each target's 32-source chunk sum is folded into FP64 accumulators; each
 // reaction (one chunk body, the warp's 32*BPT targets) is written as FP64.
 // The FP64 integrator of nb_sym64.cu then sums the partials in FP64, undoes
-// the scaling and integrates.  196 FP32 operations and one approximation
+// the scaling and integrates.  The default shape, one warp x 2 targets
+// (row blocks of 64 bodies: a triangular array of N^2 / 4 bytes), is kept at
+// every size: past N = 185k the array is cut into bands of at most 8 GiB as
+// in nb_sym.cu (symff_fold_kernel folds each band in FP64), which ran 9-22 %
+// faster on GB300 than growing the row block (315 against 288 and 259 G
+// interactions/s at N = 2^19 and 2^20).  196 FP32 operations and one approximation
 // per pair (98 per interaction); results within a few 1e-15 of the FP64
 // oracle (FP64 arithmetic: a few 1e-16), not bit-identical (NB_ALGO_EXACT is).
 // Range: the scaled squared distances and eps2 must stay normal floats:
