@@ -16,7 +16,8 @@ pytestmark = pytest.mark.gpu
 # "symfx": the symmetric FP32 kernel with its fixed-point source side;
 # "symband": the symmetric kernel with its triangular array in three bands
 MODES = [("f32", "fast"), ("f32", "sym"), ("f32", "symfx"), ("f32", "symband"), ("f32", "exact"), ("f64", "exact"),
-         ("f64", "sym"), ("f64", "symband"), ("f64", "sym64"), ("f32comp", "fast"), ("f32comp", "sym")]
+         ("f64", "sym"), ("f64", "symband"), ("f64", "sym64"), ("f32comp", "fast"), ("f32comp", "sym"),
+         ("f32comp", "symband")]
 
 
 def system(n, prec, algo, **kw):
@@ -389,7 +390,7 @@ def test_zero_softening_is_nan_like_the_reference(cuda, prec, algo):
 
 TOL = {("f32", "fast"): 2e-5, ("f32", "sym"): 2e-5, ("f32", "symfx"): 2e-5, ("f32", "symband"): 2e-5,
        ("f32", "exact"): 2e-5, ("f64", "exact"): 1e-14, ("f64", "sym"): 1e-13, ("f64", "symband"): 1e-13,
-       ("f64", "sym64"): 1e-13, ("f32comp", "fast"): 2e-6, ("f32comp", "sym"): 2e-6}
+       ("f64", "sym64"): 1e-13, ("f32comp", "fast"): 2e-6, ("f32comp", "sym"): 2e-6, ("f32comp", "symband"): 2e-6}
 
 
 @pytest.mark.parametrize("prec,algo", MODES)

@@ -144,13 +144,40 @@ def test_compensated_run_host_frames(cuda, algo):
         assert frames[k].tobytes() == want[k].tobytes()
 
 
-@pytest.mark.parametrize("n,shape", [(65536, (32, 12)), (1048576, (256, 12))])
-def test_compensated_sym_default_shape(cuda, n, shape):
+@pytest.mark.parametrize("n,shape,bands", [(65536, (32, 12), 1), (1048576, (128, 12), 2)])
+def test_compensated_sym_default_shape(cuda, n, shape, bands):
     """Compensated symmetric plan: one-warp CTAs x 12 targets unless the
-    source-side array's hi and lo halves would pass 8 GiB (then 4 and 8 warps)."""
+    source-side array's hi and lo halves would pass 8 GiB, then 4 warps x 12,
+    in bands of at most 8 GiB beyond that (11.5 GB in two bands at N = 2^20)."""
     with NBodySystem(n, "f32comp", "sym") as s:
-        info = s.plan_info()
+        info, src = s.plan_info(), s.source_info()
     assert (info["block"], info["bpt"]) == shape
+    assert src["bands"] == bands and src["mib"] <= 8192, src
+
+
+@pytest.mark.parametrize("n", [3000, 20000])
+@pytest.mark.parametrize("bands", [2, 5])
+def test_compensated_sym_bands(cuda, n, bands):
+    """The compensated kernel in bands: the fold keeps each body's (sum,
+    compensation) pair as the compensated integrator does, so accelerations
+    stay within the compensated tolerance of the FP64 oracle, and steps
+    agree with the one-pass plan to float rounding."""
+    p, v = ics.plummer(n, seed=n + 5)
+    eps2 = 1e-3
+    # the pair terms read float positions
+    want = oracle.accel(p.astype(np.float32).astype(np.float64), float(np.float32(eps2)))
+    outs = []
+    for kw in ({}, {"bands": bands}):
+        with NBodySystem(n, "f32comp", "sym", kick="physical", eps2=eps2, damping=1.0, dt=1e-3, **kw) as s:
+            s.set_state(p, v)
+            a = s.accel()
+            s.step(8)
+            outs.append((a, s.get_state()[0], s.source_info()))
+    assert outs[1][2]["bands"] > 1
+    for a, _, _ in outs:
+        assert body_err(a, want).max() <= 2e-6
+    rel = np.linalg.norm(outs[0][1][:, :3] - outs[1][1][:, :3], axis=1) / (np.linalg.norm(outs[0][1][:, :3], axis=1) + 0.1)
+    assert rel.max() <= 1e-6
 
 
 def test_f64_energy_paths_agree_and_timing(cuda, capsys):

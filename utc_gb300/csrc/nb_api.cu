@@ -373,12 +373,13 @@ int nb_create(const nb_params *p, nb_ctx **out)
             const size_t halves = comp_sym(c) ? 2 : 1;  // compensated: hi and lo blocks
             if ((st = nb::sym_plan(p->n, p->block ? p->block / 32 : 0, p->bpt, c->device, &c->splan,
                                    comp_sym(c) ? 1 : 0, comp_sym(c) ? NB_SOURCE_AUTO : p->source_side,
-                                   comp_sym(c) ? -1 : p->bands)) ||
+                                   p->bands)) ||
                 (st = dev_alloc((void **)&c->sym_t,
                                 halves * c->splan.slots * c->splan.rb * sizeof(float4),
                                 "symmetric scratch allocation")) ||
                 (c->splan.nbands > 1 &&
-                 (st = dev_alloc(&c->sym_acc, n * sizeof(float4), "per-body sums of the banded source side"))) ||
+                 (st = dev_alloc(&c->sym_acc, halves * n * sizeof(float4),
+                                 "per-body sums of the banded source side"))) ||
                 (st = dev_alloc((void **)&c->sym_s, halves * c->splan.spart_size * sizeof(float4),
                                 c->splan.fixed ? "symmetric source-side accumulators (48 B per body)"
                                                : "symmetric source-side array (about N^2/(2 rb) entries; "
@@ -561,12 +562,12 @@ static int step_once(nb_ctx *c, cudaStream_t s, void *acc_out, cudaEvent_t *ev =
     int st;
     if (ev) NB_CUDA(cudaEventRecord(ev[0], s));
     if (comp_sym(c)) {
-        st = nb::sym_force(c->splan, c->pos32, (float)p.eps2, c->sym_t, c->sym_s, nullptr, s);
+        st = nb::sym_force(c->splan, c->pos32, (float)p.eps2, c->sym_t, c->sym_s, (float4 *)c->sym_acc, s);
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[1], s));
         if (!st)
             st = nb::sym_comp_integrate(c->splan, c->sym_t, c->sym_s, (double4 *)c->pos[0], c->pos32,
                                         (float4 *)c->vel, c->vel_lo, (float)p.damping, (float)p.dt,
-                                        p.dt, p.kick, (float)p.G, (double4 *)acc_out, s);
+                                        p.dt, p.kick, (float)p.G, (double4 *)acc_out, s, (const float4 *)c->sym_acc);
         if (!st && ev) NB_CUDA(cudaEventRecord(ev[2], s));
         return st;  // positions are updated in place: no ping-pong
     }
@@ -1149,7 +1150,7 @@ int nb_launches_per_step(nb_ctx *c)
     if (!c) return -1;
     if (c->p.n == 0) return 0;
     // a banded symmetric plan: a force and a fold launch per band
-    const int bands = (uses_sym(c) || f64_sym(c)) && c->splan.nbands > 1 ? c->splan.nbands : 0;
+    const int bands = (uses_sym(c) || comp_sym(c) || f64_sym(c)) && c->splan.nbands > 1 ? c->splan.nbands : 0;
     if (ff_sym(c)) return 4 + (bands ? 2 * bands - 1 : 0);  // scale reduction, split, force, integrate
     if (bands) return 2 * bands + 1;
     return (uses_fast(c) || is_comp(c) || f64_sym(c)) ? 2 : 1;
@@ -1205,7 +1206,7 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
             if (f64_sym(c)) return nb::sym64_plan(p.n, a, b, c->device, sp);
             return nb::sym_plan(p.n, a, b, c->device, sp, comp_sym(c) ? 1 : 0,
                                 comp_sym(c) ? NB_SOURCE_AUTO : (c->splan.fixed ? NB_SOURCE_FIXED : NB_SOURCE_TRIANGULAR),
-                                comp_sym(c) ? -1 : p.bands);
+                                p.bands);
         }
         return nb::fast_plan(p.n, a, b, p.ctas_per_sm, c->device, fp, is_comp(c) ? nb::SK_COMP : 0);
     };
@@ -1267,7 +1268,7 @@ int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *
     bool banded = false;
     for (const Cand &v : viable) banded = banded || (symm && v.sp.nbands > 1);
     if (banded && !c->sym_acc) {
-        cudaError_t ea = nb::dmalloc(&c->sym_acc, (size_t)p.n * ent);
+        cudaError_t ea = nb::dmalloc(&c->sym_acc, halves * (size_t)p.n * ent);
         if (ea != cudaSuccess) return nb::cuda_error(ea, "autotune scratch allocation");
     }
     if (!symm) {  // the directed scratch also serves the energy pass

@@ -361,7 +361,8 @@ inline long long sym_fx_entries(int n) { return 3ll * n + 1; }
 // bands, -1 = never (the shape grows instead, as compensated plans do).
 int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp = 0, int source_side = 0,
              int bands = 0);
-// accsum: n float4, the per-body sums of banded plans (unused otherwise)
+// accsum: the per-body sums of banded plans (n float4; compensated plans
+// 2 n: sums, then compensations), unused otherwise
 int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, float4 *spart,
               float4 *accsum, cudaStream_t s);
 // consume (fixed plans): zero the accumulators after reading them, ready for
@@ -403,10 +404,13 @@ int ff_scale_split(const double4 *pos, int n, int sms, float4 *H, float4 *M, flo
                    cudaStream_t s);
 
 // Compensated kick / drift from compensated symmetric partials, or
-// (acc_out != nullptr) the bare FP64 accelerations (nb_precision.cu)
+// (acc_out != nullptr) the bare FP64 accelerations (nb_precision.cu);
+// banded plans take accsum (2 n float4: the folded sums, then their
+// compensations)
 int sym_comp_integrate(const SymPlan &p, const float4 *tpart, const float4 *spart, double4 *pos64,
                        float4 *pos32, float4 *vhi, float4 *vlo, float damping, float dt,
-                       double dt64, int kick, float G, double4 *acc_out, cudaStream_t s);
+                       double dt64, int kick, float G, double4 *acc_out, cudaStream_t s,
+                       const float4 *accsum = nullptr);
 
 // One reverse step's per-body update given the summed pair terms (o, odm):
 //   lx <- lx + out;  lv <- D mu;  gm += dm (+ D dt mu.a in reference mode)

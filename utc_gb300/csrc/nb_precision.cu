@@ -163,30 +163,36 @@ __global__ void sym_comp_integrate_kernel(const float4 *__restrict__ tpart, cons
                                           long long total, int grid, double4 *__restrict__ pos64,
                                           float4 *__restrict__ pos32, float4 *__restrict__ vhi,
                                           float4 *__restrict__ vlo, float damping, float dt,
-                                          double dt64, int kick, float G, double4 *__restrict__ acc_out)
+                                          double dt64, int kick, float G, double4 *__restrict__ acc_out,
+                                          const float4 *__restrict__ accsum)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int rc = rb / 32;
-    const int I = i / rb;
-    const int c0 = sk_owner(sym_prefix(I, nc, rc), total, grid);
-    const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1, total, grid);
-    const int li = i - I * rb;
     float4 S = make_float4(0.f, 0.f, 0.f, 0.f), C = S;
-    float e;
-    auto add = [&](const float4 h, const float4 l) {
-        two_sum(S.x, h.x, S.x, e); C.x = __fadd_rn(C.x, __fadd_rn(e, l.x));
-        two_sum(S.y, h.y, S.y, e); C.y = __fadd_rn(C.y, __fadd_rn(e, l.y));
-        two_sum(S.z, h.z, S.z, e); C.z = __fadd_rn(C.z, __fadd_rn(e, l.z));
-    };
-    for (int c = c0; c <= c1; ++c) {
-        const size_t k = (size_t)(c + I) * rb + li;
-        add(tpart[k], tpart[tlo + k]);
-    }
-    long long off = (long long)i - rb;  // row r at soff(r) + i - (r + 1) rb
-    for (int r = 0; r < I; ++r) {
-        add(spart[off], spart[slo + off]);
-        off += (long long)n - (long long)(r + 2) * rb;
+    if (accsum) {  // banded plan: the compensated fold's (S, C)
+        S = accsum[i];
+        C = accsum[(size_t)n + i];
+    } else {
+        const int rc = rb / 32;
+        const int I = i / rb;
+        const int c0 = sk_owner(sym_prefix(I, nc, rc), total, grid);
+        const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1, total, grid);
+        const int li = i - I * rb;
+        float e;
+        auto add = [&](const float4 h, const float4 l) {
+            two_sum(S.x, h.x, S.x, e); C.x = __fadd_rn(C.x, __fadd_rn(e, l.x));
+            two_sum(S.y, h.y, S.y, e); C.y = __fadd_rn(C.y, __fadd_rn(e, l.y));
+            two_sum(S.z, h.z, S.z, e); C.z = __fadd_rn(C.z, __fadd_rn(e, l.z));
+        };
+        for (int c = c0; c <= c1; ++c) {
+            const size_t k = (size_t)(c + I) * rb + li;
+            add(tpart[k], tpart[tlo + k]);
+        }
+        long long off = (long long)i - rb;  // row r at soff(r) + i - (r + 1) rb
+        for (int r = 0; r < I; ++r) {
+            add(spart[off], spart[slo + off]);
+            off += (long long)n - (long long)(r + 2) * rb;
+        }
     }
     if (acc_out) {
         acc_out[i] = make_double4((double)S.x + (double)C.x, (double)S.y + (double)C.y,
@@ -306,13 +312,14 @@ int comp_integrate(const SkPlan &p, const float4 *partial, double4 *pos64, float
 
 int sym_comp_integrate(const SymPlan &p, const float4 *tpart, const float4 *spart, double4 *pos64,
                        float4 *pos32, float4 *vhi, float4 *vlo, float damping, float dt,
-                       double dt64, int kick, float G, double4 *acc_out, cudaStream_t s)
+                       double dt64, int kick, float G, double4 *acc_out, cudaStream_t s, const float4 *accsum)
 {
     if (p.n == 0) return NB_OK;
     if (!p.comp) return set_error(NB_ERR_INVALID, "sym_comp_integrate needs a compensated plan");
+    if (p.nbands > 1 && !accsum) return set_error(NB_ERR_INVALID, "sym_comp_integrate: a banded plan needs its sums");
     sym_comp_integrate_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(
         tpart, spart, (long long)p.slots * p.rb, p.spart_size, p.n, p.rb, p.nc, p.nrb, p.total,
-        p.grid, pos64, pos32, vhi, vlo, damping, dt, dt64, kick, G, acc_out);
+        p.grid, pos64, pos32, vhi, vlo, damping, dt, dt64, kick, G, acc_out, p.nbands > 1 ? accsum : nullptr);
     NB_LAUNCH_CHECK("sym_comp_integrate_kernel launch");
     return NB_OK;
 }

@@ -557,6 +557,52 @@ __global__ void __launch_bounds__(256) sym_fold_kernel(const float4 *__restrict_
     accsum[i] = make_float4(ax, ay, az, 0.f);
 }
 
+// The compensated fold: running (S, C) per body in accsum[0..n) and
+// accsum[n..2n), each partial (hi, lo) added as the compensated integrator
+// adds it (two-sum into S, its error and lo into C).
+__global__ void __launch_bounds__(256) sym_fold_comp_kernel(const float4 *__restrict__ tpart,
+                                                            const float4 *__restrict__ spart, long long tlo,
+                                                            long long slo, float4 *__restrict__ accsum, int n,
+                                                            int rb, int nc, long long it0, long long bt, int gb,
+                                                            int r0, int r1, long long soff0, int first)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int I = i / rb;
+    if (I < r0) return;
+    float4 S = make_float4(0.f, 0.f, 0.f, 0.f), C = S;
+    if (!first) {
+        S = accsum[i];
+        C = accsum[(size_t)n + i];
+    }
+    float e;
+    auto add = [&](const float4 h, const float4 l) {
+        two_sum(S.x, h.x, S.x, e);
+        C.x = __fadd_rn(C.x, __fadd_rn(e, l.x));
+        two_sum(S.y, h.y, S.y, e);
+        C.y = __fadd_rn(C.y, __fadd_rn(e, l.y));
+        two_sum(S.z, h.z, S.z, e);
+        C.z = __fadd_rn(C.z, __fadd_rn(e, l.z));
+    };
+    if (I < r1) {
+        const int rc = rb / 32;
+        const int c0 = sk_owner(sym_prefix(I, nc, rc) - it0, bt, gb);
+        const int c1 = sk_owner(sym_prefix(I + 1, nc, rc) - 1 - it0, bt, gb);
+        const int li = i - I * rb;
+        for (int c = c0; c <= c1; ++c) {
+            const size_t k = (size_t)(c + I - r0) * rb + li;
+            add(tpart[k], tpart[tlo + k]);
+        }
+    }
+    const int rend = I < r1 ? I : r1;
+    for (int r = r0; r < rend; ++r) {
+        const long long k = sym_soff(r, n, rb) - soff0 + (i - (long long)(r + 1) * rb);
+        add(spart[k], spart[slo + k]);
+    }
+    accsum[i] = S;
+    accsum[(size_t)n + i] = C;
+}
+
 typedef void (*sym_kernel_t)(const float4 *, int, float, float4 *, float4 *, long long, int, int,
                              long long, long long, long long, int, long long);
 
@@ -567,7 +613,12 @@ typedef void (*sym_kernel_t)(const float4 *, int, float, float4 *, float4 *, lon
 static sym_kernel_t sym_kernel_for(int w, int bpt, int comp, int fixed = 0, int band = 0)
 {
     if (band) {  // banded triangular plans: the default shapes
-        if (comp || fixed) return nullptr;
+        if (fixed) return nullptr;
+        if (comp) {
+            if (w == 1 && bpt == 12) return sym_force_kernel<1, 12, 8, true, false, true>;
+            if (w == 4 && bpt == 12) return sym_force_kernel<4, 12, 2, true, false, true>;
+            return nullptr;
+        }
         if (w == 1 && bpt == 16) return sym_force_kernel<1, 16, 8, false, false, true>;
         if (w == 4 && bpt == 20) return sym_force_kernel<4, 20, 2, false, false, true>;
         if (w == 1 && bpt == 8) return sym_force_kernel<1, 8, 8, false, false, true>;
@@ -613,9 +664,9 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int s
         return set_error(NB_ERR_UNSUPPORTED, "the compensated kernel keeps its triangular (hi, lo) source side");
     int fixed = source_side == NB_SOURCE_FIXED ? 1 : 0;
     const bool given = warps != 0 || bpt != 0;
-    // plain triangular plans go to bands where the array would pass the
-    // budget; compensated plans and bands = -1 grow the row block instead
-    const bool may_band = !comp && !fixed && bands >= 0;
+    // triangular plans go to bands where the array would pass the budget;
+    // bands = -1 grows the row block instead
+    const bool may_band = !fixed && bands >= 0;
     SymPlan p;
     for (int attempt = 0; attempt < 2; ++attempt) {
         if (!given && fixed) {
@@ -634,7 +685,7 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int s
             // (2560) while the source-side array is over budget, and beyond
             // that 4 x 20 in bands (without bands: 8 x 24, 6144).
             // Compensated (hi and lo halves): 1 x 12 (384), 4 x 12 (1536),
-            // 8 x 12 (3072).
+            // then 4 x 12 in bands (without bands: 8 x 12, 3072).
             static const int plain[3][2] = {{1, 16}, {4, 20}, {8, 24}};
             static const int compd[3][2] = {{1, 12}, {4, 12}, {8, 12}};
             const int(*shapes)[2] = comp ? compd : plain;
@@ -675,10 +726,10 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int s
         p.spart_size = fixed ? sym_fx_entries(n) : sym_spart_entries(n, p.rb);
         p.band_row[0] = 0;
         p.band_row[1] = p.nrb;
-        if (may_band && !fixed && n > 0 && (bands > 1 || p.spart_size * (long long)sizeof(float4) > kSymSpartBudget)) {
+        const long long entry = (comp ? 2 : 1) * (long long)sizeof(float4);  // hi and lo halves
+        if (may_band && !fixed && n > 0 && (bands > 1 || p.spart_size * entry > kSymSpartBudget)) {
             long long mx = 0;
-            const int k = sym_make_bands(n, p.rb, kSymSpartBudget / (long long)sizeof(float4), bands > 1 ? bands : 0,
-                                         p.band_row, &mx);
+            const int k = sym_make_bands(n, p.rb, kSymSpartBudget / entry, bands > 1 ? bands : 0, p.band_row, &mx);
             if (k == 0) {
                 // more bands than a plan holds (N above about 3.6e7 with the
                 // 4 x 20 shape): the automatic choice takes the fixed-point
@@ -699,7 +750,8 @@ int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp, int s
         return set_error(NB_ERR_UNSUPPORTED, p.fixed ? "symmetric kernel shape not compiled with the fixed-point "
                                                        "source side (one warp x 4, 8 or 16 targets)"
                                          : p.nbands > 1 ? "symmetric kernel shape not compiled for bands (one warp "
-                                                          "x 4, 8 or 16 targets, 4 warps x 20)"
+                                                          "x 4, 8 or 16 targets, 4 warps x 20; compensated: "
+                                                          "1 or 4 warps x 12)"
                                                         : "symmetric kernel shape not compiled");
     p.total = n > 0 ? sym_prefix(p.nrb, p.nc, p.rb / 32) : 0;
     int sms = 0, occ = 0;
@@ -793,8 +845,12 @@ int sym_force(const SymPlan &p, const float4 *pos, float eps2, float4 *tpart, fl
         const int gb = (int)(bt < p.grid ? bt : p.grid);
         k<<<gb, 32 * p.warps, 0, s>>>(pos, p.n, eps2, tpart, spart, bt, p.nc, p.nrb, tlo, slo, it0, r0, soff0);
         NB_LAUNCH_CHECK("sym_force_kernel launch");
-        sym_fold_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(tpart, spart, accsum, p.n, p.rb, p.nc, it0, bt, gb, r0, r1,
-                                                          soff0, b == 0);
+        if (p.comp)
+            sym_fold_comp_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(tpart, spart, tlo, slo, accsum, p.n, p.rb, p.nc,
+                                                                   it0, bt, gb, r0, r1, soff0, b == 0);
+        else
+            sym_fold_kernel<<<(p.n + 255) / 256, 256, 0, s>>>(tpart, spart, accsum, p.n, p.rb, p.nc, it0, bt, gb, r0,
+                                                              r1, soff0, b == 0);
         NB_LAUNCH_CHECK("sym_fold_kernel launch");
     }
     return NB_OK;
