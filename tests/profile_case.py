@@ -3,7 +3,7 @@
     python tests/profile_case.py --n 65536 --steps 4 [--algo fast|sym|exact]
         [--precision f32|f32comp|f64] [--case step|adjoint|batch]
         [--block B --bpt K] [--kick physical|reference] [--systems S]
-        [--source-side auto|triangular|fixed]
+        [--source-side auto|triangular|fixed] [--bands K]
 
 case step:    `steps` steps of a seeded Plummer sphere (eps2=1e-4, dt=1e-4)
               through the C ABI;
@@ -39,6 +39,8 @@ def main():
     ap.add_argument("--systems", type=int, default=64)
     ap.add_argument("--source-side", default="auto", choices=["auto", "triangular", "fixed"],
                     help="source side of the symmetric FP32 kernel")
+    ap.add_argument("--bands", type=int, default=0,
+                    help="symmetric kernels: the triangular array in about K bands (0 = automatic)")
     a = ap.parse_args()
     import torch
 
@@ -75,14 +77,16 @@ def main():
     p, v = ics.plummer(a.n, seed=0)
     eps2 = 1e-4 if a.precision in ("f32comp", "f64") else np.float32(1e-4)
     with NBodySystem(a.n, a.precision, a.algo, kick=a.kick, eps2=eps2, damping=1.0,
-                     dt=np.float32(1e-4), block=a.block, bpt=a.bpt, source_side=a.source_side) as s:
+                     dt=np.float32(1e-4), block=a.block, bpt=a.bpt, source_side=a.source_side,
+                     bands=a.bands) as s:
         if a.precision in ("f32comp", "f64"):
             s.set_state(p, v)
         else:
             s.set_state(ics.f32(p), ics.f32(v))
         s.step(a.steps)
         torch.cuda.synchronize()
-        print("ok", a.n, a.steps, s.plan_info() if a.algo in ("fast", "sym") else a.algo)
+        print("ok", a.n, a.steps, s.plan_info() if a.algo in ("fast", "sym") else a.algo,
+              s.source_info() if a.algo == "sym" else "")
 
 
 if __name__ == "__main__":
