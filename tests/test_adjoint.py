@@ -21,10 +21,13 @@ def rel(a, b):
 
 def system(n, algo, **kw):
     """algo "fast": directed forward and VJP kernels; "sym": symmetric ones;
-    "symfx": symmetric ones, the forward with its fixed-point source side
-    (the automatic choice for N above about 1.66e6)."""
+    "symfx": symmetric ones, the forward with its fixed-point source side;
+    "symband": symmetric ones, the forward's triangular array in three bands
+    (what large N runs)."""
     if algo == "symfx":
         return NBodySystem(n, "f32", "sym", source_side="fixed", **kw)
+    if algo == "symband":
+        return NBodySystem(n, "f32", "sym", bands=3, **kw)
     return NBodySystem(n, "f32", algo, **kw)
 
 
@@ -43,7 +46,7 @@ def gpu_grads(pos32, vel32, y, kick, eps2, dt, damping, steps, every, G=1.0, alg
         return pT, gx0[:, :3].cpu().numpy(), gv0[:, :3].cpu().numpy(), gm.cpu().numpy()
 
 
-@pytest.mark.parametrize("algo", ["fast", "sym", "symfx"])
+@pytest.mark.parametrize("algo", ["fast", "sym", "symfx", "symband"])
 @pytest.mark.parametrize("kick", ["physical", "reference"])
 @pytest.mark.parametrize("n,steps,every", [(96, 30, 7), (1000, 20, 20), (257, 12, 1), (3000, 6, 4)])
 def test_adjoint_matches_fp64_reference(cuda, algo, kick, n, steps, every):
@@ -62,7 +65,7 @@ def test_adjoint_matches_fp64_reference(cuda, algo, kick, n, steps, every):
     assert rel(gm, rm) <= 1e-4
 
 
-@pytest.mark.parametrize("algo", ["fast", "sym", "symfx"])
+@pytest.mark.parametrize("algo", ["fast", "sym", "symfx", "symband"])
 def test_checkpoint_interval_does_not_change_gradients(cuda, algo):
     n, steps = 300, 24
     p64, v64 = ics.uniform_cube(n, seed=3)
@@ -122,7 +125,7 @@ def test_autograd_function_loss_gradients(cuda):
     assert torch.equal(m.grad, dm)
 
 
-@pytest.mark.parametrize("algo", ["fast", "sym", "symfx"])
+@pytest.mark.parametrize("algo", ["fast", "sym", "symfx", "symband"])
 @pytest.mark.parametrize("kick", ["physical", "reference"])
 def test_second_backward_recomputes_every_segment(cuda, algo, kick):
     """The forward pass leaves the last segment's states in place and the first

@@ -110,3 +110,46 @@ def test_random_case_more(cuda, c):
             s.step(c["steps"])
             wp, wv = s.get_state()
     assert gp.tobytes() == wp.tobytes() and gv.tobytes() == wv.tobytes()
+
+
+def cases_bands(count=18, seed=4051):
+    """A third sweep: the symmetric kernels with their triangular array in
+    2 to 8 bands (float, compensated and float-float double state), against
+    the same context stepped in one pass and, for float state, the FP64
+    oracle."""
+    rng = np.random.default_rng(seed)
+    precs = ["f32", "f64", "f32comp"]
+    for k in range(count):
+        yield dict(k=k, prec=precs[k % 3], n=int(np.exp(rng.uniform(np.log(600), np.log(9000)))),
+                   bands=int(rng.integers(2, 9)), kick=["reference", "physical"][int(rng.integers(2))],
+                   eps2=float(10 ** rng.uniform(-4, -1)), damping=float(rng.choice([1.0, 0.999, 0.995])),
+                   dt=float(10 ** rng.uniform(-4, -2)), G=float(rng.uniform(0.5, 2.0)),
+                   steps=int(rng.integers(1, 5)), ic=["plummer", "cube"][int(rng.integers(2))],
+                   seed=int(rng.integers(1 << 30)))
+
+
+@pytest.mark.parametrize("c", list(cases_bands()), ids=lambda c: f"{c['k']}-{c['prec']}-n{c['n']}-b{c['bands']}")
+def test_random_case_bands(cuda, c):
+    n, prec = c["n"], c["prec"]
+    T = np.float32 if prec == "f32" else np.float64
+    p, v = (ics.plummer if c["ic"] == "plummer" else ics.uniform_cube)(n, seed=c["seed"])
+    pos, vel = p.astype(T), v.astype(T)
+    eps2, damp, dt, G = (float(T(c[k])) for k in ("eps2", "damping", "dt", "G"))
+    out = []
+    for bands in (0, c["bands"]):
+        with NBodySystem(n, prec, "sym", kick=c["kick"], eps2=eps2, damping=damp, dt=dt, G=G, bands=bands) as s:
+            s.set_state(pos, vel)
+            s.step(c["steps"])
+            out.append((s.get_state()[0], s.source_info()))
+    assert c["bands"] == 0 or out[1][1]["bands"] >= 1
+    (a, _), (b, _) = out
+    scale = np.linalg.norm(np.asarray(a, np.float64)[:, :3], axis=1) + 0.1
+    rel = np.linalg.norm(np.asarray(b, np.float64)[:, :3] - np.asarray(a, np.float64)[:, :3], axis=1) / scale
+    assert rel.max() <= {"f32": 1e-5, "f32comp": 1e-9, "f64": 1e-13}[prec], rel.max()
+    if prec == "f32":
+        km = oracle.KICK_REFERENCE if c["kick"] == "reference" else oracle.KICK_PHYSICAL
+        wp, _ = oracle.step(np.asarray(pos, np.float64), np.asarray(vel, np.float64), eps2, damp, dt, c["steps"],
+                            kick_mode=km, G=G)
+        rel = np.linalg.norm(np.asarray(b, np.float64)[:, :3] - wp[:, :3], axis=1) / (
+            np.linalg.norm(wp[:, :3], axis=1) + 0.1)
+        assert rel.max() <= 1e-5, rel.max()
