@@ -378,8 +378,9 @@ int nb_source_info(nb_ctx *ctx, int *info4);
 
 /* Time every compiled launch shape of the context's force kernel on its
  * current state (`reps` steps each; the state is restored) and keep the
- * fastest; shapes whose symmetric source-side array would pass 8 GiB are
- * skipped.  cache_path (may be NULL) is a text file of earlier choices keyed
+ * fastest; a symmetric shape whose triangular source-side array would pass
+ * 8 GiB is timed in bands (skipped if it has no banded form).  cache_path
+ * (may be NULL) is a text file of earlier choices keyed
  * by device, precision, algorithm and n: a hit applies the cached shape
  * without timing.  chosen2 = {threads per CTA, bodies per lane}.  Drops
  * captured step graphs and a recorded adjoint forward pass; the reference-

@@ -1158,9 +1158,10 @@ int nb_launches_per_step(nb_ctx *c)
 
 // Single-system autotuner: every compiled shape of the context's force
 // kernel is timed on the current state (saved and restored), the fastest
-// is kept.  Candidates whose symmetric source-side array would pass the
-// budget are skipped; the scratch is sized for the largest candidate tried
-// and kept, so no step reallocates afterwards.
+// is kept.  Symmetric candidates whose triangular array would pass the
+// budget are planned in bands (skipped when the shape has no banded form);
+// the scratch is sized for the largest candidate tried and kept, so no step
+// reallocates afterwards.
 int nb_autotune(nb_ctx *c, int reps, const char *cache_path, void *stream, int *chosen2)
 {
     if (int rs = refuse_shard(c, "nb_autotune")) return rs;
