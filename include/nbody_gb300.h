@@ -120,12 +120,14 @@ typedef struct nb_params {
                          reactions on the source bodies; other contexts and
                          batches ignore it (a value outside the enum is
                          NB_ERR_INVALID everywhere) */
-    int bands;        /* NB_ALGO_SYM with the triangular source side (NB_F32
-                         and NB_F64): 0 = cut the rows into bands only where
-                         the array would pass 8 GiB; k > 1 = about k bands
-                         (smaller scratch; for tests and tight memory);
-                         other values NB_ERR_INVALID; other contexts and
-                         batches ignore it */
+    int bands;        /* NB_ALGO_SYM with the triangular source side (NB_F32,
+                         NB_F32_COMP and NB_F64): 0 = cut the rows into bands
+                         only where the array would pass 8 GiB; k in 2..512 =
+                         k bands (fewer where there are fewer row blocks,
+                         more where 8 GiB needs more): smaller scratch, for
+                         tests and tight memory; other values
+                         NB_ERR_INVALID; other contexts and batches ignore
+                         it */
     int reserved[2];
 } nb_params;
 

@@ -40,7 +40,7 @@ def main():
     ap.add_argument("--source-side", default="auto", choices=["auto", "triangular", "fixed"],
                     help="source side of the symmetric FP32 kernel")
     ap.add_argument("--bands", type=int, default=0,
-                    help="symmetric kernels: the triangular array in about K bands (0 = automatic)")
+                    help="symmetric kernels: the triangular array in K bands (0 = automatic)")
     a = ap.parse_args()
     import torch
 

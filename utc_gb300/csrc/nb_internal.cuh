@@ -319,37 +319,54 @@ inline long long sym_spart_entries(int n, int rb)
 // bigger row block or to bands.
 constexpr long long kSymSpartBudget = 8ll << 30;
 
-// Cuts the row blocks of a triangular plan into bands whose source-side
-// entries stay within cap (want > 0: about `want` bands of equal size
-// instead); fills rows[0..k] and the largest band's entry count and returns
-// the band count k, or 0 when more than SymPlan::kMaxBands would be needed.
-// A row's entries are n - (r + 1) rb (none for the last row block).
-inline int sym_make_bands(int n, int rb, long long cap, int want, int *rows, long long *max_entries)
+// Bands of a triangular plan: consecutive row blocks, a new band started
+// whenever the next row's entries (n - (r + 1) rb; none for the last row
+// block) would take the band past cap.  Fills rows[0..k] (when rows is not
+// null) and the largest band's entry count; returns the band count k, or 0
+// when more than `limit` bands would be needed.
+inline int sym_band_rows(int n, int rb, long long cap, int limit, int *rows, long long *max_entries)
 {
     const int nrb = (n + rb - 1) / rb;
-    if (want > 0) {
-        const long long total = sym_spart_entries(n, rb);
-        cap = (total + want - 1) / want;
-        if (cap < 1) cap = 1;
-    }
     int k = 0;
     long long acc = 0, mx = 0;
-    rows[0] = 0;
+    if (rows) rows[0] = 0;
     for (int r = 0; r < nrb; ++r) {
         const long long e = r < nrb - 1 ? (long long)n - (long long)(r + 1) * rb : 0;
         if (acc > 0 && acc + e > cap) {
-            if (k + 1 >= SymPlan::kMaxBands) return 0;
-            rows[++k] = r;
+            if (++k >= limit) return 0;
+            if (rows) rows[k] = r;
             mx = acc > mx ? acc : mx;
             acc = 0;
         }
         acc += e;
     }
     mx = acc > mx ? acc : mx;
-    rows[++k] = nrb;
-    *max_entries = mx;
-    return k;
+    if (rows) rows[k + 1] = nrb;
+    if (max_entries) *max_entries = mx;
+    return k + 1;
 }
+
+// The bands of a plan whose source-side entries must stay within cap: as
+// few as that needs, or (want > 1) as many as the smallest cap that still
+// gives at most `want` bands needs, if that is more.  Returns the band
+// count, or 0 beyond SymPlan::kMaxBands.
+inline int sym_make_bands(int n, int rb, long long cap, int want, int *rows, long long *max_entries)
+{
+    if (want > 1) {
+        const long long total = sym_spart_entries(n, rb);
+        long long lo = (total + want - 1) / want, hi = total;
+        if (lo < 1) lo = 1;
+        if (hi < lo) hi = lo;
+        while (lo < hi) {  // the smallest cap with at most `want` bands
+            const long long mid = lo + (hi - lo) / 2;
+            if (sym_band_rows(n, rb, mid, want, nullptr, nullptr) != 0) hi = mid;
+            else lo = mid + 1;
+        }
+        if (lo < cap) cap = lo;
+    }
+    return sym_band_rows(n, rb, cap, SymPlan::kMaxBands, rows, max_entries);
+}
+
 // float4 entries of the fixed-point source side: 6 n 64-bit accumulators
 // (hi x, y, z then lo x, y, z, each n long) and one float4 record: the sum of
 // |m| over the bodies and the scale factors (sym_fx_prepare).
@@ -357,8 +374,8 @@ inline long long sym_fx_entries(int n) { return 3ll * n + 1; }
 
 // source_side: nb_source_side (NB_SOURCE_AUTO / TRIANGULAR / FIXED), for
 // plain plans; compensated plans are always triangular.  bands: 0 = bands
-// only where the triangular array would pass the budget, k > 0 = about k
-// bands, -1 = never (the shape grows instead, as compensated plans do).
+// only where the triangular array would pass the budget, k > 1 = k bands
+// (sym_make_bands), -1 = never (the shape grows instead).
 int sym_plan(int n, int warps, int bpt, int device, SymPlan *pl, int comp = 0, int source_side = 0,
              int bands = 0);
 // accsum: the per-body sums of banded plans (n float4; compensated plans

@@ -66,7 +66,7 @@ class NBodySystem:
         p.source_side = {"auto": N.NB_SOURCE_AUTO, "triangular": N.NB_SOURCE_TRIANGULAR,
                          "fixed": N.NB_SOURCE_FIXED}[source_side]
         # symmetric kernels with the triangular array: 0 = bands only where it
-        # would pass 8 GiB, k > 1 = about k bands
+        # would pass 8 GiB, k > 1 = k bands (at most as many as row blocks)
         p.bands = int(bands)
         self.params = p
         self.n = int(n)
