@@ -166,8 +166,9 @@ __global__ void sym_comp_integrate_kernel(const float4 *__restrict__ tpart, cons
                                           double dt64, int kick, float G, double4 *__restrict__ acc_out,
                                           const float4 *__restrict__ accsum)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    // bodies from the last one down: the longest row walks start first
+    const int i = n - 1 - (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < 0) return;
     float4 S = make_float4(0.f, 0.f, 0.f, 0.f), C = S;
     if (accsum) {  // banded plan: the compensated fold's (S, C)
         S = accsum[i];

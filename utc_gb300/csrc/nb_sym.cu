@@ -425,7 +425,9 @@ __global__ void __launch_bounds__(32 * W) sym_force_kernel_f2(const float4 *__re
 // q, q+4, ... in order, and the quad combines its four sums as
 // (s0 + s1) + (s2 + s3) (fixed order: deterministic).  The row walk, up to
 // nrb - 1 entries for the last row block, is what bounds the kernel; split
-// four ways it is a quarter as long.
+// four ways it is a quarter as long.  Bodies are taken from the last one
+// down, so the blocks with the longest walks start first instead of forming
+// the tail (19.7 -> 18.1 us at N = 65536 on GB300; the sums are the same).
 constexpr int kSymIntegBlock = 256;
 
 // fxacc != nullptr: the fixed-point source side; thread 0 of the quad adds
@@ -439,8 +441,8 @@ __global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
     unsigned long long *__restrict__ fxacc, int consume, const float4 *__restrict__ accsum)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = (int)(t >> 2), q = (int)(t & 3);
-    const bool live = i < n;  // dead threads still take part in the shuffles
+    const int i = n - 1 - (int)(t >> 2), q = (int)(t & 3);
+    const bool live = i >= 0;  // dead threads still take part in the shuffles
     float ax = 0.f, ay = 0.f, az = 0.f;
     if (live && accsum) {
         if (q == 0) {
@@ -516,15 +518,16 @@ __global__ void __launch_bounds__(kSymIntegBlock) sym_integrate_kernel(
 // per body, the running sum (zero before the first band) plus, if the body's
 // row block is in the band, its target-side slots in CTA order, then the
 // band's source-side rows before the body's row block in row order.  Fixed
-// order throughout: deterministic.
+// order throughout: deterministic.  Bodies from the last one down, as in
+// sym_integrate_kernel (the longest row walks first).
 __global__ void __launch_bounds__(256) sym_fold_kernel(const float4 *__restrict__ tpart,
                                                        const float4 *__restrict__ spart,
                                                        float4 *__restrict__ accsum, int n, int rb, int nc,
                                                        long long it0, long long bt, int gb, int r0, int r1,
                                                        long long soff0, int first)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int i = n - 1 - (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < 0) return;
     const int I = i / rb;
     if (I < r0) return;  // rows before the band get nothing from it (r0 = 0 for the first band)
     float ax = 0.f, ay = 0.f, az = 0.f;
@@ -566,8 +569,8 @@ __global__ void __launch_bounds__(256) sym_fold_comp_kernel(const float4 *__rest
                                                             int rb, int nc, long long it0, long long bt, int gb,
                                                             int r0, int r1, long long soff0, int first)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int i = n - 1 - (int)(blockIdx.x * blockDim.x + threadIdx.x);  // longest walks first
+    if (i < 0) return;
     const int I = i / rb;
     if (I < r0) return;
     float4 S = make_float4(0.f, 0.f, 0.f, 0.f), C = S;

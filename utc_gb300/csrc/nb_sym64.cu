@@ -147,8 +147,9 @@ __global__ void sym64_integrate_kernel(const double4 *__restrict__ pos_old, doub
                                        const unsigned long long *__restrict__ ffrange,
                                        const double4 *__restrict__ accsum)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    // bodies from the last one down: the longest row walks start first
+    const int i = n - 1 - (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < 0) return;
     // w: the potential sum_j m_j / sqrt(d2), j != i, when the force pass
     // recorded it (the float-float energy pass), else 0
     double ax = 0.0, ay = 0.0, az = 0.0, aw = 0.0;

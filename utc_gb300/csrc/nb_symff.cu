@@ -369,8 +369,8 @@ __global__ void __launch_bounds__(256) symff_fold_kernel(const double4 *__restri
                                                          long long it0, long long bt, int gb, int r0, int r1,
                                                          long long soff0, int first)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int i = n - 1 - (int)(blockIdx.x * blockDim.x + threadIdx.x);  // longest walks first
+    if (i < 0) return;
     const int I = i / rb;
     if (I < r0) return;  // rows before the band get nothing from it (r0 = 0 for the first band)
     double4 a = first ? make_double4(0.0, 0.0, 0.0, 0.0) : accsum[i];
