@@ -348,9 +348,11 @@ __global__ void __launch_bounds__(kAdjUpdBlock) adj_update_sym_kernel(
     float4 *__restrict__ lx, float4 *__restrict__ lv, float *__restrict__ gm, float4 *__restrict__ gbuf,
     float damping, float dt, int kick, float G, int want_next_g)
 {
+    // bodies from the last one down, as in sym_integrate_kernel: the blocks
+    // with the longest row walks start first
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = (int)(t >> 2), q = (int)(t & 3);
-    const bool live = i < n;  // dead threads still take part in the shuffles
+    const int i = n - 1 - (int)(t >> 2), q = (int)(t & 3);
+    const bool live = i >= 0;  // dead threads still take part in the shuffles
     float ox = 0.f, oy = 0.f, oz = 0.f, odm = 0.f;
     if (live) {
         const int rc = rb / 32;
